@@ -1,0 +1,201 @@
+/* C-ABI of libmumag_cuda.so: the GB300 backend of the micromagnetic hot path of
+ * MaMMoS-project/mumag_matrixfree2 (energy and gradient, demag Poisson solve, minimizer update).
+ *
+ * Conventions (those of the reference's own C-ABI, src/cpp/cpp_mkl_minimizer.cpp:26-764):
+ *  - caller-owned contiguous arrays; float64; int32 zero-based indices; node vectors are (N,3)
+ *    row-major with xyz interleaved (index 3*i+c);
+ *  - inputs/outputs through pointers; no exception crosses the ABI;
+ *  - every call returns an int status: 0 OK, > 0 a soft condition (MM_MAXITER, MM_NONFINITE,
+ *    MM_BREAKDOWN), < 0 an error (see mm_status_str, and mm_last_error for the message);
+ *  - host pointers unless the function name ends in _dev (then device pointers on the current
+ *    device, e.g. torch tensors' data_ptr());
+ *  - one CUDA stream per problem; a problem is not thread-safe, several problems may coexist.
+ */
+#ifndef MUMAG_CUDA_H
+#define MUMAG_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MM_OK 0
+#define MM_MAXITER 1
+#define MM_NONFINITE 2
+#define MM_BREAKDOWN 3
+#define MM_ERR_ARG -1
+#define MM_ERR_OOM -2
+#define MM_ERR_CUDA -3
+#define MM_ERR_STATE -4
+#define MM_ERR_SETUP -5
+
+#define MM_PRECOND_NONE 0
+#define MM_PRECOND_JACOBI 1
+#define MM_PRECOND_AMG 2   /* SA-AMG V-cycle, damped-Jacobi smoothing (reference "amg")        */
+#define MM_PRECOND_AMGCL 3 /* SA-AMG V-cycle, SPAI0 smoothing (reference "amgcl", the default)  */
+
+#define MM_METHOD_PCOHEN_HS 0
+#define MM_METHOD_LBFGS 1
+#define MM_METHOD_WG_NP 2
+
+typedef struct mm_problem mm_problem;
+
+/* Minimizer parameters; field meanings follow LoopParams (src/hysteresis_loop.py:34-125). */
+typedef struct {
+  int method;           /* MM_METHOD_* */
+  int max_iter;
+  int pc_iters;
+  int pc_auto;
+  int ls_max_evals;     /* 15 in the reference's steps */
+  int L;                /* CG restart period; <= 0 means N */
+  int memory;           /* L-BFGS history */
+  int wg_gamma;         /* BB: number of initial line-search steps */
+  double tau_f, eps_a, tau0;
+  double ls_eta1, ls_eta2, ls_C, ls_c;
+  double pc_force_eta, pc_force_alpha, pc_stagnation_nu, pc_reg;
+  double cg_tol;        /* tolerance of the initial Poisson solve */
+  double phi_tol;       /* tolerance of the line-search Poisson solves; <= 0: min(cg_tol, 0.1 tau_f) */
+  int cg_maxiter;
+} mm_min_params;
+
+typedef struct {
+  int iters, evals, preco_iters, demag_iters;
+  double E, gnorm, seconds;
+  int status;
+} mm_min_info;
+
+/* ---- setup helpers ------------------------------------------------------------------------ */
+
+/* Orientation fix (swap local nodes 1,2 where det J < 0), volumes, inv(J)^T (E,3,3) and shape
+ * gradients (E,4,3).  Replaces compute_volume_JinvT / compute_grad_phi_from_JinvT,
+ * src/loop.py:56-102. */
+int mm_geom_compute(int n_nodes, int n_elems, const double* knt, const int* conn_in, int* conn_out,
+                    double* volume, double* JinvT, double* grad_phi);
+
+/* Dirichlet mask: 0.0 on nodes of faces owned by one tetrahedron, else 1.0.
+ * Replaces find_outer_boundary_mask, src/add_shell.py:105-136. */
+int mm_boundary_mask(int n_nodes, int n_elems, const int* conn, double* mask);
+
+/* Morton (10 bits per axis) node and element permutations (stable on equal keys).
+ * Replaces the target="gpu" branch of reorder_mesh, src/reorder_mesh.py:19-30,85-100. */
+int mm_morton_order(int n_nodes, int n_elems, const double* knt, const int* conn, int* node_perm,
+                    int* elem_perm);
+
+/* ---- host-only setup (no GPU needed): the assembled operators and the SA hierarchy --------- */
+
+typedef struct mm_setup mm_setup;
+
+/* Assemble the energy operator and (when reg >= 0) the Poisson matrix with its SA hierarchy on the
+ * host, exactly as mm_create + mm_build_poisson do.  Lets a caller inspect or reuse the setup. */
+int mm_setup_create(int n_nodes, int n_elems, const int* conn, const double* volume, const double* grad_phi,
+                    const int* mat_id, int n_mat, const double* A_lookup, const double* K1_lookup,
+                    const double* Js_lookup, const double* k_easy, const double* boundary_mask, double reg,
+                    int max_levels, int max_coarse, mm_setup** out);
+int mm_setup_destroy(mm_setup* s);
+/* Energy operator: magnetic rows, entries per row (col, material), exchange w, anisotropy q,
+ * demag gradient G (3 per entry) and demag source D (3 per entry). */
+int mm_setup_energy_info(mm_setup* s, int* n_rows, int64_t* nnz, int* single_axis);
+int mm_setup_energy_export(mm_setup* s, int* rows, int* ptr, int* col, int* mat, double* w, double* q,
+                           double* G, double* D, double* diag_exchange);
+int mm_setup_levels(mm_setup* s, int* n_levels);
+int mm_setup_level_info(mm_setup* s, int level, int* n, int64_t* nnz_A, int64_t* nnz_P, int* n_cols_P);
+int mm_setup_level_export(mm_setup* s, int level, int* A_ptr, int* A_col, double* A_val, int* P_ptr,
+                          int* P_col, double* P_val, int* agg);
+
+/* ---- problem ------------------------------------------------------------------------------ */
+
+/* Upload an oriented mesh with its materials (reduced units) and assemble the energy operator.
+ * M_nodal: sum_e Js_e Ve / 4 per node; boundary_mask may be NULL (then the Poisson solve projects
+ * out the mean, as make_solve_U does without a mask, src/poisson_solve.py:535-536).
+ * Replaces make_energy_kernels (src/energy_kernels.py:82-142) and the operator assembly of
+ * src/amg_utils.py:741-789 / src/loop.py:1133-1166. */
+int mm_create(int n_nodes, int n_elems, const int* conn, const double* volume, const double* grad_phi,
+              const int* mat_id, int n_mat, const double* A_lookup, const double* K1_lookup,
+              const double* Js_lookup, const double* k_easy, double V_mag, const double* M_nodal,
+              const double* boundary_mask, mm_problem** out);
+int mm_destroy(mm_problem* h);
+
+/* Assemble the Poisson matrix (src/amg_utils.py:21-84) and build the preconditioner
+ * (src/poisson_solve.py:566-639).  max_levels / max_coarse bound the SA hierarchy. */
+int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels, int max_coarse,
+                     int* n_levels);
+/* Hierarchy introspection (tests): rows, nnz(A), nnz(P) of level l. */
+int mm_amg_level_info(mm_problem* h, int level, int* n, int64_t* nnz_A, int64_t* nnz_P);
+/* Copy level l's operator (CSR) and aggregates (n, -1 = none; all -1 on the coarsest level). */
+int mm_amg_export_level(mm_problem* h, int level, int* A_ptr, int* A_col, double* A_val, int* agg);
+
+/* Energy and gradient: E = 1/2 m.(g + g_z) / V_mag, g = (K m + G U + g_z) / V_mag with
+ * g_z = -2 M_nodal (B_ext + B_bias).  B_bias may be NULL.
+ * Replaces energy_and_grad (src/energy_kernels.py:147-180,340-459) and the C++
+ * evaluate_energy_and_grad (src/cpp/cpp_mkl_minimizer.cpp:178-206). */
+int mm_energy_grad(mm_problem* h, const double* m, const double* U, const double* B_ext,
+                   const double* B_bias, double* E, double* g);
+int mm_energy_grad_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B_ext,
+                       const double* d_B_bias, double* E, double* d_g);
+
+/* Exchange + anisotropy Hessian action C v / V_mag.
+ * Replaces local_grad_only (src/energy_kernels.py:190-195,272-338). */
+int mm_local_grad(mm_problem* h, const double* v, double* out);
+
+/* Diagonal of the exchange operator / V_mag (src/energy_kernels.py:492-566). */
+int mm_exchange_diagonal(mm_problem* h, double* d);
+
+/* Demag right-hand side b = D m (src/poisson_solve.py:173-186,254-280) and b.b. */
+int mm_rhs(mm_problem* h, const double* m, double* b, double* bnorm2);
+
+/* Poisson operator y = A U (src/poisson_solve.py:166-171,210-252). */
+int mm_apply_A(mm_problem* h, const double* U, double* y);
+
+/* One preconditioner application z = M^-1 r (src/amg_utils.py:491-623). */
+int mm_precond(mm_problem* h, const double* r, double* z);
+
+/* Demag solve: b = D m, PCG from U_inout to relative residual tol (recursive residual, as
+ * src/poisson_solve.py:422-478), U_inout <- U.  rel_res = sqrt(r.r / b.b).
+ * Returns MM_MAXITER when maxiter was reached first.
+ * Replaces solve_U (src/poisson_solve.py:748-771) and the C++ solve_poisson
+ * (src/cpp/cpp_mkl_minimizer.cpp:208-231). */
+int mm_solve_u(mm_problem* h, const double* m, double* U_inout, double tol, int maxiter, int* iters,
+               double* rel_res);
+int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U_inout, double tol, int maxiter,
+                   int* iters, double* rel_res);
+
+/* Override the node weights of the minimizers (default: inv_M_rel = V_mag / M_nodal where
+ * M_nodal > 1e-20 else 0; inv_M_prec = 1/d where d > 1e-20 else 1, d the exchange diagonal,
+ * src/hysteresis_loop.py:340-353).  Either pointer may be NULL to keep the default. */
+int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec);
+
+/* Minimize the energy for one applied field, m_inout and U_inout updated in place.
+ * Replaces make_minimizer(...).minimize (src/minimizers.py:2927-4098) for pcohen_hs, lbfgs and
+ * wg_np, and run_cpp_pcohen_hs_minimization (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
+int mm_minimize(mm_problem* h, const double* B_ext, double* m_inout, double* U_inout,
+                const mm_min_params* prm, mm_min_info* info);
+
+/* Time one hot kernel in isolation: `reps` launches on the problem's stream, each preceded by a
+ * write of a buffer larger than L2 (so every launch streams its operands from HBM), timed with CUDA
+ * events around the launch.  Returns the mean launch time and the algorithmic bytes per launch
+ * (every array counted once at its stored width).  kernel: MM_KERNEL_*. */
+#define MM_KERNEL_SPMV_A 0   /* level-0 product y = A x                                   */
+#define MM_KERNEL_SMOOTH 1   /* level-0 SPAI0 smoothing x' = x + s .* (b - A x)           */
+#define MM_KERNEL_ENERGY 2   /* energy + gradient over the magnetic rows                  */
+#define MM_KERNEL_HESSIAN 3  /* local Hessian action over the magnetic rows               */
+int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, double* bytes_per_launch);
+
+/* Device time of the last demag solve (mm_solve_u / mm_solve_u_dev), measured with CUDA events
+ * recorded on the problem's stream around all of its kernels (host<->device copies excluded). */
+int mm_last_solve_ms(mm_problem* h, double* ms);
+/* Number of kernels this problem has launched since it was created. */
+int mm_launch_count(mm_problem* h, int64_t* count);
+
+/* Wait for the problem's stream. */
+int mm_sync(mm_problem* h);
+const char* mm_status_str(int status);
+const char* mm_last_error(mm_problem* h);
+/* Library version string. */
+const char* mm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MUMAG_CUDA_H */

@@ -1,0 +1,1513 @@
+// C-ABI of libmumag_cuda.so: problem handle, device buffers, Poisson PCG with the SA-AMG
+// V-cycle, energy operators and the minimizers, all orchestrated on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mumag_cuda.h"
+#include "mm_kernels.cuh"
+#include "mm_setup.h"
+
+using mmk::BS;
+using mmk::MAXG;
+
+namespace {
+
+struct Fail {
+  int code;
+  std::string msg;
+};
+
+#define CK(x)                                                                                         \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess)                                                                            \
+      throw Fail{e_ == cudaErrorMemoryAllocation ? MM_ERR_OOM : MM_ERR_CUDA,                          \
+                 std::string(#x) + ": " + cudaGetErrorString(e_) + " (" + __FILE__ + ":" +           \
+                     std::to_string(__LINE__) + ")"};                                                 \
+  } while (0)
+
+#define LAUNCH_CHECK()      \
+  do {                      \
+    ++h->n_launch;          \
+    CK(cudaGetLastError()); \
+  } while (0)
+
+inline int grid_elem(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + BS - 1) / BS, MAXG)); }
+inline int grid_rows(int64_t n, int tpr) {
+  const int rpb = BS / tpr;
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + rpb - 1) / rpb, MAXG));
+}
+
+int pick_tpr(int64_t nnz, int64_t rows) {
+  const double avg = rows > 0 ? (double)nnz / (double)rows : 1.0;
+  if (avg <= 3.0) return 2;
+  if (avg <= 10.0) return 4;
+  if (avg <= 24.0) return 8;
+  if (avg <= 48.0) return 16;
+  return 32;
+}
+
+struct DevMat {
+  int n_rows = 0, n_cols = 0;
+  int64_t nnz = 0;
+  int* ptr = nullptr;
+  int* col = nullptr;
+  double* val = nullptr;
+  int tpr = 4;
+};
+
+struct DevLevel {
+  DevMat A, P, R;
+  double* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
+  double* b = nullptr;    // right-hand side of this level (levels >= 1)
+  double* x = nullptr;    // iterate (pre-smoothing, prolongation)
+  double* x2 = nullptr;   // post-smoothed iterate (levels >= 1)
+  double* res = nullptr;  // residual
+  int n = 0;
+};
+
+thread_local std::string g_create_error;
+
+enum Slot { SL_BB0, SL_BB, SL_R2, SL_RZ, SL_PAP, SL_SUM, SL_E, SL_MAX, SL_A, SL_B, SL_C, SL_D, NSLOTS };
+
+}  // namespace
+
+struct mm_problem {
+  int N = 0, E = 0, n_mat = 0;
+  double V_mag = 1.0, inv_Vmag = 1.0;
+  cudaStream_t st = nullptr;
+  std::vector<void*> allocs;
+  std::string err;
+  int64_t n_launch = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_solve_ms = 0.0;
+
+  // host copies used by the setup
+  std::vector<int> conn, mat_id;
+  std::vector<double> volume, grad_phi, mask_h;
+  bool has_mask = false;
+
+  // energy operator
+  mm::EnergyOp eop_h;
+  mmk::EnergyDev eop{};
+  int eop_tpr = 8;
+  double* d_Mn = nullptr;
+  double* d_inv_M_rel = nullptr;
+  double* d_inv_M_prec = nullptr;
+  double* d_diag_ex = nullptr;
+
+  // Poisson
+  bool poisson_built = false;
+  int precond = MM_PRECOND_AMGCL;
+  double reg = 1e-12;
+  std::vector<mm::AmgLevel> amg_h;
+  std::vector<DevLevel> lv;
+  double* d_Ainv = nullptr;
+  int n_coarse = 0;
+  double* d_jac = nullptr;  // Jacobi preconditioner 1/(diag+eps)
+  double *d_b = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_Ap = nullptr;
+  double* d_part = nullptr;
+  mmk::Scalars* d_sc = nullptr;
+  mmk::Scalars* h_sc = nullptr;  // pinned
+  double* h_part = nullptr;      // pinned, MAXG * 2
+
+  // staging buffers for host-pointer calls
+  double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
+
+  // minimizer workspace (allocated on first use)
+  bool min_ready = false;
+  double *w_gt = nullptr, *w_gte = nullptr, *w_gprev = nullptr, *w_y = nullptr, *w_d = nullptr,
+         *w_dprev = nullptr, *w_H = nullptr, *w_mt = nullptr, *w_Ut = nullptr, *w_gt_trial = nullptr,
+         *w_graw = nullptr, *w_r3 = nullptr, *w_z3 = nullptr, *w_p3 = nullptr, *w_Ap3 = nullptr,
+         *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr;
+  std::vector<double*> w_S, w_Y;
+
+  double* part(Slot s) const { return d_part + (size_t)s * MAXG; }
+
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc(&p, n * sizeof(T)));
+    allocs.push_back(p);
+    return (T*)p;
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    T* p = alloc<T>(v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return p;
+  }
+  DevMat upload(const mm::HostCSR& A) {
+    DevMat d;
+    d.n_rows = A.n_rows;
+    d.n_cols = A.n_cols;
+    d.nnz = A.nnz();
+    d.ptr = upload(A.ptr);
+    d.col = upload(A.col);
+    d.val = upload(A.val);
+    d.tpr = pick_tpr(d.nnz, d.n_rows);
+    return d;
+  }
+  void sync() { CK(cudaStreamSynchronize(st)); }
+};
+
+// =============================================================================================
+// launch helpers
+// =============================================================================================
+namespace {
+
+#define TPR_SWITCH(tpr, ...)                         \
+  switch (tpr) {                                     \
+    case 2: { constexpr int T = 2; __VA_ARGS__; } break;   \
+    case 4: { constexpr int T = 4; __VA_ARGS__; } break;   \
+    case 8: { constexpr int T = 8; __VA_ARGS__; } break;   \
+    case 16: { constexpr int T = 16; __VA_ARGS__; } break; \
+    default: { constexpr int T = 32; __VA_ARGS__; } break; \
+  }
+
+template <int MODE>
+void spmv(mm_problem* h, const DevMat& A, const double* x, const double* b, const double* s, double* y,
+          const int* done) {
+  const int g = grid_rows(A.n_rows, A.tpr);
+  TPR_SWITCH(A.tpr, (mmk::k_spmv<T, MODE><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, x, b, s, y, done)));
+  LAUNCH_CHECK();
+}
+
+double host_sum(mm_problem* h, Slot s, int count) {
+  CK(cudaMemcpyAsync(h->h_part, h->part(s), count * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  h->sync();
+  double v = 0.0;
+  for (int i = 0; i < count; ++i) v += h->h_part[i];
+  return v;
+}
+
+double host_max(mm_problem* h, Slot s, int count) {
+  CK(cudaMemcpyAsync(h->h_part, h->part(s), count * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  h->sync();
+  double v = 0.0;
+  for (int i = 0; i < count; ++i) v = std::max(v, h->h_part[i]);
+  return v;
+}
+
+
+}  // namespace
+
+namespace mmk {
+__global__ void __launch_bounds__(BS) k_mul(int n, const double* __restrict__ s, const double* __restrict__ r,
+                                            double* __restrict__ out) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = s[i] * r[i];
+}
+
+// r = b - A x ; partial r.r ; xv = s .* r
+template <int TPR>
+__global__ void __launch_bounds__(BS) k_init_residual(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                                      const double* __restrict__ val, const double* __restrict__ x,
+                                                      const double* __restrict__ b, double* __restrict__ r,
+                                                      const double* __restrict__ s, double* __restrict__ xv,
+                                                      double* __restrict__ part) {
+  constexpr int RPB = BS / TPR;
+  const int lane = threadIdx.x % TPR;
+  double d = 0.0;
+  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
+    const int row = rb + threadIdx.x / TPR;
+    const bool valid = row < n;
+    const double ax = row_dot<TPR>(ptr, col, val, x, row, valid, lane);
+    if (valid && lane == 0) {
+      const double ri = b[row] - ax;
+      r[row] = ri;
+      d = fma(ri, ri, d);
+      if (s) xv[row] = s[row] * ri;
+    }
+  }
+  d = block_sum(d);
+  if (threadIdx.x == 0) part[blockIdx.x] = d;
+}
+
+__global__ void k_finalize_solve(Scalars* sc, const double* __restrict__ part_r2, int n_r2,
+                                 const double* __restrict__ part_bb0, int n_bb0, double* out2) {
+  const double r2 = reduce_partials(part_r2, n_r2);
+  const double bb = reduce_partials(part_bb0, n_bb0);
+  if (threadIdx.x == 0) {
+    out2[0] = r2;
+    out2[1] = bb;
+  }
+}
+
+// partials of a.(b - c) and d.(b - c)
+__global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict__ a, const double* __restrict__ d,
+                                                 const double* __restrict__ b, const double* __restrict__ c,
+                                                 double* __restrict__ pa, double* __restrict__ pd) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    const double df = b[i] - c[i];
+    s1 = fma(a[i], df, s1);
+    s2 = fma(d[i], df, s2);
+  }
+  s1 = block_sum(s1);
+  s2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    pa[blockIdx.x] = s1;
+    pd[blockIdx.x] = s2;
+  }
+}
+
+// y = P_m(y) for every history vector (L-BFGS transport) is k_tangent in place
+}  // namespace mmk
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// V-cycle (enqueue only).  Level 0's pre-smoothed iterate lv[0].x must already hold s0 .* r.
+// in_loop: the level-0 residual kernel also performs the PCG convergence test.
+// ---------------------------------------------------------------------------------------------
+void enqueue_vcycle(mm_problem* h, const double* r, double* z, bool in_loop, const int* done) {
+  auto& lv = h->lv;
+  const int L = (int)lv.size();
+  if (L == 1) {
+    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, done);
+    LAUNCH_CHECK();
+    mmk::k_dot<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, r, z, h->part(SL_RZ));
+    LAUNCH_CHECK();
+    return;
+  }
+  // descend
+  for (int l = 0; l < L - 1; ++l) {
+    DevLevel& c = lv[l];
+    if (l == 0) {
+      if (in_loop) {
+        const int g = grid_rows(c.A.n_rows, c.A.tpr);
+        TPR_SWITCH(c.A.tpr, (mmk::k_vc_residual0<T><<<g, BS, 0, h->st>>>(
+                                c.A.n_rows, c.A.ptr, c.A.col, c.A.val, c.x, r, c.res, h->part(SL_R2),
+                                grid_elem(h->N), h->d_sc)));
+        LAUNCH_CHECK();
+      } else {
+        spmv<1>(h, c.A, c.x, r, nullptr, c.res, done);
+      }
+    } else {
+      spmv<1>(h, c.A, c.x, c.b, nullptr, c.res, done);
+    }
+    DevLevel& nx = lv[l + 1];
+    const bool coarsest = (l + 1 == L - 1);
+    const int g = grid_rows(c.R.n_rows, c.R.tpr);
+    TPR_SWITCH(c.R.tpr, (mmk::k_restrict<T><<<g, BS, 0, h->st>>>(c.R.n_rows, c.R.ptr, c.R.col, c.R.val, c.res, nx.b,
+                                                                  coarsest ? nullptr : nx.s, nx.x, done)));
+    LAUNCH_CHECK();
+  }
+  // coarsest
+  {
+    DevLevel& c = lv[L - 1];
+    mmk::k_dense_mv<<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, h->d_Ainv, c.b, c.x2, done);
+    LAUNCH_CHECK();
+  }
+  // ascend
+  for (int l = L - 2; l >= 0; --l) {
+    DevLevel& c = lv[l];
+    const double* e = lv[l + 1].x2;
+    spmv<3>(h, c.P, e, c.x, nullptr, c.x, done);  // x += P e
+    const double* bl = (l == 0) ? r : c.b;
+    double* out = (l == 0) ? z : c.x2;
+    const int g = grid_rows(c.A.n_rows, c.A.tpr);
+    TPR_SWITCH(c.A.tpr, (mmk::k_smooth_dot<T><<<g, BS, 0, h->st>>>(c.A.n_rows, c.A.ptr, c.A.col, c.A.val, c.x, bl, c.s,
+                                                                    out, l == 0 ? h->part(SL_RZ) : nullptr, done)));
+    LAUNCH_CHECK();
+  }
+}
+
+// number of r.z partials written by the preconditioner (k_smooth_dot on level 0, else k_dot)
+int rz_count(mm_problem* h) {
+  const bool amg = h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL;
+  if (amg && h->lv.size() > 1) return grid_rows(h->lv[0].A.n_rows, h->lv[0].A.tpr);
+  return grid_elem(h->N);
+}
+
+// preconditioner application z = M^-1 r outside the PCG loop; writes the r.z partials to SL_RZ
+void enqueue_precond(mm_problem* h, const double* r, double* z) {
+  const int N = h->N;
+  if (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) {
+    if (h->lv.size() > 1) {
+      mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->lv[0].s, r, h->lv[0].x);
+      LAUNCH_CHECK();
+    }
+    enqueue_vcycle(h, r, z, false, nullptr);
+  } else {
+    if (h->precond == MM_PRECOND_JACOBI) {
+      mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_jac, r, z);
+    } else {
+      CK(cudaMemcpyAsync(z, r, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    }
+    LAUNCH_CHECK();
+    mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, r, z, h->part(SL_RZ));
+    LAUNCH_CHECK();
+  }
+}
+
+// z = M^-1 r for Jacobi / no preconditioner / a one-level hierarchy (dense solve); r.z partials in SL_RZ
+void apply_M_simple(mm_problem* h, const double* r, double* z) {
+  const int N = h->N;
+  if (h->precond == MM_PRECOND_JACOBI) {
+    mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_jac, r, z);
+  } else if (h->precond == MM_PRECOND_NONE) {
+    CK(cudaMemcpyAsync(z, r, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  } else {
+    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, nullptr);
+  }
+  LAUNCH_CHECK();
+  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, r, z, h->part(SL_RZ));
+  LAUNCH_CHECK();
+}
+
+// one PCG iteration for the non-AMG preconditioners (host-free scalars as in the AMG path)
+void enqueue_simple_iteration(mm_problem* h, double* x, bool first) {
+  const int N = h->N;
+  const DevMat& A = h->lv[0].A;
+  const int g = grid_rows(A.n_rows, A.tpr);
+  TPR_SWITCH(A.tpr, (mmk::k_pcg_dir<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_z, h->d_p, h->d_Ap,
+                                                             h->part(SL_RZ), grid_elem(N), h->part(SL_R2),
+                                                             grid_elem(N), h->part(SL_PAP), h->d_sc, first)));
+  LAUNCH_CHECK();
+  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_r, h->d_p, h->d_Ap, nullptr, nullptr, h->part(SL_PAP),
+                                                   g, h->part(SL_RZ), grid_elem(N), h->part(SL_R2), h->d_sc);
+  LAUNCH_CHECK();
+  // z = M^-1 r; the following k_pcg_dir re-tests convergence before it uses z
+  apply_M_simple(h, h->d_r, h->d_z);
+}
+
+void enqueue_amg_iteration(mm_problem* h, double* x, bool first) {
+  const int N = h->N;
+  DevLevel& l0 = h->lv[0];
+  const DevMat& A = l0.A;
+  const int g = grid_rows(A.n_rows, A.tpr);
+  const int n_rz = rz_count(h);
+  TPR_SWITCH(A.tpr, (mmk::k_pcg_dir<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_z, h->d_p, h->d_Ap,
+                                                             h->part(SL_RZ), n_rz, h->part(SL_R2), grid_elem(N),
+                                                             h->part(SL_PAP), h->d_sc, first)));
+  LAUNCH_CHECK();
+  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_r, h->d_p, h->d_Ap, h->lv.size() > 1 ? l0.s : nullptr,
+                                                   l0.x, h->part(SL_PAP), g, h->part(SL_RZ), n_rz, h->part(SL_R2),
+                                                   h->d_sc);
+  LAUNCH_CHECK();
+  enqueue_vcycle(h, h->d_r, h->d_z, true, &h->d_sc->done);
+}
+
+// PCG on device buffers: b already in h->d_b with raw b.b partials in SL_BB0.
+int run_pcg(mm_problem* h, double* x, double tol, int maxiter, int* iters, double* rel_res) {
+  const int N = h->N;
+  const bool zero_mean = !h->has_mask;
+  const bool amg = (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL);
+  if (zero_mean) {
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->part(SL_SUM));
+    LAUNCH_CHECK();
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->part(SL_SUM), grid_elem(N));
+    LAUNCH_CHECK();
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM));
+    LAUNCH_CHECK();
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM), grid_elem(N));
+    LAUNCH_CHECK();
+  }
+  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, nullptr, h->part(SL_BB));
+  LAUNCH_CHECK();
+  mmk::k_pcg_init_scalars<<<1, BS, 0, h->st>>>(h->d_sc, h->part(SL_BB), grid_elem(N), tol, maxiter);
+  LAUNCH_CHECK();
+  // r = b - A x, r.r, level-0 pre-smoothing; z = M^-1 r
+  const DevMat& A = h->lv[0].A;
+  {
+    const int g = grid_rows(A.n_rows, A.tpr);
+    const bool presmooth = amg && h->lv.size() > 1;
+    // the r.r partials must be laid out like k_pcg_step's (grid_elem(N) blocks): reduce via k_dot
+    TPR_SWITCH(A.tpr, (mmk::k_init_residual<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, x, h->d_b, h->d_r,
+                                                                      presmooth ? h->lv[0].s : nullptr, h->lv[0].x,
+                                                                      h->part(SL_A))));
+    LAUNCH_CHECK();
+    mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_r, nullptr, h->part(SL_R2));
+    LAUNCH_CHECK();
+  }
+  if (amg && h->lv.size() > 1) enqueue_vcycle(h, h->d_r, h->d_z, false, nullptr);
+  else apply_M_simple(h, h->d_r, h->d_z);
+  int it_block = 4;
+  for (int i = 0;; ++i) {
+    if (amg && h->lv.size() > 1) {
+      enqueue_amg_iteration(h, x, i == 0);
+    } else {
+      enqueue_simple_iteration(h, x, i == 0);
+    }
+    if ((i + 1) % it_block == 0 || i == 0) {
+      CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+      h->sync();
+      if (h->h_sc->done) break;
+      if (i > maxiter + 8) break;
+    }
+  }
+  if (zero_mean) {
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM));
+    LAUNCH_CHECK();
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM), grid_elem(N));
+    LAUNCH_CHECK();
+  }
+  double* d_out2 = h->part(SL_D);
+  mmk::k_finalize_solve<<<1, BS, 0, h->st>>>(h->d_sc, h->part(SL_R2), grid_elem(N), h->part(SL_BB0), grid_elem(h->N),
+                                              d_out2);
+  LAUNCH_CHECK();
+  double out2[2];
+  CK(cudaMemcpyAsync(out2, d_out2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+  h->sync();
+  if (iters) *iters = h->h_sc->it;
+  const double rr = std::sqrt(out2[0] / (out2[1] + 1e-30));
+  if (rel_res) *rel_res = rr;
+  if (!std::isfinite(rr)) return MM_NONFINITE;
+  return (h->h_sc->it >= maxiter && out2[0] > h->h_sc->tol2) ? MM_MAXITER : MM_OK;
+}
+
+// b = D m on device (magnetic rows), raw b.b partials in SL_BB0
+void enqueue_rhs(mm_problem* h, const double* m) {
+  const int N = h->N;
+  if (!h->has_mask) CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
+  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
+  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<T><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b, nullptr)));
+  LAUNCH_CHECK();
+  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, nullptr, h->part(SL_BB0));
+  LAUNCH_CHECK();
+}
+
+int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters, double* rel_res) {
+  if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called before a solve"};
+  CK(cudaEventRecord(h->ev0, h->st));
+  enqueue_rhs(h, d_m);
+  const int rc = run_pcg(h, d_U, tol, maxiter, iters, rel_res);
+  CK(cudaEventRecord(h->ev1, h->st));
+  CK(cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->last_solve_ms = ms;
+  return rc;
+}
+
+double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
+                  double* d_g) {
+  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
+  TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
+                                                                      d_bias, h->inv_Vmag, d_g, h->part(SL_E))));
+  LAUNCH_CHECK();
+  return 0.5 * host_sum(h, SL_E, g) * h->inv_Vmag;
+}
+
+void local_grad_dev(mm_problem* h, const double* d_v, double* d_out) {
+  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
+  TPR_SWITCH(h->eop_tpr, (mmk::k_local_grad<T><<<g, BS, 0, h->st>>>(h->eop, d_v, h->inv_Vmag, d_out)));
+  LAUNCH_CHECK();
+}
+
+template <class F>
+int guarded(mm_problem* h, F&& f) {
+  try {
+    return f();
+  } catch (const Fail& e) {
+    if (h) h->err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (h) h->err = "host allocation failed";
+    return MM_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (h) h->err = e.what();
+    return MM_ERR_SETUP;
+  }
+}
+
+}  // namespace
+
+// =============================================================================================
+// minimizer (host-driven control flow on device vectors, as src/minimizers.py's step functions)
+// =============================================================================================
+namespace {
+
+struct MinCtx {
+  mm_problem* h;
+  int N;
+  double B[3];
+  double phi_tol;
+  const mm_min_params* prm;
+  int demag = 0, evals = 0, preco = 0;
+};
+
+void ensure_min_buffers(mm_problem* h, int memory) {
+  const size_t n3 = 3 * (size_t)h->N;
+  if (!h->min_ready) {
+    double** bufs[] = {&h->w_gt, &h->w_gte, &h->w_gprev, &h->w_y, &h->w_d, &h->w_dprev, &h->w_H, &h->w_mt,
+                       &h->w_gt_trial, &h->w_graw, &h->w_r3, &h->w_z3, &h->w_p3, &h->w_Ap3, &h->w_tmp,
+                       &h->w_mprev, &h->w_gtprev};
+    for (double** b : bufs) {
+      *b = h->alloc<double>(n3);
+      CK(cudaMemsetAsync(*b, 0, n3 * sizeof(double), h->st));
+    }
+    h->w_Ut = h->alloc<double>(h->N);
+    h->min_ready = true;
+  }
+  while ((int)h->w_S.size() < memory) {
+    double* s = h->alloc<double>(n3);
+    double* y = h->alloc<double>(n3);
+    CK(cudaMemsetAsync(s, 0, n3 * sizeof(double), h->st));
+    CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
+    h->w_S.push_back(s);
+    h->w_Y.push_back(y);
+  }
+}
+
+double dev_dot(mm_problem* h, int n, const double* a, const double* b) {
+  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, a, b, h->part(SL_A));
+  LAUNCH_CHECK();
+  return host_sum(h, SL_A, grid_elem(n));
+}
+
+double dev_absmax(mm_problem* h, int n, const double* a) {
+  mmk::k_absmax<<<grid_elem(n), BS, 0, h->st>>>(n, a, h->part(SL_MAX));
+  LAUNCH_CHECK();
+  return host_max(h, SL_MAX, grid_elem(n));
+}
+
+// energy + gradient of (m, U) into g, E returned
+double eval(MinCtx& c, const double* m, const double* U, double* g) {
+  return energy_dev(c.h, m, U, c.B, c.h->d_bias, g);
+}
+
+// solve_U(m, U (warm start, in place), tol) -> iterations
+int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
+  int it = 0;
+  double rr = 0.0;
+  const int cg_maxiter = c.prm->cg_maxiter > 0 ? c.prm->cg_maxiter : 2000;
+  solve_dev(c.h, m, U, tol, cg_maxiter, &it, &rr);
+  return it;
+}
+
+// Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations
+int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y) {
+  mm_problem* h = c.h;
+  const int N = c.N, n3 = 3 * N;
+  const int ge = grid_elem(N);
+  CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
+  CK(cudaMemcpyAsync(h->w_r3, gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->part(SL_B));
+  LAUNCH_CHECK();
+  CK(cudaMemcpyAsync(h->w_p3, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  double rho = host_sum(h, SL_B, ge);
+  const double target = tol * tol * rho;
+  double Q = 0.0;
+  int it = 0;
+  bool done = false;
+  const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
+  while (it < c.prm->pc_iters && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
+    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<T><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, c.prm->pc_reg,
+                                                                     h->inv_Vmag, h->w_Ap3, h->part(SL_C))));
+    LAUNCH_CHECK();
+    const double pAp = host_sum(h, SL_C, gP);
+    const bool neg = pAp <= 0.0;
+    const double alpha = rho / (pAp + 1e-30);
+    const double dq = 0.5 * alpha * rho;
+    const bool stag = (it > 0) && (dq <= c.prm->pc_stagnation_nu * Q);
+    done = neg || stag;
+    mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, alpha, y, h->w_r3, h->w_p3, h->w_Ap3, h->d_inv_M_prec, h->w_z3,
+                                             h->part(SL_B), done ? 0 : 1);
+    LAUNCH_CHECK();
+    const double rho_next = host_sum(h, SL_B, ge);
+    if (!done) {
+      mmk::k_xpay<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
+      LAUNCH_CHECK();
+    }
+    rho = rho_next;
+    Q = Q + dq;
+    ++it;
+  }
+  // fallback direction, clipping, descent check
+  // z_fb = gte .* inv_M_prec  (into w_z3)
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_z3, h->part(SL_B));
+  LAUNCH_CHECK();
+  const double yn = std::sqrt(dev_dot(h, n3, y, nullptr));
+  const double zn = std::sqrt(dev_dot(h, n3, h->w_z3, nullptr));
+  if (yn > 10.0 * zn) {
+    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, 10.0 * zn / (yn + 1e-30), y);
+    LAUNCH_CHECK();
+  }
+  if (!(dev_dot(h, n3, y, gte) > 1e-12)) {
+    CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  }
+  return it;
+}
+
+struct LSResult {
+  double tau, E;
+  int evals, demag;
+  bool accepted;
+};
+
+// Curvilinear Armijo search (src/minimizers.py:265-385).  On acceptance the trial state is in
+// (w_mt, w_Ut, w_gt_trial); otherwise the caller keeps (m, U, g_raw).
+LSResult armijo(MinCtx& c, const double* m, double pg, const double* H, double E0, const double* U_base, double s0) {
+  mm_problem* h = c.h;
+  const int N = c.N;
+  const mm_min_params* p = c.prm;
+  LSResult res{0.0, E0, 0, 0, false};
+  if (pg >= 0) return res;
+  CK(cudaMemcpyAsync(h->w_Ut, U_base, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  auto D = [&](double s, double& E_t) {
+    mmk::k_cayley<<<grid_elem(N), BS, 0, h->st>>>(N, m, H, s, h->w_mt);
+    LAUNCH_CHECK();
+    res.demag += demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
+    E_t = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
+    if (!std::isfinite(E_t)) E_t = 1e20;
+    return (E_t - E0) / (s * pg + 1e-30);
+  };
+  const int max_evals = p->ls_max_evals > 0 ? p->ls_max_evals : 15;
+  double s = s0, s_min = 0.0, d_v = 0.0, E_v = E0;
+  int it_exp = 0, it_con = 0;
+  bool done = false;
+  while (it_exp < max_evals && !done) {
+    double E_t;
+    const double d = D(s, E_t);
+    d_v = d;
+    E_v = E_t;
+    const bool stop = (std::fabs(1.0 - d) >= p->ls_eta2) || (d < 0);
+    if (!stop) {
+      s_min = s;
+      s = p->ls_C * s;
+    }
+    ++it_exp;
+    done = stop;
+  }
+  done = (d_v >= p->ls_eta1) && (d_v < 1e10);
+  while (it_con < max_evals && !done) {
+    s = s_min + p->ls_c * (s - s_min);
+    double E_t;
+    const double d = D(s, E_t);
+    d_v = d;
+    E_v = E_t;
+    done = (d >= p->ls_eta1) && (d < 1e10);
+    ++it_con;
+  }
+  res.evals = it_exp + it_con;
+  if (d_v >= 0) {
+    res.tau = s;
+    res.E = E_v;
+    res.accepted = true;
+  }
+  return res;
+}
+
+bool check_conv(int it, double E, double E_prev, double diff_m, double gnorm, const mm_min_params* p) {
+  if (it <= 0) return false;
+  const bool u1 = (E_prev - E) < p->tau_f * (1.0 + std::fabs(E));
+  const bool u2 = diff_m < std::sqrt(p->tau_f) * 2.0;
+  const bool u3 = gnorm <= std::pow(p->tau_f, 1.0 / 3.0) * (1.0 + std::fabs(E));
+  const bool u4 = gnorm < p->eps_a;
+  return (u1 && u2 && u3) || u4;
+}
+
+// accept the line-search trial: m <- w_mt, U <- w_Ut, g_raw <- w_gt_trial (buffer swaps)
+void accept_trial(mm_problem* h, double*& m, double*& U, double*& graw) {
+  std::swap(m, h->w_mt);
+  std::swap(U, h->w_Ut);
+  std::swap(graw, h->w_gt_trial);
+}
+
+int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const mm_min_params* prm,
+                 mm_min_info* info) {
+  const int N = h->N, n3 = 3 * N;
+  const int ge = grid_elem(N);
+  ensure_min_buffers(h, prm->method == MM_METHOD_LBFGS ? std::max(1, prm->memory) : 0);
+  MinCtx c{h, N, {B[0], B[1], B[2]}, prm->phi_tol > 0 ? prm->phi_tol : std::min(prm->cg_tol, 0.1 * prm->tau_f), prm};
+  auto t0 = std::chrono::steady_clock::now();
+  double* graw = h->w_graw;
+  mmk::k_normalize<<<ge, BS, 0, h->st>>>(N, m);
+  LAUNCH_CHECK();
+  c.demag += demag_solve(c, m, U, prm->cg_tol);
+  double E = eval(c, m, U, graw);
+  mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->part(SL_MAX));
+  LAUNCH_CHECK();
+  double gnorm = host_max(h, SL_MAX, ge);
+  c.evals = 1;
+  // state: g (previous g_tan_ext or g_tan), y, d
+  CK(cudaMemcpyAsync(h->w_gprev, prm->method == MM_METHOD_PCOHEN_HS ? h->w_gte : h->w_gt, n3 * sizeof(double),
+                     cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemcpyAsync(h->w_dprev, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_dprev);
+  LAUNCH_CHECK();
+  CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  const int L = prm->L > 0 ? prm->L : N;
+  const int mem = std::max(1, prm->memory);
+  std::vector<double> rho_h(mem, 0.0);
+  int hist_it = 0;
+  int it = 0;
+  bool conv = false;
+  while (!conv && it < prm->max_iter) {
+    const double E_prev = E;
+    mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->part(SL_MAX));
+    LAUNCH_CHECK();
+    const double gnorm_inf = host_max(h, SL_MAX, ge);
+    double conv_gnorm = gnorm_inf;
+    double pg = 0.0, s0 = 1.0;
+    double* H = h->w_H;
+    if (prm->method == MM_METHOD_PCOHEN_HS) {
+      const double pc_tol = prm->pc_auto ? std::min(prm->pc_force_eta, std::pow(gnorm_inf, prm->pc_force_alpha)) : 0.0;
+      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol, h->w_y);
+      const double gsm = dev_absmax(h, n3, h->w_y);
+      // HS beta
+      mmk::k_dot2diff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->part(SL_A),
+                                                       h->part(SL_B));
+      LAUNCH_CHECK();
+      const double num = host_sum(h, SL_A, grid_elem(n3));
+      const double den = host_sum(h, SL_B, grid_elem(n3)) + 1e-30;
+      const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
+      mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_dprev, beta, h->w_gte, graw, h->w_d, h->part(SL_A),
+                                              h->part(SL_B));
+      LAUNCH_CHECK();
+      const double dg = host_sum(h, SL_A, ge);
+      pg = host_sum(h, SL_B, ge);
+      if (dg > 0) {
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_y, 0.0, h->w_d);
+        LAUNCH_CHECK();
+        pg = dev_dot(h, n3, graw, h->w_d);
+      }
+      conv_gnorm = gsm;
+      gnorm = gsm;
+    } else if (prm->method == MM_METHOD_LBFGS) {
+      // two-loop recursion on g_tan_ext (src/minimizers.py:1284-1312)
+      const int n_hist = std::min(hist_it, mem);
+      std::vector<double> alphas(mem, 0.0);
+      double* q = h->w_y;
+      CK(cudaMemcpyAsync(q, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+      for (int i = 0; i < n_hist; ++i) {
+        const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
+        const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
+        LAUNCH_CHECK();
+        alphas[idx] = a;
+      }
+      const int last = ((hist_it - 1) % mem + mem) % mem;
+      double gamma = 1.0;
+      if (hist_it > 0) {
+        // y_last . (y_last .* inv_M_rel)
+        mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->part(SL_B));
+        LAUNCH_CHECK();
+        const double yMy = host_sum(h, SL_B, ge);
+        gamma = dev_dot(h, n3, h->w_S[last], h->w_Y[last]) / (yMy + 1e-30);
+      }
+      gamma = std::min(std::max(gamma, 1e-3), 1e3);
+      // r = gamma q .* inv_M_rel
+      mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, h->w_d, h->part(SL_B));
+      LAUNCH_CHECK();
+      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, gamma, h->w_d);
+      LAUNCH_CHECK();
+      for (int i = 0; i < n_hist; ++i) {
+        const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
+        const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], h->w_d);
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, h->w_d);
+        LAUNCH_CHECK();
+      }
+      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_d);
+      LAUNCH_CHECK();
+      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) {
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gt, 0.0, h->w_d);
+        LAUNCH_CHECK();
+      }
+      pg = dev_dot(h, n3, graw, h->w_d);
+      s0 = (it == 0) ? prm->tau0 : 1.0;
+      gnorm = gnorm_inf;
+    } else {  // wg_np: Barzilai-Borwein (src/minimizers.py:1715-1798)
+      // s = m - m_prev ; y = g_tan - g_tan_prev
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, m, 0.0, h->w_tmp);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_mprev, 1.0, h->w_tmp);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, h->w_gt, 0.0, h->w_y);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gtprev, 1.0, h->w_y);
+      LAUNCH_CHECK();
+      const double sty = dev_dot(h, n3, h->w_tmp, h->w_y);
+      const double sts = dev_dot(h, n3, h->w_tmp, nullptr);
+      const double yty = dev_dot(h, n3, h->w_y, nullptr);
+      const double tau1 = sts / (sty + 1e-30), tau2 = sty / (yty + 1e-30);
+      double tau_bb = (it % 2 != 0) ? tau1 : tau2;
+      tau_bb = std::min(std::max(std::fabs(tau_bb), 1e-6), 1e3);
+      // d = -g_tan so that H = m x d = -(m x z) and pg = g_raw . d
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gt, 0.0, h->w_d);
+      LAUNCH_CHECK();
+      pg = dev_dot(h, n3, graw, h->w_d);
+      gnorm = gnorm_inf;
+      if (it >= prm->wg_gamma) {
+        mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_d, H);
+        LAUNCH_CHECK();
+        mmk::k_cayley<<<ge, BS, 0, h->st>>>(N, m, H, tau_bb, h->w_mt);
+        LAUNCH_CHECK();
+        CK(cudaMemcpyAsync(h->w_Ut, U, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        c.demag += demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
+        const double E_new = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
+        c.evals += 1;
+        mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->part(SL_MAX));
+        LAUNCH_CHECK();
+        const double dm = host_max(h, SL_MAX, grid_elem(n3));
+        conv = check_conv(it, E_new, E_prev, dm, gnorm_inf, prm);
+        CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        accept_trial(h, m, U, graw);
+        E = E_new;
+        ++it;
+        continue;
+      }
+    }
+    mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_d, H);
+    LAUNCH_CHECK();
+    LSResult ls = armijo(c, m, pg, H, E_prev, U, s0);
+    c.evals += ls.evals;
+    c.demag += ls.demag;
+    double dm = 0.0;
+    if (ls.accepted) {
+      mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->part(SL_MAX));
+      LAUNCH_CHECK();
+      dm = host_max(h, SL_MAX, grid_elem(n3));
+    }
+    const double E_new = ls.accepted ? ls.E : E_prev;
+    conv = check_conv(it, E_new, E_prev, dm, conv_gnorm, prm);
+    if (prm->method == MM_METHOD_PCOHEN_HS) {
+      // g_prev <- g_tan_ext, d_prev <- d  (y_prev is not needed by the HS beta)
+      std::swap(h->w_gprev, h->w_gte);
+      std::swap(h->w_dprev, h->w_d);
+      if (ls.accepted) accept_trial(h, m, U, graw);
+    } else if (prm->method == MM_METHOD_LBFGS) {
+      const double tau = ls.accepted ? ls.tau : 0.0;
+      double* m_new = ls.accepted ? h->w_mt : m;
+      double* g_new = ls.accepted ? h->w_gt_trial : graw;
+      // s_new = P(m_new, d tau), y_new = P(m_new, g_new) - P(m_new, g_tan_ext)
+      double* s_new = h->w_tmp;
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, tau, h->w_d, 0.0, s_new);
+      LAUNCH_CHECK();
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, s_new, s_new);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, g_new, 0.0, h->w_r3);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gte, 1.0, h->w_r3);
+      LAUNCH_CHECK();
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_r3, h->w_r3);
+      LAUNCH_CHECK();
+      const double curv = dev_dot(h, n3, h->w_r3, s_new);
+      const bool ok = curv > 1e-12 * dev_dot(h, n3, s_new, nullptr);
+      for (int i = 0; i < mem; ++i) {
+        mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_S[i], h->w_S[i]);
+        LAUNCH_CHECK();
+        mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_Y[i], h->w_Y[i]);
+        LAUNCH_CHECK();
+      }
+      LAUNCH_CHECK();
+      if (ok) {
+        const int idx = hist_it % mem;
+        CK(cudaMemcpyAsync(h->w_S[idx], s_new, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        CK(cudaMemcpyAsync(h->w_Y[idx], h->w_r3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        rho_h[idx] = 1.0 / (curv + 1e-30);
+        ++hist_it;
+      }
+      if (ls.accepted) accept_trial(h, m, U, graw);
+    } else {
+      CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+      CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+      if (ls.accepted) accept_trial(h, m, U, graw);
+    }
+    E = E_new;
+    ++it;
+  }
+  h->w_graw = graw;
+  h->sync();
+  auto t1 = std::chrono::steady_clock::now();
+  if (info) {
+    info->iters = it;
+    info->evals = c.evals;
+    info->preco_iters = c.preco;
+    info->demag_iters = c.demag;
+    info->E = E;
+    info->gnorm = gnorm;
+    info->seconds = std::chrono::duration<double>(t1 - t0).count();
+    info->status = (it >= prm->max_iter && !conv) ? MM_MAXITER : MM_OK;
+  }
+  return std::isfinite(E) ? MM_OK : MM_NONFINITE;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C-ABI
+// =============================================================================================
+extern "C" {
+
+const char* mm_version(void) { return "mumag_cuda 0.1 (sm_103a)"; }
+
+const char* mm_status_str(int s) {
+  switch (s) {
+    case MM_OK: return "ok";
+    case MM_MAXITER: return "iteration limit reached";
+    case MM_NONFINITE: return "non-finite value";
+    case MM_BREAKDOWN: return "breakdown";
+    case MM_ERR_ARG: return "invalid argument";
+    case MM_ERR_OOM: return "out of memory";
+    case MM_ERR_CUDA: return "CUDA error";
+    case MM_ERR_STATE: return "invalid call order";
+    case MM_ERR_SETUP: return "setup failed";
+    default: return "unknown status";
+  }
+}
+
+const char* mm_last_error(mm_problem* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int mm_geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn_out, double* volume,
+                    double* JinvT, double* grad_phi) {
+  if (N <= 0 || E <= 0 || !knt || !conn_in || !conn_out || !volume || !JinvT || !grad_phi) return MM_ERR_ARG;
+  return guarded(nullptr, [&] {
+    mm::geom_compute(N, E, knt, conn_in, conn_out, volume, JinvT, grad_phi);
+    return MM_OK;
+  });
+}
+
+int mm_boundary_mask(int N, int E, const int* conn, double* mask) {
+  if (N <= 0 || E <= 0 || !conn || !mask) return MM_ERR_ARG;
+  return guarded(nullptr, [&] {
+    mm::boundary_mask(N, E, conn, mask);
+    return MM_OK;
+  });
+}
+
+int mm_morton_order(int N, int E, const double* knt, const int* conn, int* node_perm, int* elem_perm) {
+  if (N <= 0 || E <= 0 || !knt || !conn || !node_perm || !elem_perm) return MM_ERR_ARG;
+  return guarded(nullptr, [&] {
+    mm::morton_order(N, E, knt, conn, node_perm, elem_perm);
+    return MM_OK;
+  });
+}
+
+struct mm_setup {
+  mm::EnergyOp eop;
+  std::vector<mm::AmgLevel> amg;
+};
+
+int mm_setup_create(int N, int E, const int* conn, const double* volume, const double* grad_phi, const int* mat_id,
+                    int n_mat, const double* A_lookup, const double* K1_lookup, const double* Js_lookup,
+                    const double* k_easy, const double* boundary_mask, double reg, int max_levels, int max_coarse,
+                    mm_setup** out) {
+  if (!out || N <= 0 || E <= 0 || n_mat <= 0 || !conn || !volume || !grad_phi || !mat_id || !A_lookup ||
+      !K1_lookup || !Js_lookup || !k_easy)
+    return MM_ERR_ARG;
+  *out = nullptr;
+  mm_setup* s = new mm_setup();
+  const int rc = guarded(nullptr, [&] {
+    for (int e = 0; e < 4 * E; ++e)
+      if (conn[e] < 0 || conn[e] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
+    s->eop = mm::assemble_energy(N, E, conn, volume, grad_phi, mat_id, n_mat, A_lookup, K1_lookup, Js_lookup, k_easy);
+    if (reg >= 0) {
+      mm::HostCSR A = mm::assemble_poisson(N, E, conn, volume, grad_phi, boundary_mask, reg);
+      mm::AmgParams prm;
+      prm.max_levels = max_levels > 0 ? max_levels : 10;
+      prm.max_coarse = max_coarse > 0 ? max_coarse : 1000;
+      s->amg = mm::build_amg(A, prm);
+    }
+    return MM_OK;
+  });
+  if (rc != MM_OK) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return MM_OK;
+}
+
+int mm_setup_destroy(mm_setup* s) {
+  if (!s) return MM_ERR_ARG;
+  delete s;
+  return MM_OK;
+}
+
+int mm_setup_energy_info(mm_setup* s, int* n_rows, int64_t* nnz, int* single_axis) {
+  if (!s) return MM_ERR_ARG;
+  if (n_rows) *n_rows = s->eop.n_rows;
+  if (nnz) *nnz = (int64_t)s->eop.col.size();
+  if (single_axis) *single_axis = s->eop.single_axis ? 1 : 0;
+  return MM_OK;
+}
+
+int mm_setup_energy_export(mm_setup* s, int* rows, int* ptr, int* col, int* mat, double* w, double* q, double* G,
+                           double* D, double* diag_exchange) {
+  if (!s) return MM_ERR_ARG;
+  const mm::EnergyOp& o = s->eop;
+  if (rows) std::copy(o.rows.begin(), o.rows.end(), rows);
+  if (ptr) std::copy(o.ptr.begin(), o.ptr.end(), ptr);
+  if (col) std::copy(o.col.begin(), o.col.end(), col);
+  if (mat) std::copy(o.mat.begin(), o.mat.end(), mat);
+  if (w) std::copy(o.w.begin(), o.w.end(), w);
+  if (q) std::copy(o.q.begin(), o.q.end(), q);
+  for (size_t k = 0; k < o.col.size(); ++k) {
+    if (G) {
+      G[3 * k] = o.gx[k];
+      G[3 * k + 1] = o.gy[k];
+      G[3 * k + 2] = o.gz[k];
+    }
+    if (D) {
+      D[3 * k] = o.dx[k];
+      D[3 * k + 1] = o.dy[k];
+      D[3 * k + 2] = o.dz[k];
+    }
+  }
+  if (diag_exchange) std::copy(o.diag_exchange.begin(), o.diag_exchange.end(), diag_exchange);
+  return MM_OK;
+}
+
+int mm_setup_levels(mm_setup* s, int* n_levels) {
+  if (!s || !n_levels) return MM_ERR_ARG;
+  *n_levels = (int)s->amg.size();
+  return MM_OK;
+}
+
+int mm_setup_level_info(mm_setup* s, int level, int* n, int64_t* nnz_A, int64_t* nnz_P, int* n_cols_P) {
+  if (!s || level < 0 || level >= (int)s->amg.size()) return MM_ERR_ARG;
+  const mm::AmgLevel& L = s->amg[level];
+  if (n) *n = L.A.n_rows;
+  if (nnz_A) *nnz_A = L.A.nnz();
+  if (nnz_P) *nnz_P = L.P.nnz();
+  if (n_cols_P) *n_cols_P = L.P.n_cols;
+  return MM_OK;
+}
+
+int mm_setup_level_export(mm_setup* s, int level, int* A_ptr, int* A_col, double* A_val, int* P_ptr, int* P_col,
+                          double* P_val, int* agg) {
+  if (!s || level < 0 || level >= (int)s->amg.size()) return MM_ERR_ARG;
+  const mm::AmgLevel& L = s->amg[level];
+  if (A_ptr) std::copy(L.A.ptr.begin(), L.A.ptr.end(), A_ptr);
+  if (A_col) std::copy(L.A.col.begin(), L.A.col.end(), A_col);
+  if (A_val) std::copy(L.A.val.begin(), L.A.val.end(), A_val);
+  if (P_ptr && !L.P.ptr.empty()) std::copy(L.P.ptr.begin(), L.P.ptr.end(), P_ptr);
+  if (P_col) std::copy(L.P.col.begin(), L.P.col.end(), P_col);
+  if (P_val) std::copy(L.P.val.begin(), L.P.val.end(), P_val);
+  if (agg) {
+    if (L.agg.empty()) std::fill(agg, agg + L.A.n_rows, -1);
+    else std::copy(L.agg.begin(), L.agg.end(), agg);
+  }
+  return MM_OK;
+}
+
+int mm_create(int N, int E, const int* conn, const double* volume, const double* grad_phi, const int* mat_id,
+              int n_mat, const double* A_lookup, const double* K1_lookup, const double* Js_lookup,
+              const double* k_easy, double V_mag, const double* M_nodal, const double* boundary_mask,
+              mm_problem** out) {
+  if (!out || N <= 0 || E <= 0 || n_mat <= 0 || !conn || !volume || !grad_phi || !mat_id || !A_lookup ||
+      !K1_lookup || !Js_lookup || !k_easy || !M_nodal || !(V_mag > 0))
+    return MM_ERR_ARG;
+  *out = nullptr;
+  mm_problem* h = new mm_problem();
+  int rc = guarded(h, [&] {
+    for (int e = 0; e < 4 * E; ++e)
+      if (conn[e] < 0 || conn[e] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
+    h->N = N;
+    h->E = E;
+    h->n_mat = n_mat;
+    h->V_mag = V_mag;
+    h->inv_Vmag = 1.0 / V_mag;
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&h->ev0));
+    CK(cudaEventCreate(&h->ev1));
+    h->conn.assign(conn, conn + 4 * (size_t)E);
+    h->mat_id.assign(mat_id, mat_id + E);
+    h->volume.assign(volume, volume + E);
+    h->grad_phi.assign(grad_phi, grad_phi + 12 * (size_t)E);
+    h->has_mask = boundary_mask != nullptr;
+    if (h->has_mask) h->mask_h.assign(boundary_mask, boundary_mask + N);
+    h->eop_h = mm::assemble_energy(N, E, conn, volume, grad_phi, mat_id, n_mat, A_lookup, K1_lookup, Js_lookup,
+                                   k_easy);
+    const mm::EnergyOp& o = h->eop_h;
+    mmk::EnergyDev& d = h->eop;
+    d.n_rows = o.n_rows;
+    d.rows = h->upload(o.rows);
+    d.ptr = h->upload(o.ptr);
+    d.col = h->upload(o.col);
+    d.mat = h->upload(o.mat);
+    d.w = h->upload(o.w);
+    d.q = h->upload(o.q);
+    d.gx = h->upload(o.gx);
+    d.gy = h->upload(o.gy);
+    d.gz = h->upload(o.gz);
+    d.dx = h->upload(o.dx);
+    d.dy = h->upload(o.dy);
+    d.dz = h->upload(o.dz);
+    d.kax = h->upload(std::vector<double>(k_easy, k_easy + 3 * (size_t)n_mat));
+    d.single_axis = o.single_axis ? 1 : 0;
+    d.axis0 = o.mat.empty() ? 0 : o.mat[0];
+    h->eop_tpr = pick_tpr((int64_t)o.col.size(), std::max(1, o.n_rows));
+    h->d_Mn = h->upload(std::vector<double>(M_nodal, M_nodal + N));
+    // default node weights (src/hysteresis_loop.py:340-353)
+    std::vector<double> imr(N), imp(N), dex(N);
+    for (int i = 0; i < N; ++i) {
+      imr[i] = M_nodal[i] > 1e-20 ? V_mag / M_nodal[i] : 0.0;
+      dex[i] = o.diag_exchange[i] * h->inv_Vmag;
+      imp[i] = dex[i] > 1e-20 ? 1.0 / dex[i] : 1.0;
+    }
+    h->d_inv_M_rel = h->upload(imr);
+    h->d_inv_M_prec = h->upload(imp);
+    h->d_diag_ex = h->upload(dex);
+    const size_t n3 = 3 * (size_t)N;
+    h->d_m = h->alloc<double>(n3);
+    h->d_U = h->alloc<double>(N);
+    h->d_g = h->alloc<double>(n3);
+    h->d_v = h->alloc<double>(n3);
+    h->d_out = h->alloc<double>(n3);
+    h->d_b = h->alloc<double>(N);
+    CK(cudaMemsetAsync(h->d_g, 0, n3 * sizeof(double), h->st));
+    CK(cudaMemsetAsync(h->d_out, 0, n3 * sizeof(double), h->st));
+    CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
+    h->d_part = h->alloc<double>((size_t)NSLOTS * MAXG);
+    CK(cudaMemsetAsync(h->d_part, 0, (size_t)NSLOTS * MAXG * sizeof(double), h->st));
+    h->d_sc = h->alloc<mmk::Scalars>(1);
+    CK(cudaMallocHost(&h->h_sc, sizeof(mmk::Scalars)));
+    CK(cudaMallocHost(&h->h_part, MAXG * sizeof(double)));
+    h->sync();
+    return MM_OK;
+  });
+  if (rc != MM_OK) {
+    g_create_error = h->err;
+    mm_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return MM_OK;
+}
+
+int mm_destroy(mm_problem* h) {
+  if (!h) return MM_ERR_ARG;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->h_sc) cudaFreeHost(h->h_sc);
+  if (h->h_part) cudaFreeHost(h->h_part);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return MM_OK;
+}
+
+int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels, int max_coarse, int* n_levels) {
+  if (!h || precond_type < MM_PRECOND_NONE || precond_type > MM_PRECOND_AMGCL) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (h->poisson_built) throw Fail{MM_ERR_STATE, "Poisson operator already built"};
+    h->reg = reg;
+    h->precond = precond_type;
+    mm::HostCSR A = mm::assemble_poisson(h->N, h->E, h->conn.data(), h->volume.data(), h->grad_phi.data(),
+                                         h->has_mask ? h->mask_h.data() : nullptr, reg);
+    const bool amg = precond_type == MM_PRECOND_AMG || precond_type == MM_PRECOND_AMGCL;
+    if (amg) {
+      mm::AmgParams prm;
+      prm.max_levels = max_levels > 0 ? max_levels : 10;
+      prm.max_coarse = max_coarse > 0 ? max_coarse : 1000;
+      h->amg_h = mm::build_amg(A, prm);
+    } else {
+      h->amg_h.clear();
+      mm::AmgLevel L0;
+      L0.A = A;
+      h->amg_h.push_back(L0);
+    }
+    const int L = (int)h->amg_h.size();
+    h->lv.resize(L);
+    for (int l = 0; l < L; ++l) {
+      const mm::AmgLevel& hl = h->amg_h[l];
+      DevLevel& dl = h->lv[l];
+      dl.n = hl.A.n_rows;
+      dl.A = h->upload(hl.A);
+      if (l < L - 1) {
+        dl.P = h->upload(hl.P);
+        dl.R = h->upload(hl.R);
+      }
+      if (amg) {
+        std::vector<double> s(dl.n);
+        for (int i = 0; i < dl.n; ++i)
+          s[i] = precond_type == MM_PRECOND_AMGCL ? hl.spai0[i] : 0.6667 / (hl.diag[i] + 1e-30);
+        dl.s = h->upload(s);
+      }
+      dl.b = h->alloc<double>(dl.n);
+      dl.x = h->alloc<double>(dl.n);
+      dl.x2 = h->alloc<double>(dl.n);
+      dl.res = h->alloc<double>(dl.n);
+    }
+    if (amg) {
+      const mm::HostCSR& Ac = h->amg_h.back().A;
+      h->n_coarse = Ac.n_rows;
+      h->d_Ainv = h->upload(mm::dense_inverse(Ac));
+    } else {
+      std::vector<double> jac(h->N, 1.0);
+      std::vector<double> dg(h->N, 0.0);
+      for (int r = 0; r < A.n_rows; ++r)
+        for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+          if (A.col[k] == r) dg[r] = A.val[k];
+      for (int i = 0; i < h->N; ++i) jac[i] = 1.0 / (dg[i] + 1e-30);
+      h->d_jac = h->upload(jac);
+    }
+    h->d_r = h->alloc<double>(h->N);
+    h->d_z = h->alloc<double>(h->N);
+    h->d_p = h->alloc<double>(h->N);
+    h->d_Ap = h->alloc<double>(h->N);
+    h->sync();
+    h->poisson_built = true;
+    if (n_levels) *n_levels = L;
+    return MM_OK;
+  });
+}
+
+int mm_amg_level_info(mm_problem* h, int level, int* n, int64_t* nnz_A, int64_t* nnz_P) {
+  if (!h || !h->poisson_built || level < 0 || level >= (int)h->amg_h.size()) return MM_ERR_ARG;
+  const mm::AmgLevel& L = h->amg_h[level];
+  if (n) *n = L.A.n_rows;
+  if (nnz_A) *nnz_A = L.A.nnz();
+  if (nnz_P) *nnz_P = L.P.nnz();
+  return MM_OK;
+}
+
+int mm_amg_export_level(mm_problem* h, int level, int* A_ptr, int* A_col, double* A_val, int* agg) {
+  if (!h || !h->poisson_built || level < 0 || level >= (int)h->amg_h.size()) return MM_ERR_ARG;
+  const mm::AmgLevel& L = h->amg_h[level];
+  if (A_ptr) std::copy(L.A.ptr.begin(), L.A.ptr.end(), A_ptr);
+  if (A_col) std::copy(L.A.col.begin(), L.A.col.end(), A_col);
+  if (A_val) std::copy(L.A.val.begin(), L.A.val.end(), A_val);
+  if (agg) {
+    if (L.agg.empty()) std::fill(agg, agg + L.A.n_rows, -1);
+    else std::copy(L.agg.begin(), L.agg.end(), agg);
+  }
+  return MM_OK;
+}
+
+int mm_energy_grad(mm_problem* h, const double* m, const double* U, const double* B, const double* B_bias, double* E,
+                   double* g) {
+  if (!h || !m || !U || !B || !E || !g) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    const size_t n3 = 3 * (size_t)h->N;
+    CK(cudaMemcpyAsync(h->d_m, m, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    const double* dbias = nullptr;
+    if (B_bias) {
+      if (!h->d_bias) h->d_bias = h->alloc<double>(n3);
+      CK(cudaMemcpyAsync(h->d_bias, B_bias, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      dbias = h->d_bias;
+    }
+    *E = energy_dev(h, h->d_m, h->d_U, B, dbias, h->d_g);
+    CK(cudaMemcpyAsync(g, h->d_g, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return std::isfinite(*E) ? MM_OK : MM_NONFINITE;
+  });
+}
+
+int mm_energy_grad_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
+                       double* E, double* d_g) {
+  if (!h || !d_m || !d_U || !B || !E || !d_g) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    CK(cudaMemsetAsync(d_g, 0, 3 * (size_t)h->N * sizeof(double), h->st));
+    *E = energy_dev(h, d_m, d_U, B, d_bias, d_g);
+    return std::isfinite(*E) ? MM_OK : MM_NONFINITE;
+  });
+}
+
+int mm_local_grad(mm_problem* h, const double* v, double* out) {
+  if (!h || !v || !out) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    const size_t n3 = 3 * (size_t)h->N;
+    CK(cudaMemcpyAsync(h->d_v, v, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    local_grad_dev(h, h->d_v, h->d_out);
+    CK(cudaMemcpyAsync(out, h->d_out, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_exchange_diagonal(mm_problem* h, double* d) {
+  if (!h || !d) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    CK(cudaMemcpyAsync(d, h->d_diag_ex, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_rhs(mm_problem* h, const double* m, double* b, double* bnorm2) {
+  if (!h || !m || !b) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->d_b, 0, h->N * sizeof(double), h->st));
+    enqueue_rhs(h, h->d_m);
+    const double bb = host_sum(h, SL_BB0, grid_elem(h->N));
+    if (bnorm2) *bnorm2 = bb;
+    CK(cudaMemcpyAsync(b, h->d_b, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_apply_A(mm_problem* h, const double* U, double* y) {
+  if (!h || !U || !y) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    spmv<0>(h, h->lv[0].A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+    CK(cudaMemcpyAsync(y, h->d_out, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_precond(mm_problem* h, const double* r, double* z) {
+  if (!h || !r || !z) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    CK(cudaMemcpyAsync(h->d_U, r, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    enqueue_precond(h, h->d_U, h->d_out);
+    CK(cudaMemcpyAsync(z, h->d_out, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_solve_u(mm_problem* h, const double* m, double* U, double tol, int maxiter, int* iters, double* rel_res) {
+  if (!h || !m || !U || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    const int rc = solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res);
+    CK(cudaMemcpyAsync(U, h->d_U, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return rc;
+  });
+}
+
+int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters,
+                   double* rel_res) {
+  if (!h || !d_m || !d_U || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;
+  return guarded(h, [&] { return solve_dev(h, d_m, d_U, tol, maxiter, iters, rel_res); });
+}
+
+int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec) {
+  if (!h) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (inv_M_rel)
+      CK(cudaMemcpyAsync(h->d_inv_M_rel, inv_M_rel, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    if (inv_M_prec)
+      CK(cudaMemcpyAsync(h->d_inv_M_prec, inv_M_prec, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_minimize(mm_problem* h, const double* B, double* m, double* U, const mm_min_params* prm, mm_min_info* info) {
+  if (!h || !B || !m || !U || !prm) return MM_ERR_ARG;
+  if (prm->method < MM_METHOD_PCOHEN_HS || prm->method > MM_METHOD_WG_NP || prm->max_iter < 0) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    const size_t n3 = 3 * (size_t)h->N;
+    // the minimizer owns d_m / d_U as its state buffers; they may be swapped with its trial buffers
+    CK(cudaMemcpyAsync(h->d_m, m, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    double* dm = h->d_m;
+    double* dU = h->d_U;
+    const int rc = minimize_dev(h, B, dm, dU, prm, info);
+    CK(cudaMemcpyAsync(m, dm, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(U, dU, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    // keep the staging pointers valid whichever buffers ended up holding the state
+    h->d_m = dm;
+    h->d_U = dU;
+    return rc;
+  });
+}
+
+int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* bytes) {
+  if (!h || reps <= 0 || kernel < MM_KERNEL_SPMV_A || kernel > MM_KERNEL_HESSIAN) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if ((kernel == MM_KERNEL_SPMV_A || kernel == MM_KERNEL_SMOOTH) && !h->poisson_built)
+      throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    const size_t flush_n = (size_t)256 << 20;  // 256 MiB > L2
+    char* flush = nullptr;
+    CK(cudaMalloc(&flush, flush_n));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int N = h->N;
+    double acc = 0.0, nbytes = 0.0;
+    const DevLevel* l0 = h->poisson_built ? &h->lv[0] : nullptr;
+    auto launch = [&]() {
+      if (kernel == MM_KERNEL_SPMV_A) {
+        spmv<0>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+      } else if (kernel == MM_KERNEL_SMOOTH) {
+        const DevMat& A = l0->A;
+        const double* s = l0->s ? l0->s : h->d_U;
+        const int g = grid_rows(A.n_rows, A.tpr);
+        TPR_SWITCH(A.tpr, (mmk::k_smooth_dot<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_U, h->d_b, s,
+                                                                      h->d_out, h->part(SL_RZ), nullptr)));
+        LAUNCH_CHECK();
+      } else if (kernel == MM_KERNEL_ENERGY) {
+        const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
+        TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
+                                                                            1.0, nullptr, h->inv_Vmag, h->d_g,
+                                                                            h->part(SL_E))));
+        LAUNCH_CHECK();
+      } else {
+        local_grad_dev(h, h->d_m, h->d_out);
+      }
+    };
+    const mm::EnergyOp& o = h->eop_h;
+    const double nnzE = (double)o.col.size(), nrE = (double)o.n_rows;
+    if (kernel == MM_KERNEL_SPMV_A) {
+      const double nnz = (double)l0->A.nnz;
+      nbytes = nnz * 12.0 + (N + 1.0) * 4.0 + N * 8.0 * 2.0;
+    } else if (kernel == MM_KERNEL_SMOOTH) {
+      const double nnz = (double)l0->A.nnz;
+      nbytes = nnz * 12.0 + (N + 1.0) * 4.0 + N * 8.0 * 4.0;
+    } else if (kernel == MM_KERNEL_ENERGY) {
+      // entries: col, mat, w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3)
+      nbytes = nnzE * (4.0 + 4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0;
+    } else {
+      nbytes = nnzE * (4.0 + 4.0 + 8.0 * 2.0) + nrE * 8.0 + nrE * 8.0 * 6.0;
+    }
+    launch();  // warm-up
+    for (int r = 0; r < reps; ++r) {
+      CK(cudaMemsetAsync(flush, r & 0xff, flush_n, h->st));
+      CK(cudaEventRecord(e0, h->st));
+      launch();
+      CK(cudaEventRecord(e1, h->st));
+      CK(cudaEventSynchronize(e1));
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, e0, e1));
+      acc += t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(flush);
+    if (ms) *ms = acc / reps;
+    if (bytes) *bytes = nbytes;
+    return MM_OK;
+  });
+}
+
+int mm_last_solve_ms(mm_problem* h, double* ms) {
+  if (!h || !ms) return MM_ERR_ARG;
+  *ms = h->last_solve_ms;
+  return MM_OK;
+}
+
+int mm_launch_count(mm_problem* h, int64_t* count) {
+  if (!h || !count) return MM_ERR_ARG;
+  *count = h->n_launch;
+  return MM_OK;
+}
+
+int mm_sync(mm_problem* h) {
+  if (!h) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    h->sync();
+    return MM_OK;
+  });
+}
+
+}  // extern "C"

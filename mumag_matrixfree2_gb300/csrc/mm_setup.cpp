@@ -1,0 +1,565 @@
+// Host setup of the hot path (C++17, compiled without floating-point contraction so that sums
+// follow the element order stated below on every host).
+#include "mm_setup.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+
+namespace mm {
+
+// ---------------------------------------------------------------------------------------------
+// geometry: orientation fix, volume, inv(J)^T and shape-function gradients (src/loop.py:56-102)
+// ---------------------------------------------------------------------------------------------
+static inline double det3(const double J[3][3]) {
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn_out, double* volume, double* JinvT,
+                  double* grad_phi) {
+  for (int e = 0; e < E; ++e) {
+    int c[4] = {conn_in[4 * e], conn_in[4 * e + 1], conn_in[4 * e + 2], conn_in[4 * e + 3]};
+    for (int a = 0; a < 4; ++a)
+      if (c[a] < 0 || c[a] >= N) throw std::runtime_error("connectivity index out of range");
+    double J[3][3];
+    auto build = [&]() {
+      for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 3; ++i) J[i][k] = knt[3 * c[k + 1] + i] - knt[3 * c[0] + i];
+    };
+    build();
+    double d = det3(J);
+    if (d < 0) {
+      std::swap(c[1], c[2]);
+      build();
+      d = det3(J);
+    }
+    for (int a = 0; a < 4; ++a) conn_out[4 * e + a] = c[a];
+    volume[e] = std::fabs(d) / 6.0;
+    // inverse via the adjugate
+    double inv[3][3];
+    inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / d;
+    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / d;
+    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / d;
+    inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / d;
+    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / d;
+    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / d;
+    inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / d;
+    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / d;
+    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / d;
+    double* T = JinvT + 9 * e;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) T[3 * i + j] = inv[j][i];
+    // grad phi_a = JinvT . ghat_a with ghat_0 = (-1,-1,-1), ghat_k = e_k
+    double* g = grad_phi + 12 * e;
+    for (int i = 0; i < 3; ++i) {
+      g[3 * 1 + i] = T[3 * i + 0];
+      g[3 * 2 + i] = T[3 * i + 1];
+      g[3 * 3 + i] = T[3 * i + 2];
+      g[3 * 0 + i] = (-T[3 * i + 0] - T[3 * i + 1]) - T[3 * i + 2];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// boundary mask: nodes of faces that belong to exactly one tetrahedron (src/add_shell.py:105-136)
+// ---------------------------------------------------------------------------------------------
+void boundary_mask(int N, int E, const int* conn, double* mask) {
+  static const int fp[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+  std::vector<std::array<int, 3>> faces((size_t)E * 4);
+  for (int e = 0; e < E; ++e)
+    for (int f = 0; f < 4; ++f) {
+      std::array<int, 3> t = {conn[4 * e + fp[f][0]], conn[4 * e + fp[f][1]], conn[4 * e + fp[f][2]]};
+      std::sort(t.begin(), t.end());
+      faces[(size_t)4 * e + f] = t;
+    }
+  std::sort(faces.begin(), faces.end());
+  for (int i = 0; i < N; ++i) mask[i] = 1.0;
+  size_t i = 0, n = faces.size();
+  while (i < n) {
+    size_t j = i + 1;
+    while (j < n && faces[j] == faces[i]) ++j;
+    if (j - i == 1)
+      for (int k = 0; k < 3; ++k) mask[faces[i][k]] = 0.0;
+    i = j;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Morton order of nodes and element centroids, 10 bits per axis (src/reorder_mesh.py:19-30,85-100)
+// ---------------------------------------------------------------------------------------------
+static inline int64_t morton30(int64_t x, int64_t y, int64_t z) {
+  int64_t code = 0;
+  for (int i = 0; i < 10; ++i) {
+    code |= ((x >> i) & 1) << (3 * i + 2);
+    code |= ((y >> i) & 1) << (3 * i + 1);
+    code |= ((z >> i) & 1) << (3 * i);
+  }
+  return code;
+}
+
+void morton_order(int N, int E, const double* knt, const int* conn, int* node_perm, int* elem_perm) {
+  double mn[3], den[3];
+  for (int i = 0; i < 3; ++i) {
+    double lo = knt[i], hi = knt[i];
+    for (int n = 1; n < N; ++n) {
+      lo = std::min(lo, knt[3 * n + i]);
+      hi = std::max(hi, knt[3 * n + i]);
+    }
+    mn[i] = lo;
+    den[i] = (hi - lo) == 0.0 ? 1.0 : (hi - lo);
+  }
+  auto quant = [&](double v, int i) { return (int64_t)(int32_t)(((v - mn[i]) / den[i]) * 1023.0); };
+  std::vector<int64_t> key(N);
+  for (int n = 0; n < N; ++n) key[n] = morton30(quant(knt[3 * n], 0), quant(knt[3 * n + 1], 1), quant(knt[3 * n + 2], 2));
+  std::iota(node_perm, node_perm + N, 0);
+  std::stable_sort(node_perm, node_perm + N, [&](int a, int b) { return key[a] < key[b]; });
+  std::vector<int64_t> ekey(E);
+  for (int e = 0; e < E; ++e) {
+    double c[3];
+    for (int i = 0; i < 3; ++i) {
+      double s = knt[3 * conn[4 * e] + i];
+      s = s + knt[3 * conn[4 * e + 1] + i];
+      s = s + knt[3 * conn[4 * e + 2] + i];
+      s = s + knt[3 * conn[4 * e + 3] + i];
+      c[i] = s / 4.0;
+    }
+    ekey[e] = morton30(quant(c[0], 0), quant(c[1], 1), quant(c[2], 2));
+  }
+  std::iota(elem_perm, elem_perm + E, 0);
+  std::stable_sort(elem_perm, elem_perm + E, [&](int a, int b) { return ekey[a] < ekey[b]; });
+}
+
+// ---------------------------------------------------------------------------------------------
+// assembly helpers
+// ---------------------------------------------------------------------------------------------
+struct NodeElems {
+  std::vector<int> ptr, elem;
+};
+
+static NodeElems node_elements(int N, int E, const int* conn, const std::vector<char>* use = nullptr) {
+  NodeElems ne;
+  ne.ptr.assign(N + 1, 0);
+  for (int e = 0; e < E; ++e) {
+    if (use && !(*use)[e]) continue;
+    for (int a = 0; a < 4; ++a) ne.ptr[conn[4 * e + a] + 1]++;
+  }
+  for (int i = 0; i < N; ++i) ne.ptr[i + 1] += ne.ptr[i];
+  ne.elem.resize(ne.ptr[N]);
+  std::vector<int> fill(ne.ptr.begin(), ne.ptr.end() - 1);
+  for (int e = 0; e < E; ++e) {
+    if (use && !(*use)[e]) continue;
+    for (int a = 0; a < 4; ++a) ne.elem[fill[conn[4 * e + a]]++] = e;
+  }
+  return ne;
+}
+
+static inline double dot3(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static inline int find_col(const int* cols, int n, int c) {
+  const int* p = std::lower_bound(cols, cols + n, c);
+  return (int)(p - cols);
+}
+
+// Drop exactly-zero entries (scipy's CSR arithmetic keeps only non-zero results).
+static void drop_zeros(HostCSR& A) {
+  int w = 0;
+  std::vector<int> nptr(A.n_rows + 1, 0);
+  for (int r = 0; r < A.n_rows; ++r) {
+    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+      if (A.val[k] != 0.0) {
+        A.col[w] = A.col[k];
+        A.val[w] = A.val[k];
+        ++w;
+      }
+    nptr[r + 1] = w;
+  }
+  A.ptr = nptr;
+  A.col.resize(w);
+  A.val.resize(w);
+}
+
+HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, const double* gp, const double* mask,
+                         double reg) {
+  NodeElems ne = node_elements(N, E, conn);
+  HostCSR A;
+  A.n_rows = A.n_cols = N;
+  A.ptr.assign(N + 1, 0);
+  std::vector<int> tmp;
+  for (int i = 0; i < N; ++i) {
+    tmp.clear();
+    for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
+      int e = ne.elem[k];
+      for (int b = 0; b < 4; ++b) tmp.push_back(conn[4 * e + b]);
+    }
+    tmp.push_back(i);
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    A.ptr[i + 1] = A.ptr[i] + (int)tmp.size();
+    A.col.insert(A.col.end(), tmp.begin(), tmp.end());
+  }
+  A.val.assign(A.col.size(), 0.0);
+  // element order accumulation: K_ab = Ve (grad phi_a . grad phi_b)
+  for (int e = 0; e < E; ++e) {
+    const double* g = gp + 12 * e;
+    for (int a = 0; a < 4; ++a) {
+      int r = conn[4 * e + a];
+      const int* rc = A.col.data() + A.ptr[r];
+      int rn = A.ptr[r + 1] - A.ptr[r];
+      for (int b = 0; b < 4; ++b) {
+        int pos = find_col(rc, rn, conn[4 * e + b]);
+        A.val[A.ptr[r] + pos] += volume[e] * dot3(g + 3 * a, g + 3 * b);
+      }
+    }
+  }
+  if (mask) {
+    for (int r = 0; r < N; ++r)
+      for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+        if (mask[r] == 0.0 || mask[A.col[k]] == 0.0) A.val[k] = 0.0;
+  }
+  for (int r = 0; r < N; ++r) {
+    int pos = find_col(A.col.data() + A.ptr[r], A.ptr[r + 1] - A.ptr[r], r);
+    A.val[A.ptr[r] + pos] += reg;
+    if (mask && mask[r] == 0.0) A.val[A.ptr[r] + pos] = 1.0;
+  }
+  drop_zeros(A);
+  return A;
+}
+
+EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, const double* gp, const int* mat_id,
+                         int n_mat, const double* Alu, const double* K1lu, const double* Jslu, const double* k_easy) {
+  EnergyOp op;
+  op.n_mat = n_mat;
+  std::vector<char> use(E, 0);
+  std::vector<char> mat_used(n_mat, 0);
+  for (int e = 0; e < E; ++e) {
+    int g = mat_id[e] - 1;
+    if (g < 0 || g >= n_mat) throw std::runtime_error("material id out of range");
+    if (Alu[g] != 0.0 || K1lu[g] != 0.0 || Jslu[g] != 0.0) {
+      use[e] = 1;
+      mat_used[g] = 1;
+    }
+  }
+  // single easy axis when every material that carries anisotropy shares one axis
+  int first = -1;
+  op.single_axis = true;
+  for (int g = 0; g < n_mat; ++g) {
+    if (!mat_used[g] || K1lu[g] == 0.0) continue;
+    if (first < 0) first = g;
+    else if (k_easy[3 * g] != k_easy[3 * first] || k_easy[3 * g + 1] != k_easy[3 * first + 1] ||
+             k_easy[3 * g + 2] != k_easy[3 * first + 2])
+      op.single_axis = false;
+  }
+  NodeElems ne = node_elements(N, E, conn, &use);
+  op.diag_exchange.assign(N, 0.0);
+  op.ptr.push_back(0);
+  std::vector<std::pair<int, int>> keys;
+  for (int i = 0; i < N; ++i) {
+    if (ne.ptr[i + 1] == ne.ptr[i]) continue;
+    keys.clear();
+    for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
+      int e = ne.elem[k];
+      int g = op.single_axis ? 0 : mat_id[e] - 1;
+      for (int b = 0; b < 4; ++b) keys.emplace_back(conn[4 * e + b], g);
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    op.rows.push_back(i);
+    for (auto& kv : keys) {
+      op.col.push_back(kv.first);
+      op.mat.push_back(kv.second);
+    }
+    op.ptr.push_back((int)op.col.size());
+  }
+  op.n_rows = (int)op.rows.size();
+  size_t nnz = op.col.size();
+  op.w.assign(nnz, 0.0);
+  op.q.assign(nnz, 0.0);
+  op.gx.assign(nnz, 0.0);
+  op.gy.assign(nnz, 0.0);
+  op.gz.assign(nnz, 0.0);
+  op.dx.assign(nnz, 0.0);
+  op.dy.assign(nnz, 0.0);
+  op.dz.assign(nnz, 0.0);
+  std::vector<int> row_of(N, -1);
+  for (int r = 0; r < op.n_rows; ++r) row_of[op.rows[r]] = r;
+  for (int e = 0; e < E; ++e) {
+    if (!use[e]) continue;
+    int g = mat_id[e] - 1;
+    int gk = op.single_axis ? 0 : g;
+    const double* G = gp + 12 * e;
+    double cA = 2.0 * Alu[g] * volume[e];
+    double cK = 2.0 * K1lu[g] * volume[e] / 20.0;
+    double cG = 2.0 * Jslu[g] * volume[e] / 4.0;
+    double cD = Jslu[g] * volume[e] / 4.0;
+    for (int a = 0; a < 4; ++a) {
+      int node = conn[4 * e + a];
+      int r = row_of[node];
+      op.diag_exchange[node] += cA * dot3(G + 3 * a, G + 3 * a);
+      int base = op.ptr[r], n = op.ptr[r + 1] - base;
+      for (int b = 0; b < 4; ++b) {
+        int cb = conn[4 * e + b];
+        // entries are sorted by (col, mat): find the matching pair
+        int lo = 0, hi = n;
+        while (lo < hi) {
+          int mid = (lo + hi) / 2;
+          int mc = op.col[base + mid], mg = op.mat[base + mid];
+          if (mc < cb || (mc == cb && mg < gk)) lo = mid + 1;
+          else hi = mid;
+        }
+        int k = base + lo;
+        op.w[k] += cA * dot3(G + 3 * a, G + 3 * b);
+        op.q[k] += cK * (a == b ? 2.0 : 1.0);
+        op.gx[k] += cG * G[3 * b + 0];
+        op.gy[k] += cG * G[3 * b + 1];
+        op.gz[k] += cG * G[3 * b + 2];
+        op.dx[k] += cD * G[3 * a + 0];
+        op.dy[k] += cD * G[3 * a + 1];
+        op.dz[k] += cD * G[3 * a + 2];
+      }
+    }
+  }
+  if (op.single_axis) {
+    // all entries refer to the shared axis; remember which material carries it
+    for (auto& m : op.mat) m = first < 0 ? 0 : first;
+  }
+  return op;
+}
+
+// ---------------------------------------------------------------------------------------------
+// smoothed aggregation (the project's own algorithm; restated by the oracle for parity)
+// ---------------------------------------------------------------------------------------------
+static HostCSR transpose(const HostCSR& A) {
+  HostCSR T;
+  T.n_rows = A.n_cols;
+  T.n_cols = A.n_rows;
+  T.ptr.assign(T.n_rows + 1, 0);
+  for (int c : A.col) T.ptr[c + 1]++;
+  for (int i = 0; i < T.n_rows; ++i) T.ptr[i + 1] += T.ptr[i];
+  T.col.resize(A.col.size());
+  T.val.resize(A.col.size());
+  std::vector<int> fill(T.ptr.begin(), T.ptr.end() - 1);
+  for (int r = 0; r < A.n_rows; ++r)
+    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) {
+      int p = fill[A.col[k]]++;
+      T.col[p] = r;
+      T.val[p] = A.val[k];
+    }
+  return T;
+}
+
+// C = A * B (Gustavson), sums in the order of A's sorted columns; exact zeros dropped; columns sorted.
+static HostCSR spgemm(const HostCSR& A, const HostCSR& B) {
+  HostCSR C;
+  C.n_rows = A.n_rows;
+  C.n_cols = B.n_cols;
+  C.ptr.assign(C.n_rows + 1, 0);
+  std::vector<double> acc(B.n_cols, 0.0);
+  std::vector<int> mark(B.n_cols, -1), cols;
+  for (int i = 0; i < A.n_rows; ++i) {
+    cols.clear();
+    for (int ka = A.ptr[i]; ka < A.ptr[i + 1]; ++ka) {
+      int k = A.col[ka];
+      double a = A.val[ka];
+      for (int kb = B.ptr[k]; kb < B.ptr[k + 1]; ++kb) {
+        int j = B.col[kb];
+        if (mark[j] != i) {
+          mark[j] = i;
+          acc[j] = 0.0;
+          cols.push_back(j);
+        }
+        acc[j] += a * B.val[kb];
+      }
+    }
+    std::sort(cols.begin(), cols.end());
+    for (int j : cols)
+      if (acc[j] != 0.0) {
+        C.col.push_back(j);
+        C.val.push_back(acc[j]);
+      }
+    C.ptr[i + 1] = (int)C.col.size();
+  }
+  return C;
+}
+
+static std::vector<double> diag_of(const HostCSR& A) {
+  std::vector<double> d(A.n_rows, 0.0);
+  for (int r = 0; r < A.n_rows; ++r)
+    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+      if (A.col[k] == r) d[r] = A.val[k];
+  return d;
+}
+
+static std::vector<double> spai0_of(const HostCSR& A, const std::vector<double>& d) {
+  std::vector<double> s(A.n_rows);
+  for (int r = 0; r < A.n_rows; ++r) {
+    double ss = 0.0;
+    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) ss += A.val[k] * A.val[k];
+    s[r] = d[r] / (ss + 1e-30);
+  }
+  return s;
+}
+
+static std::vector<int> aggregate(const HostCSR& A, const std::vector<double>& d, double theta, int& nagg) {
+  int n = A.n_rows;
+  const double t2 = theta * theta;
+  // strength pattern
+  std::vector<int> sptr(n + 1, 0), scol;
+  for (int i = 0; i < n; ++i) {
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+      int j = A.col[k];
+      double v = A.val[k];
+      if (j != i && v * v > t2 * std::fabs(d[i] * d[j])) scol.push_back(j);
+    }
+    sptr[i + 1] = (int)scol.size();
+  }
+  std::vector<int> agg(n, -1);
+  nagg = 0;
+  for (int i = 0; i < n; ++i) {  // pass 1
+    if (agg[i] >= 0 || sptr[i + 1] == sptr[i]) continue;
+    bool free_nb = true;
+    for (int k = sptr[i]; k < sptr[i + 1]; ++k)
+      if (agg[scol[k]] >= 0) {
+        free_nb = false;
+        break;
+      }
+    if (!free_nb) continue;
+    agg[i] = nagg;
+    for (int k = sptr[i]; k < sptr[i + 1]; ++k) agg[scol[k]] = nagg;
+    ++nagg;
+  }
+  std::vector<int> after1 = agg;
+  for (int i = 0; i < n; ++i) {  // pass 2
+    if (after1[i] >= 0) continue;
+    for (int k = sptr[i]; k < sptr[i + 1]; ++k)
+      if (after1[scol[k]] >= 0) {
+        agg[i] = after1[scol[k]];
+        break;
+      }
+  }
+  for (int i = 0; i < n; ++i) {  // pass 3
+    if (agg[i] >= 0 || sptr[i + 1] == sptr[i]) continue;
+    agg[i] = nagg;
+    for (int k = sptr[i]; k < sptr[i + 1]; ++k)
+      if (agg[scol[k]] < 0) agg[scol[k]] = nagg;
+    ++nagg;
+  }
+  return agg;
+}
+
+std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
+  std::vector<AmgLevel> levels;
+  HostCSR Acur = A0;
+  double theta = prm.theta0;
+  while (true) {
+    AmgLevel L;
+    L.A = Acur;
+    L.diag = diag_of(Acur);
+    L.spai0 = spai0_of(Acur, L.diag);
+    levels.push_back(L);
+    int n = Acur.n_rows;
+    if (n <= prm.max_coarse || (int)levels.size() >= prm.max_levels) break;
+    int nagg = 0;
+    std::vector<int> agg = aggregate(Acur, levels.back().diag, theta, nagg);
+    if (nagg == 0 || nagg >= n) break;
+    // tentative prolongator
+    std::vector<int> size(nagg, 0);
+    for (int a : agg)
+      if (a >= 0) size[a]++;
+    HostCSR T;
+    T.n_rows = n;
+    T.n_cols = nagg;
+    T.ptr.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      if (agg[i] >= 0) {
+        T.col.push_back(agg[i]);
+        T.val.push_back(1.0 / std::sqrt((double)size[agg[i]]));
+      }
+      T.ptr[i + 1] = (int)T.col.size();
+    }
+    // Gershgorin bound of rho(D^-1 A) and damped-Jacobi smoothing
+    const std::vector<double>& d = levels.back().diag;
+    double rho = 0.0;
+    bool any = false;
+    for (int i = 0; i < n; ++i) {
+      if (std::fabs(d[i]) <= 0.0) continue;
+      double rs = 0.0;
+      for (int k = Acur.ptr[i]; k < Acur.ptr[i + 1]; ++k) rs += std::fabs(Acur.val[k]);
+      rho = any ? std::max(rho, rs / std::fabs(d[i])) : rs / std::fabs(d[i]);
+      any = true;
+    }
+    if (!any) rho = 1.0;
+    double omega = (4.0 / 3.0) / rho;
+    HostCSR AT = spgemm(Acur, T);
+    HostCSR P;
+    P.n_rows = n;
+    P.n_cols = nagg;
+    P.ptr.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      double dinv = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
+      int ka = AT.ptr[i], kt = T.ptr[i];
+      while (ka < AT.ptr[i + 1] || kt < T.ptr[i + 1]) {
+        int ca = ka < AT.ptr[i + 1] ? AT.col[ka] : INT32_MAX;
+        int ct = kt < T.ptr[i + 1] ? T.col[kt] : INT32_MAX;
+        int c = std::min(ca, ct);
+        double tv = (ct == c) ? T.val[kt++] : 0.0;
+        double av = (ca == c) ? AT.val[ka++] : 0.0;
+        double v = tv - omega * (dinv * av);
+        if (v != 0.0) {
+          P.col.push_back(c);
+          P.val.push_back(v);
+        }
+      }
+      P.ptr[i + 1] = (int)P.col.size();
+    }
+    HostCSR R = transpose(P);
+    HostCSR RA = spgemm(R, Acur);
+    HostCSR Ac = spgemm(RA, P);
+    levels.back().P = P;
+    levels.back().R = R;
+    levels.back().agg = agg;
+    Acur = Ac;
+    theta *= 0.5;
+  }
+  return levels;
+}
+
+std::vector<double> dense_inverse(const HostCSR& A) {
+  int n = A.n_rows;
+  std::vector<double> M((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
+  for (int r = 0; r < n; ++r) {
+    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) M[(size_t)r * n + A.col[k]] = A.val[k];
+    I[(size_t)r * n + r] = 1.0;
+  }
+  for (int c = 0; c < n; ++c) {  // Gauss-Jordan with partial pivoting
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(M[(size_t)r * n + c]) > std::fabs(M[(size_t)piv * n + c])) piv = r;
+    if (M[(size_t)piv * n + c] == 0.0) throw std::runtime_error("coarsest AMG matrix is singular");
+    if (piv != c)
+      for (int k = 0; k < n; ++k) {
+        std::swap(M[(size_t)c * n + k], M[(size_t)piv * n + k]);
+        std::swap(I[(size_t)c * n + k], I[(size_t)piv * n + k]);
+      }
+    double inv = 1.0 / M[(size_t)c * n + c];
+    for (int k = 0; k < n; ++k) {
+      M[(size_t)c * n + k] *= inv;
+      I[(size_t)c * n + k] *= inv;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = M[(size_t)r * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) {
+        M[(size_t)r * n + k] -= f * M[(size_t)c * n + k];
+        I[(size_t)r * n + k] -= f * I[(size_t)c * n + k];
+      }
+    }
+  }
+  return I;
+}
+
+}  // namespace mm

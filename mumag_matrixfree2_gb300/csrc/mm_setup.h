@@ -1,0 +1,63 @@
+// Host-side (C++) setup of the micromagnetic hot path: mesh geometry, Dirichlet mask, Morton
+// order, assembly of the compressed-row operators and the smoothed-aggregation hierarchy.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace mm {
+
+struct HostCSR {
+  int n_rows = 0, n_cols = 0;
+  std::vector<int> ptr, col;
+  std::vector<double> val;
+  int64_t nnz() const { return ptr.empty() ? 0 : ptr.back(); }
+};
+
+// Per-magnetic-row operator of the energy, the local Hessian and the demag right-hand side.
+// Row r belongs to node rows[r]; entry k couples it to node col[k] through elements of material
+// mat[k] (0-based).  For an entry (a, b):
+//   w   = sum_e 2 A_e Ve grad(phi_a).grad(phi_b)                    (exchange, K_ex)
+//   q   = sum_e 2 K1_e Ve / 20 * (1 + delta_ab)                      (anisotropy, used as -q (k.v_b) k)
+//   G   = sum_e 2 Js_e Ve / 4 * grad(phi_b)                          (demag gradient, g_a += G U_b)
+//   D   = sum_e Js_e Ve / 4 * grad(phi_a)                            (demag source, b_a += D . m_b)
+struct EnergyOp {
+  int n_rows = 0;
+  std::vector<int> rows, ptr, col, mat;
+  std::vector<double> w, q, gx, gy, gz, dx, dy, dz;
+  int n_mat = 0;
+  bool single_axis = true;
+  std::vector<double> diag_exchange;  // w_aa per node (N)
+};
+
+struct AmgLevel {
+  HostCSR A, P, R;
+  std::vector<double> spai0, diag;
+  std::vector<int> agg;  // aggregate of each row (-1 = none), empty on the coarsest level
+};
+
+struct AmgParams {
+  int max_levels = 10;
+  int max_coarse = 1000;
+  double theta0 = 0.08;
+};
+
+// geometry (src/loop.py:56-102)
+void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn_out, double* volume,
+                  double* JinvT, double* grad_phi);
+// Dirichlet mask (src/add_shell.py:105-136)
+void boundary_mask(int N, int E, const int* conn, double* mask);
+// Morton order (src/reorder_mesh.py:19-30,85-100); stable on ties
+void morton_order(int N, int E, const double* knt, const int* conn, int* node_perm, int* elem_perm);
+
+// Poisson stiffness with Dirichlet identity rows/columns and regularisation (src/amg_utils.py:21-84)
+HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, const double* grad_phi,
+                         const double* mask, double reg);
+EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, const double* grad_phi,
+                         const int* mat_id, int n_mat, const double* A, const double* K1, const double* Js,
+                         const double* k_easy);
+
+std::vector<AmgLevel> build_amg(const HostCSR& A, const AmgParams& prm);
+std::vector<double> dense_inverse(const HostCSR& A);  // row-major n x n; throws on singular
+
+}  // namespace mm

@@ -1,0 +1,235 @@
+"""Device problem: one mesh with its materials resident on the GPU behind libmumag_cuda.
+
+``Problem`` is the thin object every factory of this package (``make_energy_kernels``,
+``make_solve_U``, ``make_minimizer``) shares, so the mesh and operators are uploaded once.  Host
+arrays (numpy) go through the host-pointer entry points; CUDA torch tensors go through the ``_dev``
+entry points without a copy.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, dptr, f64, i32, lib
+
+
+def _is_torch_cuda(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+@dataclass
+class MinimizerParams:
+    """Defaults of the reference's CLI (``src/loop.py:578-700``) for the minimizer parameters."""
+
+    method: str = "pcohen_hs"
+    max_iter: int = 2000
+    tau_f: float = 1e-8
+    eps_a: float = 1e-12
+    tau0: float = 1e-2
+    ls_eta1: float = 0.1
+    ls_eta2: float = 0.1
+    ls_C: float = 2.0
+    ls_c: float = 0.5
+    ls_max_evals: int = 15
+    pc_iters: int = 10
+    pc_auto: bool = True
+    pc_force_eta: float = 0.5
+    pc_force_alpha: float = 0.5
+    pc_stagnation_nu: float = 0.01
+    pc_reg: float = 0.0
+    memory: int = 5
+    wg_gamma: int = 5
+    L: int | None = None
+    cg_tol: float = 1e-8
+    phi_tol: float | None = None
+    cg_maxiter: int = 2000
+
+    def to_c(self) -> _abi.MinParams:
+        if self.method not in _abi.METHODS:
+            raise ValueError(f"method {self.method!r} is not available in the cuda backend "
+                             f"(available: {sorted(_abi.METHODS)})")
+        return _abi.MinParams(
+            method=_abi.METHODS[self.method], max_iter=int(self.max_iter), pc_iters=int(self.pc_iters),
+            pc_auto=1 if self.pc_auto else 0, ls_max_evals=int(self.ls_max_evals), L=int(self.L or 0),
+            memory=int(self.memory), wg_gamma=int(self.wg_gamma), tau_f=self.tau_f, eps_a=self.eps_a,
+            tau0=self.tau0, ls_eta1=self.ls_eta1, ls_eta2=self.ls_eta2, ls_C=self.ls_C, ls_c=self.ls_c,
+            pc_force_eta=self.pc_force_eta, pc_force_alpha=self.pc_force_alpha,
+            pc_stagnation_nu=self.pc_stagnation_nu, pc_reg=self.pc_reg, cg_tol=self.cg_tol,
+            phi_tol=-1.0 if self.phi_tol is None else float(self.phi_tol), cg_maxiter=int(self.cg_maxiter))
+
+
+class Problem:
+    """A mesh, its materials and (after ``build_poisson``) the demag solver, resident on the GPU."""
+
+    def __init__(self, conn, volume, grad_phi, mat_id, A_lookup, K1_lookup, Js_lookup, k_easy, V_mag, M_nodal,
+                 boundary_mask=None, n_nodes: int | None = None):
+        self.conn = i32(np.asarray(conn)[:, :4])
+        self.N = int(n_nodes if n_nodes is not None else self.conn.max() + 1)
+        self.E = int(self.conn.shape[0])
+        volume, grad_phi = f64(volume), f64(grad_phi, (self.E, 4, 3))
+        mat_id = i32(mat_id)
+        A, K1, Js = f64(np.ravel(A_lookup)), f64(np.ravel(K1_lookup)), f64(np.ravel(Js_lookup))
+        k = f64(k_easy, (len(A), 3))
+        M = f64(M_nodal).reshape(-1)
+        mask = None if boundary_mask is None else f64(boundary_mask).reshape(-1)
+        self.V_mag = float(V_mag)
+        self.has_mask = mask is not None
+        h = C.c_void_p()
+        check("mm_create", lib().mm_create(
+            self.N, self.E, _abi.iptr(self.conn), dptr(volume), dptr(grad_phi), _abi.iptr(mat_id), len(A), dptr(A),
+            dptr(K1), dptr(Js), dptr(k), self.V_mag, dptr(M), dptr(mask), C.byref(h)))
+        self.h = h
+        self.poisson_built = False
+        self.n_levels = 0
+
+    # -- lifetime --------------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, fn, rc):
+        return check(fn, rc, self.h)
+
+    # -- Poisson ---------------------------------------------------------------------------------
+    def build_poisson(self, reg=1e-12, precond_type="amgcl", max_levels=10, max_coarse=1000) -> int:
+        if precond_type == "chebyshev":
+            raise ValueError("the chebyshev preconditioner is not part of the cuda backend; use amgcl")
+        nl = C.c_int()
+        self._check("mm_build_poisson", lib().mm_build_poisson(self.h, float(reg), _abi.PRECOND[precond_type],
+                                                               int(max_levels), int(max_coarse), C.byref(nl)))
+        self.poisson_built = True
+        self.n_levels = nl.value
+        return nl.value
+
+    def amg_levels(self) -> list[dict]:
+        import scipy.sparse as sp
+
+        out = []
+        for lvl in range(self.n_levels):
+            n, nA, nP = C.c_int(), C.c_int64(), C.c_int64()
+            self._check("mm_amg_level_info", lib().mm_amg_level_info(self.h, lvl, C.byref(n), C.byref(nA), C.byref(nP)))
+            ptr, col, val = np.empty(n.value + 1, np.int32), np.empty(nA.value, np.int32), np.empty(nA.value)
+            agg = np.empty(n.value, np.int32)
+            self._check("mm_amg_export_level", lib().mm_amg_export_level(self.h, lvl, _abi.iptr(ptr), _abi.iptr(col),
+                                                                         dptr(val), _abi.iptr(agg)))
+            out.append(dict(A=sp.csr_matrix((val, col, ptr), shape=(n.value, n.value)), agg=agg,
+                            nnz_P=int(nP.value)))
+        return out
+
+    def apply_A(self, U):
+        U = f64(U)
+        y = np.empty(self.N)
+        self._check("mm_apply_A", lib().mm_apply_A(self.h, dptr(U), dptr(y)))
+        return y
+
+    def precond(self, r):
+        r = f64(r)
+        z = np.empty(self.N)
+        self._check("mm_precond", lib().mm_precond(self.h, dptr(r), dptr(z)))
+        return z
+
+    def rhs(self, m):
+        m = f64(m, (self.N, 3))
+        b = np.empty(self.N)
+        bb = C.c_double()
+        self._check("mm_rhs", lib().mm_rhs(self.h, dptr(m), dptr(b), C.byref(bb)))
+        return b, bb.value
+
+    def solve_u(self, m, x0, tol, maxiter=2000):
+        """(U, iterations, rel_res, status).  Torch CUDA tensors are solved in place, without copies."""
+        it, rr = C.c_int(), C.c_double()
+        if _is_torch_cuda(m):
+            U = x0 if _is_torch_cuda(x0) else None
+            if U is None:
+                raise TypeError("x0 must be a CUDA tensor when m is one")
+            rc = self._check("mm_solve_u_dev", lib().mm_solve_u_dev(self.h, C.c_void_p(m.data_ptr()),
+                                                                    C.c_void_p(U.data_ptr()), float(tol), int(maxiter),
+                                                                    C.byref(it), C.byref(rr)))
+            return U, it.value, rr.value, rc
+        m = f64(m, (self.N, 3))
+        U = f64(x0).reshape(-1).copy()
+        rc = self._check("mm_solve_u", lib().mm_solve_u(self.h, dptr(m), dptr(U), float(tol), int(maxiter),
+                                                        C.byref(it), C.byref(rr)))
+        return U, it.value, rr.value, rc
+
+    # -- energy ------------------------------------------------------------------------------------
+    def energy_and_grad(self, m, U, B_ext, B_bias=None):
+        B = f64(B_ext).reshape(3)
+        E = C.c_double()
+        if _is_torch_cuda(m):
+            import torch
+
+            g = torch.empty_like(m)
+            bias = None if B_bias is None else C.c_void_p(B_bias.data_ptr())
+            self._check("mm_energy_grad_dev", lib().mm_energy_grad_dev(self.h, C.c_void_p(m.data_ptr()),
+                                                                       C.c_void_p(U.data_ptr()), dptr(B), bias,
+                                                                       C.byref(E), C.c_void_p(g.data_ptr())))
+            return E.value, g
+        m = f64(m, (self.N, 3))
+        U = f64(U).reshape(-1)
+        bias = None if B_bias is None else f64(B_bias, (self.N, 3))
+        g = np.empty((self.N, 3))
+        self._check("mm_energy_grad", lib().mm_energy_grad(self.h, dptr(m), dptr(U), dptr(B), dptr(bias),
+                                                           C.byref(E), dptr(g)))
+        return E.value, g
+
+    def local_grad(self, v):
+        v = f64(v, (self.N, 3))
+        out = np.empty((self.N, 3))
+        self._check("mm_local_grad", lib().mm_local_grad(self.h, dptr(v), dptr(out)))
+        return out
+
+    def exchange_diagonal(self):
+        d = np.empty(self.N)
+        self._check("mm_exchange_diagonal", lib().mm_exchange_diagonal(self.h, dptr(d)))
+        return d
+
+    # -- minimizer ---------------------------------------------------------------------------------
+    def set_node_weights(self, inv_M_rel=None, inv_M_prec=None):
+        a = None if inv_M_rel is None else f64(inv_M_rel).reshape(-1)
+        b = None if inv_M_prec is None else f64(inv_M_prec).reshape(-1)
+        self._check("mm_set_node_weights", lib().mm_set_node_weights(self.h, dptr(a), dptr(b)))
+
+    def minimize(self, B_ext, m0, U0, params: MinimizerParams):
+        if not self.poisson_built:
+            raise RuntimeError("build_poisson() must be called before minimize()")
+        B = f64(B_ext).reshape(3)
+        m = f64(m0, (self.N, 3)).copy()
+        U = f64(U0).reshape(-1).copy()
+        info = _abi.MinInfo()
+        prm = params.to_c()
+        self._check("mm_minimize", lib().mm_minimize(self.h, dptr(B), dptr(m), dptr(U), C.byref(prm), C.byref(info)))
+        return m, U, dict(iters=info.iters, evals=info.evals, preco_iters=info.preco_iters,
+                          demag_iters=info.demag_iters, E=info.E, gnorm=info.gnorm, time=info.seconds,
+                          status=info.status)
+
+    def time_kernel(self, kernel: str, reps: int = 20):
+        """(mean ms per launch with L2 flushed before each, algorithmic bytes per launch)."""
+        ms, nb = C.c_double(), C.c_double()
+        self._check("mm_time_kernel", lib().mm_time_kernel(self.h, _abi.KERNELS[kernel], int(reps), C.byref(ms),
+                                                           C.byref(nb)))
+        return ms.value, nb.value
+
+    def last_solve_ms(self) -> float:
+        ms = C.c_double()
+        self._check("mm_last_solve_ms", lib().mm_last_solve_ms(self.h, C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check("mm_launch_count", lib().mm_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def sync(self):
+        self._check("mm_sync", lib().mm_sync(self.h))

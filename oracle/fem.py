@@ -247,14 +247,24 @@ def assemble_K_eff(p: Problem) -> sp.csr_matrix:
     return K
 
 
-def assembled_operators(p: Problem, reg=1e-12):
-    """A, D (blocked N x 3N), G (blocked 3N x N) and K_eff as ``src/loop.py:1089-1166,1199-1201`` builds them."""
-    A = assemble_poisson(p, reg=reg, with_boundary=p.boundary_mask is not None)
-    Dx, Dy, Dz = assemble_divergence(p)
-    D = sp.hstack([Dx, Dy, Dz]).tocsr()
-    N = p.N
-    G = sp.vstack([2.0 * D[:, :N].T, 2.0 * D[:, N:2 * N].T, 2.0 * D[:, 2 * N:].T]).tocsr()
-    return {"A": A, "D": D, "G": G, "K_eff": assemble_K_eff(p)}
+def assembled_operators(p: Problem, reg=1e-12, parts=("A", "D", "G", "K_eff")):
+    """A, D (blocked N x 3N), G (blocked 3N x N) and K_eff as ``src/loop.py:1089-1166,1199-1201`` builds them.
+
+    ``parts`` limits the work to what a caller needs (the Poisson solve needs A and D only).
+    """
+    out = {}
+    if "A" in parts:
+        out["A"] = assemble_poisson(p, reg=reg, with_boundary=p.boundary_mask is not None)
+    if "D" in parts or "G" in parts:
+        Dx, Dy, Dz = assemble_divergence(p)
+        D = sp.hstack([Dx, Dy, Dz]).tocsr()
+        out["D"] = D
+        if "G" in parts:
+            N = p.N
+            out["G"] = sp.vstack([2.0 * D[:, :N].T, 2.0 * D[:, N:2 * N].T, 2.0 * D[:, 2 * N:].T]).tocsr()
+    if "K_eff" in parts:
+        out["K_eff"] = assemble_K_eff(p)
+    return out
 
 
 def energy_and_grad_asm(p: Problem, ops, m, U, B_ext, B_bias=None):
@@ -290,3 +300,32 @@ def spai0_diagonal(A: sp.csr_matrix) -> np.ndarray:
     """M_ii = a_ii / sum_j a_ij^2, ``src/amg_utils.py:87-111``."""
     A2 = sp.csr_matrix((A.data**2, A.indices, A.indptr), shape=A.shape)
     return A.diagonal() / (np.asarray(A2.sum(axis=1)).ravel() + 1e-30)
+
+
+# --------------------------------------------------------------------------------------------
+# Morton reorder (src/reorder_mesh.py:19-30, 85-117)
+# --------------------------------------------------------------------------------------------
+def morton_encode(q: np.ndarray) -> np.ndarray:
+    """Interleave three 10-bit coordinates into a 30-bit key, ``src/reorder_mesh.py:19-30``."""
+    x, y, z = (q[:, i].astype(np.int64) for i in range(3))
+    code = np.zeros(q.shape[0], dtype=np.int64)
+    for i in range(10):
+        code |= ((x >> i) & 1) << (3 * i + 2)
+        code |= ((y >> i) & 1) << (3 * i + 1)
+        code |= ((z >> i) & 1) << (3 * i)
+    return code
+
+
+def morton_order(knt: np.ndarray, conn: np.ndarray):
+    """(node_perm, elem_perm) of ``reorder_mesh(target="gpu")``, ``src/reorder_mesh.py:85-100``.
+
+    The reference sorts with numpy's default (unstable) argsort; this restatement uses a stable
+    sort, which gives the same permutation whenever the keys are distinct.
+    """
+    knt = np.asarray(knt, np.float64)
+    lo, hi = knt.min(axis=0), knt.max(axis=0)
+    den = np.where(hi - lo == 0, 1.0, hi - lo)
+    node_perm = np.argsort(morton_encode(((knt - lo) / den * 1023).astype(np.int32)), kind="stable")
+    cen = np.mean(knt[np.asarray(conn)[:, :4].astype(np.int64)], axis=1)
+    elem_perm = np.argsort(morton_encode(((cen - lo) / den * 1023).astype(np.int32)), kind="stable")
+    return node_perm, elem_perm

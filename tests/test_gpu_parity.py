@@ -1,0 +1,163 @@
+"""GPU kernels (through the C-ABI) against the FP64 oracle.  Tolerances are stated per check:
+FP64 operators to 1e-10 relative (the reference's parity bar for energies and gradients), the
+potential to the PCG tolerance, integer work bit-exact."""
+
+import numpy as np
+import pytest
+
+from mumag_matrixfree2_gb300 import fem_utils
+from mumag_matrixfree2_gb300.cuda_backend import MinimizerParams
+from oracle import fem as ofem
+from oracle import minimize as omin
+from oracle import poisson as opo
+
+from .helpers import case, random_state
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10  # FP64 parity bar for energies, gradients and operator products
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def small(cuda_ok):
+    s, p, Js_ref = case("cube16_h2_air48")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    ops = ofem.assembled_operators(p)
+    return s, p, ops, prob
+
+
+def test_energy_and_gradient(small):
+    s, p, ops, prob = small
+    m = random_state(p.N, seed=1)
+    U = np.random.default_rng(2).standard_normal(p.N)
+    B = np.array([0.1, -0.05, -0.3])
+    E, g = prob.energy_and_grad(m, U, B)
+    E0, g0 = ofem.energy_and_grad_asm(p, ops, m, U, B)
+    assert abs(E - E0) <= RTOL * abs(E0)
+    assert rel(g, g0) <= RTOL
+    bias = 0.01 * np.random.default_rng(3).standard_normal((p.N, 3))
+    E, g = prob.energy_and_grad(m, U, B, bias)
+    E0, g0 = ofem.energy_and_grad_asm(p, ops, m, U, B, bias)
+    assert abs(E - E0) <= RTOL * abs(E0) and rel(g, g0) <= RTOL
+
+
+def test_energy_multi_axis(cuda_ok):
+    s, p, _ = case("cube8_h2_air24", tilt_axis=True)
+    prob = fem_utils.make_problem(s)
+    ops = ofem.assembled_operators(p)
+    m = random_state(p.N, seed=4)
+    U = np.random.default_rng(5).standard_normal(p.N)
+    E, g = prob.energy_and_grad(m, U, [0.0, 0.0, 0.2])
+    E0, g0 = ofem.energy_and_grad_mf(p, m, U, [0.0, 0.0, 0.2])
+    assert abs(E - E0) <= RTOL * abs(E0) and rel(g, g0) <= RTOL
+
+
+def test_local_hessian_rhs_and_diagonal(small):
+    s, p, ops, prob = small
+    v = np.random.default_rng(6).standard_normal((p.N, 3))
+    assert rel(prob.local_grad(v), ofem.local_grad_only_asm(p, ops, v)) <= RTOL
+    m = random_state(p.N, seed=7)
+    b, bb = prob.rhs(m)
+    b0 = ofem.rhs_from_m_asm(ops, m)
+    assert rel(b, b0) <= RTOL and abs(bb - b0 @ b0) <= RTOL * (b0 @ b0)
+    assert rel(prob.exchange_diagonal(), ofem.exchange_diagonal(p)) <= RTOL
+
+
+def test_poisson_operator_and_vcycle(small):
+    s, p, ops, prob = small
+    U = np.random.default_rng(8).standard_normal(p.N)
+    assert rel(prob.apply_A(U), ops["A"] @ U) <= RTOL
+    H = opo.build_hierarchy(ops["A"])
+    r = np.random.default_rng(9).standard_normal(p.N)
+    z0 = opo.vcycle_spai0(H, lambda v: ops["A"] @ v, r)
+    assert rel(prob.precond(r), z0) <= 1e-9
+
+
+@pytest.mark.parametrize("precond", ["amgcl", "amg", "jacobi", "none"])
+def test_solve_matches_oracle(cuda_ok, precond):
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, precond)
+    su = opo.SolveU(p, precond_type=precond, cg_tol=1e-10)
+    m = random_state(p.N, seed=10)
+    U0, it0, rr0 = su(m, np.zeros(p.N), 1e-10, return_info=True)
+    U, it, rr, rc = prob.solve_u(m, np.zeros(p.N), 1e-10)
+    assert rc == 0 and rr <= 1e-10
+    assert abs(it - it0) <= 1, (it, it0)
+    assert rel(U, U0) <= 1e-8
+    # warm start from the converged potential of a nearby state
+    m2 = random_state(p.N, seed=11, amplitude=0.31)
+    U0b, it0b, _ = su(m2, U0, 1e-10, return_info=True)
+    Ub, itb, rrb, _ = prob.solve_u(m2, U, 1e-10)
+    assert abs(itb - it0b) <= 1 and rrb <= 1e-10 and rel(Ub, U0b) <= 1e-8
+
+
+def test_solve_cfg_mesh_and_determinism(cuda_ok):
+    s, p, _ = case("cube40_h2_air200")
+    prob = fem_utils.make_problem(s)
+    nl = prob.build_poisson(1e-12, "amgcl")
+    assert nl == 3
+    su = opo.SolveU(p, ofem.assembled_operators(p, parts=("A", "D")), cg_tol=1e-10)
+    m = random_state(p.N, seed=12, amplitude=0.05)
+    U0, it0, rr0 = su(m, np.zeros(p.N), 1e-10, return_info=True)
+    U1, it1, rr1, _ = prob.solve_u(m, np.zeros(p.N), 1e-10)
+    U2, it2, rr2, _ = prob.solve_u(m, np.zeros(p.N), 1e-10)
+    assert abs(it1 - it0) <= 1 and rr1 <= 1e-10
+    assert rel(U1, U0) <= 1e-8
+    assert it1 == it2 and np.array_equal(U1, U2)  # fixed grids and fixed reduction trees
+
+
+def test_solve_without_mask_projects_the_mean(cuda_ok):
+    s, p, _ = case("cube8_h2_air24", with_boundary=False)
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    su = opo.SolveU(p, cg_tol=1e-9)
+    m = random_state(p.N, seed=13)
+    U0, it0, _ = su(m, np.zeros(p.N), 1e-9, return_info=True)
+    U, it, rr, _ = prob.solve_u(m, np.zeros(p.N), 1e-9)
+    assert abs(it - it0) <= 1 and abs(U.mean()) < 1e-12 * np.abs(U).max()
+    assert rel(U, U0) <= 1e-6
+
+
+def test_maxiter_is_reported(cuda_ok):
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    U, it, rr, rc = prob.solve_u(random_state(p.N, seed=14), np.zeros(p.N), 1e-14, maxiter=2)
+    assert it == 2 and rc == 1 and rr > 1e-14
+
+
+def _oracle_ops(p, ops, su):
+    d = ofem.exchange_diagonal(p)
+    return omin.Ops(
+        energy_and_grad=lambda m, U, B: ofem.energy_and_grad_asm(p, ops, m, U, B),
+        local_grad_only=lambda v: ofem.local_grad_only_asm(p, ops, v),
+        solve_U=lambda m, x0, tol: su(m, x0, tol, return_info=True),
+        inv_M_rel=np.where(p.M_nodal > 1e-20, p.V_mag / np.where(p.M_nodal > 0, p.M_nodal, 1), 0.0)[:, None],
+        inv_M_prec=np.where(d > 1e-20, 1.0 / np.where(d > 0, d, 1), 1.0)[:, None],
+    )
+
+
+@pytest.mark.parametrize("method", ["pcohen_hs", "lbfgs", "wg_np"])
+def test_minimizer_matches_oracle(cuda_ok, method):
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    ops = ofem.assembled_operators(p)
+    su = opo.SolveU(p, ops, cg_tol=1e-10)
+    O = _oracle_ops(p, ops, su)
+    m0 = random_state(p.N, seed=15, amplitude=0.2)
+    B = np.array([0.0, 0.0, -0.3])
+    prm = omin.Params(max_iter=12, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+    m_ref, U_ref, info_ref = omin.minimize(O, m0, B, np.zeros(p.N), prm, method)
+    mp = MinimizerParams(method=method, max_iter=12, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+    m, U, info = prob.minimize(B, m0, np.zeros(p.N), mp)
+    assert info["iters"] == info_ref["iters"]
+    assert info["evals"] == info_ref["evals"]
+    assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
+    assert np.max(np.abs(m - m_ref)) <= 1e-7
