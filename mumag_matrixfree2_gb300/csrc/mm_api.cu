@@ -54,28 +54,15 @@ int pick_tpr(int64_t nnz, int64_t rows) {
   return 32;
 }
 
-struct DevMat {
-  int n_rows = 0, n_cols = 0;
-  int64_t nnz = 0;
-  int* ptr = nullptr;
-  int* col = nullptr;
-  double* val = nullptr;
-  int tpr = 4;
-};
-
-struct DevLevel {
-  DevMat A, P, R;
-  double* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
-  double* b = nullptr;    // right-hand side of this level (levels >= 1)
-  double* x = nullptr;    // iterate (pre-smoothing, prolongation)
-  double* x2 = nullptr;   // post-smoothed iterate (levels >= 1)
-  double* res = nullptr;  // residual
-  int n = 0;
+// sliced ELL with slice height 32, built from a CSR with sorted columns (padding: value 0, own row
+// index as column, so padded lanes read a valid address)
+struct DevSell {
+  mmk::Sell s{};
+  int64_t nnz = 0;     // stored non-zeros (without padding)
+  int64_t stored = 0;  // entries including padding
 };
 
 thread_local std::string g_create_error;
-
-enum Slot { SL_BB0, SL_BB, SL_R2, SL_RZ, SL_PAP, SL_SUM, SL_E, SL_MAX, SL_A, SL_B, SL_C, SL_D, NSLOTS };
 
 }  // namespace
 
@@ -108,15 +95,28 @@ struct mm_problem {
   int precond = MM_PRECOND_AMGCL;
   double reg = 1e-12;
   std::vector<mm::AmgLevel> amg_h;
-  std::vector<DevLevel> lv;
+  struct Level {
+    DevSell A, P, R;
+    double* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
+    double* b = nullptr;    // right-hand side (levels >= 1)
+    double* x = nullptr;    // iterate (pre-smoothing, prolongation)
+    double* x2 = nullptr;   // post-smoothed iterate (levels >= 1)
+    double* res = nullptr;  // residual
+    int n = 0;
+  };
+  std::vector<Level> lv;
   double* d_Ainv = nullptr;
   int n_coarse = 0;
   double* d_jac = nullptr;  // Jacobi preconditioner 1/(diag+eps)
-  double *d_b = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_Ap = nullptr;
-  double* d_part = nullptr;
+  double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_Ap = nullptr;
+  double* d_part = nullptr;      // NRED x MAXG block partials
   mmk::Scalars* d_sc = nullptr;
   mmk::Scalars* h_sc = nullptr;  // pinned
-  double* h_part = nullptr;      // pinned, MAXG * 2
+  // the PCG iteration loop as a graph with a conditional WHILE node
+  cudaGraph_t loop_graph = nullptr;
+  cudaGraphExec_t loop_exec = nullptr;
+  bool graph_failed = false;
+  int64_t iter_launches = 0;  // kernels in one loop trip
 
   // staging buffers for host-pointer calls
   double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
@@ -128,8 +128,6 @@ struct mm_problem {
          *w_graw = nullptr, *w_r3 = nullptr, *w_z3 = nullptr, *w_p3 = nullptr, *w_Ap3 = nullptr,
          *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr;
   std::vector<double*> w_S, w_Y;
-
-  double* part(Slot s) const { return d_part + (size_t)s * MAXG; }
 
   template <class T>
   T* alloc(size_t n) {
@@ -145,16 +143,47 @@ struct mm_problem {
     if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
   }
-  DevMat upload(const mm::HostCSR& A) {
-    DevMat d;
-    d.n_rows = A.n_rows;
-    d.n_cols = A.n_cols;
+  DevSell upload_sell(const mm::HostCSR& A) {
+    const int n = A.n_rows;
+    const int ns = (n + 31) / 32;
+    std::vector<int> sptr(ns + 1, 0);
+    for (int s = 0; s < ns; ++s) {
+      int w = 0;
+      for (int r = 32 * s; r < std::min(n, 32 * s + 32); ++r) w = std::max(w, A.ptr[r + 1] - A.ptr[r]);
+      sptr[s + 1] = sptr[s] + 32 * w;
+    }
+    std::vector<int> col(sptr[ns]);
+    std::vector<double> val(sptr[ns], 0.0);
+    for (int s = 0; s < ns; ++s) {
+      const int w = (sptr[s + 1] - sptr[s]) / 32;
+      for (int l = 0; l < 32; ++l) {
+        const int r = 32 * s + l;
+        const int len = r < n ? A.ptr[r + 1] - A.ptr[r] : 0;
+        for (int k = 0; k < w; ++k) {
+          const size_t at = (size_t)sptr[s] + 32 * k + l;
+          if (k < len) {
+            col[at] = A.col[A.ptr[r] + k];
+            val[at] = A.val[A.ptr[r] + k];
+          } else {
+            col[at] = r < n ? std::min(r, std::max(A.n_cols - 1, 0)) : 0;
+            val[at] = 0.0;
+          }
+        }
+      }
+    }
+    DevSell d;
+    d.s.n = n;
+    d.s.sptr = upload(sptr);
+    d.s.col = upload(col);
+    d.s.val = upload(val);
     d.nnz = A.nnz();
-    d.ptr = upload(A.ptr);
-    d.col = upload(A.col);
-    d.val = upload(A.val);
-    d.tpr = pick_tpr(d.nnz, d.n_rows);
+    d.stored = sptr[ns];
     return d;
+  }
+  double red(int slot) {
+    CK(cudaMemcpyAsync(&h_sc->red[slot], &d_sc->red[slot], sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return h_sc->red[slot];
   }
   void sync() { CK(cudaStreamSynchronize(st)); }
 };
@@ -163,6 +192,19 @@ struct mm_problem {
 // launch helpers
 // =============================================================================================
 namespace {
+
+using mmk::R_A;
+using mmk::R_B;
+using mmk::R_BB;
+using mmk::R_BB0;
+using mmk::R_C;
+using mmk::R_D;
+using mmk::R_E;
+using mmk::R_MAX;
+using mmk::R_PAP;
+using mmk::R_R2;
+using mmk::R_RZ;
+using mmk::R_SUM;
 
 #define TPR_SWITCH(tpr, ...)                         \
   switch (tpr) {                                     \
@@ -174,95 +216,16 @@ namespace {
   }
 
 template <int MODE>
-void spmv(mm_problem* h, const DevMat& A, const double* x, const double* b, const double* s, double* y,
+void sell(mm_problem* h, const DevSell& A, const double* x, const double* b, const double* s, double* y,
           const int* done) {
-  const int g = grid_rows(A.n_rows, A.tpr);
-  TPR_SWITCH(A.tpr, (mmk::k_spmv<T, MODE><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, x, b, s, y, done)));
+  mmk::k_sell<MODE><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
   LAUNCH_CHECK();
 }
 
-double host_sum(mm_problem* h, Slot s, int count) {
-  CK(cudaMemcpyAsync(h->h_part, h->part(s), count * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  h->sync();
-  double v = 0.0;
-  for (int i = 0; i < count; ++i) v += h->h_part[i];
-  return v;
+void dot(mm_problem* h, int n, const double* x, const double* y, int slot) {
+  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, x, y, h->d_sc, h->d_part, slot);
+  LAUNCH_CHECK();
 }
-
-double host_max(mm_problem* h, Slot s, int count) {
-  CK(cudaMemcpyAsync(h->h_part, h->part(s), count * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  h->sync();
-  double v = 0.0;
-  for (int i = 0; i < count; ++i) v = std::max(v, h->h_part[i]);
-  return v;
-}
-
-
-}  // namespace
-
-namespace mmk {
-__global__ void __launch_bounds__(BS) k_mul(int n, const double* __restrict__ s, const double* __restrict__ r,
-                                            double* __restrict__ out) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = s[i] * r[i];
-}
-
-// r = b - A x ; partial r.r ; xv = s .* r
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_init_residual(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                      const double* __restrict__ val, const double* __restrict__ x,
-                                                      const double* __restrict__ b, double* __restrict__ r,
-                                                      const double* __restrict__ s, double* __restrict__ xv,
-                                                      double* __restrict__ part) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  double d = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double ax = row_dot<TPR>(ptr, col, val, x, row, valid, lane);
-    if (valid && lane == 0) {
-      const double ri = b[row] - ax;
-      r[row] = ri;
-      d = fma(ri, ri, d);
-      if (s) xv[row] = s[row] * ri;
-    }
-  }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
-}
-
-__global__ void k_finalize_solve(Scalars* sc, const double* __restrict__ part_r2, int n_r2,
-                                 const double* __restrict__ part_bb0, int n_bb0, double* out2) {
-  const double r2 = reduce_partials(part_r2, n_r2);
-  const double bb = reduce_partials(part_bb0, n_bb0);
-  if (threadIdx.x == 0) {
-    out2[0] = r2;
-    out2[1] = bb;
-  }
-}
-
-// partials of a.(b - c) and d.(b - c)
-__global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict__ a, const double* __restrict__ d,
-                                                 const double* __restrict__ b, const double* __restrict__ c,
-                                                 double* __restrict__ pa, double* __restrict__ pd) {
-  double s1 = 0.0, s2 = 0.0;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
-    const double df = b[i] - c[i];
-    s1 = fma(a[i], df, s1);
-    s2 = fma(d[i], df, s2);
-  }
-  s1 = block_sum(s1);
-  s2 = block_sum(s2);
-  if (threadIdx.x == 0) {
-    pa[blockIdx.x] = s1;
-    pd[blockIdx.x] = s2;
-  }
-}
-
-// y = P_m(y) for every history vector (L-BFGS transport) is k_tangent in place
-}  // namespace mmk
-
-namespace {
 
 // ---------------------------------------------------------------------------------------------
 // V-cycle (enqueue only).  Level 0's pre-smoothed iterate lv[0].x must already hold s0 .* r.
@@ -271,217 +234,207 @@ namespace {
 void enqueue_vcycle(mm_problem* h, const double* r, double* z, bool in_loop, const int* done) {
   auto& lv = h->lv;
   const int L = (int)lv.size();
-  if (L == 1) {
-    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, done);
-    LAUNCH_CHECK();
-    mmk::k_dot<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, r, z, h->part(SL_RZ));
-    LAUNCH_CHECK();
-    return;
-  }
-  // descend
   for (int l = 0; l < L - 1; ++l) {
-    DevLevel& c = lv[l];
+    auto& c = lv[l];
     if (l == 0) {
       if (in_loop) {
-        const int g = grid_rows(c.A.n_rows, c.A.tpr);
-        TPR_SWITCH(c.A.tpr, (mmk::k_vc_residual0<T><<<g, BS, 0, h->st>>>(
-                                c.A.n_rows, c.A.ptr, c.A.col, c.A.val, c.x, r, c.res, h->part(SL_R2),
-                                grid_elem(h->N), h->d_sc)));
+        mmk::k_vc_residual0<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, h->d_sc);
         LAUNCH_CHECK();
       } else {
-        spmv<1>(h, c.A, c.x, r, nullptr, c.res, done);
+        sell<1>(h, c.A, c.x, r, nullptr, c.res, done);
       }
     } else {
-      spmv<1>(h, c.A, c.x, c.b, nullptr, c.res, done);
+      sell<1>(h, c.A, c.x, c.b, nullptr, c.res, done);
     }
-    DevLevel& nx = lv[l + 1];
+    auto& nx = lv[l + 1];
     const bool coarsest = (l + 1 == L - 1);
-    const int g = grid_rows(c.R.n_rows, c.R.tpr);
-    TPR_SWITCH(c.R.tpr, (mmk::k_restrict<T><<<g, BS, 0, h->st>>>(c.R.n_rows, c.R.ptr, c.R.col, c.R.val, c.res, nx.b,
-                                                                  coarsest ? nullptr : nx.s, nx.x, done)));
+    mmk::k_restrict<<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x, done);
     LAUNCH_CHECK();
   }
-  // coarsest
   {
-    DevLevel& c = lv[L - 1];
+    auto& c = lv[L - 1];
     mmk::k_dense_mv<<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, h->d_Ainv, c.b, c.x2, done);
     LAUNCH_CHECK();
   }
-  // ascend
   for (int l = L - 2; l >= 0; --l) {
-    DevLevel& c = lv[l];
-    const double* e = lv[l + 1].x2;
-    spmv<3>(h, c.P, e, c.x, nullptr, c.x, done);  // x += P e
+    auto& c = lv[l];
+    sell<3>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
     const double* bl = (l == 0) ? r : c.b;
     double* out = (l == 0) ? z : c.x2;
-    const int g = grid_rows(c.A.n_rows, c.A.tpr);
-    TPR_SWITCH(c.A.tpr, (mmk::k_smooth_dot<T><<<g, BS, 0, h->st>>>(c.A.n_rows, c.A.ptr, c.A.col, c.A.val, c.x, bl, c.s,
-                                                                    out, l == 0 ? h->part(SL_RZ) : nullptr, done)));
+    mmk::k_smooth_dot<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, bl, c.s, out, h->d_sc,
+                                                         l == 0 ? h->d_part : nullptr, done);
     LAUNCH_CHECK();
   }
 }
 
-// number of r.z partials written by the preconditioner (k_smooth_dot on level 0, else k_dot)
-int rz_count(mm_problem* h) {
-  const bool amg = h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL;
-  if (amg && h->lv.size() > 1) return grid_rows(h->lv[0].A.n_rows, h->lv[0].A.tpr);
-  return grid_elem(h->N);
+bool amg_multilevel(mm_problem* h) {
+  return (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) && h->lv.size() > 1;
 }
 
-// preconditioner application z = M^-1 r outside the PCG loop; writes the r.z partials to SL_RZ
-void enqueue_precond(mm_problem* h, const double* r, double* z) {
-  const int N = h->N;
-  if (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) {
-    if (h->lv.size() > 1) {
-      mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->lv[0].s, r, h->lv[0].x);
-      LAUNCH_CHECK();
-    }
-    enqueue_vcycle(h, r, z, false, nullptr);
-  } else {
-    if (h->precond == MM_PRECOND_JACOBI) {
-      mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_jac, r, z);
-    } else {
-      CK(cudaMemcpyAsync(z, r, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-    }
-    LAUNCH_CHECK();
-    mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, r, z, h->part(SL_RZ));
-    LAUNCH_CHECK();
-  }
-}
-
-// z = M^-1 r for Jacobi / no preconditioner / a one-level hierarchy (dense solve); r.z partials in SL_RZ
-void apply_M_simple(mm_problem* h, const double* r, double* z) {
+// z = M^-1 r for Jacobi / no preconditioner / a one-level hierarchy (dense solve); r.z -> red[R_RZ]
+void apply_M_simple(mm_problem* h, const double* r, double* z, const int* done) {
   const int N = h->N;
   if (h->precond == MM_PRECOND_JACOBI) {
     mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_jac, r, z);
+    LAUNCH_CHECK();
   } else if (h->precond == MM_PRECOND_NONE) {
     CK(cudaMemcpyAsync(z, r, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   } else {
-    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, nullptr);
+    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, done);
+    LAUNCH_CHECK();
   }
-  LAUNCH_CHECK();
-  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, r, z, h->part(SL_RZ));
-  LAUNCH_CHECK();
+  dot(h, N, r, z, R_RZ);
 }
 
-// one PCG iteration for the non-AMG preconditioners (host-free scalars as in the AMG path)
-void enqueue_simple_iteration(mm_problem* h, double* x, bool first) {
-  const int N = h->N;
-  const DevMat& A = h->lv[0].A;
-  const int g = grid_rows(A.n_rows, A.tpr);
-  TPR_SWITCH(A.tpr, (mmk::k_pcg_dir<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_z, h->d_p, h->d_Ap,
-                                                             h->part(SL_RZ), grid_elem(N), h->part(SL_R2),
-                                                             grid_elem(N), h->part(SL_PAP), h->d_sc, first)));
-  LAUNCH_CHECK();
-  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_r, h->d_p, h->d_Ap, nullptr, nullptr, h->part(SL_PAP),
-                                                   g, h->part(SL_RZ), grid_elem(N), h->part(SL_R2), h->d_sc);
-  LAUNCH_CHECK();
-  // z = M^-1 r; the following k_pcg_dir re-tests convergence before it uses z
-  apply_M_simple(h, h->d_r, h->d_z);
+// preconditioner application outside the PCG loop
+void enqueue_precond(mm_problem* h, const double* r, double* z) {
+  if (amg_multilevel(h)) {
+    mmk::k_mul<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, h->lv[0].s, r, h->lv[0].x);
+    LAUNCH_CHECK();
+    enqueue_vcycle(h, r, z, false, nullptr);
+  } else {
+    apply_M_simple(h, r, z, nullptr);
+  }
 }
 
-void enqueue_amg_iteration(mm_problem* h, double* x, bool first) {
+// one PCG iteration on x = d_x (all scalars stay on the device)
+void enqueue_iteration(mm_problem* h) {
   const int N = h->N;
-  DevLevel& l0 = h->lv[0];
-  const DevMat& A = l0.A;
-  const int g = grid_rows(A.n_rows, A.tpr);
-  const int n_rz = rz_count(h);
-  TPR_SWITCH(A.tpr, (mmk::k_pcg_dir<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_z, h->d_p, h->d_Ap,
-                                                             h->part(SL_RZ), n_rz, h->part(SL_R2), grid_elem(N),
-                                                             h->part(SL_PAP), h->d_sc, first)));
+  auto& l0 = h->lv[0];
+  mmk::k_pcg_dir<<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, h->d_z, h->d_p, h->d_Ap, h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_r, h->d_p, h->d_Ap, h->lv.size() > 1 ? l0.s : nullptr,
-                                                   l0.x, h->part(SL_PAP), g, h->part(SL_RZ), n_rz, h->part(SL_R2),
-                                                   h->d_sc);
+  const bool ml = amg_multilevel(h);
+  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_x, h->d_r, h->d_p, h->d_Ap, ml ? l0.s : nullptr, l0.x,
+                                                   h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  enqueue_vcycle(h, h->d_r, h->d_z, true, &h->d_sc->done);
+  if (ml) enqueue_vcycle(h, h->d_r, h->d_z, true, &h->d_sc->done);
+  else apply_M_simple(h, h->d_r, h->d_z, &h->d_sc->done);
 }
 
-// PCG on device buffers: b already in h->d_b with raw b.b partials in SL_BB0.
-int run_pcg(mm_problem* h, double* x, double tol, int maxiter, int* iters, double* rel_res) {
+// Build the loop graph: WHILE (condition) { iteration; k_set_cond }.  Returns false when the
+// driver cannot build conditional graphs (the host-polled loop is used then).
+bool build_loop_graph(mm_problem* h) {
+  if (h->loop_exec) return true;
+  if (h->graph_failed) return false;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  cudaGraphConditionalHandle hnd;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t node;
+  if (ok) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hnd;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      const int64_t saved = h->n_launch;
+      try {
+        enqueue_iteration(h);
+        mmk::k_set_cond<<<1, 32, 0, h->st>>>(hnd, h->d_sc);
+      } catch (const Fail&) {
+        ok = false;
+      }
+      h->iter_launches = h->n_launch - saved + 1;
+      h->n_launch = saved;
+      cudaGraph_t out = nullptr;
+      const bool end_ok = cudaStreamEndCapture(h->st, &out) == cudaSuccess;
+      ok = ok && end_ok;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();  // clear a sticky-free error from the failed attempt
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    h->graph_failed = true;
+    return false;
+  }
+  h->loop_graph = g;
+  h->loop_exec = ex;
+  return true;
+}
+
+// PCG on device buffers: x = d_x (initial guess in, solution out), b in d_b with b.b in red[R_BB0].
+int run_pcg(mm_problem* h, double tol, int maxiter, int* iters, double* rel_res) {
   const int N = h->N;
+  double* x = h->d_x;
   const bool zero_mean = !h->has_mask;
-  const bool amg = (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL);
   if (zero_mean) {
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->part(SL_SUM));
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->part(SL_SUM), grid_elem(N));
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, R_SUM);
     LAUNCH_CHECK();
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM));
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM), grid_elem(N));
-    LAUNCH_CHECK();
-  }
-  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, nullptr, h->part(SL_BB));
-  LAUNCH_CHECK();
-  mmk::k_pcg_init_scalars<<<1, BS, 0, h->st>>>(h->d_sc, h->part(SL_BB), grid_elem(N), tol, maxiter);
-  LAUNCH_CHECK();
-  // r = b - A x, r.r, level-0 pre-smoothing; z = M^-1 r
-  const DevMat& A = h->lv[0].A;
-  {
-    const int g = grid_rows(A.n_rows, A.tpr);
-    const bool presmooth = amg && h->lv.size() > 1;
-    // the r.r partials must be laid out like k_pcg_step's (grid_elem(N) blocks): reduce via k_dot
-    TPR_SWITCH(A.tpr, (mmk::k_init_residual<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, x, h->d_b, h->d_r,
-                                                                      presmooth ? h->lv[0].s : nullptr, h->lv[0].x,
-                                                                      h->part(SL_A))));
-    LAUNCH_CHECK();
-    mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_r, nullptr, h->part(SL_R2));
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
     LAUNCH_CHECK();
   }
-  if (amg && h->lv.size() > 1) enqueue_vcycle(h, h->d_r, h->d_z, false, nullptr);
-  else apply_M_simple(h, h->d_r, h->d_z);
-  int it_block = 4;
-  for (int i = 0;; ++i) {
-    if (amg && h->lv.size() > 1) {
-      enqueue_amg_iteration(h, x, i == 0);
-    } else {
-      enqueue_simple_iteration(h, x, i == 0);
-    }
-    if ((i + 1) % it_block == 0 || i == 0) {
-      CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
-      h->sync();
-      if (h->h_sc->done) break;
-      if (i > maxiter + 8) break;
+  dot(h, N, h->d_b, nullptr, R_BB);
+  mmk::k_pcg_init_scalars<<<1, 32, 0, h->st>>>(h->d_sc, tol, maxiter);
+  LAUNCH_CHECK();
+  const bool ml = amg_multilevel(h);
+  auto& l0 = h->lv[0];
+  mmk::k_init_residual<<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, x, h->d_b, h->d_r, ml ? l0.s : nullptr, l0.x, h->d_sc,
+                                                        h->d_part);
+  LAUNCH_CHECK();
+  if (ml) enqueue_vcycle(h, h->d_r, h->d_z, false, nullptr);
+  else apply_M_simple(h, h->d_r, h->d_z, nullptr);
+  if (build_loop_graph(h)) {
+    CK(cudaGraphLaunch(h->loop_exec, h->st));
+    h->n_launch += h->iter_launches;  // counted per trip below, once the trip count is known
+  } else {
+    for (int i = 0;; ++i) {
+      enqueue_iteration(h);
+      if ((i + 1) % 4 == 0) {
+        CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+        h->sync();
+        if (h->h_sc->done || i > maxiter + 8) break;
+      }
     }
   }
   if (zero_mean) {
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM));
+    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->part(SL_SUM), grid_elem(N));
+    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
     LAUNCH_CHECK();
   }
-  double* d_out2 = h->part(SL_D);
-  mmk::k_finalize_solve<<<1, BS, 0, h->st>>>(h->d_sc, h->part(SL_R2), grid_elem(N), h->part(SL_BB0), grid_elem(h->N),
-                                              d_out2);
-  LAUNCH_CHECK();
-  double out2[2];
-  CK(cudaMemcpyAsync(out2, d_out2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   h->sync();
+  if (h->loop_exec) h->n_launch += (int64_t)(h->h_sc->loops - 1) * h->iter_launches;
   if (iters) *iters = h->h_sc->it;
-  const double rr = std::sqrt(out2[0] / (out2[1] + 1e-30));
+  const double r2 = h->h_sc->red[R_R2], bb = h->h_sc->red[R_BB0];
+  const double rr = std::sqrt(r2 / (bb + 1e-30));
   if (rel_res) *rel_res = rr;
   if (!std::isfinite(rr)) return MM_NONFINITE;
-  return (h->h_sc->it >= maxiter && out2[0] > h->h_sc->tol2) ? MM_MAXITER : MM_OK;
+  return (h->h_sc->it >= maxiter && r2 > h->h_sc->tol2) ? MM_MAXITER : MM_OK;
 }
 
-// b = D m on device (magnetic rows), raw b.b partials in SL_BB0
+// b = D m on device (magnetic rows), b.b -> red[R_BB0]
 void enqueue_rhs(mm_problem* h, const double* m) {
   const int N = h->N;
   if (!h->has_mask) CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
   const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<T><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b, nullptr)));
+  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<T><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b)));
   LAUNCH_CHECK();
-  mmk::k_dot<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, nullptr, h->part(SL_BB0));
-  LAUNCH_CHECK();
+  dot(h, N, h->d_b, nullptr, R_BB0);
 }
 
+// demag solve with the potential in d_U (in/out)
 int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters, double* rel_res) {
   if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called before a solve"};
   CK(cudaEventRecord(h->ev0, h->st));
+  if (d_U != h->d_x) CK(cudaMemcpyAsync(h->d_x, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   enqueue_rhs(h, d_m);
-  const int rc = run_pcg(h, d_U, tol, maxiter, iters, rel_res);
+  const int rc = run_pcg(h, tol, maxiter, iters, rel_res);
+  if (d_U != h->d_x) CK(cudaMemcpyAsync(d_U, h->d_x, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   CK(cudaEventRecord(h->ev1, h->st));
   CK(cudaEventSynchronize(h->ev1));
   float ms = 0.f;
@@ -494,9 +447,10 @@ double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const dou
                   double* d_g) {
   const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
   TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
-                                                                      d_bias, h->inv_Vmag, d_g, h->part(SL_E))));
+                                                                      d_bias, h->inv_Vmag, d_g, h->d_sc,
+                                                                      h->d_part)));
   LAUNCH_CHECK();
-  return 0.5 * host_sum(h, SL_E, g) * h->inv_Vmag;
+  return 0.5 * h->red(R_E) * h->inv_Vmag;
 }
 
 void local_grad_dev(mm_problem* h, const double* d_v, double* d_out) {
@@ -511,12 +465,14 @@ int guarded(mm_problem* h, F&& f) {
     return f();
   } catch (const Fail& e) {
     if (h) h->err = e.msg;
+    else g_create_error = e.msg;
     return e.code;
   } catch (const std::bad_alloc&) {
     if (h) h->err = "host allocation failed";
     return MM_ERR_OOM;
   } catch (const std::exception& e) {
     if (h) h->err = e.what();
+    else g_create_error = e.what();
     return MM_ERR_SETUP;
   }
 }
@@ -561,15 +517,14 @@ void ensure_min_buffers(mm_problem* h, int memory) {
 }
 
 double dev_dot(mm_problem* h, int n, const double* a, const double* b) {
-  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, a, b, h->part(SL_A));
-  LAUNCH_CHECK();
-  return host_sum(h, SL_A, grid_elem(n));
+  dot(h, n, a, b, R_A);
+  return h->red(R_A);
 }
 
 double dev_absmax(mm_problem* h, int n, const double* a) {
-  mmk::k_absmax<<<grid_elem(n), BS, 0, h->st>>>(n, a, h->part(SL_MAX));
+  mmk::k_absmax<<<grid_elem(n), BS, 0, h->st>>>(n, a, h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  return host_max(h, SL_MAX, grid_elem(n));
+  return h->red(R_MAX);
 }
 
 // energy + gradient of (m, U) into g, E returned
@@ -593,10 +548,10 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   const int ge = grid_elem(N);
   CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
   CK(cudaMemcpyAsync(h->w_r3, gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->part(SL_B));
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
   LAUNCH_CHECK();
   CK(cudaMemcpyAsync(h->w_p3, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  double rho = host_sum(h, SL_B, ge);
+  double rho = h->red(R_B);
   const double target = tol * tol * rho;
   double Q = 0.0;
   int it = 0;
@@ -604,18 +559,18 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
   while (it < c.prm->pc_iters && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
     TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<T><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, c.prm->pc_reg,
-                                                                     h->inv_Vmag, h->w_Ap3, h->part(SL_C))));
+                                                                     h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part, R_C)));
     LAUNCH_CHECK();
-    const double pAp = host_sum(h, SL_C, gP);
+    const double pAp = h->red(R_C);
     const bool neg = pAp <= 0.0;
     const double alpha = rho / (pAp + 1e-30);
     const double dq = 0.5 * alpha * rho;
     const bool stag = (it > 0) && (dq <= c.prm->pc_stagnation_nu * Q);
     done = neg || stag;
     mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, alpha, y, h->w_r3, h->w_p3, h->w_Ap3, h->d_inv_M_prec, h->w_z3,
-                                             h->part(SL_B), done ? 0 : 1);
+                                             h->d_sc, h->d_part, R_B, done ? 0 : 1);
     LAUNCH_CHECK();
-    const double rho_next = host_sum(h, SL_B, ge);
+    const double rho_next = h->red(R_B);
     if (!done) {
       mmk::k_xpay<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
       LAUNCH_CHECK();
@@ -626,7 +581,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   }
   // fallback direction, clipping, descent check
   // z_fb = gte .* inv_M_prec  (into w_z3)
-  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_z3, h->part(SL_B));
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
   LAUNCH_CHECK();
   const double yn = std::sqrt(dev_dot(h, n3, y, nullptr));
   const double zn = std::sqrt(dev_dot(h, n3, h->w_z3, nullptr));
@@ -727,9 +682,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
   LAUNCH_CHECK();
   c.demag += demag_solve(c, m, U, prm->cg_tol);
   double E = eval(c, m, U, graw);
-  mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->part(SL_MAX));
+  mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  double gnorm = host_max(h, SL_MAX, ge);
+  double gnorm = h->red(R_MAX);
   c.evals = 1;
   // state: g (previous g_tan_ext or g_tan), y, d
   CK(cudaMemcpyAsync(h->w_gprev, prm->method == MM_METHOD_PCOHEN_HS ? h->w_gte : h->w_gt, n3 * sizeof(double),
@@ -747,9 +702,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
   bool conv = false;
   while (!conv && it < prm->max_iter) {
     const double E_prev = E;
-    mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->part(SL_MAX));
+    mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->d_sc, h->d_part);
     LAUNCH_CHECK();
-    const double gnorm_inf = host_max(h, SL_MAX, ge);
+    const double gnorm_inf = h->red(R_MAX);
     double conv_gnorm = gnorm_inf;
     double pg = 0.0, s0 = 1.0;
     double* H = h->w_H;
@@ -758,17 +713,17 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol, h->w_y);
       const double gsm = dev_absmax(h, n3, h->w_y);
       // HS beta
-      mmk::k_dot2diff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->part(SL_A),
-                                                       h->part(SL_B));
+      mmk::k_dot2diff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc,
+                                                       h->d_part);
       LAUNCH_CHECK();
-      const double num = host_sum(h, SL_A, grid_elem(n3));
-      const double den = host_sum(h, SL_B, grid_elem(n3)) + 1e-30;
+      const double num = h->red(R_A);
+      const double den = h->red(R_B) + 1e-30;
       const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
-      mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_dprev, beta, h->w_gte, graw, h->w_d, h->part(SL_A),
-                                              h->part(SL_B));
+      mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_dprev, beta, h->w_gte, graw, h->w_d, h->d_sc,
+                                              h->d_part);
       LAUNCH_CHECK();
-      const double dg = host_sum(h, SL_A, ge);
-      pg = host_sum(h, SL_B, ge);
+      const double dg = h->red(R_A);
+      pg = h->red(R_B);
       if (dg > 0) {
         mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_y, 0.0, h->w_d);
         LAUNCH_CHECK();
@@ -793,14 +748,14 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       double gamma = 1.0;
       if (hist_it > 0) {
         // y_last . (y_last .* inv_M_rel)
-        mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->part(SL_B));
+        mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->d_sc, h->d_part, R_B);
         LAUNCH_CHECK();
-        const double yMy = host_sum(h, SL_B, ge);
+        const double yMy = h->red(R_B);
         gamma = dev_dot(h, n3, h->w_S[last], h->w_Y[last]) / (yMy + 1e-30);
       }
       gamma = std::min(std::max(gamma, 1e-3), 1e3);
       // r = gamma q .* inv_M_rel
-      mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, h->w_d, h->part(SL_B));
+      mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, h->w_d, h->d_sc, h->d_part, R_B);
       LAUNCH_CHECK();
       mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, gamma, h->w_d);
       LAUNCH_CHECK();
@@ -849,9 +804,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
         c.demag += demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
         const double E_new = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
         c.evals += 1;
-        mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->part(SL_MAX));
+        mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
         LAUNCH_CHECK();
-        const double dm = host_max(h, SL_MAX, grid_elem(n3));
+        const double dm = h->red(R_MAX);
         conv = check_conv(it, E_new, E_prev, dm, gnorm_inf, prm);
         CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
         CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
@@ -868,9 +823,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     c.demag += ls.demag;
     double dm = 0.0;
     if (ls.accepted) {
-      mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->part(SL_MAX));
+      mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
       LAUNCH_CHECK();
-      dm = host_max(h, SL_MAX, grid_elem(n3));
+      dm = h->red(R_MAX);
     }
     const double E_new = ls.accepted ? ls.E : E_prev;
     conv = check_conv(it, E_new, E_prev, dm, conv_gnorm, prm);
@@ -1163,11 +1118,13 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     CK(cudaMemsetAsync(h->d_g, 0, n3 * sizeof(double), h->st));
     CK(cudaMemsetAsync(h->d_out, 0, n3 * sizeof(double), h->st));
     CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
-    h->d_part = h->alloc<double>((size_t)NSLOTS * MAXG);
-    CK(cudaMemsetAsync(h->d_part, 0, (size_t)NSLOTS * MAXG * sizeof(double), h->st));
+    h->d_x = h->alloc<double>(N);
+    CK(cudaMemsetAsync(h->d_x, 0, N * sizeof(double), h->st));
+    h->d_part = h->alloc<double>((size_t)mmk::NRED * MAXG);
+    CK(cudaMemsetAsync(h->d_part, 0, (size_t)mmk::NRED * MAXG * sizeof(double), h->st));
     h->d_sc = h->alloc<mmk::Scalars>(1);
+    CK(cudaMemsetAsync(h->d_sc, 0, sizeof(mmk::Scalars), h->st));  // ticket counters start at zero
     CK(cudaMallocHost(&h->h_sc, sizeof(mmk::Scalars)));
-    CK(cudaMallocHost(&h->h_part, MAXG * sizeof(double)));
     h->sync();
     return MM_OK;
   });
@@ -1183,9 +1140,10 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
 int mm_destroy(mm_problem* h) {
   if (!h) return MM_ERR_ARG;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
+  if (h->loop_graph) cudaGraphDestroy(h->loop_graph);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
-  if (h->h_part) cudaFreeHost(h->h_part);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->st) cudaStreamDestroy(h->st);
@@ -1217,12 +1175,12 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
     h->lv.resize(L);
     for (int l = 0; l < L; ++l) {
       const mm::AmgLevel& hl = h->amg_h[l];
-      DevLevel& dl = h->lv[l];
+      auto& dl = h->lv[l];
       dl.n = hl.A.n_rows;
-      dl.A = h->upload(hl.A);
+      dl.A = h->upload_sell(hl.A);
       if (l < L - 1) {
-        dl.P = h->upload(hl.P);
-        dl.R = h->upload(hl.R);
+        dl.P = h->upload_sell(hl.P);
+        dl.R = h->upload_sell(hl.R);
       }
       if (amg) {
         std::vector<double> s(dl.n);
@@ -1338,7 +1296,7 @@ int mm_rhs(mm_problem* h, const double* m, double* b, double* bnorm2) {
     CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemsetAsync(h->d_b, 0, h->N * sizeof(double), h->st));
     enqueue_rhs(h, h->d_m);
-    const double bb = host_sum(h, SL_BB0, grid_elem(h->N));
+    const double bb = h->red(R_BB0);
     if (bnorm2) *bnorm2 = bb;
     CK(cudaMemcpyAsync(b, h->d_b, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     h->sync();
@@ -1351,7 +1309,7 @@ int mm_apply_A(mm_problem* h, const double* U, double* y) {
   return guarded(h, [&] {
     if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
     CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    spmv<0>(h, h->lv[0].A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+    sell<0>(h, h->lv[0].A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
     CK(cudaMemcpyAsync(y, h->d_out, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     h->sync();
     return MM_OK;
@@ -1435,22 +1393,20 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     CK(cudaEventCreate(&e1));
     const int N = h->N;
     double acc = 0.0, nbytes = 0.0;
-    const DevLevel* l0 = h->poisson_built ? &h->lv[0] : nullptr;
+    const mm_problem::Level* l0 = h->poisson_built ? &h->lv[0] : nullptr;
     auto launch = [&]() {
       if (kernel == MM_KERNEL_SPMV_A) {
-        spmv<0>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+        sell<0>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
       } else if (kernel == MM_KERNEL_SMOOTH) {
-        const DevMat& A = l0->A;
         const double* s = l0->s ? l0->s : h->d_U;
-        const int g = grid_rows(A.n_rows, A.tpr);
-        TPR_SWITCH(A.tpr, (mmk::k_smooth_dot<T><<<g, BS, 0, h->st>>>(A.n_rows, A.ptr, A.col, A.val, h->d_U, h->d_b, s,
-                                                                      h->d_out, h->part(SL_RZ), nullptr)));
+        mmk::k_smooth_dot<<<grid_elem(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
+                                                                nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
         const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
         TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
                                                                             1.0, nullptr, h->inv_Vmag, h->d_g,
-                                                                            h->part(SL_E))));
+                                                                            h->d_sc, h->d_part)));
         LAUNCH_CHECK();
       } else {
         local_grad_dev(h, h->d_m, h->d_out);
@@ -1458,12 +1414,13 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     };
     const mm::EnergyOp& o = h->eop_h;
     const double nnzE = (double)o.col.size(), nrE = (double)o.n_rows;
+    // algorithmic bytes: stored non-zeros (8 B value + 4 B column), slice pointers, vectors once
     if (kernel == MM_KERNEL_SPMV_A) {
       const double nnz = (double)l0->A.nnz;
-      nbytes = nnz * 12.0 + (N + 1.0) * 4.0 + N * 8.0 * 2.0;
+      nbytes = nnz * 12.0 + ((N + 31) / 32 + 1.0) * 4.0 + N * 8.0 * 2.0;
     } else if (kernel == MM_KERNEL_SMOOTH) {
       const double nnz = (double)l0->A.nnz;
-      nbytes = nnz * 12.0 + (N + 1.0) * 4.0 + N * 8.0 * 4.0;
+      nbytes = nnz * 12.0 + ((N + 31) / 32 + 1.0) * 4.0 + N * 8.0 * 4.0;
     } else if (kernel == MM_KERNEL_ENERGY) {
       // entries: col, mat, w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3)
       nbytes = nnzE * (4.0 + 4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0;

@@ -1,13 +1,15 @@
 // Device kernels of the micromagnetic hot path (sm_103a).
 //
-// Conventions
-//  * Every reduction is deterministic: a kernel writes one partial per block (fixed grid, fixed
-//    in-block tree), and its consumers re-reduce the partials in a fixed order (every block of the
-//    consumer computes the same value, so no extra launch is needed to finalise a scalar).
-//  * Compressed-row kernels map TPR consecutive lanes to one row (TPR = 32 is warp-per-row); lanes
-//    stride the row's entries and combine with xor shuffles, so each row sums in a fixed order.
-//  * Iterative kernels read a device "done" flag first and return when it is set; a converged
-//    solve therefore ignores the launches still queued behind it.
+// Design notes (GB300):
+//  * FP64 issue rate is ~1/64 of FP32 on this part, so FP64 instructions are budgeted like memory
+//    traffic: every product is one DFMA per stored non-zero, with no shuffle reductions on the
+//    fine levels (thread-per-row sliced-ELL storage, slice height 32, columns sorted per row).
+//  * Every reduction is deterministic: each block writes one partial (fixed grid, fixed in-block
+//    tree); the last block to arrive (atomic ticket) sums the partials in block order and stores
+//    the scalar in Scalars::red.  Consumers read one scalar.
+//  * Iterative kernels read the device "done" flag first and return when it is set, so queued
+//    iterations after convergence cost a launch and nothing else; the PCG loop itself runs inside
+//    a CUDA graph whose conditional WHILE node is driven by k_set_cond.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -15,17 +17,20 @@
 
 namespace mmk {
 
-constexpr int BS = 256;       // threads per block for every kernel here
-constexpr int MAXG = 1216;    // 152 SMs x 8 blocks: upper bound of any grid (and of partial slots)
+constexpr int BS = 256;    // threads per block for every kernel here
+constexpr int MAXG = 4096; // upper bound of any grid, and of the partials of one reduction
 
-struct Scalars {              // device-resident solver scalars (one instance per solver context)
-  double tol2;                // tol^2 * b.b
-  double rz_prev;             // r.z of the previous PCG iteration
-  double bnorm2;              // b.b before zero-mean projection
-  int it;                     // completed PCG iterations
-  int done;                   // 1 once converged or out of iterations
+enum RedSlot { R_BB0, R_BB, R_R2, R_RZ, R_PAP, R_SUM, R_E, R_MAX, R_A, R_B, R_C, R_D, NRED };
+
+struct Scalars {
+  double tol2;      // tol^2 * b.b
+  double rz_prev;   // r.z of the previous PCG iteration
+  int it;           // completed PCG iterations
+  int done;         // 1 once converged or out of iterations
   int maxiter;
-  int pad;
+  int loops;        // graph-loop trips (hard stop for the conditional node)
+  double red[NRED];
+  unsigned cnt[NRED];
 };
 
 // ------------------------------------------------------------------------------------------
@@ -43,169 +48,148 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
-// Sum over the block; the result is returned to every thread.
-__device__ __forceinline__ double block_sum(double v) {
+// Sum (or max) over the block; the result is returned to every thread.
+template <bool MAX>
+__device__ __forceinline__ double block_reduce(double v) {
   __shared__ double s_red[BS / 32];
   __shared__ double s_out;
-  v = warp_sum(v);
+  v = MAX ? warp_max(v) : warp_sum(v);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) s_red[wid] = v;
   __syncthreads();
   if (wid == 0) {
     double t = lane < BS / 32 ? s_red[lane] : 0.0;
-    t = warp_sum(t);
+    t = MAX ? warp_max(t) : warp_sum(t);
     if (lane == 0) s_out = t;
   }
   __syncthreads();
   return s_out;
 }
+__device__ __forceinline__ double block_sum(double v) { return block_reduce<false>(v); }
 
-__device__ __forceinline__ double block_max(double v) {
-  __shared__ double s_red[BS / 32];
-  __shared__ double s_out;
-  v = warp_max(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) s_red[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    double t = lane < BS / 32 ? s_red[lane] : 0.0;
-    t = warp_max(t);
-    if (lane == 0) s_out = t;
+// Grid reduction of up to two values into sc->red[slot0], sc->red[slot1] (slot1 < 0: one value).
+// Partials go to part + slot * MAXG; the ticket counter of slot0 elects the finishing block.
+template <bool MAX = false>
+__device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, double* part, int slot0,
+                                            int slot1 = -1) {
+  __shared__ unsigned s_last;
+  v0 = block_reduce<MAX>(v0);
+  if (slot1 >= 0) v1 = block_reduce<MAX>(v1);
+  if (threadIdx.x == 0) {
+    part[(size_t)slot0 * MAXG + blockIdx.x] = v0;
+    if (slot1 >= 0) part[(size_t)slot1 * MAXG + blockIdx.x] = v1;
+    __threadfence();
+    const unsigned t = atomicAdd(&sc->cnt[slot0], 1u);
+    s_last = (t == gridDim.x - 1) ? 1u : 0u;
   }
   __syncthreads();
-  return s_out;
+  if (s_last) {
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) {
+      const double pa = __ldcg(part + (size_t)slot0 * MAXG + i);
+      a = MAX ? fmax(a, pa) : a + pa;
+      if (slot1 >= 0) {
+        const double pb = __ldcg(part + (size_t)slot1 * MAXG + i);
+        b = MAX ? fmax(b, pb) : b + pb;
+      }
+    }
+    a = block_reduce<MAX>(a);
+    if (slot1 >= 0) b = block_reduce<MAX>(b);
+    if (threadIdx.x == 0) {
+      sc->red[slot0] = a;
+      if (slot1 >= 0) sc->red[slot1] = b;
+      sc->cnt[slot0] = 0u;
+    }
+  }
 }
 
-// Re-reduce `count` block partials; identical result in every block.
-__device__ __forceinline__ double reduce_partials(const double* __restrict__ part, int count) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < count; i += BS) v += part[i];
-  return block_sum(v);
-}
+// ------------------------------------------------------------------------------------------
+// sliced ELL (slice height 32): entry k of row r lives at sptr[r/32] + 32 k + r%32
+// ------------------------------------------------------------------------------------------
+struct Sell {
+  int n;
+  const int* sptr;
+  const int* col;
+  const double* val;
+};
 
-__device__ __forceinline__ double reduce_partials_max(const double* __restrict__ part, int count) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < count; i += BS) v = fmax(v, part[i]);
-  return block_max(v);
-}
-
-template <int TPR>
-__device__ __forceinline__ double group_sum(double v) {
-#pragma unroll
-  for (int o = TPR / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// sum_k val[k] x[col[k]] over one row, TPR lanes; result valid on every lane of the group
-template <int TPR>
-__device__ __forceinline__ double row_dot(const int* __restrict__ ptr, const int* __restrict__ col,
-                                          const double* __restrict__ val, const double* __restrict__ x, int row,
-                                          bool valid, int lane) {
+__device__ __forceinline__ double sell_row(const Sell& A, const double* __restrict__ x, int row) {
+  const int s = row >> 5;
+  const int b0 = __ldg(A.sptr + s);
+  const int w = (__ldg(A.sptr + s + 1) - b0) >> 5;
+  const int base = b0 + (row & 31);
   double acc = 0.0;
-  if (valid) {
-    const int s = ptr[row], e = ptr[row + 1];
-    for (int k = s + lane; k < e; k += TPR) acc = fma(val[k], __ldg(x + col[k]), acc);
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    const int c = __ldg(A.col + base + 32 * k);
+    acc = fma(__ldg(A.val + base + 32 * k), __ldg(x + c), acc);
   }
-  return group_sum<TPR>(acc);
+  return acc;
 }
 
-// ------------------------------------------------------------------------------------------
-// compressed-row products used by the PCG and the V-cycle
-// ------------------------------------------------------------------------------------------
-// mode 0: y = A x ; mode 1: y = b - A x ; mode 2: y = x + s .* (b - A x) ; mode 3: y = x + A e (P e)
-template <int TPR, int MODE>
-__global__ void __launch_bounds__(BS) k_spmv(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                             const double* __restrict__ val, const double* __restrict__ x,
-                                             const double* __restrict__ b, const double* __restrict__ s,
-                                             double* __restrict__ y, const int* __restrict__ done) {
+// mode 0: y = A x ; 1: y = b - A x ; 2: y = x + s .* (b - A x) ; 3: y = b + A x (prolongation)
+template <int MODE>
+__global__ void __launch_bounds__(BS) k_sell(Sell A, const double* __restrict__ x, const double* b,
+                                             const double* __restrict__ s, double* y, const int* __restrict__ done) {
   if (done && *done) return;
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double ax = row_dot<TPR>(ptr, col, val, x, row, valid, lane);
-    if (valid && lane == 0) {
-      if (MODE == 0) y[row] = ax;
-      else if (MODE == 1) y[row] = b[row] - ax;
-      else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);
-      else y[row] = b[row] + ax;  // prolongation: y = b + P e, with x := e
-    }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
+    const double ax = sell_row(A, x, row);
+    if (MODE == 0) y[row] = ax;
+    else if (MODE == 1) y[row] = b[row] - ax;
+    else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);
+    else y[row] = b[row] + ax;
   }
 }
 
-// y = A x and one partial of x.y per block
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_spmv_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                 const double* __restrict__ val, const double* __restrict__ x,
-                                                 double* __restrict__ y, double* __restrict__ part) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
+// r = b - A x ; r.r -> red[R_R2] ; xv = s .* r (level-0 pre-smoothing from zero)
+__global__ void __launch_bounds__(BS) k_init_residual(Sell A, const double* __restrict__ x,
+                                                      const double* __restrict__ b, double* __restrict__ r,
+                                                      const double* __restrict__ s, double* __restrict__ xv,
+                                                      Scalars* sc, double* part) {
   double d = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double ax = row_dot<TPR>(ptr, col, val, x, row, valid, lane);
-    if (valid && lane == 0) {
-      y[row] = ax;
-      d = fma(x[row], ax, d);
-    }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
+    const double ri = b[row] - sell_row(A, x, row);
+    r[row] = ri;
+    d = fma(ri, ri, d);
+    if (s) xv[row] = s[row] * ri;
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, R_R2);
 }
 
-// PCG direction update fused with the operator product (iteration i):
-//   rz = sum(part_rz); beta = first ? 0 : rz / (rz_prev + eps)
-//   y = A z ; p = z + beta p ; Ap = y + beta Ap ; partial p.Ap
-// A p_new = A z + beta A p_old, so the product is taken on z, which is complete before the launch.
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_pcg_dir(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                const double* __restrict__ val, const double* __restrict__ z,
-                                                double* __restrict__ p, double* __restrict__ Ap,
-                                                const double* __restrict__ part_rz, int n_rz,
-                                                const double* __restrict__ part_r2, int n_r2,
-                                                double* __restrict__ part_pAp, Scalars* sc, int first) {
+// PCG direction update fused with the operator product:
+//   stop when r.r <= tol2 or it >= maxiter;  beta = it == 0 ? 0 : rz / (rz_prev + eps)
+//   y = A z ; p = z + beta p ; Ap = y + beta Ap ; p.Ap -> red[R_PAP]
+// (A p_new = A z + beta A p_old, so the product is taken on z, complete before the launch)
+__global__ void __launch_bounds__(BS) k_pcg_dir(Sell A, const double* __restrict__ z, double* __restrict__ p,
+                                                double* __restrict__ Ap, Scalars* sc, double* part) {
   if (sc->done) return;
-  const double r2 = reduce_partials(part_r2, n_r2);
-  if (r2 <= sc->tol2 || sc->it >= sc->maxiter) {
+  if (sc->red[R_R2] <= sc->tol2 || sc->it >= sc->maxiter) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
     return;
   }
-  const double rz = reduce_partials(part_rz, n_rz);
-  const double beta = first ? 0.0 : rz / (sc->rz_prev + 1e-30);
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
+  const double beta = sc->it == 0 ? 0.0 : sc->red[R_RZ] / (sc->rz_prev + 1e-30);
   double d = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double az = row_dot<TPR>(ptr, col, val, z, row, valid, lane);
-    if (valid && lane == 0) {
-      const double pn = z[row] + beta * p[row];
-      const double apn = az + beta * Ap[row];
-      p[row] = pn;
-      Ap[row] = apn;
-      d = fma(pn, apn, d);
-    }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
+    const double az = sell_row(A, z, row);
+    const double pn = z[row] + beta * p[row];
+    const double apn = az + beta * Ap[row];
+    p[row] = pn;
+    Ap[row] = apn;
+    d = fma(pn, apn, d);
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part_pAp[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, R_PAP);
 }
 
-// x += alpha p ; r -= alpha Ap ; partial r.r ; V-cycle pre-smoothing from zero: xv = s .* r
+// alpha = rz / (p.Ap + eps); x += alpha p ; r -= alpha Ap ; r.r -> red[R_R2] ; xv = s .* r
 __global__ void __launch_bounds__(BS) k_pcg_step(int n, double* __restrict__ x, double* __restrict__ r,
                                                  const double* __restrict__ p, const double* __restrict__ Ap,
-                                                 const double* __restrict__ s0, double* __restrict__ xv,
-                                                 const double* __restrict__ part_pAp, int n_pap,
-                                                 const double* __restrict__ part_rz, int n_rz,
-                                                 double* __restrict__ part_r2, Scalars* sc) {
+                                                 const double* __restrict__ s0, double* __restrict__ xv, Scalars* sc,
+                                                 double* part) {
   if (sc->done) return;
-  const double pAp = reduce_partials(part_pAp, n_pap);
-  const double rz = reduce_partials(part_rz, n_rz);
-  const double alpha = rz / (pAp + 1e-30);
+  const double rz = sc->red[R_RZ];
+  const double alpha = rz / (sc->red[R_PAP] + 1e-30);
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
     x[i] = x[i] + alpha * p[i];
@@ -214,55 +198,34 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, double* __restrict__ x, 
     d = fma(ri, ri, d);
     if (s0) xv[i] = s0[i] * ri;
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) {
-    part_r2[blockIdx.x] = d;
-    if (blockIdx.x == 0) {
-      sc->rz_prev = rz;
-      sc->it += 1;
-    }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz_prev = rz;
+    sc->it += 1;
   }
+  grid_reduce(d, 0.0, sc, part, R_R2);
 }
 
-// V-cycle level-0 residual with the convergence test: stops the solve when r.r <= tol2.
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_vc_residual0(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                     const double* __restrict__ val, const double* __restrict__ xv,
-                                                     const double* __restrict__ r, double* __restrict__ res,
-                                                     const double* __restrict__ part_r2, int n_r2, Scalars* sc) {
+// level-0 residual res = r - A xv, with the PCG convergence test first
+__global__ void __launch_bounds__(BS) k_vc_residual0(Sell A, const double* __restrict__ xv, const double* __restrict__ r,
+                                                     double* __restrict__ res, Scalars* sc) {
   if (sc->done) return;
-  const double r2 = reduce_partials(part_r2, n_r2);
-  if (r2 <= sc->tol2 || sc->it >= sc->maxiter) {
+  if (sc->red[R_R2] <= sc->tol2 || sc->it >= sc->maxiter) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
     return;
   }
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double ax = row_dot<TPR>(ptr, col, val, xv, row, valid, lane);
-    if (valid && lane == 0) res[row] = r[row] - ax;
-  }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS)
+    res[row] = r[row] - sell_row(A, xv, row);
 }
 
 // restriction b_c = R res, fused with the coarse pre-smoothing from zero x_c = s_c .* b_c
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_restrict(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                 const double* __restrict__ val, const double* __restrict__ res,
-                                                 double* __restrict__ bc, const double* __restrict__ sc_diag,
-                                                 double* __restrict__ xc, const int* __restrict__ done) {
+__global__ void __launch_bounds__(BS) k_restrict(Sell R, const double* __restrict__ res, double* __restrict__ bc,
+                                                 const double* __restrict__ s_c, double* __restrict__ xc,
+                                                 const int* __restrict__ done) {
   if (done && *done) return;
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double v = row_dot<TPR>(ptr, col, val, res, row, valid, lane);
-    if (valid && lane == 0) {
-      bc[row] = v;
-      if (sc_diag) xc[row] = sc_diag[row] * v;
-    }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < R.n; row += gridDim.x * BS) {
+    const double v = sell_row(R, res, row);
+    bc[row] = v;
+    if (s_c) xc[row] = s_c[row] * v;
   }
 }
 
@@ -281,74 +244,73 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const double* __restrict
   }
 }
 
-// post-smoothing that also produces the PCG partial r.z when it writes the level-0 result
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_smooth_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                   const double* __restrict__ val, const double* __restrict__ x,
-                                                   const double* __restrict__ b, const double* __restrict__ s,
-                                                   double* __restrict__ y, double* __restrict__ part,
-                                                   const int* __restrict__ done) {
+// post-smoothing y = x + s .* (b - A x); with `part` it also reduces b.y into red[R_RZ]
+// (level 0: b = r and y = z)
+__global__ void __launch_bounds__(BS) k_smooth_dot(Sell A, const double* __restrict__ x, const double* __restrict__ b,
+                                                   const double* __restrict__ s, double* __restrict__ y, Scalars* sc,
+                                                   double* part, const int* __restrict__ done) {
   if (done && *done) return;
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
   double d = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < n; rb += gridDim.x * RPB) {
-    const int row = rb + threadIdx.x / TPR;
-    const bool valid = row < n;
-    const double ax = row_dot<TPR>(ptr, col, val, x, row, valid, lane);
-    if (valid && lane == 0) {
-      const double yi = x[row] + s[row] * (b[row] - ax);
-      y[row] = yi;
-      d = fma(b[row], yi, d);
-    }
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
+    const double yi = x[row] + s[row] * (b[row] - sell_row(A, x, row));
+    y[row] = yi;
+    d = fma(b[row], yi, d);
   }
-  if (part) {
-    d = block_sum(d);
-    if (threadIdx.x == 0) part[blockIdx.x] = d;
+  if (part) grid_reduce(d, 0.0, sc, part, R_RZ);
+}
+
+// condition of the graph's WHILE node: keep looping until done (bounded by maxiter + 2 trips)
+__global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    sc->loops += 1;
+    const bool more = !sc->done && sc->loops <= sc->maxiter + 2;
+    cudaGraphSetConditional(hnd, more ? 1u : 0u);
   }
 }
 
 // ------------------------------------------------------------------------------------------
 // vector kernels
 // ------------------------------------------------------------------------------------------
-// part = x.y (y == nullptr: x.x)
+// x.y (y == nullptr: x.x) -> red[slot]
 __global__ void __launch_bounds__(BS) k_dot(int n, const double* __restrict__ x, const double* __restrict__ y,
-                                            double* __restrict__ part) {
+                                            Scalars* sc, double* part, int slot) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d = fma(x[i], y ? y[i] : x[i], d);
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, slot);
 }
 
-__global__ void __launch_bounds__(BS) k_sum(int n, const double* __restrict__ x, double* __restrict__ part) {
+__global__ void __launch_bounds__(BS) k_sum(int n, const double* __restrict__ x, Scalars* sc, double* part, int slot) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d += x[i];
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// x -= sum(part)/n
-__global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, const double* __restrict__ part,
-                                                 int n_part) {
-  const double mean = reduce_partials(part, n_part) / (double)n;
+// x -= red[slot] / n
+__global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, const Scalars* sc, int slot) {
+  const double mean = sc->red[slot] / (double)n;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) x[i] = x[i] - mean;
 }
 
-// PCG initialisation: tol2 = tol^2 * sum(part_bb), bnorm2 stored; x *= mask (optional)
-__global__ void k_pcg_init_scalars(Scalars* sc, const double* __restrict__ part_bb, int n_bb, double tol,
-                                   int maxiter) {
-  const double bb = reduce_partials(part_bb, n_bb);
-  if (threadIdx.x == 0) {
-    sc->tol2 = tol * tol * bb;
+// out = s .* r
+__global__ void __launch_bounds__(BS) k_mul(int n, const double* __restrict__ s, const double* __restrict__ r,
+                                            double* __restrict__ out) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = s[i] * r[i];
+}
+
+// PCG start: tol2 = tol^2 * red[R_BB]; counters reset
+__global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    sc->tol2 = tol * tol * sc->red[R_BB];
     sc->it = 0;
     sc->done = 0;
+    sc->loops = 0;
     sc->maxiter = maxiter;
     sc->rz_prev = 0.0;
   }
 }
 
 // ------------------------------------------------------------------------------------------
-// energy, local Hessian and demag source over the magnetic rows
+// energy, local Hessian and demag source over the magnetic rows (TPR lanes per row)
 // ------------------------------------------------------------------------------------------
 struct EnergyDev {
   int n_rows;
@@ -368,6 +330,13 @@ struct EnergyDev {
   int single_axis;
   int axis0;            // material whose axis every entry uses when single_axis
 };
+
+template <int TPR>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 
 template <int TPR>
 __device__ __forceinline__ void exch_aniso_row(const EnergyDev& op, int r, bool valid, int lane,
@@ -402,13 +371,13 @@ __device__ __forceinline__ void exch_aniso_row(const EnergyDev& op, int r, bool 
   az = group_sum<TPR>(az);
 }
 
-// g = (K m + G U + g_z) / V_mag on the magnetic rows; partial of m.(g_quad + 2 g_z)
+// g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E]
 template <int TPR>
 __global__ void __launch_bounds__(BS) k_energy_grad(EnergyDev op, const double* __restrict__ m,
                                                     const double* __restrict__ U, const double* __restrict__ Mn,
                                                     double Bx, double By, double Bz, const double* __restrict__ Bbias,
-                                                    double inv_Vmag, double* __restrict__ g,
-                                                    double* __restrict__ part) {
+                                                    double inv_Vmag, double* __restrict__ g, Scalars* sc,
+                                                    double* part) {
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
   double en = 0.0;
@@ -447,8 +416,7 @@ __global__ void __launch_bounds__(BS) k_energy_grad(EnergyDev op, const double* 
       g[3 * a + 2] = gz * inv_Vmag;
     }
   }
-  en = block_sum(en);
-  if (threadIdx.x == 0) part[blockIdx.x] = en;
+  grid_reduce(en, 0.0, sc, part, R_E);
 }
 
 // out = C v / V_mag on the magnetic rows
@@ -471,12 +439,12 @@ __global__ void __launch_bounds__(BS) k_local_grad(EnergyDev op, const double* _
   }
 }
 
-// Inner-PCG operator P p = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows; partial p.Pp
+// Inner-PCG operator P p = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows; p.Pp -> red[slot]
 template <int TPR>
 __global__ void __launch_bounds__(BS) k_apply_P(EnergyDev op, const double* __restrict__ m,
                                                 const double* __restrict__ gext, const double* __restrict__ p,
-                                                double reg, double inv_Vmag, double* __restrict__ Ap,
-                                                double* __restrict__ part) {
+                                                double reg, double inv_Vmag, double* __restrict__ Ap, Scalars* sc,
+                                                double* part, int slot) {
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
   double d = 0.0;
@@ -501,17 +469,14 @@ __global__ void __launch_bounds__(BS) k_apply_P(EnergyDev op, const double* __re
       d += px * ox + py * oy + pz * oz;
     }
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// b = D m on the magnetic rows (other rows are left untouched), partial b.b
+// b = D m on the magnetic rows (other rows untouched)
 template <int TPR>
-__global__ void __launch_bounds__(BS) k_rhs(EnergyDev op, const double* __restrict__ m, double* __restrict__ b,
-                                            double* __restrict__ part) {
+__global__ void __launch_bounds__(BS) k_rhs(EnergyDev op, const double* __restrict__ m, double* __restrict__ b) {
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
-  double bb = 0.0;
   for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
     const int r = rb + threadIdx.x / TPR;
     const bool valid = r < op.n_rows;
@@ -524,24 +489,17 @@ __global__ void __launch_bounds__(BS) k_rhs(EnergyDev op, const double* __restri
       }
     }
     acc = group_sum<TPR>(acc);
-    if (valid && lane == 0) {
-      b[op.rows[r]] = acc;
-      bb = fma(acc, acc, bb);
-    }
-  }
-  if (part) {
-    bb = block_sum(bb);
-    if (threadIdx.x == 0) part[blockIdx.x] = bb;
+    if (valid && lane == 0) b[op.rows[r]] = acc;
   }
 }
 
 // ------------------------------------------------------------------------------------------
 // minimizer vector kernels (3-vectors per node, xyz interleaved)
 // ------------------------------------------------------------------------------------------
-// g_tan = P_m(g .* inv_M_rel), g_tan_ext = P_m(g); partial max |g_tan|
+// g_tan = P_m(g .* inv_M_rel), g_tan_ext = P_m(g); max |g_tan| -> red[R_MAX]
 __global__ void __launch_bounds__(BS) k_tangent2(int N, const double* __restrict__ m, const double* __restrict__ g,
                                                  const double* __restrict__ inv_M_rel, double* __restrict__ gt,
-                                                 double* __restrict__ gte, double* __restrict__ part_max) {
+                                                 double* __restrict__ gte, Scalars* sc, double* part) {
   double mx_ = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
@@ -551,33 +509,30 @@ __global__ void __launch_bounds__(BS) k_tangent2(int N, const double* __restrict
     const double ds = m0 * s0 + m1 * s1 + m2 * s2;
     const double t0 = s0 - ds * m0, t1 = s1 - ds * m1, t2 = s2 - ds * m2;
     const double de = m0 * g0 + m1 * g1 + m2 * g2;
-    if (gt) {
-      gt[3 * i] = t0;
-      gt[3 * i + 1] = t1;
-      gt[3 * i + 2] = t2;
-    }
+    gt[3 * i] = t0;
+    gt[3 * i + 1] = t1;
+    gt[3 * i + 2] = t2;
     gte[3 * i] = g0 - de * m0;
     gte[3 * i + 1] = g1 - de * m1;
     gte[3 * i + 2] = g2 - de * m2;
     mx_ = fmax(mx_, fmax(fabs(t0), fmax(fabs(t1), fabs(t2))));
   }
-  mx_ = block_max(mx_);
-  if (threadIdx.x == 0) part_max[blockIdx.x] = mx_;
+  grid_reduce<true>(mx_, 0.0, sc, part, R_MAX);
 }
 
 // out = P_m(v)
-__global__ void __launch_bounds__(BS) k_tangent(int N, const double* __restrict__ m, const double* __restrict__ v,
-                                                double* __restrict__ out) {
+__global__ void __launch_bounds__(BS) k_tangent(int N, const double* __restrict__ m, const double* v, double* out) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
-    const double d = m0 * v[3 * i] + m1 * v[3 * i + 1] + m2 * v[3 * i + 2];
-    out[3 * i] = v[3 * i] - d * m0;
-    out[3 * i + 1] = v[3 * i + 1] - d * m1;
-    out[3 * i + 2] = v[3 * i + 2] - d * m2;
+    const double v0 = v[3 * i], v1 = v[3 * i + 1], v2 = v[3 * i + 2];
+    const double d = m0 * v0 + m1 * v1 + m2 * v2;
+    out[3 * i] = v0 - d * m0;
+    out[3 * i + 1] = v1 - d * m1;
+    out[3 * i + 2] = v2 - d * m2;
   }
 }
 
-// Cayley update with renormalisation: m_out = cayley(m, H, tau)
+// Cayley update with renormalisation: out = cayley(m, H, tau)
 __global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__ m, const double* __restrict__ H,
                                                double tau, double* __restrict__ out) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
@@ -608,9 +563,9 @@ __global__ void __launch_bounds__(BS) k_normalize(int N, double* __restrict__ m)
   }
 }
 
-// z = r .* w (per node), partial r.z
+// z = r .* w (per node); r.z -> red[slot]
 __global__ void __launch_bounds__(BS) k_scale3_dot(int N, const double* __restrict__ r, const double* __restrict__ w,
-                                                   double* __restrict__ z, double* __restrict__ part) {
+                                                   double* __restrict__ z, Scalars* sc, double* part, int slot) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double s = w[i];
@@ -620,15 +575,14 @@ __global__ void __launch_bounds__(BS) k_scale3_dot(int N, const double* __restri
     z[3 * i + 2] = z2;
     d += r[3 * i] * z0 + r[3 * i + 1] * z1 + r[3 * i + 2] * z2;
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// y += a p ; r -= a Ap ; z = r .* w ; partial r.z   (inner PCG of the local Hessian)
+// y += a p ; r -= a Ap ; z = r .* w ; r.z -> red[slot]   (inner PCG of the local Hessian)
 __global__ void __launch_bounds__(BS) k_inner_step(int N, double a, double* __restrict__ y, double* __restrict__ r,
                                                    const double* __restrict__ p, const double* __restrict__ Ap,
-                                                   const double* __restrict__ w, double* __restrict__ z,
-                                                   double* __restrict__ part, int update) {
+                                                   const double* __restrict__ w, double* __restrict__ z, Scalars* sc,
+                                                   double* part, int slot, int update) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double s = w[i];
@@ -644,11 +598,10 @@ __global__ void __launch_bounds__(BS) k_inner_step(int N, double a, double* __re
       d += rc * zc;
     }
   }
-  d = block_sum(d);
-  if (threadIdx.x == 0) part[blockIdx.x] = d;
+  grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// y = x + a * y (axpby with unit x)
+// y = x + a * y
 __global__ void __launch_bounds__(BS) k_xpay(int n, const double* __restrict__ x, double a, double* __restrict__ y) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = x[i] + a * y[i];
 }
@@ -664,39 +617,44 @@ __global__ void __launch_bounds__(BS) k_scale(int n, double a, double* __restric
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * y[i];
 }
 
-// partial max |x|
-__global__ void __launch_bounds__(BS) k_absmax(int n, const double* __restrict__ x, double* __restrict__ part) {
+// max |x| -> red[R_MAX]
+__global__ void __launch_bounds__(BS) k_absmax(int n, const double* __restrict__ x, Scalars* sc, double* part) {
   double v = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) v = fmax(v, fabs(x[i]));
-  v = block_max(v);
-  if (threadIdx.x == 0) part[blockIdx.x] = v;
+  grid_reduce<true>(v, 0.0, sc, part, R_MAX);
 }
 
-// partial max |x - y|
+// max |x - y| -> red[R_MAX]
 __global__ void __launch_bounds__(BS) k_absmaxdiff(int n, const double* __restrict__ x, const double* __restrict__ y,
-                                                   double* __restrict__ part) {
+                                                   Scalars* sc, double* part) {
   double v = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) v = fmax(v, fabs(x[i] - y[i]));
-  v = block_max(v);
-  if (threadIdx.x == 0) part[blockIdx.x] = v;
+  grid_reduce<true>(v, 0.0, sc, part, R_MAX);
 }
 
-// d = -y + beta * P_m(d_prev); H = m x d; partials d.gte (slot 0) and g_raw.d (slot 1, stride n_part)
+// a.(b - c) -> red[R_A] and d.(b - c) -> red[R_B]
+__global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict__ a, const double* __restrict__ d,
+                                                 const double* __restrict__ b, const double* __restrict__ c,
+                                                 Scalars* sc, double* part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    const double df = b[i] - c[i];
+    s1 = fma(a[i], df, s1);
+    s2 = fma(d[i], df, s2);
+  }
+  grid_reduce(s1, s2, sc, part, R_A, R_B);
+}
+
+// d = -y + beta * P_m(d_prev); d.gte -> red[R_A]; g_raw.d -> red[R_B]
 __global__ void __launch_bounds__(BS) k_direction(int N, const double* __restrict__ m, const double* __restrict__ y,
                                                   const double* __restrict__ dprev, double beta,
                                                   const double* __restrict__ gte, const double* __restrict__ graw,
-                                                  double* __restrict__ d, double* __restrict__ part_dg,
-                                                  double* __restrict__ part_pg) {
+                                                  double* __restrict__ d, Scalars* sc, double* part) {
   double s1 = 0.0, s2 = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
-    double dp0 = 0, dp1 = 0, dp2 = 0;
-    if (dprev) {
-      const double a = m0 * dprev[3 * i] + m1 * dprev[3 * i + 1] + m2 * dprev[3 * i + 2];
-      dp0 = dprev[3 * i] - a * m0;
-      dp1 = dprev[3 * i + 1] - a * m1;
-      dp2 = dprev[3 * i + 2] - a * m2;
-    }
+    const double a = m0 * dprev[3 * i] + m1 * dprev[3 * i + 1] + m2 * dprev[3 * i + 2];
+    const double dp0 = dprev[3 * i] - a * m0, dp1 = dprev[3 * i + 1] - a * m1, dp2 = dprev[3 * i + 2] - a * m2;
     const double d0 = -y[3 * i] + beta * dp0, d1 = -y[3 * i + 1] + beta * dp1, d2 = -y[3 * i + 2] + beta * dp2;
     d[3 * i] = d0;
     d[3 * i + 1] = d1;
@@ -704,12 +662,7 @@ __global__ void __launch_bounds__(BS) k_direction(int N, const double* __restric
     s1 += d0 * gte[3 * i] + d1 * gte[3 * i + 1] + d2 * gte[3 * i + 2];
     s2 += graw[3 * i] * d0 + graw[3 * i + 1] * d1 + graw[3 * i + 2] * d2;
   }
-  s1 = block_sum(s1);
-  s2 = block_sum(s2);
-  if (threadIdx.x == 0) {
-    part_dg[blockIdx.x] = s1;
-    part_pg[blockIdx.x] = s2;
-  }
+  grid_reduce(s1, s2, sc, part, R_A, R_B);
 }
 
 // H = m x d
