@@ -181,6 +181,12 @@ int mm_minimize(mm_problem* h, const double* B_ext, double* m_inout, double* U_i
 #define MM_KERNEL_HESSIAN 3  /* local Hessian action over the magnetic rows               */
 int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, double* bytes_per_launch);
 
+/* Solver options.  MM_OPT_GRAPH (default 1): run the PCG iterations inside a CUDA graph whose
+ * conditional WHILE node loops on the device until convergence; 0 polls the device flag from the
+ * host every four iterations (same kernels, same results). */
+#define MM_OPT_GRAPH 1
+int mm_set_option(mm_problem* h, int option, int value);
+
 /* Device time of the last demag solve (mm_solve_u / mm_solve_u_dev), measured with CUDA events
  * recorded on the problem's stream around all of its kernels (host<->device copies excluded). */
 int mm_last_solve_ms(mm_problem* h, double* ms);

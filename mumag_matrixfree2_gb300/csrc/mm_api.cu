@@ -54,13 +54,27 @@ int pick_tpr(int64_t nnz, int64_t rows) {
   return 32;
 }
 
-// sliced ELL with slice height 32, built from a CSR with sorted columns (padding: value 0, own row
-// index as column, so padded lanes read a valid address)
+// A level operator on the device, in one of two layouts:
+//  * sliced ELL, slice height 32, one thread per row (tpr == 1): large matrices with short rows;
+//    padding entries carry value 0 and a valid column;
+//  * compressed rows with tpr lanes per row (2..32): small matrices with long rows.
 struct DevSell {
   mmk::Sell s{};
+  mmk::Csr c{};
+  int tpr = 1;
   int64_t nnz = 0;     // stored non-zeros (without padding)
   int64_t stored = 0;  // entries including padding
 };
+
+// Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
+// lanes per row to reach ~256Ki threads, capped by the average row length.
+int choose_tpr(int64_t rows, int64_t nnz) {
+  if (rows >= 65536) return 1;
+  const double avg = rows > 0 ? (double)nnz / (double)rows : 1.0;
+  int t = 2;
+  while (t < 32 && (rows * t < 262144) && t < avg) t *= 2;
+  return t;
+}
 
 thread_local std::string g_create_error;
 
@@ -116,6 +130,7 @@ struct mm_problem {
   cudaGraph_t loop_graph = nullptr;
   cudaGraphExec_t loop_exec = nullptr;
   bool graph_failed = false;
+  bool use_graph = true;
   int64_t iter_launches = 0;  // kernels in one loop trip
 
   // staging buffers for host-pointer calls
@@ -143,7 +158,19 @@ struct mm_problem {
     if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
   }
-  DevSell upload_sell(const mm::HostCSR& A) {
+  DevSell upload_mat(const mm::HostCSR& A, bool force_sell = false) {
+    const int tpr = force_sell ? 1 : choose_tpr(A.n_rows, A.nnz());
+    if (tpr > 1) {
+      DevSell d;
+      d.tpr = tpr;
+      d.c.n = A.n_rows;
+      d.c.ptr = upload(A.ptr);
+      d.c.col = upload(A.col);
+      d.c.val = upload(A.val);
+      d.s.n = A.n_rows;
+      d.nnz = d.stored = A.nnz();
+      return d;
+    }
     const int n = A.n_rows;
     const int ns = (n + 31) / 32;
     std::vector<int> sptr(ns + 1, 0);
@@ -218,12 +245,17 @@ using mmk::R_SUM;
 template <int MODE>
 void sell(mm_problem* h, const DevSell& A, const double* x, const double* b, const double* s, double* y,
           const int* done) {
-  mmk::k_sell<MODE><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
+  if (A.tpr == 1) {
+    mmk::k_sell<MODE><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
+  } else {
+    const int g = grid_rows(A.c.n, A.tpr);
+    TPR_SWITCH(A.tpr, (mmk::k_csr<T, MODE><<<g, BS, 0, h->st>>>(A.c, x, b, s, y, done)));
+  }
   LAUNCH_CHECK();
 }
 
-void dot(mm_problem* h, int n, const double* x, const double* y, int slot) {
-  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, x, y, h->d_sc, h->d_part, slot);
+void dot(mm_problem* h, int n, const double* x, const double* y, int slot, int post = mmk::POST_NONE) {
+  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, x, y, h->d_sc, h->d_part, slot, post);
   LAUNCH_CHECK();
 }
 
@@ -248,7 +280,13 @@ void enqueue_vcycle(mm_problem* h, const double* r, double* z, bool in_loop, con
     }
     auto& nx = lv[l + 1];
     const bool coarsest = (l + 1 == L - 1);
-    mmk::k_restrict<<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x, done);
+    if (c.R.tpr == 1) {
+      mmk::k_restrict<<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x, done);
+    } else {
+      const int g = grid_rows(nx.n, c.R.tpr);
+      TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<T><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b, coarsest ? nullptr : nx.s,
+                                                                        nx.x, done)));
+    }
     LAUNCH_CHECK();
   }
   {
@@ -259,11 +297,12 @@ void enqueue_vcycle(mm_problem* h, const double* r, double* z, bool in_loop, con
   for (int l = L - 2; l >= 0; --l) {
     auto& c = lv[l];
     sell<3>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
-    const double* bl = (l == 0) ? r : c.b;
-    double* out = (l == 0) ? z : c.x2;
-    mmk::k_smooth_dot<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, bl, c.s, out, h->d_sc,
-                                                         l == 0 ? h->d_part : nullptr, done);
-    LAUNCH_CHECK();
+    if (l == 0) {
+      mmk::k_smooth_dot<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, h->d_sc, h->d_part, done);
+      LAUNCH_CHECK();
+    } else {
+      sell<2>(h, c.A, c.x, c.b, c.s, c.x2, done);
+    }
   }
 }
 
@@ -283,7 +322,7 @@ void apply_M_simple(mm_problem* h, const double* r, double* z, const int* done) 
     mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, done);
     LAUNCH_CHECK();
   }
-  dot(h, N, r, z, R_RZ);
+  dot(h, N, r, z, R_RZ, mmk::POST_RZ);
 }
 
 // preconditioner application outside the PCG loop
@@ -368,11 +407,11 @@ int run_pcg(mm_problem* h, double tol, int maxiter, int* iters, double* rel_res)
   double* x = h->d_x;
   const bool zero_mean = !h->has_mask;
   if (zero_mean) {
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, h->d_part, R_SUM);
+    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
     mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, R_SUM);
     LAUNCH_CHECK();
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
+    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
     mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
     LAUNCH_CHECK();
@@ -387,9 +426,9 @@ int run_pcg(mm_problem* h, double tol, int maxiter, int* iters, double* rel_res)
   LAUNCH_CHECK();
   if (ml) enqueue_vcycle(h, h->d_r, h->d_z, false, nullptr);
   else apply_M_simple(h, h->d_r, h->d_z, nullptr);
-  if (build_loop_graph(h)) {
+  if (h->use_graph && build_loop_graph(h)) {
     CK(cudaGraphLaunch(h->loop_exec, h->st));
-    h->n_launch += h->iter_launches;  // counted per trip below, once the trip count is known
+    h->n_launch += h->iter_launches;  // one trip; the other trips are counted once their number is known
   } else {
     for (int i = 0;; ++i) {
       enqueue_iteration(h);
@@ -401,14 +440,14 @@ int run_pcg(mm_problem* h, double tol, int maxiter, int* iters, double* rel_res)
     }
   }
   if (zero_mean) {
-    mmk::k_sum<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
+    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
     LAUNCH_CHECK();
     mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
     LAUNCH_CHECK();
   }
   CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   h->sync();
-  if (h->loop_exec) h->n_launch += (int64_t)(h->h_sc->loops - 1) * h->iter_launches;
+  if (h->use_graph && h->loop_exec) h->n_launch += (int64_t)(h->h_sc->loops - 1) * h->iter_launches;
   if (iters) *iters = h->h_sc->it;
   const double r2 = h->h_sc->red[R_R2], bb = h->h_sc->red[R_BB0];
   const double rr = std::sqrt(r2 / (bb + 1e-30));
@@ -1177,10 +1216,10 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
       const mm::AmgLevel& hl = h->amg_h[l];
       auto& dl = h->lv[l];
       dl.n = hl.A.n_rows;
-      dl.A = h->upload_sell(hl.A);
+      dl.A = h->upload_mat(hl.A, l == 0);  // level 0 feeds the fused PCG kernels: always sliced ELL
       if (l < L - 1) {
-        dl.P = h->upload_sell(hl.P);
-        dl.R = h->upload_sell(hl.R);
+        dl.P = h->upload_mat(hl.P);
+        dl.R = h->upload_mat(hl.R);
       }
       if (amg) {
         std::vector<double> s(dl.n);
@@ -1445,6 +1484,15 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     if (bytes) *bytes = nbytes;
     return MM_OK;
   });
+}
+
+int mm_set_option(mm_problem* h, int option, int value) {
+  if (!h) return MM_ERR_ARG;
+  if (option == MM_OPT_GRAPH) {
+    h->use_graph = value != 0;
+    return MM_OK;
+  }
+  return MM_ERR_ARG;
 }
 
 int mm_last_solve_ms(mm_problem* h, double* ms) {

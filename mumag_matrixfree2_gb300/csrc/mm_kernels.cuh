@@ -24,14 +24,22 @@ enum RedSlot { R_BB0, R_BB, R_R2, R_RZ, R_PAP, R_SUM, R_E, R_MAX, R_A, R_B, R_C,
 
 struct Scalars {
   double tol2;      // tol^2 * b.b
-  double rz_prev;   // r.z of the previous PCG iteration
+  double rz;        // current r.z
+  double alpha;     // rz / (p.Ap + eps), set when p.Ap is reduced
+  double beta;      // rz_new / (rz_old + eps), set when r.z is reduced (0 for the first direction)
   int it;           // completed PCG iterations
-  int done;         // 1 once converged or out of iterations
+  int done;         // 1 once converged or out of iterations (set when r.r is reduced)
   int maxiter;
   int loops;        // graph-loop trips (hard stop for the conditional node)
+  int rz_valid;     // 0 until the first r.z of a solve is reduced
+  int pad;
   double red[NRED];
   unsigned cnt[NRED];
 };
+
+// Scalar follow-ups computed once, by the block that finishes a reduction (so that no thread of
+// the consumer kernels spends FP64 divides or compares on them).
+enum Post { POST_NONE, POST_PAP, POST_R2_STEP, POST_R2_INIT, POST_RZ, POST_MEAN };
 
 // ------------------------------------------------------------------------------------------
 // deterministic reductions
@@ -72,7 +80,7 @@ __device__ __forceinline__ double block_sum(double v) { return block_reduce<fals
 // Partials go to part + slot * MAXG; the ticket counter of slot0 elects the finishing block.
 template <bool MAX = false>
 __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, double* part, int slot0,
-                                            int slot1 = -1) {
+                                            int slot1 = -1, int post = POST_NONE, double post_arg = 0.0) {
   __shared__ unsigned s_last;
   v0 = block_reduce<MAX>(v0);
   if (slot1 >= 0) v1 = block_reduce<MAX>(v1);
@@ -101,6 +109,18 @@ __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, d
       sc->red[slot0] = a;
       if (slot1 >= 0) sc->red[slot1] = b;
       sc->cnt[slot0] = 0u;
+      if (post == POST_PAP) {
+        sc->alpha = sc->rz / (a + 1e-30);
+      } else if (post == POST_R2_STEP || post == POST_R2_INIT) {
+        if (post == POST_R2_STEP) sc->it += 1;
+        if (a <= sc->tol2 || sc->it >= sc->maxiter) sc->done = 1;
+      } else if (post == POST_RZ) {
+        sc->beta = sc->rz_valid ? a / (sc->rz + 1e-30) : 0.0;
+        sc->rz = a;
+        sc->rz_valid = 1;
+      } else if (post == POST_MEAN) {
+        sc->red[slot0] = a / post_arg;
+      }
     }
   }
 }
@@ -129,6 +149,68 @@ __device__ __forceinline__ double sell_row(const Sell& A, const double* __restri
   return acc;
 }
 
+// ------------------------------------------------------------------------------------------
+// compressed rows with TPR lanes per row (small levels with long rows, where one thread per row
+// would leave most of the GPU idle)
+// ------------------------------------------------------------------------------------------
+struct Csr {
+  int n;
+  const int* ptr;
+  const int* col;
+  const double* val;
+};
+
+template <int TPR>
+__device__ __forceinline__ double csr_row(const Csr& A, const double* __restrict__ x, int row, bool valid, int lane) {
+  double acc = 0.0;
+  if (valid) {
+    const int s = __ldg(A.ptr + row), e = __ldg(A.ptr + row + 1);
+    for (int k = s + lane; k < e; k += TPR) acc = fma(__ldg(A.val + k), __ldg(x + __ldg(A.col + k)), acc);
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// same modes as k_sell
+template <int TPR, int MODE>
+__global__ void __launch_bounds__(BS) k_csr(Csr A, const double* __restrict__ x, const double* b,
+                                            const double* __restrict__ s, double* y, const int* __restrict__ done) {
+  if (done && *done) return;
+  constexpr int RPB = BS / TPR;
+  const int lane = threadIdx.x % TPR;
+  for (int rb = blockIdx.x * RPB; rb < A.n; rb += gridDim.x * RPB) {
+    const int row = rb + threadIdx.x / TPR;
+    const bool valid = row < A.n;
+    const double ax = csr_row<TPR>(A, x, row, valid, lane);
+    if (valid && lane == 0) {
+      if (MODE == 0) y[row] = ax;
+      else if (MODE == 1) y[row] = b[row] - ax;
+      else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);
+      else y[row] = b[row] + ax;
+    }
+  }
+}
+
+// restriction with compressed rows, fused with the coarse pre-smoothing from zero
+template <int TPR>
+__global__ void __launch_bounds__(BS) k_restrict_csr(Csr R, const double* __restrict__ res, double* __restrict__ bc,
+                                                     const double* __restrict__ s_c, double* __restrict__ xc,
+                                                     const int* __restrict__ done) {
+  if (done && *done) return;
+  constexpr int RPB = BS / TPR;
+  const int lane = threadIdx.x % TPR;
+  for (int rb = blockIdx.x * RPB; rb < R.n; rb += gridDim.x * RPB) {
+    const int row = rb + threadIdx.x / TPR;
+    const bool valid = row < R.n;
+    const double v = csr_row<TPR>(R, res, row, valid, lane);
+    if (valid && lane == 0) {
+      bc[row] = v;
+      if (s_c) xc[row] = s_c[row] * v;
+    }
+  }
+}
+
 // mode 0: y = A x ; 1: y = b - A x ; 2: y = x + s .* (b - A x) ; 3: y = b + A x (prolongation)
 template <int MODE>
 __global__ void __launch_bounds__(BS) k_sell(Sell A, const double* __restrict__ x, const double* b,
@@ -155,7 +237,7 @@ __global__ void __launch_bounds__(BS) k_init_residual(Sell A, const double* __re
     d = fma(ri, ri, d);
     if (s) xv[row] = s[row] * ri;
   }
-  grid_reduce(d, 0.0, sc, part, R_R2);
+  grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_INIT);
 }
 
 // PCG direction update fused with the operator product:
@@ -165,11 +247,7 @@ __global__ void __launch_bounds__(BS) k_init_residual(Sell A, const double* __re
 __global__ void __launch_bounds__(BS) k_pcg_dir(Sell A, const double* __restrict__ z, double* __restrict__ p,
                                                 double* __restrict__ Ap, Scalars* sc, double* part) {
   if (sc->done) return;
-  if (sc->red[R_R2] <= sc->tol2 || sc->it >= sc->maxiter) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
-    return;
-  }
-  const double beta = sc->it == 0 ? 0.0 : sc->red[R_RZ] / (sc->rz_prev + 1e-30);
+  const double beta = sc->beta;
   double d = 0.0;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
     const double az = sell_row(A, z, row);
@@ -179,7 +257,7 @@ __global__ void __launch_bounds__(BS) k_pcg_dir(Sell A, const double* __restrict
     Ap[row] = apn;
     d = fma(pn, apn, d);
   }
-  grid_reduce(d, 0.0, sc, part, R_PAP);
+  grid_reduce(d, 0.0, sc, part, R_PAP, -1, POST_PAP);
 }
 
 // alpha = rz / (p.Ap + eps); x += alpha p ; r -= alpha Ap ; r.r -> red[R_R2] ; xv = s .* r
@@ -188,8 +266,7 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, double* __restrict__ x, 
                                                  const double* __restrict__ s0, double* __restrict__ xv, Scalars* sc,
                                                  double* part) {
   if (sc->done) return;
-  const double rz = sc->red[R_RZ];
-  const double alpha = rz / (sc->red[R_PAP] + 1e-30);
+  const double alpha = sc->alpha;
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
     x[i] = x[i] + alpha * p[i];
@@ -198,21 +275,13 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, double* __restrict__ x, 
     d = fma(ri, ri, d);
     if (s0) xv[i] = s0[i] * ri;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sc->rz_prev = rz;
-    sc->it += 1;
-  }
-  grid_reduce(d, 0.0, sc, part, R_R2);
+  grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
 
 // level-0 residual res = r - A xv, with the PCG convergence test first
 __global__ void __launch_bounds__(BS) k_vc_residual0(Sell A, const double* __restrict__ xv, const double* __restrict__ r,
                                                      double* __restrict__ res, Scalars* sc) {
   if (sc->done) return;
-  if (sc->red[R_R2] <= sc->tol2 || sc->it >= sc->maxiter) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
-    return;
-  }
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS)
     res[row] = r[row] - sell_row(A, xv, row);
 }
@@ -256,7 +325,7 @@ __global__ void __launch_bounds__(BS) k_smooth_dot(Sell A, const double* __restr
     y[row] = yi;
     d = fma(b[row], yi, d);
   }
-  if (part) grid_reduce(d, 0.0, sc, part, R_RZ);
+  if (part) grid_reduce(d, 0.0, sc, part, R_RZ, -1, POST_RZ);
 }
 
 // condition of the graph's WHILE node: keep looping until done (bounded by maxiter + 2 trips)
@@ -273,21 +342,22 @@ __global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
 // ------------------------------------------------------------------------------------------
 // x.y (y == nullptr: x.x) -> red[slot]
 __global__ void __launch_bounds__(BS) k_dot(int n, const double* __restrict__ x, const double* __restrict__ y,
-                                            Scalars* sc, double* part, int slot) {
+                                            Scalars* sc, double* part, int slot, int post = POST_NONE) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d = fma(x[i], y ? y[i] : x[i], d);
-  grid_reduce(d, 0.0, sc, part, slot);
+  grid_reduce(d, 0.0, sc, part, slot, -1, post);
 }
 
-__global__ void __launch_bounds__(BS) k_sum(int n, const double* __restrict__ x, Scalars* sc, double* part, int slot) {
+// mean of x -> red[slot]
+__global__ void __launch_bounds__(BS) k_mean(int n, const double* __restrict__ x, Scalars* sc, double* part, int slot) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d += x[i];
-  grid_reduce(d, 0.0, sc, part, slot);
+  grid_reduce(d, 0.0, sc, part, slot, -1, POST_MEAN, (double)n);
 }
 
-// x -= red[slot] / n
+// x -= red[slot] (a mean computed by k_mean)
 __global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, const Scalars* sc, int slot) {
-  const double mean = sc->red[slot] / (double)n;
+  const double mean = sc->red[slot];
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) x[i] = x[i] - mean;
 }
 
@@ -305,7 +375,9 @@ __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
     sc->done = 0;
     sc->loops = 0;
     sc->maxiter = maxiter;
-    sc->rz_prev = 0.0;
+    sc->rz = 0.0;
+    sc->rz_valid = 0;
+    sc->alpha = sc->beta = 0.0;
   }
 }
 

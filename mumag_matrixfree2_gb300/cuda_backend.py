@@ -221,6 +221,10 @@ class Problem:
                                                            C.byref(nb)))
         return ms.value, nb.value
 
+    def set_option(self, name: str, value: int):
+        opts = {"graph": 1}
+        self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
+
     def last_solve_ms(self) -> float:
         ms = C.c_double()
         self._check("mm_last_solve_ms", lib().mm_last_solve_ms(self.h, C.byref(ms)))
