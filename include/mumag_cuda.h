@@ -134,6 +134,24 @@ int mm_energy_grad(mm_problem* h, const double* m, const double* U, const double
 int mm_energy_grad_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B_ext,
                        const double* d_B_bias, double* E, double* d_g);
 
+/* Energy and gradient for callers that cannot allocate device memory at call time — for example
+ * code that records the call into its own CUDA graph (allocation is not capturable), or an
+ * application that owns all device memory through a fixed pool and forbids allocations once it
+ * runs.  No counterpart in the reference: it is mm_energy_grad_dev with the scratch of its energy
+ * reduction (one partial per block of 32 magnetic rows, a ticket counter and the total) held in a
+ * file-scope static device array of MM_NOALLOC_SCRATCH_BYTES instead of the problem's workspace,
+ * and it calls no allocating routine.  Inputs and outputs are caller-owned device pointers
+ * (d_B_bias may be NULL); E is a host pointer, written after the problem's stream is synchronized.
+ * Limit: at most MM_NOALLOC_MAX_ROWS magnetic rows (larger problems get MM_ERR_ARG).
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) for that
+ * device; make that first call before any stream capture.  Every call shares the one array (its
+ * ticket counter is cleared by each call), so calls that may overlap on the GPU — from different
+ * streams or problems — race and must be serialized by the caller. */
+#define MM_NOALLOC_MAX_ROWS 1048576
+#define MM_NOALLOC_SCRATCH_BYTES 262400
+int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const double* d_U, const double* B_ext,
+                           const double* d_B_bias, double* E, double* d_g);
+
 /* Exchange + anisotropy Hessian action C v / V_mag.
  * Replaces local_grad_only (src/energy_kernels.py:190-195,272-338). */
 int mm_local_grad(mm_problem* h, const double* v, double* out);

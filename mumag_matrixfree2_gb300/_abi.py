@@ -66,6 +66,7 @@ SIGNATURES = {
     "mm_amg_export_level": (C.c_int, [_vp, C.c_int, _ip, _ip, _dp, _ip]),
     "mm_energy_grad": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "mm_energy_grad_dev": (C.c_int, [_vp, _vp, _vp, _dp, _vp, _dp, _vp]),
+    "mm_energy_grad_noalloc": (C.c_int, [_vp, _vp, _vp, _dp, _vp, _dp, _vp]),
     "mm_local_grad": (C.c_int, [_vp, _dp, _dp]),
     "mm_exchange_diagonal": (C.c_int, [_vp, _dp]),
     "mm_rhs": (C.c_int, [_vp, _dp, _dp, _dp]),

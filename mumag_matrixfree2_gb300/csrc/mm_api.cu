@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -931,6 +932,130 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
 }
 
 }  // namespace
+
+// =============================================================================================
+// allocation-free energy + gradient (see mm_energy_grad_noalloc in include/mumag_cuda.h)
+// =============================================================================================
+namespace {
+
+constexpr int NOALLOC_TPR = 8;                                   // lanes per magnetic row
+constexpr int NOALLOC_RPB = BS / NOALLOC_TPR;                    // rows per block (32)
+constexpr int NOALLOC_MAX_BLOCKS = MM_NOALLOC_MAX_ROWS / NOALLOC_RPB;
+// layout: [0, MAX_BLOCKS) block partials | total | ticket counter (as unsigned) | padding
+constexpr int NOALLOC_WORDS = NOALLOC_MAX_BLOCKS + 32;
+static_assert(NOALLOC_WORDS * sizeof(double) == MM_NOALLOC_SCRATCH_BYTES, "scratch size");
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_WORDS];
+
+// One block per 32 magnetic rows (no grid-stride loop, so the block count follows the row count).
+__global__ void __launch_bounds__(BS) k_energy_grad_noalloc(mmk::EnergyDev op, const double* __restrict__ m,
+                                                            const double* __restrict__ U,
+                                                            const double* __restrict__ Mn, double Bx, double By,
+                                                            double Bz, const double* __restrict__ Bbias,
+                                                            double inv_Vmag, double* __restrict__ g,
+                                                            double* scratch) {
+  constexpr int TPR = NOALLOC_TPR;
+  const int lane = threadIdx.x % TPR;
+  const int r = blockIdx.x * NOALLOC_RPB + threadIdx.x / TPR;
+  const bool valid = r < op.n_rows;
+  double ax, ay, az;
+  mmk::exch_aniso_row<TPR>(op, r, valid, lane, m, ax, ay, az);
+  double ux = 0, uy = 0, uz = 0;
+  if (valid) {
+    const int s = op.ptr[r], e = op.ptr[r + 1];
+    for (int k = s + lane; k < e; k += TPR) {
+      const double u = __ldg(U + op.col[k]);
+      ux += op.gx[k] * u;
+      uy += op.gy[k] * u;
+      uz += op.gz[k] * u;
+    }
+  }
+  ux = mmk::group_sum<TPR>(ux);
+  uy = mmk::group_sum<TPR>(uy);
+  uz = mmk::group_sum<TPR>(uz);
+  double en = 0.0;
+  if (valid && lane == 0) {
+    const int a = op.rows[r];
+    double bx = Bx, by = By, bz = Bz;
+    if (Bbias) {
+      bx += Bbias[3 * a];
+      by += Bbias[3 * a + 1];
+      bz += Bbias[3 * a + 2];
+    }
+    const double mn = -2.0 * Mn[a];
+    const double zx = mn * bx, zy = mn * by, zz = mn * bz;
+    const double gx = (ax + ux) + zx, gy = (ay + uy) + zy, gz = (az + uz) + zz;
+    en = m[3 * a] * (gx + zx) + m[3 * a + 1] * (gy + zy) + m[3 * a + 2] * (gz + zz);
+    g[3 * a] = gx * inv_Vmag;
+    g[3 * a + 1] = gy * inv_Vmag;
+    g[3 * a + 2] = gz * inv_Vmag;
+  }
+  // deterministic reduction: partials in block order, summed by the last block to arrive
+  __shared__ unsigned s_last;
+  en = mmk::block_sum(en);
+  unsigned* ticket = reinterpret_cast<unsigned*>(scratch + NOALLOC_MAX_BLOCKS + 1);
+  if (threadIdx.x == 0) {
+    scratch[blockIdx.x] = en;
+    __threadfence();
+    s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) t += __ldcg(scratch + i);
+    t = mmk::block_sum(t);
+    if (threadIdx.x == 0) {
+      scratch[NOALLOC_MAX_BLOCKS] = t;
+      *ticket = 0u;
+    }
+  }
+}
+
+// Device address of g_noalloc_scratch for the current device, looked up once per device.
+double* noalloc_scratch_for_current_device() {
+  static std::mutex mu;
+  static double* addr[256] = {};
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) throw Fail{MM_ERR_CUDA, "device ordinal out of range"};
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = static_cast<double*>(p);
+  }
+  return addr[dev];
+}
+
+}  // namespace
+
+extern "C" int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const double* d_U, const double* B,
+                                      const double* d_bias, double* E, double* d_g) {
+  if (!h || !d_m || !d_U || !B || !E || !d_g) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (h->eop.n_rows > MM_NOALLOC_MAX_ROWS)
+      throw Fail{MM_ERR_ARG, "mm_energy_grad_noalloc: " + std::to_string(h->eop.n_rows) +
+                                 " magnetic rows exceed MM_NOALLOC_MAX_ROWS (" +
+                                 std::to_string(MM_NOALLOC_MAX_ROWS) + "); use mm_energy_grad_dev"};
+    double* scratch = noalloc_scratch_for_current_device();
+    unsigned* ticket = reinterpret_cast<unsigned*>(scratch + NOALLOC_MAX_BLOCKS + 1);
+    CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned), h->st));                  // must start at zero
+    CK(cudaMemsetAsync(scratch + NOALLOC_MAX_BLOCKS, 0, sizeof(double), h->st));  // total (empty mesh)
+    CK(cudaMemsetAsync(d_g, 0, 3 * (size_t)h->N * sizeof(double), h->st));
+    const int blocks = (h->eop.n_rows + NOALLOC_RPB - 1) / NOALLOC_RPB;
+    if (blocks > 0) {
+      k_energy_grad_noalloc<<<blocks, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2], d_bias,
+                                                      h->inv_Vmag, d_g, scratch);
+      LAUNCH_CHECK();
+    }
+    double total = 0.0;
+    CK(cudaMemcpyAsync(&total, scratch + NOALLOC_MAX_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    *E = 0.5 * total * h->inv_Vmag;
+    return std::isfinite(*E) ? MM_OK : MM_NONFINITE;
+  });
+}
 
 // =============================================================================================
 // C-ABI
