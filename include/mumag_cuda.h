@@ -203,7 +203,19 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * conditional WHILE node loops on the device until convergence; 0 polls the device flag from the
  * host every four iterations (same kernels, same results). */
 #define MM_OPT_GRAPH 1
+/* MM_OPT_PRECISION (before mm_build_poisson): MM_PRECISION_FP64 (default) is the reference's plain
+ * FP64 PCG; MM_PRECISION_MIXED keeps U, the right-hand side and the true residual in FP64 and solves
+ * each correction with an FP32 copy of the hierarchy (FP32 products, FP64 inner products), repeating
+ * until the FP64 residual meets the same tolerance (iterative refinement). */
+#define MM_OPT_PRECISION 2
+#define MM_PRECISION_FP64 0
+#define MM_PRECISION_MIXED 1
+/* MM_OPT_MIXED_ETA_E6: relative residual reduction asked of each FP32 correction solve, in units of
+ * 1e-6 (default 10, i.e. 1e-5). */
+#define MM_OPT_MIXED_ETA_E6 3
 int mm_set_option(mm_problem* h, int option, int value);
+/* Refinement steps (FP32 correction solves) of the last mixed-precision solve. */
+int mm_last_refinements(mm_problem* h, int* steps);
 
 /* Device time of the last demag solve (mm_solve_u / mm_solve_u_dev), measured with CUDA events
  * recorded on the problem's stream around all of its kernels (host<->device copies excluded). */

@@ -78,6 +78,7 @@ SIGNATURES = {
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "mm_last_refinements": (C.c_int, [_vp, _ip]),
     "mm_last_solve_ms": (C.c_int, [_vp, _dp]),
     "mm_launch_count": (C.c_int, [_vp, _lp]),
     "mm_sync": (C.c_int, [_vp]),

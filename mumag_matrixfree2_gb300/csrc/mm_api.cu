@@ -59,12 +59,41 @@ int pick_tpr(int64_t nnz, int64_t rows) {
 //  * sliced ELL, slice height 32, one thread per row (tpr == 1): large matrices with short rows;
 //    padding entries carry value 0 and a valid column;
 //  * compressed rows with tpr lanes per row (2..32): small matrices with long rows.
-struct DevSell {
-  mmk::Sell s{};
-  mmk::Csr c{};
+template <class T>
+struct DevMatT {
+  mmk::SellT<T> s{};
+  mmk::CsrT<T> c{};
   int tpr = 1;
   int64_t nnz = 0;     // stored non-zeros (without padding)
   int64_t stored = 0;  // entries including padding
+};
+
+template <class T>
+struct LevelT {
+  DevMatT<T> A, P, R;
+  T* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
+  T* b = nullptr;    // right-hand side (levels >= 1)
+  T* x = nullptr;    // iterate (pre-smoothing, prolongation)
+  T* x2 = nullptr;   // post-smoothed iterate (levels >= 1)
+  T* res = nullptr;  // residual
+  int n = 0;
+};
+
+// One PCG + preconditioner context in one precision: FP64 for the plain method, FP32 for the inner
+// correction solves of the mixed-precision method.  Reductions are always FP64 (Scalars).
+template <class T>
+struct SolverT {
+  bool built = false;
+  std::vector<LevelT<T>> lv;
+  T* Ainv = nullptr;  // dense inverse of the coarsest level
+  int n_coarse = 0;
+  T* jac = nullptr;   // Jacobi preconditioner 1/(diag+eps)
+  T *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr;
+  mmk::Scalars* sc = nullptr;
+  cudaGraph_t graph = nullptr;        // the PCG iteration loop, conditional WHILE node
+  cudaGraphExec_t exec = nullptr;
+  bool graph_failed = false;
+  int64_t iter_launches = 0;          // kernels in one loop trip
 };
 
 // Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
@@ -110,29 +139,19 @@ struct mm_problem {
   int precond = MM_PRECOND_AMGCL;
   double reg = 1e-12;
   std::vector<mm::AmgLevel> amg_h;
-  struct Level {
-    DevSell A, P, R;
-    double* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
-    double* b = nullptr;    // right-hand side (levels >= 1)
-    double* x = nullptr;    // iterate (pre-smoothing, prolongation)
-    double* x2 = nullptr;   // post-smoothed iterate (levels >= 1)
-    double* res = nullptr;  // residual
-    int n = 0;
-  };
-  std::vector<Level> lv;
-  double* d_Ainv = nullptr;
-  int n_coarse = 0;
-  double* d_jac = nullptr;  // Jacobi preconditioner 1/(diag+eps)
-  double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_Ap = nullptr;
-  double* d_part = nullptr;      // NRED x MAXG block partials
-  mmk::Scalars* d_sc = nullptr;
+  SolverT<double> s64;           // plain FP64 method (and the outer residual of the mixed one)
+  SolverT<float> s32;            // inner solves of the mixed-precision method
+  bool mixed = false;            // MM_OPT_PRECISION
+  double mixed_eta = 1e-5;       // relative reduction asked of each inner FP32 solve
+  int mixed_max_outer = 12;
+  int last_outer = 0;            // refinement steps of the last mixed solve
+  double *d_b = nullptr, *d_x = nullptr, *d_r64 = nullptr;
+  float *d_r32 = nullptr, *d_d32 = nullptr;
+  double* d_part = nullptr;      // NRED x MAXG block partials (shared by every reduction)
+  mmk::Scalars* d_sc = nullptr;  // scalars of the FP64 solver, the energy and the minimizer
+  mmk::Scalars* d_sc32 = nullptr;
   mmk::Scalars* h_sc = nullptr;  // pinned
-  // the PCG iteration loop as a graph with a conditional WHILE node
-  cudaGraph_t loop_graph = nullptr;
-  cudaGraphExec_t loop_exec = nullptr;
-  bool graph_failed = false;
   bool use_graph = true;
-  int64_t iter_launches = 0;  // kernels in one loop trip
 
   // staging buffers for host-pointer calls
   double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
@@ -159,17 +178,24 @@ struct mm_problem {
     if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
   }
-  DevSell upload_mat(const mm::HostCSR& A, bool force_sell = false) {
+  template <class T>
+  T* upload_as(const std::vector<double>& v) {
+    std::vector<T> t(v.begin(), v.end());
+    return upload(t);
+  }
+  template <class T>
+  DevMatT<T> upload_mat(const mm::HostCSR& A, bool force_sell = false) {
     const int tpr = force_sell ? 1 : choose_tpr(A.n_rows, A.nnz());
+    DevMatT<T> d;
+    d.tpr = tpr;
+    d.nnz = A.nnz();
     if (tpr > 1) {
-      DevSell d;
-      d.tpr = tpr;
       d.c.n = A.n_rows;
       d.c.ptr = upload(A.ptr);
       d.c.col = upload(A.col);
-      d.c.val = upload(A.val);
+      d.c.val = upload_as<T>(A.val);
       d.s.n = A.n_rows;
-      d.nnz = d.stored = A.nnz();
+      d.stored = A.nnz();
       return d;
     }
     const int n = A.n_rows;
@@ -199,12 +225,10 @@ struct mm_problem {
         }
       }
     }
-    DevSell d;
     d.s.n = n;
     d.s.sptr = upload(sptr);
     d.s.col = upload(col);
-    d.s.val = upload(val);
-    d.nnz = A.nnz();
+    d.s.val = upload_as<T>(val);
     d.stored = sptr[ns];
     return d;
   }
@@ -236,126 +260,137 @@ using mmk::R_SUM;
 
 #define TPR_SWITCH(tpr, ...)                         \
   switch (tpr) {                                     \
-    case 2: { constexpr int T = 2; __VA_ARGS__; } break;   \
-    case 4: { constexpr int T = 4; __VA_ARGS__; } break;   \
-    case 8: { constexpr int T = 8; __VA_ARGS__; } break;   \
-    case 16: { constexpr int T = 16; __VA_ARGS__; } break; \
-    default: { constexpr int T = 32; __VA_ARGS__; } break; \
+    case 2: { constexpr int TP = 2; __VA_ARGS__; } break;   \
+    case 4: { constexpr int TP = 4; __VA_ARGS__; } break;   \
+    case 8: { constexpr int TP = 8; __VA_ARGS__; } break;   \
+    case 16: { constexpr int TP = 16; __VA_ARGS__; } break; \
+    default: { constexpr int TP = 32; __VA_ARGS__; } break; \
   }
 
-template <int MODE>
-void sell(mm_problem* h, const DevSell& A, const double* x, const double* b, const double* s, double* y,
-          const int* done) {
+template <int MODE, class T>
+void spmv(mm_problem* h, const DevMatT<T>& A, const T* x, const T* b, const T* s, T* y, const int* done) {
   if (A.tpr == 1) {
-    mmk::k_sell<MODE><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
+    mmk::k_sell<MODE, T><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
   } else {
     const int g = grid_rows(A.c.n, A.tpr);
-    TPR_SWITCH(A.tpr, (mmk::k_csr<T, MODE><<<g, BS, 0, h->st>>>(A.c, x, b, s, y, done)));
+    TPR_SWITCH(A.tpr, (mmk::k_csr<TP, MODE><<<g, BS, 0, h->st>>>(A.c, x, b, s, y, done)));
   }
+  LAUNCH_CHECK();
+}
+
+template <class T>
+void dotT(mm_problem* h, int n, const T* x, const T* y, mmk::Scalars* sc, int slot, int post = mmk::POST_NONE) {
+  mmk::k_dot<T><<<grid_elem(n), BS, 0, h->st>>>(n, x, y, sc, h->d_part, slot, post);
   LAUNCH_CHECK();
 }
 
 void dot(mm_problem* h, int n, const double* x, const double* y, int slot, int post = mmk::POST_NONE) {
-  mmk::k_dot<<<grid_elem(n), BS, 0, h->st>>>(n, x, y, h->d_sc, h->d_part, slot, post);
-  LAUNCH_CHECK();
+  dotT<double>(h, n, x, y, h->d_sc, slot, post);
+}
+
+template <class T>
+bool multilevel(mm_problem* h, const SolverT<T>& S) {
+  return (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) && S.lv.size() > 1;
 }
 
 // ---------------------------------------------------------------------------------------------
 // V-cycle (enqueue only).  Level 0's pre-smoothed iterate lv[0].x must already hold s0 .* r.
-// in_loop: the level-0 residual kernel also performs the PCG convergence test.
+// in_loop: the level-0 residual is skipped once the solve has converged.
 // ---------------------------------------------------------------------------------------------
-void enqueue_vcycle(mm_problem* h, const double* r, double* z, bool in_loop, const int* done) {
-  auto& lv = h->lv;
+template <class T>
+void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop, const int* done) {
+  auto& lv = S.lv;
   const int L = (int)lv.size();
   for (int l = 0; l < L - 1; ++l) {
     auto& c = lv[l];
     if (l == 0) {
       if (in_loop) {
-        mmk::k_vc_residual0<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, h->d_sc);
+        mmk::k_vc_residual0<T><<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, S.sc);
         LAUNCH_CHECK();
       } else {
-        sell<1>(h, c.A, c.x, r, nullptr, c.res, done);
+        spmv<1, T>(h, c.A, c.x, r, nullptr, c.res, done);
       }
     } else {
-      sell<1>(h, c.A, c.x, c.b, nullptr, c.res, done);
+      spmv<1, T>(h, c.A, c.x, c.b, nullptr, c.res, done);
     }
     auto& nx = lv[l + 1];
     const bool coarsest = (l + 1 == L - 1);
     if (c.R.tpr == 1) {
-      mmk::k_restrict<<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x, done);
+      mmk::k_restrict<T><<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
+                                                              done);
     } else {
       const int g = grid_rows(nx.n, c.R.tpr);
-      TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<T><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b, coarsest ? nullptr : nx.s,
+      TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<TP><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b, coarsest ? nullptr : nx.s,
                                                                         nx.x, done)));
     }
     LAUNCH_CHECK();
   }
   {
     auto& c = lv[L - 1];
-    mmk::k_dense_mv<<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, h->d_Ainv, c.b, c.x2, done);
+    mmk::k_dense_mv<T><<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, S.Ainv, c.b, c.x2, done);
     LAUNCH_CHECK();
   }
   for (int l = L - 2; l >= 0; --l) {
     auto& c = lv[l];
-    sell<3>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
+    spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
     if (l == 0) {
-      mmk::k_smooth_dot<<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, h->d_sc, h->d_part, done);
+      mmk::k_smooth_dot<T><<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
       LAUNCH_CHECK();
     } else {
-      sell<2>(h, c.A, c.x, c.b, c.s, c.x2, done);
+      spmv<2, T>(h, c.A, c.x, c.b, c.s, c.x2, done);
     }
   }
 }
 
-bool amg_multilevel(mm_problem* h) {
-  return (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) && h->lv.size() > 1;
-}
-
 // z = M^-1 r for Jacobi / no preconditioner / a one-level hierarchy (dense solve); r.z -> red[R_RZ]
-void apply_M_simple(mm_problem* h, const double* r, double* z, const int* done) {
+template <class T>
+void apply_M_simple(mm_problem* h, SolverT<T>& S, const T* r, T* z, const int* done) {
   const int N = h->N;
   if (h->precond == MM_PRECOND_JACOBI) {
-    mmk::k_mul<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_jac, r, z);
+    mmk::k_mul<T><<<grid_elem(N), BS, 0, h->st>>>(N, S.jac, r, z);
     LAUNCH_CHECK();
   } else if (h->precond == MM_PRECOND_NONE) {
-    CK(cudaMemcpyAsync(z, r, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(z, r, N * sizeof(T), cudaMemcpyDeviceToDevice, h->st));
   } else {
-    mmk::k_dense_mv<<<grid_rows(h->n_coarse, 32), BS, 0, h->st>>>(h->n_coarse, h->d_Ainv, r, z, done);
+    mmk::k_dense_mv<T><<<grid_rows(S.n_coarse, 32), BS, 0, h->st>>>(S.n_coarse, S.Ainv, r, z, done);
     LAUNCH_CHECK();
   }
-  dot(h, N, r, z, R_RZ, mmk::POST_RZ);
+  dotT<T>(h, N, r, z, S.sc, R_RZ, mmk::POST_RZ);
 }
 
 // preconditioner application outside the PCG loop
-void enqueue_precond(mm_problem* h, const double* r, double* z) {
-  if (amg_multilevel(h)) {
-    mmk::k_mul<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, h->lv[0].s, r, h->lv[0].x);
+template <class T>
+void enqueue_precond(mm_problem* h, SolverT<T>& S, const T* r, T* z) {
+  if (multilevel(h, S)) {
+    mmk::k_mul<T><<<grid_elem(h->N), BS, 0, h->st>>>(h->N, S.lv[0].s, r, S.lv[0].x);
     LAUNCH_CHECK();
-    enqueue_vcycle(h, r, z, false, nullptr);
+    enqueue_vcycle<T>(h, S, r, z, false, nullptr);
   } else {
-    apply_M_simple(h, r, z, nullptr);
+    apply_M_simple<T>(h, S, r, z, nullptr);
   }
 }
 
-// one PCG iteration on x = d_x (all scalars stay on the device)
-void enqueue_iteration(mm_problem* h) {
+// one PCG iteration on x = S.x (all scalars stay on the device)
+template <class T>
+void enqueue_iteration(mm_problem* h, SolverT<T>& S) {
   const int N = h->N;
-  auto& l0 = h->lv[0];
-  mmk::k_pcg_dir<<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, h->d_z, h->d_p, h->d_Ap, h->d_sc, h->d_part);
+  auto& l0 = S.lv[0];
+  mmk::k_pcg_dir<T><<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
   LAUNCH_CHECK();
-  const bool ml = amg_multilevel(h);
-  mmk::k_pcg_step<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_x, h->d_r, h->d_p, h->d_Ap, ml ? l0.s : nullptr, l0.x,
-                                                   h->d_sc, h->d_part);
+  const bool ml = multilevel(h, S);
+  mmk::k_pcg_step<T><<<grid_elem(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
+                                                      h->d_part);
   LAUNCH_CHECK();
-  if (ml) enqueue_vcycle(h, h->d_r, h->d_z, true, &h->d_sc->done);
-  else apply_M_simple(h, h->d_r, h->d_z, &h->d_sc->done);
+  if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, true, &S.sc->done);
+  else apply_M_simple<T>(h, S, S.r, S.z, &S.sc->done);
 }
 
 // Build the loop graph: WHILE (condition) { iteration; k_set_cond }.  Returns false when the
 // driver cannot build conditional graphs (the host-polled loop is used then).
-bool build_loop_graph(mm_problem* h) {
-  if (h->loop_exec) return true;
-  if (h->graph_failed) return false;
+template <class T>
+bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
+  if (S.exec) return true;
+  if (S.graph_failed) return false;
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ex = nullptr;
   cudaGraphConditionalHandle hnd;
@@ -377,12 +412,12 @@ bool build_loop_graph(mm_problem* h) {
     if (ok) {
       const int64_t saved = h->n_launch;
       try {
-        enqueue_iteration(h);
-        mmk::k_set_cond<<<1, 32, 0, h->st>>>(hnd, h->d_sc);
+        enqueue_iteration<T>(h, S);
+        mmk::k_set_cond<<<1, 32, 0, h->st>>>(hnd, S.sc);
       } catch (const Fail&) {
         ok = false;
       }
-      h->iter_launches = h->n_launch - saved + 1;
+      S.iter_launches = h->n_launch - saved + 1;
       h->n_launch = saved;
       cudaGraph_t out = nullptr;
       const bool end_ok = cudaStreamEndCapture(h->st, &out) == cudaSuccess;
@@ -391,70 +426,50 @@ bool build_loop_graph(mm_problem* h) {
   }
   if (ok) ok = cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
   if (!ok) {
-    cudaGetLastError();  // clear a sticky-free error from the failed attempt
+    cudaGetLastError();  // clear the error of the failed attempt
     if (ex) cudaGraphExecDestroy(ex);
     if (g) cudaGraphDestroy(g);
-    h->graph_failed = true;
+    S.graph_failed = true;
     return false;
   }
-  h->loop_graph = g;
-  h->loop_exec = ex;
+  S.graph = g;
+  S.exec = ex;
   return true;
 }
 
-// PCG on device buffers: x = d_x (initial guess in, solution out), b in d_b with b.b in red[R_BB0].
-int run_pcg(mm_problem* h, double tol, int maxiter, int* iters, double* rel_res) {
+// PCG on S.x (initial guess in, solution out) for the right-hand side S.b; stops on the recursive
+// residual r.r <= tol^2 b.b or maxiter (src/poisson_solve.py:422-478).  Returns iterations and r.r.
+template <class T>
+void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out) {
   const int N = h->N;
-  double* x = h->d_x;
-  const bool zero_mean = !h->has_mask;
-  if (zero_mean) {
-    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, h->d_part, R_SUM);
-    LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_b, h->d_sc, R_SUM);
-    LAUNCH_CHECK();
-    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
-    LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
-    LAUNCH_CHECK();
-  }
-  dot(h, N, h->d_b, nullptr, R_BB);
-  mmk::k_pcg_init_scalars<<<1, 32, 0, h->st>>>(h->d_sc, tol, maxiter);
+  dotT<T>(h, N, S.b, (const T*)nullptr, S.sc, R_BB);
+  mmk::k_pcg_init_scalars<<<1, 32, 0, h->st>>>(S.sc, tol, maxiter);
   LAUNCH_CHECK();
-  const bool ml = amg_multilevel(h);
-  auto& l0 = h->lv[0];
-  mmk::k_init_residual<<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, x, h->d_b, h->d_r, ml ? l0.s : nullptr, l0.x, h->d_sc,
-                                                        h->d_part);
+  const bool ml = multilevel(h, S);
+  auto& l0 = S.lv[0];
+  mmk::k_init_residual<T><<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
+                                                           h->d_part);
   LAUNCH_CHECK();
-  if (ml) enqueue_vcycle(h, h->d_r, h->d_z, false, nullptr);
-  else apply_M_simple(h, h->d_r, h->d_z, nullptr);
-  if (h->use_graph && build_loop_graph(h)) {
-    CK(cudaGraphLaunch(h->loop_exec, h->st));
-    h->n_launch += h->iter_launches;  // one trip; the other trips are counted once their number is known
+  if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
+  else apply_M_simple<T>(h, S, S.r, S.z, nullptr);
+  const bool graph = h->use_graph && build_loop_graph<T>(h, S);
+  if (graph) {
+    CK(cudaGraphLaunch(S.exec, h->st));
   } else {
     for (int i = 0;; ++i) {
-      enqueue_iteration(h);
+      enqueue_iteration<T>(h, S);
       if ((i + 1) % 4 == 0) {
-        CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
         h->sync();
         if (h->h_sc->done || i > maxiter + 8) break;
       }
     }
   }
-  if (zero_mean) {
-    mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
-    LAUNCH_CHECK();
-    mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
-    LAUNCH_CHECK();
-  }
-  CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   h->sync();
-  if (h->use_graph && h->loop_exec) h->n_launch += (int64_t)(h->h_sc->loops - 1) * h->iter_launches;
+  if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
-  const double r2 = h->h_sc->red[R_R2], bb = h->h_sc->red[R_BB0];
-  const double rr = std::sqrt(r2 / (bb + 1e-30));
-  if (rel_res) *rel_res = rr;
-  if (!std::isfinite(rr)) return MM_NONFINITE;
-  return (h->h_sc->it >= maxiter && r2 > h->h_sc->tol2) ? MM_MAXITER : MM_OK;
+  if (r2_out) *r2_out = h->h_sc->red[R_R2];
 }
 
 // b = D m on device (magnetic rows), b.b -> red[R_BB0]
@@ -462,9 +477,51 @@ void enqueue_rhs(mm_problem* h, const double* m) {
   const int N = h->N;
   if (!h->has_mask) CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
   const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<T><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b)));
+  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<TP><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b)));
   LAUNCH_CHECK();
   dot(h, N, h->d_b, nullptr, R_BB0);
+}
+
+void sub_mean(mm_problem* h, double* x) {
+  const int N = h->N;
+  mmk::k_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, h->d_part, R_SUM);
+  LAUNCH_CHECK();
+  mmk::k_sub_mean<<<grid_elem(N), BS, 0, h->st>>>(N, x, h->d_sc, R_SUM);
+  LAUNCH_CHECK();
+}
+
+// Mixed precision: FP64 iterative refinement around FP32 inner PCG solves.  Each step computes the
+// true residual r = b - A x in FP64, solves A d = r / |r| with the FP32 hierarchy to a relative
+// residual eta (never asking more than the remaining reduction), and adds |r| d to x in FP64.
+// Stops when the FP64 residual meets |r| <= tol |b|.  Returns (inner iterations, final r.r).
+int run_mixed(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
+  const int N = h->N;
+  auto& A64 = h->s64.lv[0].A;
+  dot(h, N, h->d_b, nullptr, R_BB);
+  const double bb = h->red(R_BB);
+  int total = 0, outer = 0;
+  double rr = 0.0;
+  while (true) {
+    mmk::k_resid64<<<grid_elem(N), BS, 0, h->st>>>(A64.s, h->d_x, h->d_b, h->d_r64, h->d_sc, h->d_part);
+    LAUNCH_CHECK();
+    rr = h->red(R_R2);
+    if (!(rr > tol * tol * bb) || outer >= h->mixed_max_outer || total >= maxiter || !std::isfinite(rr)) break;
+    const double rn = std::sqrt(rr);
+    mmk::k_to_f32<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_r64, 1.0 / rn, h->d_r32, h->d_d32);
+    LAUNCH_CHECK();
+    const double need = tol * std::sqrt(bb) / rn;  // relative reduction still required
+    const double eta = std::max(h->mixed_eta, 0.5 * need);
+    int it = 0;
+    run_pcg<float>(h, h->s32, eta, std::max(1, maxiter - total), &it, nullptr);
+    total += it;
+    mmk::k_add_f32<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_x, h->d_d32, rn);
+    LAUNCH_CHECK();
+    ++outer;
+  }
+  h->last_outer = outer;
+  if (iters) *iters = total;
+  if (r2_out) *r2_out = rr;
+  return outer;
 }
 
 // demag solve with the potential in d_U (in/out)
@@ -473,20 +530,40 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   CK(cudaEventRecord(h->ev0, h->st));
   if (d_U != h->d_x) CK(cudaMemcpyAsync(h->d_x, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   enqueue_rhs(h, d_m);
-  const int rc = run_pcg(h, tol, maxiter, iters, rel_res);
+  const bool zero_mean = !h->has_mask;
+  if (zero_mean) {
+    sub_mean(h, h->d_b);
+    sub_mean(h, h->d_x);
+  }
+  int it = 0;
+  double r2 = 0.0;
+  double tol2_ref = 0.0;
+  if (h->mixed && h->s32.built) {
+    run_mixed(h, tol, maxiter, &it, &r2);
+    tol2_ref = tol * tol * h->red(R_BB);
+  } else {
+    run_pcg<double>(h, h->s64, tol, maxiter, &it, &r2);
+    tol2_ref = h->h_sc->tol2;
+  }
+  if (zero_mean) sub_mean(h, h->d_x);
   if (d_U != h->d_x) CK(cudaMemcpyAsync(d_U, h->d_x, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   CK(cudaEventRecord(h->ev1, h->st));
   CK(cudaEventSynchronize(h->ev1));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_solve_ms = ms;
-  return rc;
+  const double bb0 = h->red(R_BB0);
+  if (iters) *iters = it;
+  const double rr = std::sqrt(r2 / (bb0 + 1e-30));
+  if (rel_res) *rel_res = rr;
+  if (!std::isfinite(rr)) return MM_NONFINITE;
+  return (it >= maxiter && r2 > tol2_ref) ? MM_MAXITER : MM_OK;
 }
 
 double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
                   double* d_g) {
   const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
+  TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<TP><<<g, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
                                                                       d_bias, h->inv_Vmag, d_g, h->d_sc,
                                                                       h->d_part)));
   LAUNCH_CHECK();
@@ -495,7 +572,7 @@ double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const dou
 
 void local_grad_dev(mm_problem* h, const double* d_v, double* d_out) {
   const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_local_grad<T><<<g, BS, 0, h->st>>>(h->eop, d_v, h->inv_Vmag, d_out)));
+  TPR_SWITCH(h->eop_tpr, (mmk::k_local_grad<TP><<<g, BS, 0, h->st>>>(h->eop, d_v, h->inv_Vmag, d_out)));
   LAUNCH_CHECK();
 }
 
@@ -598,7 +675,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   bool done = false;
   const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
   while (it < c.prm->pc_iters && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
-    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<T><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, c.prm->pc_reg,
+    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, c.prm->pc_reg,
                                                                      h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part, R_C)));
     LAUNCH_CHECK();
     const double pAp = h->red(R_C);
@@ -1057,6 +1134,50 @@ extern "C" int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const do
   });
 }
 
+// Upload the hierarchy in precision T and allocate the solver's vectors.
+template <class T>
+void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, int precond_type) {
+  const int L = (int)h->amg_h.size();
+  S.lv.resize(L);
+  for (int l = 0; l < L; ++l) {
+    const mm::AmgLevel& hl = h->amg_h[l];
+    auto& dl = S.lv[l];
+    dl.n = hl.A.n_rows;
+    dl.A = h->upload_mat<T>(hl.A, l == 0);  // level 0 feeds the fused PCG kernels: always sliced ELL
+    if (l < L - 1) {
+      dl.P = h->upload_mat<T>(hl.P);
+      dl.R = h->upload_mat<T>(hl.R);
+    }
+    if (amg) {
+      std::vector<double> sd(dl.n);
+      for (int i = 0; i < dl.n; ++i)
+        sd[i] = precond_type == MM_PRECOND_AMGCL ? hl.spai0[i] : 0.6667 / (hl.diag[i] + 1e-30);
+      dl.s = h->upload_as<T>(sd);
+    }
+    dl.b = h->alloc<T>(dl.n);
+    dl.x = h->alloc<T>(dl.n);
+    dl.x2 = h->alloc<T>(dl.n);
+    dl.res = h->alloc<T>(dl.n);
+  }
+  if (amg) {
+    const mm::HostCSR& Ac = h->amg_h.back().A;
+    S.n_coarse = Ac.n_rows;
+    S.Ainv = h->upload_as<T>(mm::dense_inverse(Ac));
+  } else {
+    std::vector<double> jac(h->N, 1.0), dg(h->N, 0.0);
+    for (int r = 0; r < A.n_rows; ++r)
+      for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+        if (A.col[k] == r) dg[r] = A.val[k];
+    for (int i = 0; i < h->N; ++i) jac[i] = 1.0 / (dg[i] + 1e-30);
+    S.jac = h->upload_as<T>(jac);
+  }
+  S.r = h->alloc<T>(h->N);
+  S.z = h->alloc<T>(h->N);
+  S.p = h->alloc<T>(h->N);
+  S.Ap = h->alloc<T>(h->N);
+  S.built = true;
+}
+
 // =============================================================================================
 // C-ABI
 // =============================================================================================
@@ -1284,10 +1405,15 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
     h->d_x = h->alloc<double>(N);
     CK(cudaMemsetAsync(h->d_x, 0, N * sizeof(double), h->st));
+    h->d_r64 = h->alloc<double>(N);
+    h->d_r32 = h->alloc<float>(N);
+    h->d_d32 = h->alloc<float>(N);
     h->d_part = h->alloc<double>((size_t)mmk::NRED * MAXG);
     CK(cudaMemsetAsync(h->d_part, 0, (size_t)mmk::NRED * MAXG * sizeof(double), h->st));
     h->d_sc = h->alloc<mmk::Scalars>(1);
     CK(cudaMemsetAsync(h->d_sc, 0, sizeof(mmk::Scalars), h->st));  // ticket counters start at zero
+    h->d_sc32 = h->alloc<mmk::Scalars>(1);
+    CK(cudaMemsetAsync(h->d_sc32, 0, sizeof(mmk::Scalars), h->st));
     CK(cudaMallocHost(&h->h_sc, sizeof(mmk::Scalars)));
     h->sync();
     return MM_OK;
@@ -1304,8 +1430,10 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
 int mm_destroy(mm_problem* h) {
   if (!h) return MM_ERR_ARG;
   if (h->st) cudaStreamSynchronize(h->st);
-  if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
-  if (h->loop_graph) cudaGraphDestroy(h->loop_graph);
+  if (h->s64.exec) cudaGraphExecDestroy(h->s64.exec);
+  if (h->s64.graph) cudaGraphDestroy(h->s64.graph);
+  if (h->s32.exec) cudaGraphExecDestroy(h->s32.exec);
+  if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1336,44 +1464,16 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
       h->amg_h.push_back(L0);
     }
     const int L = (int)h->amg_h.size();
-    h->lv.resize(L);
-    for (int l = 0; l < L; ++l) {
-      const mm::AmgLevel& hl = h->amg_h[l];
-      auto& dl = h->lv[l];
-      dl.n = hl.A.n_rows;
-      dl.A = h->upload_mat(hl.A, l == 0);  // level 0 feeds the fused PCG kernels: always sliced ELL
-      if (l < L - 1) {
-        dl.P = h->upload_mat(hl.P);
-        dl.R = h->upload_mat(hl.R);
-      }
-      if (amg) {
-        std::vector<double> s(dl.n);
-        for (int i = 0; i < dl.n; ++i)
-          s[i] = precond_type == MM_PRECOND_AMGCL ? hl.spai0[i] : 0.6667 / (hl.diag[i] + 1e-30);
-        dl.s = h->upload(s);
-      }
-      dl.b = h->alloc<double>(dl.n);
-      dl.x = h->alloc<double>(dl.n);
-      dl.x2 = h->alloc<double>(dl.n);
-      dl.res = h->alloc<double>(dl.n);
+    build_solver<double>(h, h->s64, A, amg, precond_type);
+    h->s64.b = h->d_b;
+    h->s64.x = h->d_x;
+    h->s64.sc = h->d_sc;
+    if (h->mixed) {
+      build_solver<float>(h, h->s32, A, amg, precond_type);
+      h->s32.b = h->d_r32;
+      h->s32.x = h->d_d32;
+      h->s32.sc = h->d_sc32;
     }
-    if (amg) {
-      const mm::HostCSR& Ac = h->amg_h.back().A;
-      h->n_coarse = Ac.n_rows;
-      h->d_Ainv = h->upload(mm::dense_inverse(Ac));
-    } else {
-      std::vector<double> jac(h->N, 1.0);
-      std::vector<double> dg(h->N, 0.0);
-      for (int r = 0; r < A.n_rows; ++r)
-        for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
-          if (A.col[k] == r) dg[r] = A.val[k];
-      for (int i = 0; i < h->N; ++i) jac[i] = 1.0 / (dg[i] + 1e-30);
-      h->d_jac = h->upload(jac);
-    }
-    h->d_r = h->alloc<double>(h->N);
-    h->d_z = h->alloc<double>(h->N);
-    h->d_p = h->alloc<double>(h->N);
-    h->d_Ap = h->alloc<double>(h->N);
     h->sync();
     h->poisson_built = true;
     if (n_levels) *n_levels = L;
@@ -1473,7 +1573,7 @@ int mm_apply_A(mm_problem* h, const double* U, double* y) {
   return guarded(h, [&] {
     if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
     CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    sell<0>(h, h->lv[0].A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+    spmv<0, double>(h, h->s64.lv[0].A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
     CK(cudaMemcpyAsync(y, h->d_out, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     h->sync();
     return MM_OK;
@@ -1485,7 +1585,7 @@ int mm_precond(mm_problem* h, const double* r, double* z) {
   return guarded(h, [&] {
     if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
     CK(cudaMemcpyAsync(h->d_U, r, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    enqueue_precond(h, h->d_U, h->d_out);
+    enqueue_precond<double>(h, h->s64, h->d_U, h->d_out);
     CK(cudaMemcpyAsync(z, h->d_out, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     h->sync();
     return MM_OK;
@@ -1557,18 +1657,18 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     CK(cudaEventCreate(&e1));
     const int N = h->N;
     double acc = 0.0, nbytes = 0.0;
-    const mm_problem::Level* l0 = h->poisson_built ? &h->lv[0] : nullptr;
+    const LevelT<double>* l0 = h->poisson_built ? &h->s64.lv[0] : nullptr;
     auto launch = [&]() {
       if (kernel == MM_KERNEL_SPMV_A) {
-        sell<0>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
+        spmv<0, double>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
       } else if (kernel == MM_KERNEL_SMOOTH) {
         const double* s = l0->s ? l0->s : h->d_U;
-        mmk::k_smooth_dot<<<grid_elem(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
+        mmk::k_smooth_dot<double><<<grid_elem(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
                                                                 nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
         const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-        TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<T><<<g, BS, 0, h->st>>>(h->eop, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
+        TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<TP><<<g, BS, 0, h->st>>>(h->eop, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
                                                                             1.0, nullptr, h->inv_Vmag, h->d_g,
                                                                             h->d_sc, h->d_part)));
         LAUNCH_CHECK();
@@ -1617,7 +1717,24 @@ int mm_set_option(mm_problem* h, int option, int value) {
     h->use_graph = value != 0;
     return MM_OK;
   }
+  if (option == MM_OPT_PRECISION) {
+    if (h->poisson_built) return MM_ERR_STATE;  // the FP32 hierarchy is built by mm_build_poisson
+    if (value != MM_PRECISION_FP64 && value != MM_PRECISION_MIXED) return MM_ERR_ARG;
+    h->mixed = value == MM_PRECISION_MIXED;
+    return MM_OK;
+  }
+  if (option == MM_OPT_MIXED_ETA_E6) {
+    if (value <= 0 || value >= 1000000) return MM_ERR_ARG;
+    h->mixed_eta = value * 1e-6;
+    return MM_OK;
+  }
   return MM_ERR_ARG;
+}
+
+int mm_last_refinements(mm_problem* h, int* steps) {
+  if (!h || !steps) return MM_ERR_ARG;
+  *steps = h->last_outer;
+  return MM_OK;
 }
 
 int mm_last_solve_ms(mm_problem* h, double* ms) {

@@ -126,63 +126,72 @@ __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, d
 }
 
 // ------------------------------------------------------------------------------------------
-// sliced ELL (slice height 32): entry k of row r lives at sptr[r/32] + 32 k + r%32
+// Solver kernels, templated on the storage/arithmetic type T of the operator and the vectors:
+// T = double for the plain FP64 method, T = float for the inner solves of the mixed-precision
+// method.  Inner products and every reduction are accumulated in FP64 in both cases.
 // ------------------------------------------------------------------------------------------
-struct Sell {
+template <class T>
+__device__ __forceinline__ T fmaT(T a, T b, T c) { return fma(a, b, c); }
+
+// sliced ELL (slice height 32): entry k of row r lives at sptr[r/32] + 32 k + r%32
+template <class T>
+struct SellT {
   int n;
   const int* sptr;
   const int* col;
-  const double* val;
+  const T* val;
 };
+using Sell = SellT<double>;
 
-__device__ __forceinline__ double sell_row(const Sell& A, const double* __restrict__ x, int row) {
+template <class T>
+__device__ __forceinline__ T sell_row(const SellT<T>& A, const T* __restrict__ x, int row) {
   const int s = row >> 5;
   const int b0 = __ldg(A.sptr + s);
   const int w = (__ldg(A.sptr + s + 1) - b0) >> 5;
   const int base = b0 + (row & 31);
-  double acc = 0.0;
+  T acc = T(0);
 #pragma unroll 4
   for (int k = 0; k < w; ++k) {
     const int c = __ldg(A.col + base + 32 * k);
-    acc = fma(__ldg(A.val + base + 32 * k), __ldg(x + c), acc);
+    acc = fmaT<T>(__ldg(A.val + base + 32 * k), __ldg(x + c), acc);
   }
   return acc;
 }
 
-// ------------------------------------------------------------------------------------------
 // compressed rows with TPR lanes per row (small levels with long rows, where one thread per row
 // would leave most of the GPU idle)
-// ------------------------------------------------------------------------------------------
-struct Csr {
+template <class T>
+struct CsrT {
   int n;
   const int* ptr;
   const int* col;
-  const double* val;
+  const T* val;
 };
+using Csr = CsrT<double>;
 
-template <int TPR>
-__device__ __forceinline__ double csr_row(const Csr& A, const double* __restrict__ x, int row, bool valid, int lane) {
-  double acc = 0.0;
+template <int TPR, class T>
+__device__ __forceinline__ T csr_row(const CsrT<T>& A, const T* __restrict__ x, int row, bool valid, int lane) {
+  T acc = T(0);
   if (valid) {
     const int s = __ldg(A.ptr + row), e = __ldg(A.ptr + row + 1);
-    for (int k = s + lane; k < e; k += TPR) acc = fma(__ldg(A.val + k), __ldg(x + __ldg(A.col + k)), acc);
+    for (int k = s + lane; k < e; k += TPR) acc = fmaT<T>(__ldg(A.val + k), __ldg(x + __ldg(A.col + k)), acc);
   }
 #pragma unroll
   for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   return acc;
 }
 
-// same modes as k_sell
-template <int TPR, int MODE>
-__global__ void __launch_bounds__(BS) k_csr(Csr A, const double* __restrict__ x, const double* b,
-                                            const double* __restrict__ s, double* y, const int* __restrict__ done) {
+// mode 0: y = A x ; 1: y = b - A x ; 2: y = x + s .* (b - A x) ; 3: y = b + A x (prolongation)
+template <int TPR, int MODE, class T>
+__global__ void __launch_bounds__(BS) k_csr(CsrT<T> A, const T* __restrict__ x, const T* b, const T* __restrict__ s,
+                                            T* y, const int* __restrict__ done) {
   if (done && *done) return;
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
   for (int rb = blockIdx.x * RPB; rb < A.n; rb += gridDim.x * RPB) {
     const int row = rb + threadIdx.x / TPR;
     const bool valid = row < A.n;
-    const double ax = csr_row<TPR>(A, x, row, valid, lane);
+    const T ax = csr_row<TPR, T>(A, x, row, valid, lane);
     if (valid && lane == 0) {
       if (MODE == 0) y[row] = ax;
       else if (MODE == 1) y[row] = b[row] - ax;
@@ -193,9 +202,9 @@ __global__ void __launch_bounds__(BS) k_csr(Csr A, const double* __restrict__ x,
 }
 
 // restriction with compressed rows, fused with the coarse pre-smoothing from zero
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_restrict_csr(Csr R, const double* __restrict__ res, double* __restrict__ bc,
-                                                     const double* __restrict__ s_c, double* __restrict__ xc,
+template <int TPR, class T>
+__global__ void __launch_bounds__(BS) k_restrict_csr(CsrT<T> R, const T* __restrict__ res, T* __restrict__ bc,
+                                                     const T* __restrict__ s_c, T* __restrict__ xc,
                                                      const int* __restrict__ done) {
   if (done && *done) return;
   constexpr int RPB = BS / TPR;
@@ -203,7 +212,7 @@ __global__ void __launch_bounds__(BS) k_restrict_csr(Csr R, const double* __rest
   for (int rb = blockIdx.x * RPB; rb < R.n; rb += gridDim.x * RPB) {
     const int row = rb + threadIdx.x / TPR;
     const bool valid = row < R.n;
-    const double v = csr_row<TPR>(R, res, row, valid, lane);
+    const T v = csr_row<TPR, T>(R, res, row, valid, lane);
     if (valid && lane == 0) {
       bc[row] = v;
       if (s_c) xc[row] = s_c[row] * v;
@@ -211,13 +220,12 @@ __global__ void __launch_bounds__(BS) k_restrict_csr(Csr R, const double* __rest
   }
 }
 
-// mode 0: y = A x ; 1: y = b - A x ; 2: y = x + s .* (b - A x) ; 3: y = b + A x (prolongation)
-template <int MODE>
-__global__ void __launch_bounds__(BS) k_sell(Sell A, const double* __restrict__ x, const double* b,
-                                             const double* __restrict__ s, double* y, const int* __restrict__ done) {
+template <int MODE, class T>
+__global__ void __launch_bounds__(BS) k_sell(SellT<T> A, const T* __restrict__ x, const T* b,
+                                             const T* __restrict__ s, T* y, const int* __restrict__ done) {
   if (done && *done) return;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const double ax = sell_row(A, x, row);
+    const T ax = sell_row<T>(A, x, row);
     if (MODE == 0) y[row] = ax;
     else if (MODE == 1) y[row] = b[row] - ax;
     else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);
@@ -226,87 +234,90 @@ __global__ void __launch_bounds__(BS) k_sell(Sell A, const double* __restrict__ 
 }
 
 // r = b - A x ; r.r -> red[R_R2] ; xv = s .* r (level-0 pre-smoothing from zero)
-__global__ void __launch_bounds__(BS) k_init_residual(Sell A, const double* __restrict__ x,
-                                                      const double* __restrict__ b, double* __restrict__ r,
-                                                      const double* __restrict__ s, double* __restrict__ xv,
+template <class T>
+__global__ void __launch_bounds__(BS) k_init_residual(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
+                                                      T* __restrict__ r, const T* __restrict__ s, T* __restrict__ xv,
                                                       Scalars* sc, double* part) {
   double d = 0.0;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const double ri = b[row] - sell_row(A, x, row);
+    const T ri = b[row] - sell_row<T>(A, x, row);
     r[row] = ri;
-    d = fma(ri, ri, d);
+    d = fma((double)ri, (double)ri, d);
     if (s) xv[row] = s[row] * ri;
   }
   grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_INIT);
 }
 
 // PCG direction update fused with the operator product:
-//   stop when r.r <= tol2 or it >= maxiter;  beta = it == 0 ? 0 : rz / (rz_prev + eps)
 //   y = A z ; p = z + beta p ; Ap = y + beta Ap ; p.Ap -> red[R_PAP]
 // (A p_new = A z + beta A p_old, so the product is taken on z, complete before the launch)
-__global__ void __launch_bounds__(BS) k_pcg_dir(Sell A, const double* __restrict__ z, double* __restrict__ p,
-                                                double* __restrict__ Ap, Scalars* sc, double* part) {
+template <class T>
+__global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict__ z, T* __restrict__ p,
+                                                T* __restrict__ Ap, Scalars* sc, double* part) {
   if (sc->done) return;
-  const double beta = sc->beta;
+  const T beta = (T)sc->beta;
   double d = 0.0;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const double az = sell_row(A, z, row);
-    const double pn = z[row] + beta * p[row];
-    const double apn = az + beta * Ap[row];
+    const T az = sell_row<T>(A, z, row);
+    const T pn = z[row] + beta * p[row];
+    const T apn = az + beta * Ap[row];
     p[row] = pn;
     Ap[row] = apn;
-    d = fma(pn, apn, d);
+    d = fma((double)pn, (double)apn, d);
   }
   grid_reduce(d, 0.0, sc, part, R_PAP, -1, POST_PAP);
 }
 
-// alpha = rz / (p.Ap + eps); x += alpha p ; r -= alpha Ap ; r.r -> red[R_R2] ; xv = s .* r
-__global__ void __launch_bounds__(BS) k_pcg_step(int n, double* __restrict__ x, double* __restrict__ r,
-                                                 const double* __restrict__ p, const double* __restrict__ Ap,
-                                                 const double* __restrict__ s0, double* __restrict__ xv, Scalars* sc,
-                                                 double* part) {
+// x += alpha p ; r -= alpha Ap ; r.r -> red[R_R2] ; xv = s .* r
+template <class T>
+__global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                                                 const T* __restrict__ Ap, const T* __restrict__ s0, T* __restrict__ xv,
+                                                 Scalars* sc, double* part) {
   if (sc->done) return;
-  const double alpha = sc->alpha;
+  const T alpha = (T)sc->alpha;
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
     x[i] = x[i] + alpha * p[i];
-    const double ri = r[i] - alpha * Ap[i];
+    const T ri = r[i] - alpha * Ap[i];
     r[i] = ri;
-    d = fma(ri, ri, d);
+    d = fma((double)ri, (double)ri, d);
     if (s0) xv[i] = s0[i] * ri;
   }
   grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
 
-// level-0 residual res = r - A xv, with the PCG convergence test first
-__global__ void __launch_bounds__(BS) k_vc_residual0(Sell A, const double* __restrict__ xv, const double* __restrict__ r,
-                                                     double* __restrict__ res, Scalars* sc) {
+// level-0 residual res = r - A xv (skipped once the solve has converged)
+template <class T>
+__global__ void __launch_bounds__(BS) k_vc_residual0(SellT<T> A, const T* __restrict__ xv, const T* __restrict__ r,
+                                                     T* __restrict__ res, Scalars* sc) {
   if (sc->done) return;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS)
-    res[row] = r[row] - sell_row(A, xv, row);
+    res[row] = r[row] - sell_row<T>(A, xv, row);
 }
 
 // restriction b_c = R res, fused with the coarse pre-smoothing from zero x_c = s_c .* b_c
-__global__ void __launch_bounds__(BS) k_restrict(Sell R, const double* __restrict__ res, double* __restrict__ bc,
-                                                 const double* __restrict__ s_c, double* __restrict__ xc,
+template <class T>
+__global__ void __launch_bounds__(BS) k_restrict(SellT<T> R, const T* __restrict__ res, T* __restrict__ bc,
+                                                 const T* __restrict__ s_c, T* __restrict__ xc,
                                                  const int* __restrict__ done) {
   if (done && *done) return;
   for (int row = blockIdx.x * BS + threadIdx.x; row < R.n; row += gridDim.x * BS) {
-    const double v = sell_row(R, res, row);
+    const T v = sell_row<T>(R, res, row);
     bc[row] = v;
     if (s_c) xc[row] = s_c[row] * v;
   }
 }
 
 // dense coarsest solve x = Ainv b (row-major n x n), one warp per row
-__global__ void __launch_bounds__(BS) k_dense_mv(int n, const double* __restrict__ Ainv, const double* __restrict__ b,
-                                                 double* __restrict__ x, const int* __restrict__ done) {
+template <class T>
+__global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ainv, const T* __restrict__ b,
+                                                 T* __restrict__ x, const int* __restrict__ done) {
   if (done && *done) return;
   const int lane = threadIdx.x & 31;
   for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gridDim.x * (BS / 32)) {
-    const double* a = Ainv + (size_t)row * n;
-    double acc = 0.0;
-    for (int k = lane; k < n; k += 32) acc = fma(a[k], b[k], acc);
+    const T* a = Ainv + (size_t)row * n;
+    T acc = T(0);
+    for (int k = lane; k < n; k += 32) acc = fmaT<T>(a[k], b[k], acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) x[row] = acc;
@@ -315,15 +326,16 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const double* __restrict
 
 // post-smoothing y = x + s .* (b - A x); with `part` it also reduces b.y into red[R_RZ]
 // (level 0: b = r and y = z)
-__global__ void __launch_bounds__(BS) k_smooth_dot(Sell A, const double* __restrict__ x, const double* __restrict__ b,
-                                                   const double* __restrict__ s, double* __restrict__ y, Scalars* sc,
+template <class T>
+__global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
+                                                   const T* __restrict__ s, T* __restrict__ y, Scalars* sc,
                                                    double* part, const int* __restrict__ done) {
   if (done && *done) return;
   double d = 0.0;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const double yi = x[row] + s[row] * (b[row] - sell_row(A, x, row));
+    const T yi = x[row] + s[row] * (b[row] - sell_row<T>(A, x, row));
     y[row] = yi;
-    d = fma(b[row], yi, d);
+    d = fma((double)b[row], (double)yi, d);
   }
   if (part) grid_reduce(d, 0.0, sc, part, R_RZ, -1, POST_RZ);
 }
@@ -340,11 +352,13 @@ __global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
 // ------------------------------------------------------------------------------------------
 // vector kernels
 // ------------------------------------------------------------------------------------------
-// x.y (y == nullptr: x.x) -> red[slot]
-__global__ void __launch_bounds__(BS) k_dot(int n, const double* __restrict__ x, const double* __restrict__ y,
-                                            Scalars* sc, double* part, int slot, int post = POST_NONE) {
+// x.y (y == nullptr: x.x) -> red[slot], accumulated in FP64
+template <class T>
+__global__ void __launch_bounds__(BS) k_dot(int n, const T* __restrict__ x, const T* __restrict__ y, Scalars* sc,
+                                            double* part, int slot, int post = POST_NONE) {
   double d = 0.0;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d = fma(x[i], y ? y[i] : x[i], d);
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS)
+    d = fma((double)x[i], (double)(y ? y[i] : x[i]), d);
   grid_reduce(d, 0.0, sc, part, slot, -1, post);
 }
 
@@ -362,8 +376,9 @@ __global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, 
 }
 
 // out = s .* r
-__global__ void __launch_bounds__(BS) k_mul(int n, const double* __restrict__ s, const double* __restrict__ r,
-                                            double* __restrict__ out) {
+template <class T>
+__global__ void __launch_bounds__(BS) k_mul(int n, const T* __restrict__ s, const T* __restrict__ r,
+                                            T* __restrict__ out) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = s[i] * r[i];
 }
 
@@ -379,6 +394,36 @@ __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
     sc->rz_valid = 0;
     sc->alpha = sc->beta = 0.0;
   }
+}
+
+// ------------------------------------------------------------------------------------------
+// mixed-precision iterative refinement (FP64 outer residual, FP32 inner correction solve)
+// ------------------------------------------------------------------------------------------
+// r = b - A x in FP64; r.r -> red[R_R2]
+__global__ void __launch_bounds__(BS) k_resid64(Sell A, const double* __restrict__ x, const double* __restrict__ b,
+                                                double* __restrict__ r, Scalars* sc, double* part) {
+  double d = 0.0;
+  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
+    const double ri = b[row] - sell_row<double>(A, x, row);
+    r[row] = ri;
+    d = fma(ri, ri, d);
+  }
+  grid_reduce(d, 0.0, sc, part, R_R2);
+}
+
+// r32 = r * scale (the inner system is solved for a unit-norm right-hand side); d32 = 0
+__global__ void __launch_bounds__(BS) k_to_f32(int n, const double* __restrict__ r, double scale,
+                                               float* __restrict__ r32, float* __restrict__ d32) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    r32[i] = (float)(r[i] * scale);
+    d32[i] = 0.0f;
+  }
+}
+
+// x += scale * d32 in FP64
+__global__ void __launch_bounds__(BS) k_add_f32(int n, double* __restrict__ x, const float* __restrict__ d32,
+                                                double scale) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) x[i] = fma(scale, (double)d32[i], x[i]);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -222,8 +222,17 @@ class Problem:
         return ms.value, nb.value
 
     def set_option(self, name: str, value: int):
-        opts = {"graph": 1}
+        opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3}
         self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
+
+    def set_precision(self, precision: str):
+        """"fp64" (the reference's plain method) or "mixed"; call before build_poisson()."""
+        self.set_option("precision", {"fp64": 0, "mixed": 1}[precision])
+
+    def last_refinements(self) -> int:
+        n = C.c_int()
+        self._check("mm_last_refinements", lib().mm_last_refinements(self.h, C.byref(n)))
+        return n.value
 
     def last_solve_ms(self) -> float:
         ms = C.c_double()

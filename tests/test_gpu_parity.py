@@ -161,3 +161,24 @@ def test_minimizer_matches_oracle(cuda_ok, method):
     assert info["evals"] == info_ref["evals"]
     assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
     assert np.max(np.abs(m - m_ref)) <= 1e-7
+
+
+@pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
+def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
+    """FP32 correction solves inside FP64 iterative refinement: the true FP64 residual meets the
+    same tolerance and the potential matches the plain FP64 solve to that tolerance."""
+    s, p, _ = case(name)
+    plain = fem_utils.make_problem(s)
+    plain.build_poisson(1e-12, "amgcl")
+    mixed = fem_utils.make_problem(s)
+    mixed.set_precision("mixed")
+    mixed.build_poisson(1e-12, "amgcl")
+    ops = opo.SolveU(p, ofem.assembled_operators(p, parts=("A", "D")), cg_tol=1e-10)
+    m = random_state(p.N, seed=31, amplitude=0.05)
+    U64, it64, rr64, _ = plain.solve_u(m, np.zeros(p.N), 1e-10)
+    U32, it32, rr32, rc = mixed.solve_u(m, np.zeros(p.N), 1e-10)
+    assert rc == 0 and rr32 <= 1e-10 and mixed.last_refinements() >= 1
+    b = ops.rhs(m)
+    true_rr = np.linalg.norm(b - ops.apply_A(U32)) / np.linalg.norm(b)
+    assert true_rr <= 1.5e-10  # checked in FP64 on the host
+    assert rel(U32, U64) <= 1e-8
