@@ -213,6 +213,9 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 /* MM_OPT_MIXED_ETA_E6: relative residual reduction asked of each FP32 correction solve, in units of
  * 1e-6 (default 10, i.e. 1e-5). */
 #define MM_OPT_MIXED_ETA_E6 3
+/* MM_OPT_GRID_CAP: largest grid (blocks of 256 threads) of the one-row-per-thread kernels; beyond
+ * it they loop (default 4096).  Process-wide; fixed values keep every reduction deterministic. */
+#define MM_OPT_GRID_CAP 4
 int mm_set_option(mm_problem* h, int option, int value);
 /* Refinement steps (FP32 correction solves) of the last mixed-precision solve. */
 int mm_last_refinements(mm_problem* h, int* steps);

@@ -40,7 +40,12 @@ struct Fail {
     CK(cudaGetLastError()); \
   } while (0)
 
-inline int grid_elem(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + BS - 1) / BS, MAXG)); }
+// Upper bound on the blocks of a one-row-per-thread kernel (grid-stride beyond it); a tunable of
+// the problem (MM_OPT_GRID_CAP), fixed per run so reductions stay deterministic.
+int g_elem_cap = MAXG;
+inline int grid_elem(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + BS - 1) / BS, g_elem_cap));
+}
 inline int grid_rows(int64_t n, int tpr) {
   const int rpb = BS / tpr;
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + rpb - 1) / rpb, MAXG));
@@ -1721,6 +1726,11 @@ int mm_set_option(mm_problem* h, int option, int value) {
     if (h->poisson_built) return MM_ERR_STATE;  // the FP32 hierarchy is built by mm_build_poisson
     if (value != MM_PRECISION_FP64 && value != MM_PRECISION_MIXED) return MM_ERR_ARG;
     h->mixed = value == MM_PRECISION_MIXED;
+    return MM_OK;
+  }
+  if (option == MM_OPT_GRID_CAP) {
+    if (value < 1 || value > MAXG) return MM_ERR_ARG;
+    g_elem_cap = value;
     return MM_OK;
   }
   if (option == MM_OPT_MIXED_ETA_E6) {

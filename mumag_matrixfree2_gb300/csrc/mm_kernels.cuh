@@ -27,6 +27,8 @@ struct Scalars {
   double rz;        // current r.z
   double alpha;     // rz / (p.Ap + eps), set when p.Ap is reduced
   double beta;      // rz_new / (rz_old + eps), set when r.z is reduced (0 for the first direction)
+  float alpha_f;    // alpha and beta rounded once for the FP32 kernels
+  float beta_f;
   int it;           // completed PCG iterations
   int done;         // 1 once converged or out of iterations (set when r.r is reduced)
   int maxiter;
@@ -79,11 +81,22 @@ __device__ __forceinline__ double block_sum(double v) { return block_reduce<fals
 // Grid reduction of up to two values into sc->red[slot0], sc->red[slot1] (slot1 < 0: one value).
 // Partials go to part + slot * MAXG; the ticket counter of slot0 elects the finishing block.
 template <bool MAX = false>
+__device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, double* part, int slot0,
+                                            int slot1 = -1, int post = POST_NONE, double post_arg = 0.0);
+
+template <bool MAX = false>
 __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, double* part, int slot0,
                                             int slot1 = -1, int post = POST_NONE, double post_arg = 0.0) {
-  __shared__ unsigned s_last;
   v0 = block_reduce<MAX>(v0);
   if (slot1 >= 0) v1 = block_reduce<MAX>(v1);
+  grid_finish<MAX>(v0, v1, sc, part, slot0, slot1, post, post_arg);
+}
+
+// block values v0, v1 (identical in every thread of the block) -> grid total in sc->red
+template <bool MAX>
+__device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, double* part, int slot0, int slot1,
+                                            int post, double post_arg) {
+  __shared__ unsigned s_last;
   if (threadIdx.x == 0) {
     part[(size_t)slot0 * MAXG + blockIdx.x] = v0;
     if (slot1 >= 0) part[(size_t)slot1 * MAXG + blockIdx.x] = v1;
@@ -111,11 +124,13 @@ __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, d
       sc->cnt[slot0] = 0u;
       if (post == POST_PAP) {
         sc->alpha = sc->rz / (a + 1e-30);
+        sc->alpha_f = (float)sc->alpha;
       } else if (post == POST_R2_STEP || post == POST_R2_INIT) {
         if (post == POST_R2_STEP) sc->it += 1;
         if (a <= sc->tol2 || sc->it >= sc->maxiter) sc->done = 1;
       } else if (post == POST_RZ) {
         sc->beta = sc->rz_valid ? a / (sc->rz + 1e-30) : 0.0;
+        sc->beta_f = (float)sc->beta;
         sc->rz = a;
         sc->rz_valid = 1;
       } else if (post == POST_MEAN) {
@@ -132,6 +147,79 @@ __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, d
 // ------------------------------------------------------------------------------------------
 template <class T>
 __device__ __forceinline__ T fmaT(T a, T b, T c) { return fma(a, b, c); }
+
+// Inner-product accumulators.  FP64 kernels accumulate in FP64.  FP32 kernels accumulate in
+// float-float: the product of two floats is split exactly into hi + lo with one FMA (TwoProd) and
+// added with Knuth's TwoSum, so the sum keeps ~48 significant bits while using only FP32 pipes
+// (FP64 issue is ~1/64 of FP32 on this GPU); it becomes FP64 once per warp.
+template <class T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double warp_total() { return warp_sum(s); }  // valid on lane 0
+};
+template <>
+struct Acc<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ static void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+  }
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = a * b;
+    const float pe = fmaf(a, b, -p);  // exact: a*b = p + pe
+    float t, e;
+    two_sum(hi, p, t, e);
+    hi = t;
+    lo += e + pe;
+  }
+  __device__ __forceinline__ void merge(float h2, float l2) {
+    float t, e;
+    two_sum(hi, h2, t, e);
+    hi = t;
+    lo += e + l2;
+  }
+  __device__ __forceinline__ double warp_total() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+      const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+      merge(h2, l2);
+    }
+    return (double)hi + (double)lo;  // valid on lane 0
+  }
+};
+
+// A scalar in the kernel's precision (the FP32 copy is rounded once, by the reducing block).
+template <class T>
+__device__ __forceinline__ T scal(double d, float f);
+template <>
+__device__ __forceinline__ double scal<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float scal<float>(double, float f) { return f; }
+
+// Block total of an accumulator, returned to every thread (FP64 only across the warp leaders).
+template <class T>
+__device__ __forceinline__ double block_total(Acc<T>& acc) {
+  __shared__ double s_w[BS / 32];
+  __shared__ double s_out;
+  const double w = acc.warp_total();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) s_w[wid] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < BS / 32; ++i) t += s_w[i];
+    s_out = t;
+  }
+  __syncthreads();
+  return s_out;
+}
 
 // sliced ELL (slice height 32): entry k of row r lives at sptr[r/32] + 32 k + r%32
 template <class T>
@@ -238,14 +326,14 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_init_residual(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                       T* __restrict__ r, const T* __restrict__ s, T* __restrict__ xv,
                                                       Scalars* sc, double* part) {
-  double d = 0.0;
+  Acc<T> acc;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
     const T ri = b[row] - sell_row<T>(A, x, row);
     r[row] = ri;
-    d = fma((double)ri, (double)ri, d);
+    acc.add(ri, ri);
     if (s) xv[row] = s[row] * ri;
   }
-  grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_INIT);
+  grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_INIT);
 }
 
 // PCG direction update fused with the operator product:
@@ -255,17 +343,17 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict__ z, T* __restrict__ p,
                                                 T* __restrict__ Ap, Scalars* sc, double* part) {
   if (sc->done) return;
-  const T beta = (T)sc->beta;
-  double d = 0.0;
+  const T beta = scal<T>(sc->beta, sc->beta_f);
+  Acc<T> acc;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
     const T az = sell_row<T>(A, z, row);
     const T pn = z[row] + beta * p[row];
     const T apn = az + beta * Ap[row];
     p[row] = pn;
     Ap[row] = apn;
-    d = fma((double)pn, (double)apn, d);
+    acc.add(pn, apn);
   }
-  grid_reduce(d, 0.0, sc, part, R_PAP, -1, POST_PAP);
+  grid_finish(block_total(acc), 0.0, sc, part, R_PAP, -1, POST_PAP);
 }
 
 // x += alpha p ; r -= alpha Ap ; r.r -> red[R_R2] ; xv = s .* r
@@ -274,16 +362,16 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __
                                                  const T* __restrict__ Ap, const T* __restrict__ s0, T* __restrict__ xv,
                                                  Scalars* sc, double* part) {
   if (sc->done) return;
-  const T alpha = (T)sc->alpha;
-  double d = 0.0;
+  const T alpha = scal<T>(sc->alpha, sc->alpha_f);
+  Acc<T> acc;
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
     x[i] = x[i] + alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
     r[i] = ri;
-    d = fma((double)ri, (double)ri, d);
+    acc.add(ri, ri);
     if (s0) xv[i] = s0[i] * ri;
   }
-  grid_reduce(d, 0.0, sc, part, R_R2, -1, POST_R2_STEP);
+  grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
 
 // level-0 residual res = r - A xv (skipped once the solve has converged)
@@ -331,13 +419,13 @@ __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restri
                                                    const T* __restrict__ s, T* __restrict__ y, Scalars* sc,
                                                    double* part, const int* __restrict__ done) {
   if (done && *done) return;
-  double d = 0.0;
+  Acc<T> acc;
   for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
     const T yi = x[row] + s[row] * (b[row] - sell_row<T>(A, x, row));
     y[row] = yi;
-    d = fma((double)b[row], (double)yi, d);
+    acc.add(b[row], yi);
   }
-  if (part) grid_reduce(d, 0.0, sc, part, R_RZ, -1, POST_RZ);
+  if (part) grid_finish(block_total(acc), 0.0, sc, part, R_RZ, -1, POST_RZ);
 }
 
 // condition of the graph's WHILE node: keep looping until done (bounded by maxiter + 2 trips)
@@ -356,10 +444,9 @@ __global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
 template <class T>
 __global__ void __launch_bounds__(BS) k_dot(int n, const T* __restrict__ x, const T* __restrict__ y, Scalars* sc,
                                             double* part, int slot, int post = POST_NONE) {
-  double d = 0.0;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS)
-    d = fma((double)x[i], (double)(y ? y[i] : x[i]), d);
-  grid_reduce(d, 0.0, sc, part, slot, -1, post);
+  Acc<T> acc;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) acc.add(x[i], y ? y[i] : x[i]);
+  grid_finish(block_total(acc), 0.0, sc, part, slot, -1, post);
 }
 
 // mean of x -> red[slot]
@@ -393,6 +480,7 @@ __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
     sc->rz = 0.0;
     sc->rz_valid = 0;
     sc->alpha = sc->beta = 0.0;
+    sc->alpha_f = sc->beta_f = 0.0f;
   }
 }
 
