@@ -12,6 +12,7 @@
 //    a CUDA graph whose conditional WHILE node is driven by k_set_cond.
 #pragma once
 
+#include <cuda/atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -92,7 +93,10 @@ __device__ __forceinline__ void grid_reduce(double v0, double v1, Scalars* sc, d
   grid_finish<MAX>(v0, v1, sc, part, slot0, slot1, post, post_arg);
 }
 
-// block values v0, v1 (identical in every thread of the block) -> grid total in sc->red
+// block values v0, v1 (identical in every thread of the block) -> grid total in sc->red.
+// Thread 0 publishes the block's partials and takes a ticket with one acquire-release atomic (its
+// release orders the partials before the ticket); the block holding the last ticket loads every
+// partial at once (independent, unrolled loads), sums them in block order and runs the follow-up.
 template <bool MAX>
 __device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, double* part, int slot0, int slot1,
                                             int post, double post_arg) {
@@ -100,20 +104,27 @@ __device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, d
   if (threadIdx.x == 0) {
     part[(size_t)slot0 * MAXG + blockIdx.x] = v0;
     if (slot1 >= 0) part[(size_t)slot1 * MAXG + blockIdx.x] = v1;
-    __threadfence();
-    const unsigned t = atomicAdd(&sc->cnt[slot0], 1u);
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> ticket(sc->cnt[slot0]);
+    const unsigned t = ticket.fetch_add(1u, cuda::memory_order_acq_rel);
     s_last = (t == gridDim.x - 1) ? 1u : 0u;
   }
   __syncthreads();
   if (s_last) {
     __threadfence();
+    const int G = (int)gridDim.x;
+    const double* pa = part + (size_t)slot0 * MAXG;
+    const double* pb = part + (size_t)(slot1 >= 0 ? slot1 : slot0) * MAXG;
     double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) {
-      const double pa = __ldcg(part + (size_t)slot0 * MAXG + i);
-      a = MAX ? fmax(a, pa) : a + pa;
-      if (slot1 >= 0) {
-        const double pb = __ldcg(part + (size_t)slot1 * MAXG + i);
-        b = MAX ? fmax(b, pb) : b + pb;
+#pragma unroll
+    for (int k = 0; k < MAXG / BS; ++k) {
+      const int i = threadIdx.x + k * BS;
+      if (i < G) {
+        const double xa = __ldcg(pa + i);
+        a = MAX ? fmax(a, xa) : a + xa;
+        if (slot1 >= 0) {
+          const double xb = __ldcg(pb + i);
+          b = MAX ? fmax(b, xb) : b + xb;
+        }
       }
     }
     a = block_reduce<MAX>(a);
