@@ -46,6 +46,11 @@ int g_elem_cap = MAXG;
 inline int grid_elem(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + BS - 1) / BS, g_elem_cap));
 }
+// grid of the kernels that keep mmk::ILP rows per thread in flight
+inline int grid_ilp(int64_t n) {
+  const int64_t per = (int64_t)BS * mmk::ILP;
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, g_elem_cap));
+}
 inline int grid_rows(int64_t n, int tpr) {
   const int rpb = BS / tpr;
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + rpb - 1) / rpb, MAXG));
@@ -275,7 +280,7 @@ using mmk::R_SUM;
 template <int MODE, class T>
 void spmv(mm_problem* h, const DevMatT<T>& A, const T* x, const T* b, const T* s, T* y, const int* done) {
   if (A.tpr == 1) {
-    mmk::k_sell<MODE, T><<<grid_elem(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
+    mmk::k_sell<MODE, T><<<grid_ilp(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
   } else {
     const int g = grid_rows(A.c.n, A.tpr);
     TPR_SWITCH(A.tpr, (mmk::k_csr<TP, MODE><<<g, BS, 0, h->st>>>(A.c, x, b, s, y, done)));
@@ -285,7 +290,7 @@ void spmv(mm_problem* h, const DevMatT<T>& A, const T* x, const T* b, const T* s
 
 template <class T>
 void dotT(mm_problem* h, int n, const T* x, const T* y, mmk::Scalars* sc, int slot, int post = mmk::POST_NONE) {
-  mmk::k_dot<T><<<grid_elem(n), BS, 0, h->st>>>(n, x, y, sc, h->d_part, slot, post);
+  mmk::k_dot<T><<<grid_ilp(n), BS, 0, h->st>>>(n, x, y, sc, h->d_part, slot, post);
   LAUNCH_CHECK();
 }
 
@@ -310,7 +315,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     auto& c = lv[l];
     if (l == 0) {
       if (in_loop) {
-        mmk::k_vc_residual0<T><<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, S.sc);
+        mmk::k_vc_residual0<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, S.sc);
         LAUNCH_CHECK();
       } else {
         spmv<1, T>(h, c.A, c.x, r, nullptr, c.res, done);
@@ -321,7 +326,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     auto& nx = lv[l + 1];
     const bool coarsest = (l + 1 == L - 1);
     if (c.R.tpr == 1) {
-      mmk::k_restrict<T><<<grid_elem(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
+      mmk::k_restrict<T><<<grid_ilp(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
                                                               done);
     } else {
       const int g = grid_rows(nx.n, c.R.tpr);
@@ -339,7 +344,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     auto& c = lv[l];
     spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
     if (l == 0) {
-      mmk::k_smooth_dot<T><<<grid_elem(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
+      mmk::k_smooth_dot<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
       LAUNCH_CHECK();
     } else {
       spmv<2, T>(h, c.A, c.x, c.b, c.s, c.x2, done);
@@ -352,7 +357,7 @@ template <class T>
 void apply_M_simple(mm_problem* h, SolverT<T>& S, const T* r, T* z, const int* done) {
   const int N = h->N;
   if (h->precond == MM_PRECOND_JACOBI) {
-    mmk::k_mul<T><<<grid_elem(N), BS, 0, h->st>>>(N, S.jac, r, z);
+    mmk::k_mul<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.jac, r, z);
     LAUNCH_CHECK();
   } else if (h->precond == MM_PRECOND_NONE) {
     CK(cudaMemcpyAsync(z, r, N * sizeof(T), cudaMemcpyDeviceToDevice, h->st));
@@ -367,7 +372,7 @@ void apply_M_simple(mm_problem* h, SolverT<T>& S, const T* r, T* z, const int* d
 template <class T>
 void enqueue_precond(mm_problem* h, SolverT<T>& S, const T* r, T* z) {
   if (multilevel(h, S)) {
-    mmk::k_mul<T><<<grid_elem(h->N), BS, 0, h->st>>>(h->N, S.lv[0].s, r, S.lv[0].x);
+    mmk::k_mul<T><<<grid_ilp(h->N), BS, 0, h->st>>>(h->N, S.lv[0].s, r, S.lv[0].x);
     LAUNCH_CHECK();
     enqueue_vcycle<T>(h, S, r, z, false, nullptr);
   } else {
@@ -380,10 +385,10 @@ template <class T>
 void enqueue_iteration(mm_problem* h, SolverT<T>& S) {
   const int N = h->N;
   auto& l0 = S.lv[0];
-  mmk::k_pcg_dir<T><<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+  mmk::k_pcg_dir<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
   LAUNCH_CHECK();
   const bool ml = multilevel(h, S);
-  mmk::k_pcg_step<T><<<grid_elem(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
+  mmk::k_pcg_step<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
                                                       h->d_part);
   LAUNCH_CHECK();
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, true, &S.sc->done);
@@ -452,7 +457,7 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   LAUNCH_CHECK();
   const bool ml = multilevel(h, S);
   auto& l0 = S.lv[0];
-  mmk::k_init_residual<T><<<grid_elem(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
+  mmk::k_init_residual<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
                                                            h->d_part);
   LAUNCH_CHECK();
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
@@ -507,19 +512,19 @@ int run_mixed(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out
   int total = 0, outer = 0;
   double rr = 0.0;
   while (true) {
-    mmk::k_resid64<<<grid_elem(N), BS, 0, h->st>>>(A64.s, h->d_x, h->d_b, h->d_r64, h->d_sc, h->d_part);
+    mmk::k_resid64<<<grid_ilp(N), BS, 0, h->st>>>(A64.s, h->d_x, h->d_b, h->d_r64, h->d_sc, h->d_part);
     LAUNCH_CHECK();
     rr = h->red(R_R2);
     if (!(rr > tol * tol * bb) || outer >= h->mixed_max_outer || total >= maxiter || !std::isfinite(rr)) break;
     const double rn = std::sqrt(rr);
-    mmk::k_to_f32<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_r64, 1.0 / rn, h->d_r32, h->d_d32);
+    mmk::k_to_f32<<<grid_ilp(N), BS, 0, h->st>>>(N, h->d_r64, 1.0 / rn, h->d_r32, h->d_d32);
     LAUNCH_CHECK();
     const double need = tol * std::sqrt(bb) / rn;  // relative reduction still required
     const double eta = std::max(h->mixed_eta, 0.5 * need);
     int it = 0;
     run_pcg<float>(h, h->s32, eta, std::max(1, maxiter - total), &it, nullptr);
     total += it;
-    mmk::k_add_f32<<<grid_elem(N), BS, 0, h->st>>>(N, h->d_x, h->d_d32, rn);
+    mmk::k_add_f32<<<grid_ilp(N), BS, 0, h->st>>>(N, h->d_x, h->d_d32, rn);
     LAUNCH_CHECK();
     ++outer;
   }
@@ -1668,7 +1673,7 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
         spmv<0, double>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
       } else if (kernel == MM_KERNEL_SMOOTH) {
         const double* s = l0->s ? l0->s : h->d_U;
-        mmk::k_smooth_dot<double><<<grid_elem(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
+        mmk::k_smooth_dot<double><<<grid_ilp(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
                                                                 nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {

@@ -257,6 +257,51 @@ __device__ __forceinline__ T sell_row(const SellT<T>& A, const T* __restrict__ x
   return acc;
 }
 
+// Rows per thread of the one-row-per-thread kernels.  Each thread keeps ILP rows in flight (their
+// loads are issued together), so a kernel over the fine level runs as one balanced wave instead of
+// one full wave plus a short second one.
+constexpr int ILP = 2;
+
+template <class T>
+__device__ __forceinline__ void sell_rows(const SellT<T>& A, const T* __restrict__ x, const int (&row)[ILP],
+                                          T (&acc)[ILP]) {
+  int base[ILP], w[ILP];
+  int wmax = 0;
+#pragma unroll
+  for (int q = 0; q < ILP; ++q) {
+    acc[q] = T(0);
+    w[q] = 0;
+    base[q] = 0;
+    if (row[q] < A.n) {
+      const int s = row[q] >> 5;
+      const int b0 = __ldg(A.sptr + s);
+      w[q] = (__ldg(A.sptr + s + 1) - b0) >> 5;
+      base[q] = b0 + (row[q] & 31);
+    }
+    wmax = max(wmax, w[q]);
+  }
+  for (int k = 0; k < wmax; ++k) {
+    int c[ILP];
+    T v[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (k < w[q]) {
+        c[q] = __ldg(A.col + base[q] + 32 * k);
+        v[q] = __ldg(A.val + base[q] + 32 * k);
+      }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (k < w[q]) acc[q] = fmaT<T>(v[q], __ldg(x + c[q]), acc[q]);
+  }
+}
+
+// row indices of thread threadIdx.x in the block-stride step starting at rb
+__device__ __forceinline__ void rows_of(int rb, int (&row)[ILP]) {
+#pragma unroll
+  for (int q = 0; q < ILP; ++q) row[q] = rb + threadIdx.x + q * BS;
+}
+#define ROW_LOOP(n) for (int rb = blockIdx.x * BS * ILP; rb < (n); rb += gridDim.x * BS * ILP)
+
 // compressed rows with TPR lanes per row (small levels with long rows, where one thread per row
 // would leave most of the GPU idle)
 template <class T>
@@ -323,12 +368,20 @@ template <int MODE, class T>
 __global__ void __launch_bounds__(BS) k_sell(SellT<T> A, const T* __restrict__ x, const T* b,
                                              const T* __restrict__ s, T* y, const int* __restrict__ done) {
   if (done && *done) return;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const T ax = sell_row<T>(A, x, row);
-    if (MODE == 0) y[row] = ax;
-    else if (MODE == 1) y[row] = b[row] - ax;
-    else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);
-    else y[row] = b[row] + ax;
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    T ax[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(A, x, row, ax);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      if (MODE == 0) y[i] = ax[q];
+      else if (MODE == 1) y[i] = b[i] - ax[q];
+      else if (MODE == 2) y[i] = x[i] + s[i] * (b[i] - ax[q]);
+      else y[i] = b[i] + ax[q];
+    }
   }
 }
 
@@ -338,11 +391,20 @@ __global__ void __launch_bounds__(BS) k_init_residual(SellT<T> A, const T* __res
                                                       T* __restrict__ r, const T* __restrict__ s, T* __restrict__ xv,
                                                       Scalars* sc, double* part) {
   Acc<T> acc;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const T ri = b[row] - sell_row<T>(A, x, row);
-    r[row] = ri;
-    acc.add(ri, ri);
-    if (s) xv[row] = s[row] * ri;
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    T ax[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(A, x, row, ax);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const T ri = b[i] - ax[q];
+      r[i] = ri;
+      acc.add(ri, ri);
+      if (s) xv[i] = s[i] * ri;
+    }
   }
   grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_INIT);
 }
@@ -356,13 +418,21 @@ __global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict_
   if (sc->done) return;
   const T beta = scal<T>(sc->beta, sc->beta_f);
   Acc<T> acc;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const T az = sell_row<T>(A, z, row);
-    const T pn = z[row] + beta * p[row];
-    const T apn = az + beta * Ap[row];
-    p[row] = pn;
-    Ap[row] = apn;
-    acc.add(pn, apn);
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    T az[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(A, z, row, az);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const T pn = z[i] + beta * p[i];
+      const T apn = az[q] + beta * Ap[i];
+      p[i] = pn;
+      Ap[i] = apn;
+      acc.add(pn, apn);
+    }
   }
   grid_finish(block_total(acc), 0.0, sc, part, R_PAP, -1, POST_PAP);
 }
@@ -375,12 +445,19 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __
   if (sc->done) return;
   const T alpha = scal<T>(sc->alpha, sc->alpha_f);
   Acc<T> acc;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
-    x[i] = x[i] + alpha * p[i];
-    const T ri = r[i] - alpha * Ap[i];
-    r[i] = ri;
-    acc.add(ri, ri);
-    if (s0) xv[i] = s0[i] * ri;
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= n) continue;
+      x[i] = x[i] + alpha * p[i];
+      const T ri = r[i] - alpha * Ap[i];
+      r[i] = ri;
+      acc.add(ri, ri);
+      if (s0) xv[i] = s0[i] * ri;
+    }
   }
   grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
@@ -390,8 +467,15 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_vc_residual0(SellT<T> A, const T* __restrict__ xv, const T* __restrict__ r,
                                                      T* __restrict__ res, Scalars* sc) {
   if (sc->done) return;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS)
-    res[row] = r[row] - sell_row<T>(A, xv, row);
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    T ax[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(A, xv, row, ax);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < A.n) res[row[q]] = r[row[q]] - ax[q];
+  }
 }
 
 // restriction b_c = R res, fused with the coarse pre-smoothing from zero x_c = s_c .* b_c
@@ -400,10 +484,18 @@ __global__ void __launch_bounds__(BS) k_restrict(SellT<T> R, const T* __restrict
                                                  const T* __restrict__ s_c, T* __restrict__ xc,
                                                  const int* __restrict__ done) {
   if (done && *done) return;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < R.n; row += gridDim.x * BS) {
-    const T v = sell_row<T>(R, res, row);
-    bc[row] = v;
-    if (s_c) xc[row] = s_c[row] * v;
+  ROW_LOOP(R.n) {
+    int row[ILP];
+    T v[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(R, res, row, v);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= R.n) continue;
+      bc[i] = v[q];
+      if (s_c) xc[i] = s_c[i] * v[q];
+    }
   }
 }
 
@@ -431,10 +523,19 @@ __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restri
                                                    double* part, const int* __restrict__ done) {
   if (done && *done) return;
   Acc<T> acc;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const T yi = x[row] + s[row] * (b[row] - sell_row<T>(A, x, row));
-    y[row] = yi;
-    acc.add(b[row], yi);
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    T ax[ILP];
+    rows_of(rb, row);
+    sell_rows<T>(A, x, row, ax);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const T yi = x[i] + s[i] * (b[i] - ax[q]);
+      y[i] = yi;
+      acc.add(b[i], yi);
+    }
   }
   if (part) grid_finish(block_total(acc), 0.0, sc, part, R_RZ, -1, POST_RZ);
 }
@@ -456,7 +557,13 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_dot(int n, const T* __restrict__ x, const T* __restrict__ y, Scalars* sc,
                                             double* part, int slot, int post = POST_NONE) {
   Acc<T> acc;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) acc.add(x[i], y ? y[i] : x[i]);
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < n) acc.add(x[row[q]], y ? y[row[q]] : x[row[q]]);
+  }
   grid_finish(block_total(acc), 0.0, sc, part, slot, -1, post);
 }
 
@@ -477,7 +584,13 @@ __global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, 
 template <class T>
 __global__ void __launch_bounds__(BS) k_mul(int n, const T* __restrict__ s, const T* __restrict__ r,
                                             T* __restrict__ out) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = s[i] * r[i];
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < n) out[row[q]] = s[row[q]] * r[row[q]];
+  }
 }
 
 // PCG start: tol2 = tol^2 * red[R_BB]; counters reset
@@ -501,28 +614,49 @@ __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
 // r = b - A x in FP64; r.r -> red[R_R2]
 __global__ void __launch_bounds__(BS) k_resid64(Sell A, const double* __restrict__ x, const double* __restrict__ b,
                                                 double* __restrict__ r, Scalars* sc, double* part) {
-  double d = 0.0;
-  for (int row = blockIdx.x * BS + threadIdx.x; row < A.n; row += gridDim.x * BS) {
-    const double ri = b[row] - sell_row<double>(A, x, row);
-    r[row] = ri;
-    d = fma(ri, ri, d);
+  Acc<double> acc;
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    double ax[ILP];
+    rows_of(rb, row);
+    sell_rows<double>(A, x, row, ax);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const double ri = b[i] - ax[q];
+      r[i] = ri;
+      acc.add(ri, ri);
+    }
   }
-  grid_reduce(d, 0.0, sc, part, R_R2);
+  grid_finish(block_total(acc), 0.0, sc, part, R_R2);
 }
 
 // r32 = r * scale (the inner system is solved for a unit-norm right-hand side); d32 = 0
 __global__ void __launch_bounds__(BS) k_to_f32(int n, const double* __restrict__ r, double scale,
                                                float* __restrict__ r32, float* __restrict__ d32) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
-    r32[i] = (float)(r[i] * scale);
-    d32[i] = 0.0f;
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < n) {
+        r32[row[q]] = (float)(r[row[q]] * scale);
+        d32[row[q]] = 0.0f;
+      }
   }
 }
 
 // x += scale * d32 in FP64
 __global__ void __launch_bounds__(BS) k_add_f32(int n, double* __restrict__ x, const float* __restrict__ d32,
                                                 double scale) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) x[i] = fma(scale, (double)d32[i], x[i]);
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < n) x[row[q]] = fma(scale, (double)d32[row[q]], x[row[q]]);
+  }
 }
 
 // ------------------------------------------------------------------------------------------
