@@ -78,6 +78,9 @@ class Problem:
         mask = None if boundary_mask is None else f64(boundary_mask).reshape(-1)
         self.V_mag = float(V_mag)
         self.has_mask = mask is not None
+        self.mask_host = mask
+        self.precision = "fp64"
+        self.reg, self.precond_type, self.max_levels, self.max_coarse = 1e-12, "amgcl", 10, 1000
         h = C.c_void_p()
         check("mm_create", lib().mm_create(
             self.N, self.E, _abi.iptr(self.conn), dptr(volume), dptr(grad_phi), _abi.iptr(mat_id), len(A), dptr(A),
@@ -105,6 +108,7 @@ class Problem:
     def build_poisson(self, reg=1e-12, precond_type="amgcl", max_levels=10, max_coarse=1000) -> int:
         if precond_type == "chebyshev":
             raise ValueError("the chebyshev preconditioner is not part of the cuda backend; use amgcl")
+        self.reg, self.precond_type, self.max_levels, self.max_coarse = reg, precond_type, max_levels, max_coarse
         nl = C.c_int()
         self._check("mm_build_poisson", lib().mm_build_poisson(self.h, float(reg), _abi.PRECOND[precond_type],
                                                                int(max_levels), int(max_coarse), C.byref(nl)))
@@ -228,6 +232,7 @@ class Problem:
     def set_precision(self, precision: str):
         """"fp64" (the reference's plain method) or "mixed"; call before build_poisson()."""
         self.set_option("precision", {"fp64": 0, "mixed": 1}[precision])
+        self.precision = precision
 
     def last_refinements(self) -> int:
         n = C.c_int()
@@ -246,3 +251,58 @@ class Problem:
 
     def sync(self):
         self._check("mm_sync", lib().mm_sync(self.h))
+
+
+# ------------------------------------------------------------------------------------------------
+# one device problem per (mesh, materials), shared by the factories of this package
+# ------------------------------------------------------------------------------------------------
+def _digest(*arrays) -> str:
+    import hashlib
+
+    h = hashlib.sha1()
+    for a in arrays:
+        if a is None:
+            h.update(b"none")
+            continue
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64) if not isinstance(a, np.ndarray) else a)
+        h.update(str(a.shape).encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy, V_mag=None, M_nodal=None, boundary_mask=None,
+                     n_nodes=None) -> Problem:
+    """The device problem of a reference-style ``TetGeom`` and material tables (created once).
+
+    V_mag and M_nodal default to the reference's definitions (``src/loop.py:864-939``).
+    """
+    conn = np.asarray(geom.conn)
+    volume = np.asarray(geom.volume, np.float64)
+    mat_id = np.asarray(geom.mat_id, np.int32)
+    Js = np.asarray(Js_lookup, np.float64).ravel()
+    N = int(n_nodes if n_nodes is not None else (geom.x_nodes.shape[0] if getattr(geom, "x_nodes", None) is not None
+                                                 else conn.max() + 1))
+    if V_mag is None:
+        is_mag = np.isin(mat_id, np.where(Js > 0)[0] + 1)
+        V_mag = float(np.sum(volume[is_mag])) or 1.0
+    if M_nodal is None:
+        M_nodal = np.bincount(conn.reshape(-1), weights=np.repeat(0.25 * volume * Js[mat_id - 1], 4), minlength=N)
+    M_nodal = np.asarray(M_nodal, np.float64).reshape(-1)
+    key = _digest(np.asarray(A_lookup), np.asarray(K1_lookup), Js, np.asarray(k_easy), np.array([V_mag]), M_nodal,
+                  None if boundary_mask is None else np.asarray(boundary_mask, np.float64))
+    cache = getattr(geom, "_mm_problems", None)
+    if cache is None:
+        cache = {}
+        try:
+            geom._mm_problems = cache
+        except AttributeError:
+            pass
+    if key not in cache:
+        gp = getattr(geom, "grad_phi", None)
+        if gp is None:
+            JT = np.asarray(geom.JinvT, np.float64)
+            ghat = np.array([[-1.0, -1.0, -1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+            gp = np.einsum("eij,aj->eai", JT, ghat)
+        cache[key] = Problem(conn, volume, np.asarray(gp, np.float64), mat_id, A_lookup, K1_lookup, Js, k_easy,
+                             V_mag, M_nodal, boundary_mask, n_nodes=N)
+    return cache[key]

@@ -1,0 +1,85 @@
+"""``make_minimizer`` with the reference's signature (``src/minimizers.py:2927-2963``), on the GPU.
+
+Methods: "pcohen_hs" (the hysteresis loop's default, ``:950-1073``), "lbfgs" (``:1266-1381``) and
+"wg_np" (Barzilai-Borwein, ``:1706-1800``); each field step runs entirely in libmumag_cuda
+(``mm_minimize``).  The other reference methods are not part of this backend.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .cuda_backend import MinimizerParams, problem_for_geom
+
+SUPPORTED = ("pcohen_hs", "lbfgs", "wg_np")
+
+
+def tangent_grad(m, g):
+    """Project a raw gradient onto the tangent space (``src/minimizers.py:94-96``)."""
+    return g - np.sum(m * g, axis=1, keepdims=True) * m
+
+
+def cayley_update(m, H, tau):
+    """Cayley rotation with renormalisation (``src/minimizers.py:71-79``), host helper."""
+    k = 0.5 * tau * H
+    k2 = np.sum(k * k, axis=1, keepdims=True)
+    m_new = ((1.0 - k2) * m + 2.0 * np.cross(k, m) + 2.0 * np.sum(k * m, axis=1, keepdims=True) * k) / (1.0 + k2)
+    return m_new / np.linalg.norm(m_new, axis=1, keepdims=True)
+
+
+def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, node_volumes, M_nodal, solve_U,
+                   cg_tol, method: str = "pcg", **kwargs):
+    """Return minimize(m0, B_ext, **params) -> (m, U, info) running each field step on the GPU."""
+    if method not in SUPPORTED:
+        raise NotImplementedError(f"method {method!r} is not part of the cuda backend (available: {SUPPORTED})")
+    if kwargs.get("k1me") is not None:
+        raise NotImplementedError("the magnetoelastic terms are not part of the cuda backend")
+    sp = getattr(solve_U, "problem", None)
+    boundary_mask = kwargs.get("boundary_mask")
+    if boundary_mask is None and sp is not None and sp.has_mask:
+        boundary_mask = sp.mask_host
+    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask)
+    if not prob.poisson_built:
+        if sp is not None:
+            if sp.precision != "fp64":
+                prob.set_precision(sp.precision)
+            prob.build_poisson(sp.reg, sp.precond_type, sp.max_levels, sp.max_coarse)
+        else:
+            prob.build_poisson(1e-12, "amgcl")
+    memory = int(kwargs.get("memory", 5))
+    B_bias = kwargs.get("B_bias")
+
+    def minimize(m0, B_ext, **params):
+        sparse_ops = params.get("sparse_ops") or {}
+        if sparse_ops.get("inv_M_rel") is not None or sparse_ops.get("inv_M_prec") is not None:
+            prob.set_node_weights(sparse_ops.get("inv_M_rel"), sparse_ops.get("inv_M_prec"))
+        if B_bias is not None and np.any(np.asarray(B_bias) != 0):
+            raise NotImplementedError("a per-node bias field is evaluated by make_energy_kernels, not by minimize")
+        tau_f = float(params.get("tau_f", 1e-6))
+        prm = MinimizerParams(
+            method=method, max_iter=int(params.get("max_iter", 2000)), tau_f=tau_f,
+            eps_a=float(params.get("eps_a", 1e-12)), tau0=float(params.get("tau0", 1e-2)),
+            ls_eta1=float(params.get("ls_eta1", 0.1)), ls_eta2=float(params.get("ls_eta2", 0.1)),
+            ls_C=float(params.get("ls_C", 2.0)), ls_c=float(params.get("ls_c", 0.5)), ls_max_evals=15,
+            pc_iters=int(params.get("pc_iters", 10)), pc_auto=bool(params.get("pc_auto", False)),
+            pc_force_eta=float(params.get("pc_force_eta", 0.5)),
+            pc_force_alpha=float(params.get("pc_force_alpha", 0.5)),
+            pc_stagnation_nu=float(params.get("pc_stagnation_nu", 1e-3)), pc_reg=float(params.get("pc_reg", 0.0)),
+            memory=int(params.get("memory", memory)), wg_gamma=int(params.get("wg_gamma", 2)),
+            L=params.get("L"), cg_tol=float(cg_tol),
+            phi_tol=float(params["phi_tol"]) if "phi_tol" in params else float(min(cg_tol, 0.1 * tau_f)),
+            cg_maxiter=int(params.get("cg_maxiter", 2000)))
+        U0 = params.get("U0")
+        if U0 is None:
+            U0 = np.zeros(prob.N)
+        m, U, info = prob.minimize(B_ext, m0, U0, prm)
+        if params.get("verbose", True):
+            print(f"          number of iterations   : {info['iters']}")
+            print(f"number of iterations for preco   : {info['preco_iters']}")
+            print(f"number of function evaluations   : {info['evals']}")
+            print(f"number of iterations for demag   : {info['demag_iters']}")
+            print("done")
+        return m, U, info
+
+    minimize.problem = prob
+    return minimize
