@@ -216,7 +216,33 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 /* MM_OPT_GRID_CAP: largest grid (blocks of 256 threads) of the one-row-per-thread kernels; beyond
  * it they loop (default 4096).  Process-wide; fixed values keep every reduction deterministic. */
 #define MM_OPT_GRID_CAP 4
+/* MM_OPT_PROFILE (default 0): 1 runs every demag solve with the host-polled loop (synchronising
+ * after each direction/step pair, so no launch runs after convergence) and records a CUDA event pair
+ * around every solver launch; each launch's device time is added to a slot named by its kind, AMG
+ * level and precision.  For measurement only: the loop is slower than the graph. */
+#define MM_OPT_PROFILE 5
 int mm_set_option(mm_problem* h, int option, int value);
+
+/* In-solve kernel profile (MM_OPT_PROFILE).  slot = (fp32 * MM_PROF_LEVELS + level) * MM_PROF_KINDS
+ * + kind.  No reference counterpart: measurement of this backend's own kernels. */
+#define MM_PROF_PCG_DIR 0       /* y = A z ; p = z + beta p ; Ap = y + beta Ap ; p.Ap (level 0)   */
+#define MM_PROF_PCG_STEP 1      /* x += alpha p ; r -= alpha Ap ; r.r ; pre-smoothing s .* r      */
+#define MM_PROF_VC_RESIDUAL0 2  /* level-0 residual r - A x of the V-cycle                        */
+#define MM_PROF_RESIDUAL 3      /* residual b - A x on a coarse level                            */
+#define MM_PROF_RESTRICT 4      /* b_c = R res, fused with the coarse pre-smoothing              */
+#define MM_PROF_COARSE 5        /* dense coarsest solve x = Ainv b                                */
+#define MM_PROF_PROLONG 6       /* x += P e                                                      */
+#define MM_PROF_SMOOTH0 7       /* level-0 post-smoothing fused with r.z                          */
+#define MM_PROF_SMOOTH 8        /* post-smoothing on a coarse level                              */
+#define MM_PROF_INIT_RESIDUAL 9 /* r = b - A x at the start of a PCG solve                        */
+#define MM_PROF_KINDS 10
+#define MM_PROF_LEVELS 16
+#define MM_PROF_SLOTS (2 * MM_PROF_LEVELS * MM_PROF_KINDS)
+/* Copy the per-slot totals since the last reset: launches, summed device time [ms] and the
+ * algorithmic bytes of one launch (every array counted once at its stored width, padding excluded).
+ * Each array holds MM_PROF_SLOTS entries. */
+int mm_profile_read(mm_problem* h, int64_t* launches, double* total_ms, double* bytes_per_launch);
+int mm_profile_reset(mm_problem* h);
 /* Refinement steps (FP32 correction solves) of the last mixed-precision solve. */
 int mm_last_refinements(mm_problem* h, int* steps);
 

@@ -17,6 +17,11 @@ MM_OK, MM_MAXITER, MM_NONFINITE, MM_BREAKDOWN = 0, 1, 2, 3
 PRECOND = {"none": 0, "jacobi": 1, "amg": 2, "amgcl": 3}
 METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2}
 KERNELS = {"spmv_A": 0, "smooth": 1, "energy": 2, "hessian": 3}
+# in-solve profile slots: slot = (fp32 * PROF_LEVELS + level) * len(PROF_KINDS) + kind
+PROF_KINDS = ("pcg_dir", "pcg_step", "vc_residual0", "residual", "restrict", "coarse", "prolong", "smooth0",
+              "smooth", "init_residual")
+PROF_LEVELS = 16
+PROF_SLOTS = 2 * PROF_LEVELS * len(PROF_KINDS)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -78,6 +83,8 @@ SIGNATURES = {
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "mm_profile_read": (C.c_int, [_vp, _lp, _dp, _dp]),
+    "mm_profile_reset": (C.c_int, [_vp]),
     "mm_last_refinements": (C.c_int, [_vp, _ip]),
     "mm_last_solve_ms": (C.c_int, [_vp, _dp]),
     "mm_launch_count": (C.c_int, [_vp, _lp]),

@@ -130,6 +130,20 @@ struct mm_problem {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_solve_ms = 0.0;
 
+  // in-solve kernel profile (MM_OPT_PROFILE): one event pair per tagged launch, folded into the
+  // per-slot totals when the solve ends
+  struct ProfRec {
+    int slot;
+    cudaEvent_t a, b;
+  };
+  bool prof = false;
+  std::vector<ProfRec> prof_rec;
+  std::vector<cudaEvent_t> prof_pool;
+  size_t prof_used = 0;
+  int64_t prof_n[MM_PROF_SLOTS] = {};
+  double prof_ms[MM_PROF_SLOTS] = {};
+  double prof_bytes[MM_PROF_SLOTS] = {};
+
   // host copies used by the setup
   std::vector<int> conn, mat_id;
   std::vector<double> volume, grad_phi, mask_h;
@@ -248,6 +262,25 @@ struct mm_problem {
     return h_sc->red[slot];
   }
   void sync() { CK(cudaStreamSynchronize(st)); }
+  cudaEvent_t prof_event() {
+    if (prof_used == prof_pool.size()) {
+      cudaEvent_t e = nullptr;
+      CK(cudaEventCreate(&e));
+      prof_pool.push_back(e);
+    }
+    return prof_pool[prof_used++];
+  }
+  // add the recorded launches to the slot totals (the stream must be idle)
+  void prof_fold() {
+    for (const ProfRec& r : prof_rec) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, r.a, r.b));
+      prof_ms[r.slot] += t;
+      prof_n[r.slot] += 1;
+    }
+    prof_rec.clear();
+    prof_used = 0;
+  }
 };
 
 // =============================================================================================
@@ -303,6 +336,32 @@ bool multilevel(mm_problem* h, const SolverT<T>& S) {
   return (h->precond == MM_PRECOND_AMG || h->precond == MM_PRECOND_AMGCL) && S.lv.size() > 1;
 }
 
+// In-solve profile: with MM_OPT_PROFILE on, `launch` is bracketed by an event pair whose time goes
+// to the slot of (kind, level, precision); `bytes` are the launch's algorithmic bytes.
+template <class T, class F>
+void tagged(mm_problem* h, int kind, int level, double bytes, F&& launch) {
+  if (!h->prof) {
+    launch();
+    return;
+  }
+  const int lvl = std::min(level, MM_PROF_LEVELS - 1);
+  const int slot = ((sizeof(T) == 4 ? 1 : 0) * MM_PROF_LEVELS + lvl) * MM_PROF_KINDS + kind;
+  cudaEvent_t a = h->prof_event(), b = h->prof_event();
+  CK(cudaEventRecord(a, h->st));
+  launch();
+  CK(cudaEventRecord(b, h->st));
+  h->prof_bytes[slot] = bytes;
+  h->prof_rec.push_back({slot, a, b});
+}
+
+// algorithmic bytes of one pass over a stored operator: values + columns of the non-zeros (padding
+// excluded) and the slice / row pointers
+template <class T>
+double mat_bytes(const DevMatT<T>& M) {
+  const double ptrs = M.tpr == 1 ? (double)((M.s.n + 31) / 32 + 1) : (double)(M.c.n + 1);
+  return (double)M.nnz * (4.0 + sizeof(T)) + 4.0 * ptrs;
+}
+
 // ---------------------------------------------------------------------------------------------
 // V-cycle (enqueue only).  Level 0's pre-smoothed iterate lv[0].x must already hold s0 .* r.
 // in_loop: the level-0 residual is skipped once the solve has converged.
@@ -311,43 +370,52 @@ template <class T>
 void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop, const int* done) {
   auto& lv = S.lv;
   const int L = (int)lv.size();
+  const double w = sizeof(T);
   for (int l = 0; l < L - 1; ++l) {
     auto& c = lv[l];
-    if (l == 0) {
-      if (in_loop) {
+    if (l == 0 && in_loop) {
+      tagged<T>(h, MM_PROF_VC_RESIDUAL0, 0, mat_bytes(c.A) + 3.0 * w * c.n, [&] {
         mmk::k_vc_residual0<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, S.sc);
         LAUNCH_CHECK();
-      } else {
-        spmv<1, T>(h, c.A, c.x, r, nullptr, c.res, done);
-      }
+      });
     } else {
-      spmv<1, T>(h, c.A, c.x, c.b, nullptr, c.res, done);
+      tagged<T>(h, l == 0 ? MM_PROF_VC_RESIDUAL0 : MM_PROF_RESIDUAL, l, mat_bytes(c.A) + 3.0 * w * c.n,
+                [&] { spmv<1, T>(h, c.A, c.x, l == 0 ? r : c.b, nullptr, c.res, done); });
     }
     auto& nx = lv[l + 1];
     const bool coarsest = (l + 1 == L - 1);
-    if (c.R.tpr == 1) {
-      mmk::k_restrict<T><<<grid_ilp(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
-                                                              done);
-    } else {
-      const int g = grid_rows(nx.n, c.R.tpr);
-      TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<TP><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b, coarsest ? nullptr : nx.s,
-                                                                        nx.x, done)));
-    }
-    LAUNCH_CHECK();
+    const double rbytes = mat_bytes(c.R) + w * c.n + (coarsest ? 1.0 : 3.0) * w * nx.n;
+    tagged<T>(h, MM_PROF_RESTRICT, l, rbytes, [&] {
+      if (c.R.tpr == 1) {
+        mmk::k_restrict<T><<<grid_ilp(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
+                                                                done);
+      } else {
+        const int g = grid_rows(nx.n, c.R.tpr);
+        TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<TP><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b,
+                                                                          coarsest ? nullptr : nx.s, nx.x, done)));
+      }
+      LAUNCH_CHECK();
+    });
   }
   {
     auto& c = lv[L - 1];
-    mmk::k_dense_mv<T><<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, S.Ainv, c.b, c.x2, done);
-    LAUNCH_CHECK();
+    tagged<T>(h, MM_PROF_COARSE, L - 1, w * ((double)c.n * c.n + 2.0 * c.n), [&] {
+      mmk::k_dense_mv<T><<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, S.Ainv, c.b, c.x2, done);
+      LAUNCH_CHECK();
+    });
   }
   for (int l = L - 2; l >= 0; --l) {
     auto& c = lv[l];
-    spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done);  // x += P e
+    tagged<T>(h, MM_PROF_PROLONG, l, mat_bytes(c.P) + w * lv[l + 1].n + 2.0 * w * c.n,
+              [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
     if (l == 0) {
-      mmk::k_smooth_dot<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
-      LAUNCH_CHECK();
+      tagged<T>(h, MM_PROF_SMOOTH0, 0, mat_bytes(c.A) + 4.0 * w * c.n, [&] {
+        mmk::k_smooth_dot<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
+        LAUNCH_CHECK();
+      });
     } else {
-      spmv<2, T>(h, c.A, c.x, c.b, c.s, c.x2, done);
+      tagged<T>(h, MM_PROF_SMOOTH, l, mat_bytes(c.A) + 4.0 * w * c.n,
+                [&] { spmv<2, T>(h, c.A, c.x, c.b, c.s, c.x2, done); });
     }
   }
 }
@@ -380,19 +448,37 @@ void enqueue_precond(mm_problem* h, SolverT<T>& S, const T* r, T* z) {
   }
 }
 
+// first half of a PCG iteration: new direction with its operator product, then the step (sets
+// `done` on convergence)
+template <class T>
+void enqueue_dir_step(mm_problem* h, SolverT<T>& S) {
+  const int N = h->N;
+  const double w = sizeof(T);
+  auto& l0 = S.lv[0];
+  tagged<T>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * w * N, [&] {
+    mmk::k_pcg_dir<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+    LAUNCH_CHECK();
+  });
+  const bool ml = multilevel(h, S);
+  tagged<T>(h, MM_PROF_PCG_STEP, 0, (ml ? 8.0 : 6.0) * w * N, [&] {
+    mmk::k_pcg_step<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
+                                                        h->d_part);
+    LAUNCH_CHECK();
+  });
+}
+
+// second half: z = M^-1 r with r.z
+template <class T>
+void enqueue_apply_M(mm_problem* h, SolverT<T>& S) {
+  if (multilevel(h, S)) enqueue_vcycle<T>(h, S, S.r, S.z, true, &S.sc->done);
+  else apply_M_simple<T>(h, S, S.r, S.z, &S.sc->done);
+}
+
 // one PCG iteration on x = S.x (all scalars stay on the device)
 template <class T>
 void enqueue_iteration(mm_problem* h, SolverT<T>& S) {
-  const int N = h->N;
-  auto& l0 = S.lv[0];
-  mmk::k_pcg_dir<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
-  LAUNCH_CHECK();
-  const bool ml = multilevel(h, S);
-  mmk::k_pcg_step<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
-                                                      h->d_part);
-  LAUNCH_CHECK();
-  if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, true, &S.sc->done);
-  else apply_M_simple<T>(h, S, S.r, S.z, &S.sc->done);
+  enqueue_dir_step<T>(h, S);
+  enqueue_apply_M<T>(h, S);
 }
 
 // Build the loop graph: WHILE (condition) { iteration; k_set_cond }.  Returns false when the
@@ -457,14 +543,26 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   LAUNCH_CHECK();
   const bool ml = multilevel(h, S);
   auto& l0 = S.lv[0];
-  mmk::k_init_residual<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
-                                                           h->d_part);
-  LAUNCH_CHECK();
+  const double w = sizeof(T);
+  tagged<T>(h, MM_PROF_INIT_RESIDUAL, 0, mat_bytes(l0.A) + 5.0 * w * N, [&] {
+    mmk::k_init_residual<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
+                                                             h->d_part);
+    LAUNCH_CHECK();
+  });
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
   else apply_M_simple<T>(h, S, S.r, S.z, nullptr);
-  const bool graph = h->use_graph && build_loop_graph<T>(h, S);
+  const bool graph = h->use_graph && !h->prof && build_loop_graph<T>(h, S);
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
+  } else if (h->prof) {
+    // profiled: read `done` after every step so that no launch runs past convergence
+    for (int i = 0; i <= maxiter + 2; ++i) {
+      enqueue_dir_step<T>(h, S);
+      CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+      h->sync();
+      if (h->h_sc->done) break;
+      enqueue_apply_M<T>(h, S);
+    }
   } else {
     for (int i = 0;; ++i) {
       enqueue_iteration<T>(h, S);
@@ -562,6 +660,7 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_solve_ms = ms;
+  if (h->prof) h->prof_fold();
   const double bb0 = h->red(R_BB0);
   if (iters) *iters = it;
   const double rr = std::sqrt(r2 / (bb0 + 1e-30));
@@ -1448,6 +1547,7 @@ int mm_destroy(mm_problem* h) {
   if (h->h_sc) cudaFreeHost(h->h_sc);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return MM_OK;
@@ -1738,12 +1838,37 @@ int mm_set_option(mm_problem* h, int option, int value) {
     g_elem_cap = value;
     return MM_OK;
   }
+  if (option == MM_OPT_PROFILE) {
+    if (value != 0 && value != 1) return MM_ERR_ARG;
+    h->prof = value == 1;
+    return MM_OK;
+  }
   if (option == MM_OPT_MIXED_ETA_E6) {
     if (value <= 0 || value >= 1000000) return MM_ERR_ARG;
     h->mixed_eta = value * 1e-6;
     return MM_OK;
   }
   return MM_ERR_ARG;
+}
+
+int mm_profile_read(mm_problem* h, int64_t* launches, double* total_ms, double* bytes_per_launch) {
+  if (!h || !launches || !total_ms || !bytes_per_launch) return MM_ERR_ARG;
+  for (int i = 0; i < MM_PROF_SLOTS; ++i) {
+    launches[i] = h->prof_n[i];
+    total_ms[i] = h->prof_ms[i];
+    bytes_per_launch[i] = h->prof_bytes[i];
+  }
+  return MM_OK;
+}
+
+int mm_profile_reset(mm_problem* h) {
+  if (!h) return MM_ERR_ARG;
+  for (int i = 0; i < MM_PROF_SLOTS; ++i) {
+    h->prof_n[i] = 0;
+    h->prof_ms[i] = 0.0;
+    h->prof_bytes[i] = 0.0;
+  }
+  return MM_OK;
 }
 
 int mm_last_refinements(mm_problem* h, int* steps) {

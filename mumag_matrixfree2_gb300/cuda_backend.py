@@ -226,13 +226,34 @@ class Problem:
         return ms.value, nb.value
 
     def set_option(self, name: str, value: int):
-        opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4}
+        opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5}
         self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
 
     def set_precision(self, precision: str):
         """"fp64" (the reference's plain method) or "mixed"; call before build_poisson()."""
         self.set_option("precision", {"fp64": 0, "mixed": 1}[precision])
         self.precision = precision
+
+    def profile(self, reset: bool = False) -> list[dict]:
+        """In-solve kernel profile (set_option("profile", 1) first): one row per used slot with the
+        kernel kind, AMG level, precision, launches, total and mean device time and algorithmic bytes
+        per launch."""
+        n = np.zeros(_abi.PROF_SLOTS, np.int64)
+        ms = np.zeros(_abi.PROF_SLOTS)
+        nb = np.zeros(_abi.PROF_SLOTS)
+        self._check("mm_profile_read", lib().mm_profile_read(self.h, n.ctypes.data_as(_abi._lp), _abi.dptr(ms),
+                                                             _abi.dptr(nb)))
+        if reset:
+            self._check("mm_profile_reset", lib().mm_profile_reset(self.h))
+        nk = len(_abi.PROF_KINDS)
+        rows = []
+        for slot in np.nonzero(n)[0]:
+            kind, rest = int(slot) % nk, int(slot) // nk
+            level, f32 = rest % _abi.PROF_LEVELS, rest // _abi.PROF_LEVELS
+            rows.append({"kernel": _abi.PROF_KINDS[kind], "level": level, "precision": "fp32" if f32 else "fp64",
+                         "launches": int(n[slot]), "total_ms": float(ms[slot]),
+                         "ms_per_launch": float(ms[slot] / n[slot]), "bytes_per_launch": float(nb[slot])})
+        return sorted(rows, key=lambda r: -r["total_ms"])
 
     def last_refinements(self) -> int:
         n = C.c_int()
