@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-loop", action="store_true", help="skip the hysteresis-loop leg")
+    ap.add_argument("--loop-dB", type=float, default=0.1, help="field step of the loop leg [T]")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm worker processes (0: all cores)")
@@ -293,6 +295,38 @@ def timed_solves(prob, m_dev, U_dev, flush, tol, steps):
     return dev_ms, its, rrs, outer
 
 
+def run_loop(s, m0, precision, dB_T):
+    """The reference's headline loop on this workload through the public API: +8 T -> -8 T along z
+    tilted 1 deg in x-z, pcohen_hs, projected-gradient tolerance 1e-6, PCG tolerance 1e-10.  Returns
+    the loop summary; the per-step prints of run_hysteresis_loop are captured, not shown."""
+    import contextlib
+    import io
+
+    from mumag_matrixfree2_gb300 import fem_utils
+    from mumag_matrixfree2_gb300 import synthetic as syn
+    from mumag_matrixfree2_gb300.hysteresis_loop import LoopParams, coercive_field, run_hysteresis_loop
+
+    Js_ref = syn.reduced_materials([syn.Material(), syn.AIR])[4]
+    g = fem_utils.TetGeom(conn=s.geom.conn, volume=s.geom.volume, mat_id=s.geom.mat_id, grad_phi=s.geom.grad_phi,
+                          x_nodes=s.knt)  # a fresh geometry object: its own device problem
+    prm = LoopParams(h_dir=syn.tilted_field_direction(1.0), B_start=8.0 / Js_ref, B_end=-8.0 / Js_ref,
+                     dB=dB_T / Js_ref, loop=False, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10,
+                     Js_ref=Js_ref, max_iter=2000, out_dir=tempfile.mkdtemp(prefix="loop_"))
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        res = run_hysteresis_loop(s.knt, g, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, m0, prm, s.V_mag,
+                                  s.node_volumes, s.M_nodal, boundary_mask=s.boundary_mask, precond_type="amgcl",
+                                  precision=precision, write_files=False)
+    wall = time.perf_counter() - t0
+    hist, tot = res["history"], res["totals"]
+    J = hist[:, 1]
+    sw = int(np.argmax(J < 0)) if np.any(J < 0) else -1
+    return {"loop_s": tot["time"], "wall_with_setup_s": wall, "field_steps": len(hist),
+            "minimizer_iters": tot["iters"], "energy_evals": tot["evals"], "demag_pcg_iters": tot["demag"],
+            "preconditioner_iters": tot["preco"], "switch_step": sw, "switch_B_T": float(hist[sw, 0]) if sw >= 0 else None,
+            "Hc_T": coercive_field(hist[:, 0], hist[:, 1]), "_J": J}
+
+
 def run_ours(a):
     import torch
 
@@ -378,6 +412,20 @@ def run_ours(a):
                  "method": "FP32 hierarchy + FP32 PCG (FP64 inner products) inside FP64 iterative refinement; "
                            "stop on the true FP64 residual"}
 
+    loop = None
+    if not a.no_loop:
+        lp = {p_: run_loop(s, m0, p_, a.loop_dB) for p_ in (("fp64",) if a.no_mixed else ("fp64", "mixed"))}
+        J64 = lp["fp64"].pop("_J")
+        loop = {"workload": f"{a.workload}, +8 T -> -8 T in {a.loop_dB} T steps, 1 deg tilt, pcohen_hs, "
+                            "eps_a 1e-6, PCG tol 1e-10", "fp64": lp["fp64"]}
+        if "mixed" in lp:
+            Jm = lp["mixed"].pop("_J")
+            loop["mixed"] = lp["mixed"]
+            loop["mixed_speedup"] = lp["fp64"]["loop_s"] / lp["mixed"]["loop_s"]
+            loop["mixed_vs_fp64"] = {"Hc_rel_err": abs(lp["mixed"]["Hc_T"] - lp["fp64"]["Hc_T"]) / abs(lp["fp64"]["Hc_T"]),
+                                     "same_switch_step": lp["mixed"]["switch_step"] == lp["fp64"]["switch_step"],
+                                     "max_abs_dJ_T": float(np.max(np.abs(Jm - J64)))}
+
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         v_cpu, its_cpu = cpu_solves(knt, ijk, mats, m0, a.tol, 8)
@@ -412,6 +460,7 @@ def run_ours(a):
             "kernels": kernels,
             "profiled_solve_ms": prof_ms / a.profile_steps,
             "mixed": mixed,
+            "loop": loop,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,

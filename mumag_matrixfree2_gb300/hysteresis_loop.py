@@ -74,7 +74,7 @@ class LoopParams:
 
 
 def volume_averaged_J_parallel(m, conn, volume, mat_id, Js_lookup, h_dir) -> float:
-    """``src/hysteresis_loop.py:153-190`` on the host."""
+    """``src/hysteresis_loop.py:153-190`` on the host (element form, used by the tests)."""
     h = np.asarray(h_dir, np.float64)
     h = h / (np.linalg.norm(h) + 1e-30)
     m_avg = m[conn].mean(axis=1)
@@ -84,11 +84,49 @@ def volume_averaged_J_parallel(m, conn, volume, mat_id, Js_lookup, h_dir) -> flo
 
 
 def volume_averaged_m(m, conn, volume, mat_id, Js_lookup) -> np.ndarray:
-    """``src/hysteresis_loop.py:193-223`` on the host."""
+    """``src/hysteresis_loop.py:193-223`` on the host (element form, used by the tests)."""
     m_avg = m[conn].mean(axis=1)
     Js_e = np.asarray(Js_lookup)[mat_id - 1]
     Vmag = np.sum(np.where(Js_e > 0, volume, 0.0)) + 1e-30
     return np.sum(np.where(Js_e[:, None] > 0, volume[:, None] * m_avg, 0.0), axis=0) / Vmag
+
+
+def coercive_field(B, J) -> float:
+    """H_c of one descending branch as ``examples/evaluate_materials/analyze_evaluations.py:19-44``
+    evaluates it: the field where J crosses zero (linear interpolation in J-sorted order), or, if
+    larger in magnitude, the lowest field at which J is still non-negative."""
+    B = np.asarray(B, np.float64)
+    J = np.asarray(J, np.float64)
+    order = np.argsort(J)
+    zero_cross = float(np.interp(0.0, J[order], B[order]))
+    nonneg = J >= 0
+    lowest = float(B[nonneg].min()) if nonneg.any() else zero_cross
+    return max(abs(zero_cross), abs(lowest))
+
+
+class NodalAverages:
+    """The two volume averages of ``src/hysteresis_loop.py:153-223`` as nodal dot products.
+
+    Both averages are linear in m: sum_e V_e c_e mean_{a in e}(m_a) = sum_a m_a sum_{e ni a} V_e c_e / 4,
+    so the per-node weights are formed once per mesh and every field step costs one (N,3) product
+    instead of a gather over all elements.  Equal to the element form up to summation order.
+    """
+
+    def __init__(self, conn, volume, mat_id, Js_lookup, n_nodes: int):
+        conn = np.asarray(conn)
+        volume = np.asarray(volume, np.float64)
+        Js_e = np.asarray(Js_lookup, np.float64)[np.asarray(mat_id) - 1]
+        Vmag = np.sum(np.where(Js_e > 0, volume, 0.0)) + 1e-30
+        quarter = lambda c: np.repeat(0.25 * c, 4)  # noqa: E731
+        self.wJ = np.bincount(conn.reshape(-1), weights=quarter(volume * Js_e), minlength=n_nodes) / Vmag
+        self.wm = np.bincount(conn.reshape(-1), weights=quarter(np.where(Js_e > 0, volume, 0.0)),
+                              minlength=n_nodes) / Vmag
+
+    def J_parallel(self, m, h) -> float:
+        return float((self.wJ @ m) @ h)
+
+    def m_avg(self, m) -> np.ndarray:
+        return self.wm @ m
 
 
 def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, m0, params: LoopParams, V_mag,
@@ -116,10 +154,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     minimize = make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, node_volumes, M_nodal,
                               solve_U, params.cg_tol, method=params.method, memory=params.memory,
                               boundary_mask=boundary_mask)
-    conn = np.asarray(geom.conn)
-    volume = np.asarray(geom.volume)
-    mat_id = np.asarray(geom.mat_id)
     m = np.asarray(m0, np.float64)
+    avg = NodalAverages(geom.conn, geom.volume, geom.mat_id, Js_lookup, m.shape[0])
     m = m / np.linalg.norm(m, axis=1, keepdims=True)
     U = np.zeros(m.shape[0])
     B_vals = field_values(params.B_start, params.B_end, params.dB, params.loop)
@@ -135,8 +171,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                               pc_stagnation_nu=params.pc_stagnation_nu, memory=params.memory, pc_reg=params.pc_reg,
                               wg_gamma=params.wg_gamma, L=params.L, verbose=params.verbose)
         dt = time.perf_counter() - t0
-        J = volume_averaged_J_parallel(m, conn, volume, mat_id, Js_lookup, h)
-        mx, my, mz = volume_averaged_m(m, conn, volume, mat_id, Js_lookup)
+        J = avg.J_parallel(m, h)
+        mx, my, mz = avg.m_avg(m)
         B_t, J_t = float(Bmag) * params.Js_ref, J * params.Js_ref
         E_si = info["E"] * params.Js_ref**2 / (2.0 * 4e-7 * np.pi)
         history.append([B_t, J_t, mx, my, mz, E_si])
