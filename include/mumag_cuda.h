@@ -221,6 +221,17 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * around every solver launch; each launch's device time is added to a slot named by its kind, AMG
  * level and precision.  For measurement only: the loop is slower than the graph. */
 #define MM_OPT_PROFILE 5
+/* MM_OPT_PERSISTENT (default 0): 1 runs the PCG iterations of a multilevel solve (direction, step
+ * and the whole V-cycle, every level) in ONE cooperative launch whose blocks keep a fixed share of
+ * the rows of every operator and meet at grid barriers between the phases, instead of the separate
+ * kernels of the CUDA graph (MM_OPT_GRAPH).  Every barrier wait is bounded (1 s); a wait that runs
+ * out ends the launch and the solve returns MM_ERR_CUDA.  Inner products are summed in a fixed order
+ * (deterministic; they differ from the graph path at rounding level).  On the 80 nm cube (GB300) it
+ * is slower than the graph (each of the ~15 grid barriers of an iteration costs ~3 us and the fixed
+ * row shares leave fewer loads in flight), so it is off by default. */
+#define MM_OPT_PERSISTENT 6
+/* MM_OPT_PERSIST_BPSM: blocks per SM of that launch, 1..4 (0 = 4; capped by occupancy). */
+#define MM_OPT_PERSIST_BPSM 7
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* In-solve kernel profile (MM_OPT_PROFILE).  slot = (fp32 * MM_PROF_LEVELS + level) * MM_PROF_KINDS

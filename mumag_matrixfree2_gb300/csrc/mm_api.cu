@@ -13,6 +13,7 @@
 
 #include "../../include/mumag_cuda.h"
 #include "mm_kernels.cuh"
+#include "mm_persistent.cuh"
 #include "mm_setup.h"
 
 using mmk::BS;
@@ -104,6 +105,15 @@ struct SolverT {
   cudaGraphExec_t exec = nullptr;
   bool graph_failed = false;
   int64_t iter_launches = 0;          // kernels in one loop trip
+  // persistent PCG loop (one cooperative launch per solve)
+  mmk::PLev<T>* d_plev = nullptr;     // level views on the device
+  mmk::GridBar* d_bar = nullptr;      // barrier state, cleared before each launch
+  mmk::GridBar* h_bar = nullptr;      // pinned copy read back after the launch
+  int pgrid = 0;                      // co-resident grid of the launch
+  const void* pkern = nullptr;        // the kernel variant it was sized for
+  int* d_bounds = nullptr;            // block bounds of every operator (3 per level, MAXG + 1 each)
+  int pgrid_bpsm = -1;                // blocks per SM it was sized for
+  bool persist_failed = false;
 };
 
 // Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
@@ -176,6 +186,8 @@ struct mm_problem {
   mmk::Scalars* d_sc32 = nullptr;
   mmk::Scalars* h_sc = nullptr;  // pinned
   bool use_graph = true;
+  bool persistent = false;       // MM_OPT_PERSISTENT
+  int persist_bpsm = 0;          // MM_OPT_PERSIST_BPSM (0 = default)
 
   // staging buffers for host-pointer calls
   double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
@@ -533,6 +545,127 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
   return true;
 }
 
+template <class T>
+mmk::MatV<T> matv(const DevMatT<T>& M) {
+  mmk::MatV<T> v{};
+  v.tpr = M.tpr;
+  if (M.tpr == 1) {
+    v.n = M.s.n;
+    v.ptr = M.s.sptr;
+    v.col = M.s.col;
+    v.val = M.s.val;
+  } else {
+    v.n = M.c.n;
+    v.ptr = M.c.ptr;
+    v.col = M.c.col;
+    v.val = M.c.val;
+  }
+  return v;
+}
+
+// Block bounds of one operator for a G-block persistent launch: contiguous, equal ranges of slices
+// (sliced ELL) or rows (CSR).  G + 1 entries.  (Bounds balanced by stored entries were measured
+// slower on the 80 nm cube: the time of a phase follows the rows' load chains, not their entries.)
+std::vector<int> even_bounds(int n_rows, int tpr, int G) {
+  const int64_t units = tpr == 1 ? (n_rows + 31) / 32 : n_rows;
+  std::vector<int> b(G + 1);
+  for (int k = 0; k <= G; ++k) b[k] = (int)(units * k / G);
+  return b;
+}
+
+// Variant of the persistent kernel for `bpsm` blocks per SM: up to 2 blocks, 128 registers and two
+// rows in flight per thread; beyond, 64 registers (4 blocks per SM) and one row.
+template <class T>
+const void* persistent_variant(int bpsm) {
+  return bpsm <= 2 ? (const void*)mmk::k_pcg_persistent<T, 2, 2> : (const void*)mmk::k_pcg_persistent<T, 4, 1>;
+}
+
+// Level views (with the block bounds of every operator), barrier state and the co-resident grid of
+// the persistent loop: once per solver, and again when the blocks-per-SM option changes.  False when
+// the device cannot launch cooperatively.
+template <class T>
+bool setup_persistent(mm_problem* h, SolverT<T>& S) {
+  if (S.persist_failed) return false;
+  if (S.d_plev && S.pgrid_bpsm == h->persist_bpsm) return true;
+  int dev = 0, coop = 0, sms = 0, occ = 0;
+  const int want = h->persist_bpsm > 0 ? h->persist_bpsm : 4;
+  const void* kern = persistent_variant<T>(want);
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BS, 0));
+  if (!coop || occ < 1) {
+    S.persist_failed = true;
+    return false;
+  }
+  const int L = (int)S.lv.size();
+  const int G = std::min(sms * std::min(want, occ), MAXG);
+  S.pkern = kern;
+  S.pgrid = G;
+  S.pgrid_bpsm = h->persist_bpsm;
+  if (!S.d_plev) {
+    S.d_plev = h->alloc<mmk::PLev<T>>(L);
+    S.d_bar = h->alloc<mmk::GridBar>(1);
+    CK(cudaMallocHost(&S.h_bar, sizeof(mmk::GridBar)));
+    S.d_bounds = h->alloc<int>((size_t)3 * L * (MAXG + 1));
+  }
+  // bounds table: operator (l, j) (j = 0 A, 1 R, 2 P) at d_bounds + (3 l + j) (MAXG + 1)
+  std::vector<int> hb((size_t)3 * L * (MAXG + 1), 0);
+  std::vector<mmk::PLev<T>> hl(L);
+  auto put = [&](int l, int j, const mm::HostCSR& M, int tpr) {
+    const std::vector<int> b = even_bounds(M.n_rows, tpr, G);
+    std::copy(b.begin(), b.end(), hb.begin() + (size_t)(3 * l + j) * (MAXG + 1));
+    return S.d_bounds + (size_t)(3 * l + j) * (MAXG + 1);
+  };
+  for (int l = 0; l < L; ++l) {
+    const auto& d = S.lv[l];
+    const mm::AmgLevel& a = h->amg_h[l];
+    hl[l] = mmk::PLev<T>{};
+    hl[l].A = matv(d.A);
+    hl[l].A.bp = put(l, 0, a.A, d.A.tpr);
+    if (l < L - 1) {
+      hl[l].R = matv(d.R);
+      hl[l].R.bp = put(l, 1, a.R, d.R.tpr);
+      hl[l].P = matv(d.P);
+      hl[l].P.bp = put(l, 2, a.P, d.P.tpr);
+    }
+    hl[l].s = d.s;
+    hl[l].b = d.b;
+    hl[l].x = d.x;
+    hl[l].x2 = d.x2;
+    hl[l].res = d.res;
+    hl[l].n = d.n;
+  }
+  CK(cudaMemcpyAsync(S.d_plev, hl.data(), L * sizeof(mmk::PLev<T>), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(S.d_bounds, hb.data(), hb.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));  // hl and hb are locals
+  return true;
+}
+
+// The PCG iterations as one cooperative launch (the state left by the initial residual and the
+// first preconditioner application is taken over from the scalars).
+template <class T>
+void launch_persistent(mm_problem* h, SolverT<T>& S) {
+  mmk::PcgArgs<T> a{};
+  a.lv = S.d_plev;
+  a.L = (int)S.lv.size();
+  a.Ainv = S.Ainv;
+  a.nc = S.n_coarse;
+  a.x = S.x;
+  a.r = S.r;
+  a.z = S.z;
+  a.p = S.p;
+  a.Ap = S.Ap;
+  a.sc = S.sc;
+  a.part = h->d_part;
+  a.bar = S.d_bar;
+  CK(cudaMemsetAsync(S.d_bar, 0, sizeof(mmk::GridBar), h->st));
+  void* args[] = {&a};
+  CK(cudaLaunchCooperativeKernel(S.pkern, dim3(S.pgrid), dim3(BS), args, 0, h->st));
+  ++h->n_launch;
+  CK(cudaMemcpyAsync(S.h_bar, S.d_bar, sizeof(mmk::GridBar), cudaMemcpyDeviceToHost, h->st));
+}
+
 // PCG on S.x (initial guess in, solution out) for the right-hand side S.b; stops on the recursive
 // residual r.r <= tol^2 b.b or maxiter (src/poisson_solve.py:422-478).  Returns iterations and r.r.
 template <class T>
@@ -551,8 +684,11 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   });
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
   else apply_M_simple<T>(h, S, S.r, S.z, nullptr);
-  const bool graph = h->use_graph && !h->prof && build_loop_graph<T>(h, S);
-  if (graph) {
+  const bool persist = ml && h->persistent && !h->prof && setup_persistent<T>(h, S);
+  const bool graph = !persist && h->use_graph && !h->prof && build_loop_graph<T>(h, S);
+  if (persist) {
+    launch_persistent<T>(h, S);
+  } else if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
   } else if (h->prof) {
     // profiled: read `done` after every step so that no launch runs past convergence
@@ -575,6 +711,8 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   }
   CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   h->sync();
+  if (persist && S.h_bar->err != 0)
+    throw Fail{MM_ERR_CUDA, "persistent PCG: a grid-barrier wait ran out (blocks not co-resident?)"};
   if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -1545,6 +1683,8 @@ int mm_destroy(mm_problem* h) {
   if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
+  if (h->s64.h_bar) cudaFreeHost(h->s64.h_bar);
+  if (h->s32.h_bar) cudaFreeHost(h->s32.h_bar);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
@@ -1841,6 +1981,16 @@ int mm_set_option(mm_problem* h, int option, int value) {
   if (option == MM_OPT_PROFILE) {
     if (value != 0 && value != 1) return MM_ERR_ARG;
     h->prof = value == 1;
+    return MM_OK;
+  }
+  if (option == MM_OPT_PERSISTENT) {
+    if (value != 0 && value != 1) return MM_ERR_ARG;
+    h->persistent = value == 1;
+    return MM_OK;
+  }
+  if (option == MM_OPT_PERSIST_BPSM) {
+    if (value < 0 || value > 4) return MM_ERR_ARG;
+    h->persist_bpsm = value;
     return MM_OK;
   }
   if (option == MM_OPT_MIXED_ETA_E6) {

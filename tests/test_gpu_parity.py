@@ -182,3 +182,32 @@ def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     true_rr = np.linalg.norm(b - ops.apply_A(U32)) / np.linalg.norm(b)
     assert true_rr <= 1.5e-10  # checked in FP64 on the host
     assert rel(U32, U64) <= 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_persistent_loop_matches_graph_loop(cuda_ok, precision):
+    """The one-launch PCG loop (grid barriers between the phases) against the graph of separate
+    kernels: same iterations (+-1), potentials equal to the PCG tolerance, and for every
+    blocks-per-SM choice a converged, bit-reproducible solve."""
+    s, p, _ = case("cube16_h2_air48")
+    probs = []
+    for persistent in (0, 1):
+        prob = fem_utils.make_problem(s)
+        prob.set_precision(precision)
+        prob.set_option("persistent", persistent)
+        prob.build_poisson(1e-12, "amgcl")
+        probs.append(prob)
+    m = random_state(p.N, seed=21, amplitude=0.2)
+    zero = np.zeros(p.N)
+    Ug, itg, rrg, rcg = probs[0].solve_u(m, zero, 1e-10)
+    Up, itp, rrp, rcp = probs[1].solve_u(m, zero, 1e-10)
+    assert rcg == 0 and rcp == 0 and rrp <= 1e-10
+    assert abs(itp - itg) <= 1, (itp, itg)
+    assert rel(Up, Ug) <= 1e-8
+    for bpsm in (1, 2, 4):
+        probs[1].set_option("persist_bpsm", bpsm)
+        U1, it1, rr1, rc1 = probs[1].solve_u(m, zero, 1e-10)
+        U2, it2, rr2, rc2 = probs[1].solve_u(m, zero, 1e-10)
+        assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - itg) <= 1
+        assert it1 == it2 and np.array_equal(U1, U2)
+        assert rel(U1, Ug) <= 1e-8
