@@ -263,6 +263,47 @@ int mm_last_solve_ms(mm_problem* h, double* ms);
 /* Number of kernels this problem has launched since it was created. */
 int mm_launch_count(mm_problem* h, int64_t* count);
 
+/* ---- learned demag warm start ----------------------------------------------------------------
+ * No counterpart in the reference: a 3D U-Net (15 convolutions 3x3x3, 4 levels, 16/32/64/128
+ * channels, ReLU, 2x2x2 average pooling, nearest upsampling with added skips) over a G^3 voxel grid
+ * maps the voxelised change of magnetisation (3 channels) and the previous potential (1 channel) to
+ * the change of the demag potential (output channel 0).  BF16 weights and activations, FP32
+ * accumulation, FP32 master weights trained with Adam; convolutions on tcgen05 tensor cores.
+ * Parameters are one flat FP32 vector: for each layer in order w[27][c_in][c_out] (tap =
+ * (dz+1)*9 + (dy+1)*3 + (dx+1)) then b[c_out].  Voxel arrays are z-major with x fastest. */
+#define MM_UNET_LAYERS 15
+typedef struct mm_unet mm_unet;
+/* grid: level-0 edge G (multiple of 8, 16..256); batch: largest number of samples per call. */
+int mm_unet_create(int grid, int batch, mm_unet** out);
+int mm_unet_destroy(mm_unet* u);
+const char* mm_unet_last_error(mm_unet* u);
+int mm_unet_param_count(mm_unet* u, int64_t* n);
+int mm_unet_set_params(mm_unet* u, const float* params);  /* also resets the Adam state */
+int mm_unet_get_params(mm_unet* u, float* params);
+int mm_unet_get_grads(mm_unet* u, float* grads);           /* of the last mm_unet_backward */
+/* x: [nb][G^3][4] FP32 host array; y (may be NULL): [nb][G^3] output channel 0. */
+int mm_unet_forward(mm_unet* u, const float* x, int nb, float* y);
+/* Device-pointer variant; d_x NULL runs on the input already voxelised by mm_unet_voxelise_dev. */
+int mm_unet_forward_dev(mm_unet* u, const float* d_x, int nb, float* d_y);
+/* Mean squared error of output channel 0 against target [nb][G^3] over the samples of the last
+ * forward, and the gradient of every parameter. */
+int mm_unet_backward(mm_unet* u, const float* target, int nb, double* loss);
+int mm_unet_backward_dev(mm_unet* u, const float* d_target, int nb, double* loss);
+int mm_unet_adam(mm_unet* u, float lr, float beta1, float beta2, float eps);
+/* Mesh -> grid: input channels of voxel v of `sample` = sum_k w4[v][k] * (scale3 f3[idx4[v][k]][0..2],
+ * scale1 f1[idx4[v][k]]) over its 4 nodes (idx < 0 ends the list); device pointers, n_vox = G^3. */
+int mm_unet_voxelise_dev(mm_unet* u, int sample, int n_vox, const int* d_idx4, const float* d_w4,
+                         const double* d_f3, const double* d_f1, double scale3, double scale1);
+/* Grid -> mesh: d_U[node[j]] += scale * sum_k w8[j][k] y0(voxel idx8[j][k]), j < n. */
+int mm_unet_interp_add_dev(mm_unet* u, int sample, int n, const int* d_node, const int* d_idx8,
+                           const float* d_w8, double scale, double* d_U);
+/* Introspection (tests): tensor `which` (0..21, in forward order: input, e0a, s0, pool0, ..., output)
+ * lives on level `level` with `channels` channels; read one sample's activations (grad = 0) or their
+ * gradients (grad = 1) as FP32 [G_level^3][channels]. */
+int mm_unet_tensor_info(int which, int* level, int* channels);
+int mm_unet_read_tensor(mm_unet* u, int which, int grad, int sample, float* out);
+int mm_unet_sync(mm_unet* u);
+
 /* Wait for the problem's stream. */
 int mm_sync(mm_problem* h);
 const char* mm_status_str(int status);

@@ -24,6 +24,7 @@ PROF_LEVELS = 16
 PROF_SLOTS = 2 * PROF_LEVELS * len(PROF_KINDS)
 
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_int64)
 _vp = C.c_void_p
@@ -89,6 +90,24 @@ SIGNATURES = {
     "mm_last_solve_ms": (C.c_int, [_vp, _dp]),
     "mm_launch_count": (C.c_int, [_vp, _lp]),
     "mm_sync": (C.c_int, [_vp]),
+    # learned warm start
+    "mm_unet_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(_vp)]),
+    "mm_unet_destroy": (C.c_int, [_vp]),
+    "mm_unet_last_error": (C.c_char_p, [_vp]),
+    "mm_unet_param_count": (C.c_int, [_vp, _lp]),
+    "mm_unet_set_params": (C.c_int, [_vp, _fp]),
+    "mm_unet_get_params": (C.c_int, [_vp, _fp]),
+    "mm_unet_get_grads": (C.c_int, [_vp, _fp]),
+    "mm_unet_forward": (C.c_int, [_vp, _fp, C.c_int, _fp]),
+    "mm_unet_forward_dev": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "mm_unet_backward": (C.c_int, [_vp, _fp, C.c_int, _dp]),
+    "mm_unet_backward_dev": (C.c_int, [_vp, _vp, C.c_int, _dp]),
+    "mm_unet_adam": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "mm_unet_voxelise_dev": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_double, C.c_double]),
+    "mm_unet_interp_add_dev": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, _vp]),
+    "mm_unet_tensor_info": (C.c_int, [C.c_int, _ip, _ip]),
+    "mm_unet_read_tensor": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
+    "mm_unet_sync": (C.c_int, [_vp]),
 }
 
 _lib = None
