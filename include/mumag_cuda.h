@@ -178,6 +178,12 @@ int mm_solve_u(mm_problem* h, const double* m, double* U_inout, double tol, int 
 int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U_inout, double tol, int maxiter,
                    int* iters, double* rel_res);
 
+/* Add the multiple of a correction that minimises the energy-norm error of an initial guess:
+ * d_U += alpha d_c with alpha = c.(b - A U) / (c.A c), b = D m (never worse than U alone in the A-norm).
+ * Used to apply a predicted potential change (the learned warm start) before a solve.  No counterpart
+ * in the reference.  alpha may be NULL. */
+int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const double* d_c, double* alpha);
+
 /* Override the node weights of the minimizers (default: inv_M_rel = V_mag / M_nodal where
  * M_nodal > 1e-20 else 0; inv_M_prec = 1/d where d > 1e-20 else 1, d the exchange diagonal,
  * src/hysteresis_loop.py:340-353).  Either pointer may be NULL to keep the default. */
@@ -290,6 +296,9 @@ int mm_unet_forward_dev(mm_unet* u, const float* d_x, int nb, float* d_y);
 int mm_unet_backward(mm_unet* u, const float* target, int nb, double* loss);
 int mm_unet_backward_dev(mm_unet* u, const float* d_target, int nb, double* loss);
 int mm_unet_adam(mm_unet* u, float lr, float beta1, float beta2, float eps);
+/* on = 0: bias gradients are zero, so biases keep the values set (zero biases make the network
+ * positively homogeneous, f(a x) = a f(x) for a > 0, which the warm start relies on). */
+int mm_unet_set_bias_training(mm_unet* u, int on);
 /* Mesh -> grid: input channels of voxel v of `sample` = sum_k w4[v][k] * (scale3 f3[idx4[v][k]][0..2],
  * scale1 f1[idx4[v][k]]) over its 4 nodes (idx < 0 ends the list); device pointers, n_vox = G^3. */
 int mm_unet_voxelise_dev(mm_unet* u, int sample, int n_vox, const int* d_idx4, const float* d_w4,

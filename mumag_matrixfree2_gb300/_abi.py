@@ -81,6 +81,7 @@ SIGNATURES = {
     "mm_solve_u": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_int, _ip, _dp]),
     "mm_solve_u_dev": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _ip, _dp]),
     "mm_set_node_weights": (C.c_int, [_vp, _dp, _dp]),
+    "mm_scale_correction_dev": (C.c_int, [_vp, _vp, _vp, _vp, _dp]),
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
@@ -103,6 +104,7 @@ SIGNATURES = {
     "mm_unet_backward": (C.c_int, [_vp, _fp, C.c_int, _dp]),
     "mm_unet_backward_dev": (C.c_int, [_vp, _vp, C.c_int, _dp]),
     "mm_unet_adam": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "mm_unet_set_bias_training": (C.c_int, [_vp, C.c_int]),
     "mm_unet_voxelise_dev": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_double, C.c_double]),
     "mm_unet_interp_add_dev": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, _vp]),
     "mm_unet_tensor_info": (C.c_int, [C.c_int, _ip, _ip]),

@@ -1860,6 +1860,27 @@ int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U, double tol, in
   return guarded(h, [&] { return solve_dev(h, d_m, d_U, tol, maxiter, iters, rel_res); });
 }
 
+int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const double* d_c, double* alpha) {
+  if (!h || !d_m || !d_U || !d_c) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    const int N = h->N;
+    const auto& A0 = h->s64.lv[0].A;
+    enqueue_rhs(h, d_m);                                                      // d_b = D m
+    spmv<0, double>(h, A0, d_U, nullptr, nullptr, h->d_out, nullptr);         // A U
+    spmv<0, double>(h, A0, d_c, nullptr, nullptr, h->d_r64, nullptr);         // A c
+    const double cb = dev_dot(h, N, d_c, h->d_b);
+    const double cAU = dev_dot(h, N, d_c, h->d_out);
+    const double cAc = dev_dot(h, N, d_c, h->d_r64);
+    const double a = (cAc > 0.0 && std::isfinite(cAc)) ? (cb - cAU) / cAc : 0.0;
+    mmk::k_axpby<<<grid_elem(N), BS, 0, h->st>>>(N, a, d_c, 1.0, d_U);
+    LAUNCH_CHECK();
+    h->sync();
+    if (alpha) *alpha = a;
+    return MM_OK;
+  });
+}
+
 int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec) {
   if (!h) return MM_ERR_ARG;
   return guarded(h, [&] {

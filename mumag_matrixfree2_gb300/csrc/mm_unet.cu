@@ -738,6 +738,7 @@ struct mm_unet {
   float* stage_t = nullptr;    // FP32 [B][G^3] (targets / outputs)
   int* d_err = nullptr;
   int nb_fwd = 0;              // samples of the last forward
+  bool train_bias = true;      // false: bias gradients are zero (biases stay as set)
 
   template <class T>
   T* alloc(size_t n) {
@@ -825,10 +826,14 @@ struct mm_unet {
     mmn::k_sum_parts<<<grid1d(nw), 256, 0, st>>>(part, nb * ns, nw, d.cin, d.cout, l == L_E0A ? IN_CH : d.cin,
                                                  g + woff[l]);
     UCK(cudaGetLastError());
-    mmn::k_bias_part<<<dim3((unsigned)ns, (unsigned)nb), 128, 0, st>>>(dy, v, d.cout, vpb, ns, bpart);
-    UCK(cudaGetLastError());
-    mmn::k_sum_parts<<<grid1d(d.cout), 256, 0, st>>>(bpart, nb * ns, d.cout, 1, d.cout, 1, g + boff[l]);
-    UCK(cudaGetLastError());
+    if (train_bias) {
+      mmn::k_bias_part<<<dim3((unsigned)ns, (unsigned)nb), 128, 0, st>>>(dy, v, d.cout, vpb, ns, bpart);
+      UCK(cudaGetLastError());
+      mmn::k_sum_parts<<<grid1d(d.cout), 256, 0, st>>>(bpart, nb * ns, d.cout, 1, d.cout, 1, g + boff[l]);
+      UCK(cudaGetLastError());
+    } else {
+      UCK(cudaMemsetAsync(g + boff[l], 0, d.cout * sizeof(float), st));
+    }
     if (dx) conv(l, dy, dx, nb, true);
   }
 
@@ -1133,6 +1138,12 @@ int mm_unet_backward_dev(mm_unet* u, const float* d_target, int nb, double* loss
     if (loss) *loss = L;
     return MM_OK;
   });
+}
+
+int mm_unet_set_bias_training(mm_unet* u, int on) {
+  if (!u || (on != 0 && on != 1)) return MM_ERR_ARG;
+  u->train_bias = on == 1;
+  return MM_OK;
 }
 
 int mm_unet_adam(mm_unet* u, float lr, float beta1, float beta2, float eps) {

@@ -116,3 +116,80 @@ def test_training_reduces_the_loss(cuda_ok):
         losses.append(net.backward(t))
         net.adam(2e-3)
     assert losses[-1] < 0.75 * losses[0], losses[::5]
+
+
+# ------------------------------------------------------------------------------------------------
+# the warm start on a mesh: data from the plain solver's sweeps, training, and what it gains
+# ------------------------------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def sweeps(cuda_ok):
+    import torch
+
+    from mumag_matrixfree2_gb300 import fem_utils
+    from mumag_matrixfree2_gb300 import synthetic as syn
+    from mumag_matrixfree2_gb300.cuda_backend import MinimizerParams
+
+    from .helpers import case
+
+    s, _, Js_ref = case("cube40_h2_air200")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    ws = learned.WarmStart(s, grid=32, margin=10.0, batch=8, seed=1)
+    prm = MinimizerParams(tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10)
+    B = syn.field_values(8.0 / Js_ref, -8.0 / Js_ref, 0.2 / Js_ref)
+    train, pairs = [], []
+    for tilt, seed in ((10.0, 1), (30.0, 2), (45.0, 3)):
+        st, _, _ = learned.collect_sweep(prob, ws, syn.initial_state(s.N, seed=seed),
+                                         syn.tilted_field_direction(tilt), B, prm)
+        base = len(train)
+        train += st
+        pairs += [(base + i, base + i + d) for d in (1, 2) for i in range(len(st) - d)]
+    ev, nodal, _ = learned.collect_sweep(prob, ws, syn.initial_state(s.N, seed=0),
+                                         syn.tilted_field_direction(1.0), B, prm, keep_nodal=True)
+    ws.calibrate(train, pairs)
+    torch.cuda.synchronize()
+    return prob, ws, train, pairs, ev, nodal
+
+
+def test_device_transfer_matches_host_transfer(sweeps):
+    """mm_unet_voxelise_dev / forward / mm_unet_interp_add_dev (the in-solve path, no normalisation:
+    the bias-free network is homogeneous) against the torch gathers and a normalised forward."""
+    import torch
+
+    prob, ws, train, pairs, ev, nodal = sweeps
+    (ma, Ua), (mb, Ub) = nodal[10], nodal[11]
+    U_dev = Ua.clone()
+    ws.apply(mb, ma, U_dev)
+    fa = ws.fields(ma, Ua)
+    mv = ws._vox(mb) * ws.jsf[:, None]
+    fb = torch.cat([mv.float(), fa[:, 3:]], 1)
+    pred, _ = ws.predict_grid(fa, fb)
+    corr = torch.zeros_like(Ua)
+    corr[ws.k_nodes.long()] = (pred.double()[ws.k_idx8.long()] * ws.k_w8.double()).sum(1)
+    ref = Ua + corr
+    d = (U_dev - ref).abs().max().item()
+    scale = corr.abs().max().item()
+    assert scale > 0 and d <= 2e-2 * scale, (d, scale)  # bf16 activations, different input scaling
+
+
+def test_trained_warm_start_saves_pcg_iterations(sweeps):
+    """Trained on the plain solver's own sweeps, the network's prediction of U_b - U_a on a held-out
+    sweep beats U_a alone, and PCG to the same tolerance needs fewer iterations from it."""
+    prob, ws, train, pairs, ev, nodal = sweeps
+    ev_pairs = [(i, i + 1) for i in range(len(ev) - 1)]
+    err0 = np.median([ws.predict_grid(ev[a], ev[b])[1] for a, b in ev_pairs])
+    ws.train(train, pairs, steps=1500, lr=1e-3)
+    err1 = np.median([ws.predict_grid(ev[a], ev[b])[1] for a, b in ev_pairs])
+    assert err1 < 0.6 * err0, (err0, err1)
+    base = learn = 0
+    for k in range(len(nodal) - 1):
+        (ma, Ua), (mb, Ub) = nodal[k], nodal[k + 1]
+        x = Ua.clone()
+        _, it0, rr0, rc0 = prob.solve_u(mb, x, 1e-10)
+        x = Ua.clone()
+        ws.apply(mb, ma, x, prob)
+        _, it1, rr1, rc1 = prob.solve_u(mb, x, 1e-10)
+        assert rc0 == 0 and rc1 == 0 and rr1 <= 1e-10
+        base += it0
+        learn += it1
+    assert learn < base, (learn, base)
