@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-loop", action="store_true", help="skip the hysteresis-loop leg")
     ap.add_argument("--loop-dB", type=float, default=0.1, help="field step of the loop leg [T]")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start leg")
+    ap.add_argument("--learned-steps", type=int, default=2000, help="training steps of the learned leg")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm worker processes (0: all cores)")
@@ -327,6 +329,100 @@ def run_loop(s, m0, precision, dB_T):
             "Hc_T": coercive_field(hist[:, 0], hist[:, 1]), "_J": J}
 
 
+def run_learned(s, prob, pm, a):
+    """The learned warm start on this workload: training data from four plain FP64 sweeps (+8 T -> -8 T
+    in 0.2 T steps, tilts 1/15/30/45 deg, seeds 1-4), Adam on the GPU, then the held-out benchmark
+    sweep (tilt 1 deg, seed 0, 0.1 T steps): for every other field step k, the solve for m_(k+1)
+    from U_k (the plain warm start), from U_k + the prediction (scaled by the energy-optimal factor),
+    and from 0, in FP64 and in mixed precision, each to the same tolerance."""
+    import torch
+
+    from mumag_matrixfree2_gb300 import learned
+    from mumag_matrixfree2_gb300 import synthetic as syn
+    from mumag_matrixfree2_gb300.cuda_backend import MinimizerParams
+
+    Js_ref = syn.reduced_materials([syn.Material(), syn.AIR])[4]
+    G = 32
+    t0 = time.perf_counter()
+    ws = learned.WarmStart(s, grid=G, margin=20.0, batch=8, seed=0)
+    prm = MinimizerParams(method="pcohen_hs", tau_f=1e-8, eps_a=1e-6, cg_tol=a.tol, pc_iters=10)
+    train, pairs = [], []
+    for tilt, seed in ((1.0, 1), (15.0, 2), (30.0, 3), (45.0, 4)):
+        B = syn.field_values(8.0 / Js_ref, -8.0 / Js_ref, 0.2 / Js_ref)
+        st, _, _ = learned.collect_sweep(prob, ws, syn.initial_state(s.N, seed=seed), syn.tilted_field_direction(tilt),
+                                         B, prm)
+        base = len(train)
+        train += st
+        pairs += [(base + i, base + i + d) for d in (1, 2) for i in range(len(st) - d)]
+    data_s = time.perf_counter() - t0
+    B = syn.field_values(8.0 / Js_ref, -8.0 / Js_ref, 0.1 / Js_ref)
+    ev, nodal, _ = learned.collect_sweep(prob, ws, syn.initial_state(s.N, seed=0), syn.tilted_field_direction(1.0), B,
+                                         prm, keep_nodal=True)
+    ws.calibrate(train, pairs)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    losses = ws.train(train, pairs, a.learned_steps, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    val = float(np.median([ws.predict_grid(ev[i], ev[i + 1])[1] for i in range(0, len(ev) - 1, 2)]))
+    # forward alone (input voxelised in place), CUDA events around the network's stream work
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fwd = []
+    for _ in range(20):
+        torch.cuda.synchronize()
+        e0.record()
+        ws.net.forward_dev(None, None, 1)
+        e1.record()
+        torch.cuda.synchronize()
+        fwd.append(e0.elapsed_time(e1))
+    fwd_ms = float(np.median(fwd[5:]))
+    flops = sum(2.0 * 27 * ci * co * (G >> lvl) ** 3 for _, lvl, ci, co, _ in learned.LAYERS)
+    res = {k: [] for k in ("base64", "learn64", "cold64", "base_mx", "learn_mx", "ms_base64", "ms_learn64",
+                           "ms_base_mx", "ms_learn_mx", "ms_net")}
+    for k in range(0, len(nodal) - 1, 2):
+        (ma, Ua), (mb, _) = nodal[k], nodal[k + 1]
+        for tag, pr in (("64", prob), ("_mx", pm)):
+            if pr is None:
+                continue
+            x = Ua.clone()
+            _, it, rr, rc = pr.solve_u(mb, x, a.tol)
+            res["base" + tag].append(it)
+            res["ms_base" + tag].append(pr.last_solve_ms())
+            x = Ua.clone()
+            torch.cuda.synchronize()
+            e0.record()
+            ws.apply(mb, ma, x, pr)
+            e1.record()
+            torch.cuda.synchronize()
+            if tag == "64":
+                res["ms_net"].append(e0.elapsed_time(e1))
+            _, it, rr, rc = pr.solve_u(mb, x, a.tol)
+            if rc != 0 or not rr <= a.tol:
+                raise RuntimeError(f"learned warm-start solve did not converge: {rc} {rr}")
+            res["learn" + tag].append(it)
+            res["ms_learn" + tag].append(pr.last_solve_ms())
+        x = torch.zeros_like(Ua)
+        _, it, _, _ = prob.solve_u(mb, x, a.tol)
+        res["cold64"].append(it)
+    mean = {k: (float(np.mean(v)) if v else None) for k, v in res.items()}
+    out = {"grid": G, "params": ws.net.n_params, "train_pairs": len(pairs), "data_sweeps_s": data_s,
+           "train_steps": a.learned_steps, "batch": ws.batch, "train_s": train_s,
+           "train_ms_per_step": 1e3 * train_s / a.learned_steps, "final_loss": float(np.mean(losses[-50:])),
+           "val_rel_err_grid": val, "eval_solves": len(res["base64"]),
+           "pcg_iters": {"plain_warm_fp64": mean["base64"], "learned_fp64": mean["learn64"], "cold_fp64": mean["cold64"],
+                         "plain_warm_mixed": mean["base_mx"], "learned_mixed": mean["learn_mx"]},
+           "solve_ms": {"plain_warm_fp64": mean["ms_base64"], "learned_fp64": mean["ms_learn64"],
+                        "plain_warm_mixed": mean["ms_base_mx"], "learned_mixed": mean["ms_learn_mx"],
+                        "network_and_transfer": mean["ms_net"]},
+           "forward": {"ms": fwd_ms, "flop": flops, "tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                       "note": "3x3x3 convolutions, interior voxels only; tcgen05 BF16"}}
+    if mean["ms_learn_mx"] is not None:
+        out["mixed_learned_vs_plain_fp64"] = {
+            "solve_time_ratio": mean["ms_base64"] / mean["ms_learn_mx"],
+            "with_network_time_ratio": mean["ms_base64"] / (mean["ms_learn_mx"] + mean["ms_net"])}
+    return out
+
+
 def run_ours(a):
     import torch
 
@@ -412,6 +508,10 @@ def run_ours(a):
                  "method": "FP32 hierarchy + FP32 PCG (FP64 inner products) inside FP64 iterative refinement; "
                            "stop on the true FP64 residual"}
 
+    learned_leg = None
+    if not a.no_learned:
+        learned_leg = run_learned(s, prob, None if a.no_mixed else pm, a)
+
     loop = None
     if not a.no_loop:
         lp = {p_: run_loop(s, m0, p_, a.loop_dB) for p_ in (("fp64",) if a.no_mixed else ("fp64", "mixed"))}
@@ -460,6 +560,7 @@ def run_ours(a):
             "kernels": kernels,
             "profiled_solve_ms": prof_ms / a.profile_steps,
             "mixed": mixed,
+            "learned": learned_leg,
             "loop": loop,
             "cpu_baseline": cpu,
             "clocks": clk,

@@ -238,6 +238,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 #define MM_OPT_PERSISTENT 6
 /* MM_OPT_PERSIST_BPSM: blocks per SM of that launch, 1..4 (0 = 4; capped by occupancy). */
 #define MM_OPT_PERSIST_BPSM 7
+/* MM_OPT_PDL (default 1): launch the solver kernels with programmatic dependent launch, so each
+ * kernel is scheduled while its predecessor drains (every solver kernel waits for its predecessor's
+ * results at entry); 0 launches them normally.  Same results either way. */
+#define MM_OPT_PDL 8
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* In-solve kernel profile (MM_OPT_PROFILE).  slot = (fp32 * MM_PROF_LEVELS + level) * MM_PROF_KINDS

@@ -187,6 +187,7 @@ struct mm_problem {
   mmk::Scalars* h_sc = nullptr;  // pinned
   bool use_graph = true;
   bool persistent = false;       // MM_OPT_PERSISTENT
+  bool pdl = true;               // MM_OPT_PDL
   int persist_bpsm = 0;          // MM_OPT_PERSIST_BPSM (0 = default)
 
   // staging buffers for host-pointer calls
@@ -313,6 +314,24 @@ using mmk::R_R2;
 using mmk::R_RZ;
 using mmk::R_SUM;
 
+// Launch on the problem's stream with programmatic dependent launch allowed when h->pdl: the
+// kernel may be scheduled while its predecessor drains, and waits for the predecessor's results
+// itself (pdl_entry at its start).  Arguments are converted to the kernel's parameter types.
+template <typename... KArgs, typename... Args>
+void launch(mm_problem* h, void (*kern)(KArgs...), dim3 grid, dim3 block, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = h->st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = h->pdl ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+}
+
 #define TPR_SWITCH(tpr, ...)                         \
   switch (tpr) {                                     \
     case 2: { constexpr int TP = 2; __VA_ARGS__; } break;   \
@@ -325,17 +344,17 @@ using mmk::R_SUM;
 template <int MODE, class T>
 void spmv(mm_problem* h, const DevMatT<T>& A, const T* x, const T* b, const T* s, T* y, const int* done) {
   if (A.tpr == 1) {
-    mmk::k_sell<MODE, T><<<grid_ilp(A.s.n), BS, 0, h->st>>>(A.s, x, b, s, y, done);
+    launch(h, mmk::k_sell<MODE, T>, grid_ilp(A.s.n), BS, A.s, x, b, s, y, done);
   } else {
     const int g = grid_rows(A.c.n, A.tpr);
-    TPR_SWITCH(A.tpr, (mmk::k_csr<TP, MODE><<<g, BS, 0, h->st>>>(A.c, x, b, s, y, done)));
+    TPR_SWITCH(A.tpr, (launch(h, mmk::k_csr<TP, MODE, T>, g, BS, A.c, x, b, s, y, done)));
   }
   LAUNCH_CHECK();
 }
 
 template <class T>
 void dotT(mm_problem* h, int n, const T* x, const T* y, mmk::Scalars* sc, int slot, int post = mmk::POST_NONE) {
-  mmk::k_dot<T><<<grid_ilp(n), BS, 0, h->st>>>(n, x, y, sc, h->d_part, slot, post);
+  launch(h, mmk::k_dot<T>, grid_ilp(n), BS, n, x, y, sc, h->d_part, slot, post);
   LAUNCH_CHECK();
 }
 
@@ -387,7 +406,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     auto& c = lv[l];
     if (l == 0 && in_loop) {
       tagged<T>(h, MM_PROF_VC_RESIDUAL0, 0, mat_bytes(c.A) + 3.0 * w * c.n, [&] {
-        mmk::k_vc_residual0<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.res, S.sc);
+        launch(h, mmk::k_vc_residual0<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.res, S.sc);
         LAUNCH_CHECK();
       });
     } else {
@@ -399,11 +418,11 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     const double rbytes = mat_bytes(c.R) + w * c.n + (coarsest ? 1.0 : 3.0) * w * nx.n;
     tagged<T>(h, MM_PROF_RESTRICT, l, rbytes, [&] {
       if (c.R.tpr == 1) {
-        mmk::k_restrict<T><<<grid_ilp(nx.n), BS, 0, h->st>>>(c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
+        launch(h, mmk::k_restrict<T>, grid_ilp(nx.n), BS, c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
                                                                 done);
       } else {
         const int g = grid_rows(nx.n, c.R.tpr);
-        TPR_SWITCH(c.R.tpr, (mmk::k_restrict_csr<TP><<<g, BS, 0, h->st>>>(c.R.c, c.res, nx.b,
+        TPR_SWITCH(c.R.tpr, (launch(h, mmk::k_restrict_csr<TP, T>, g, BS, c.R.c, c.res, nx.b,
                                                                           coarsest ? nullptr : nx.s, nx.x, done)));
       }
       LAUNCH_CHECK();
@@ -412,7 +431,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
   {
     auto& c = lv[L - 1];
     tagged<T>(h, MM_PROF_COARSE, L - 1, w * ((double)c.n * c.n + 2.0 * c.n), [&] {
-      mmk::k_dense_mv<T><<<grid_rows(c.n, 32), BS, 0, h->st>>>(c.n, S.Ainv, c.b, c.x2, done);
+      launch(h, mmk::k_dense_mv<T>, grid_rows(c.n, 32), BS, c.n, S.Ainv, c.b, c.x2, done);
       LAUNCH_CHECK();
     });
   }
@@ -422,7 +441,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
               [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
     if (l == 0) {
       tagged<T>(h, MM_PROF_SMOOTH0, 0, mat_bytes(c.A) + 4.0 * w * c.n, [&] {
-        mmk::k_smooth_dot<T><<<grid_ilp(c.n), BS, 0, h->st>>>(c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
+        launch(h, mmk::k_smooth_dot<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
         LAUNCH_CHECK();
       });
     } else {
@@ -437,12 +456,12 @@ template <class T>
 void apply_M_simple(mm_problem* h, SolverT<T>& S, const T* r, T* z, const int* done) {
   const int N = h->N;
   if (h->precond == MM_PRECOND_JACOBI) {
-    mmk::k_mul<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.jac, r, z);
+    launch(h, mmk::k_mul<T>, grid_ilp(N), BS, N, S.jac, r, z);
     LAUNCH_CHECK();
   } else if (h->precond == MM_PRECOND_NONE) {
     CK(cudaMemcpyAsync(z, r, N * sizeof(T), cudaMemcpyDeviceToDevice, h->st));
   } else {
-    mmk::k_dense_mv<T><<<grid_rows(S.n_coarse, 32), BS, 0, h->st>>>(S.n_coarse, S.Ainv, r, z, done);
+    launch(h, mmk::k_dense_mv<T>, grid_rows(S.n_coarse, 32), BS, S.n_coarse, S.Ainv, r, z, done);
     LAUNCH_CHECK();
   }
   dotT<T>(h, N, r, z, S.sc, R_RZ, mmk::POST_RZ);
@@ -452,7 +471,7 @@ void apply_M_simple(mm_problem* h, SolverT<T>& S, const T* r, T* z, const int* d
 template <class T>
 void enqueue_precond(mm_problem* h, SolverT<T>& S, const T* r, T* z) {
   if (multilevel(h, S)) {
-    mmk::k_mul<T><<<grid_ilp(h->N), BS, 0, h->st>>>(h->N, S.lv[0].s, r, S.lv[0].x);
+    launch(h, mmk::k_mul<T>, grid_ilp(h->N), BS, h->N, S.lv[0].s, r, S.lv[0].x);
     LAUNCH_CHECK();
     enqueue_vcycle<T>(h, S, r, z, false, nullptr);
   } else {
@@ -468,12 +487,12 @@ void enqueue_dir_step(mm_problem* h, SolverT<T>& S) {
   const double w = sizeof(T);
   auto& l0 = S.lv[0];
   tagged<T>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * w * N, [&] {
-    mmk::k_pcg_dir<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+    launch(h, mmk::k_pcg_dir<T>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
     LAUNCH_CHECK();
   });
   const bool ml = multilevel(h, S);
   tagged<T>(h, MM_PROF_PCG_STEP, 0, (ml ? 8.0 : 6.0) * w * N, [&] {
-    mmk::k_pcg_step<T><<<grid_ilp(N), BS, 0, h->st>>>(N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
+    launch(h, mmk::k_pcg_step<T>, grid_ilp(N), BS, N, S.x, S.r, S.p, S.Ap, ml ? l0.s : nullptr, l0.x, S.sc,
                                                         h->d_part);
     LAUNCH_CHECK();
   });
@@ -521,7 +540,7 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
       const int64_t saved = h->n_launch;
       try {
         enqueue_iteration<T>(h, S);
-        mmk::k_set_cond<<<1, 32, 0, h->st>>>(hnd, S.sc);
+        launch(h, mmk::k_set_cond, 1, 32, hnd, S.sc);
       } catch (const Fail&) {
         ok = false;
       }
@@ -672,13 +691,13 @@ template <class T>
 void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out) {
   const int N = h->N;
   dotT<T>(h, N, S.b, (const T*)nullptr, S.sc, R_BB);
-  mmk::k_pcg_init_scalars<<<1, 32, 0, h->st>>>(S.sc, tol, maxiter);
+  launch(h, mmk::k_pcg_init_scalars, 1, 32, S.sc, tol, maxiter);
   LAUNCH_CHECK();
   const bool ml = multilevel(h, S);
   auto& l0 = S.lv[0];
   const double w = sizeof(T);
   tagged<T>(h, MM_PROF_INIT_RESIDUAL, 0, mat_bytes(l0.A) + 5.0 * w * N, [&] {
-    mmk::k_init_residual<T><<<grid_ilp(N), BS, 0, h->st>>>(l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
+    launch(h, mmk::k_init_residual<T>, grid_ilp(N), BS, l0.A.s, S.x, S.b, S.r, ml ? l0.s : nullptr, l0.x, S.sc,
                                                              h->d_part);
     LAUNCH_CHECK();
   });
@@ -748,19 +767,19 @@ int run_mixed(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out
   int total = 0, outer = 0;
   double rr = 0.0;
   while (true) {
-    mmk::k_resid64<<<grid_ilp(N), BS, 0, h->st>>>(A64.s, h->d_x, h->d_b, h->d_r64, h->d_sc, h->d_part);
+    launch(h, mmk::k_resid64, grid_ilp(N), BS, A64.s, h->d_x, h->d_b, h->d_r64, h->d_sc, h->d_part);
     LAUNCH_CHECK();
     rr = h->red(R_R2);
     if (!(rr > tol * tol * bb) || outer >= h->mixed_max_outer || total >= maxiter || !std::isfinite(rr)) break;
     const double rn = std::sqrt(rr);
-    mmk::k_to_f32<<<grid_ilp(N), BS, 0, h->st>>>(N, h->d_r64, 1.0 / rn, h->d_r32, h->d_d32);
+    launch(h, mmk::k_to_f32, grid_ilp(N), BS, N, h->d_r64, 1.0 / rn, h->d_r32, h->d_d32);
     LAUNCH_CHECK();
     const double need = tol * std::sqrt(bb) / rn;  // relative reduction still required
     const double eta = std::max(h->mixed_eta, 0.5 * need);
     int it = 0;
     run_pcg<float>(h, h->s32, eta, std::max(1, maxiter - total), &it, nullptr);
     total += it;
-    mmk::k_add_f32<<<grid_ilp(N), BS, 0, h->st>>>(N, h->d_x, h->d_d32, rn);
+    launch(h, mmk::k_add_f32, grid_ilp(N), BS, N, h->d_x, h->d_d32, rn);
     LAUNCH_CHECK();
     ++outer;
   }
@@ -1929,12 +1948,12 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     const int N = h->N;
     double acc = 0.0, nbytes = 0.0;
     const LevelT<double>* l0 = h->poisson_built ? &h->s64.lv[0] : nullptr;
-    auto launch = [&]() {
+    auto run_kernel = [&]() {
       if (kernel == MM_KERNEL_SPMV_A) {
         spmv<0, double>(h, l0->A, h->d_U, nullptr, nullptr, h->d_out, nullptr);
       } else if (kernel == MM_KERNEL_SMOOTH) {
         const double* s = l0->s ? l0->s : h->d_U;
-        mmk::k_smooth_dot<double><<<grid_ilp(l0->n), BS, 0, h->st>>>(l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
+        launch(h, mmk::k_smooth_dot<double>, grid_ilp(l0->n), BS, l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
                                                                 nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
@@ -1962,11 +1981,11 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     } else {
       nbytes = nnzE * (4.0 + 4.0 + 8.0 * 2.0) + nrE * 8.0 + nrE * 8.0 * 6.0;
     }
-    launch();  // warm-up
+    run_kernel();  // warm-up
     for (int r = 0; r < reps; ++r) {
       CK(cudaMemsetAsync(flush, r & 0xff, flush_n, h->st));
       CK(cudaEventRecord(e0, h->st));
-      launch();
+      run_kernel();
       CK(cudaEventRecord(e1, h->st));
       CK(cudaEventSynchronize(e1));
       float t = 0.f;
@@ -2002,6 +2021,25 @@ int mm_set_option(mm_problem* h, int option, int value) {
   if (option == MM_OPT_PROFILE) {
     if (value != 0 && value != 1) return MM_ERR_ARG;
     h->prof = value == 1;
+    return MM_OK;
+  }
+  if (option == MM_OPT_PDL) {
+    if (value != 0 && value != 1) return MM_ERR_ARG;
+    if (h->pdl != (value == 1)) {  // captured loop graphs hold the old launch attribute
+      for (SolverT<double>* S : {&h->s64}) {
+        if (S->exec) cudaGraphExecDestroy(S->exec);
+        if (S->graph) cudaGraphDestroy(S->graph);
+        S->exec = nullptr;
+        S->graph = nullptr;
+        S->graph_failed = false;
+      }
+      if (h->s32.exec) cudaGraphExecDestroy(h->s32.exec);
+      if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
+      h->s32.exec = nullptr;
+      h->s32.graph = nullptr;
+      h->s32.graph_failed = false;
+    }
+    h->pdl = value == 1;
     return MM_OK;
   }
   if (option == MM_OPT_PERSISTENT) {

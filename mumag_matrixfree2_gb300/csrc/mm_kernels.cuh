@@ -44,6 +44,15 @@ struct Scalars {
 // the consumer kernels spends FP64 divides or compares on them).
 enum Post { POST_NONE, POST_PAP, POST_R2_STEP, POST_R2_INIT, POST_RZ, POST_MEAN };
 
+// Programmatic dependent launch: wait until the preceding grid in the stream has completed and its
+// writes are visible, then allow the next grid to be scheduled (it waits the same way).  Both are
+// no-ops when the kernel was launched normally.  Every solver kernel starts with this, so the
+// launch latency of a kernel overlaps the drain of its predecessor.
+__device__ __forceinline__ void pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ------------------------------------------------------------------------------------------
 // deterministic reductions
 // ------------------------------------------------------------------------------------------
@@ -376,6 +385,7 @@ __device__ __forceinline__ T csr_row(const CsrT<T>& A, const T* __restrict__ x, 
 template <int TPR, int MODE, class T>
 __global__ void __launch_bounds__(BS) k_csr(CsrT<T> A, const T* __restrict__ x, const T* b, const T* __restrict__ s,
                                             T* y, const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
@@ -397,6 +407,7 @@ template <int TPR, class T>
 __global__ void __launch_bounds__(BS) k_restrict_csr(CsrT<T> R, const T* __restrict__ res, T* __restrict__ bc,
                                                      const T* __restrict__ s_c, T* __restrict__ xc,
                                                      const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   constexpr int RPB = BS / TPR;
   const int lane = threadIdx.x % TPR;
@@ -414,6 +425,7 @@ __global__ void __launch_bounds__(BS) k_restrict_csr(CsrT<T> R, const T* __restr
 template <int MODE, class T>
 __global__ void __launch_bounds__(BS) k_sell(SellT<T> A, const T* __restrict__ x, const T* b,
                                              const T* __restrict__ s, T* y, const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   ROW_LOOP(A.n) {
     int row[ILP];
@@ -437,6 +449,7 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_init_residual(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                       T* __restrict__ r, const T* __restrict__ s, T* __restrict__ xv,
                                                       Scalars* sc, double* part) {
+  pdl_entry();
   Acc<T> acc;
   ROW_LOOP(A.n) {
     int row[ILP];
@@ -462,6 +475,7 @@ __global__ void __launch_bounds__(BS) k_init_residual(SellT<T> A, const T* __res
 template <class T>
 __global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict__ z, T* __restrict__ p,
                                                 T* __restrict__ Ap, Scalars* sc, double* part) {
+  pdl_entry();
   if (sc->done) return;
   const T beta = scal<T>(sc->beta, sc->beta_f);
   Acc<T> acc;
@@ -489,6 +503,7 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                                                  const T* __restrict__ Ap, const T* __restrict__ s0, T* __restrict__ xv,
                                                  Scalars* sc, double* part) {
+  pdl_entry();
   if (sc->done) return;
   const T alpha = scal<T>(sc->alpha, sc->alpha_f);
   Acc<T> acc;
@@ -513,6 +528,7 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __
 template <class T>
 __global__ void __launch_bounds__(BS) k_vc_residual0(SellT<T> A, const T* __restrict__ xv, const T* __restrict__ r,
                                                      T* __restrict__ res, Scalars* sc) {
+  pdl_entry();
   if (sc->done) return;
   ROW_LOOP(A.n) {
     int row[ILP];
@@ -530,6 +546,7 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_restrict(SellT<T> R, const T* __restrict__ res, T* __restrict__ bc,
                                                  const T* __restrict__ s_c, T* __restrict__ xc,
                                                  const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   ROW_LOOP(R.n) {
     int row[ILP];
@@ -550,6 +567,7 @@ __global__ void __launch_bounds__(BS) k_restrict(SellT<T> R, const T* __restrict
 template <class T>
 __global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ainv, const T* __restrict__ b,
                                                  T* __restrict__ x, const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   const int lane = threadIdx.x & 31;
   for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gridDim.x * (BS / 32)) {
@@ -568,6 +586,7 @@ template <class T>
 __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                    const T* __restrict__ s, T* __restrict__ y, Scalars* sc,
                                                    double* part, const int* __restrict__ done) {
+  pdl_entry();
   if (done && *done) return;
   Acc<T> acc;
   ROW_LOOP(A.n) {
@@ -589,6 +608,7 @@ __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restri
 
 // condition of the graph's WHILE node: keep looping until done (bounded by maxiter + 2 trips)
 __global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
+  pdl_entry();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     sc->loops += 1;
     const bool more = !sc->done && sc->loops <= sc->maxiter + 2;
@@ -603,6 +623,7 @@ __global__ void k_set_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
 template <class T>
 __global__ void __launch_bounds__(BS) k_dot(int n, const T* __restrict__ x, const T* __restrict__ y, Scalars* sc,
                                             double* part, int slot, int post = POST_NONE) {
+  pdl_entry();
   Acc<T> acc;
   ROW_LOOP(n) {
     int row[ILP];
@@ -631,6 +652,7 @@ __global__ void __launch_bounds__(BS) k_sub_mean(int n, double* __restrict__ x, 
 template <class T>
 __global__ void __launch_bounds__(BS) k_mul(int n, const T* __restrict__ s, const T* __restrict__ r,
                                             T* __restrict__ out) {
+  pdl_entry();
   ROW_LOOP(n) {
     int row[ILP];
     rows_of(rb, row);
@@ -642,6 +664,7 @@ __global__ void __launch_bounds__(BS) k_mul(int n, const T* __restrict__ s, cons
 
 // PCG start: tol2 = tol^2 * red[R_BB]; counters reset
 __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
+  pdl_entry();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     sc->tol2 = tol * tol * sc->red[R_BB];
     sc->it = 0;
@@ -661,6 +684,7 @@ __global__ void k_pcg_init_scalars(Scalars* sc, double tol, int maxiter) {
 // r = b - A x in FP64; r.r -> red[R_R2]
 __global__ void __launch_bounds__(BS) k_resid64(Sell A, const double* __restrict__ x, const double* __restrict__ b,
                                                 double* __restrict__ r, Scalars* sc, double* part) {
+  pdl_entry();
   Acc<double> acc;
   ROW_LOOP(A.n) {
     int row[ILP];
@@ -682,6 +706,7 @@ __global__ void __launch_bounds__(BS) k_resid64(Sell A, const double* __restrict
 // r32 = r * scale (the inner system is solved for a unit-norm right-hand side); d32 = 0
 __global__ void __launch_bounds__(BS) k_to_f32(int n, const double* __restrict__ r, double scale,
                                                float* __restrict__ r32, float* __restrict__ d32) {
+  pdl_entry();
   ROW_LOOP(n) {
     int row[ILP];
     rows_of(rb, row);
@@ -697,6 +722,7 @@ __global__ void __launch_bounds__(BS) k_to_f32(int n, const double* __restrict__
 // x += scale * d32 in FP64
 __global__ void __launch_bounds__(BS) k_add_f32(int n, double* __restrict__ x, const float* __restrict__ d32,
                                                 double scale) {
+  pdl_entry();
   ROW_LOOP(n) {
     int row[ILP];
     rows_of(rb, row);
