@@ -242,6 +242,15 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * kernel is scheduled while its predecessor drains (every solver kernel waits for its predecessor's
  * results at entry); 0 launches them normally.  Same results either way. */
 #define MM_OPT_PDL 8
+/* MM_OPT_COARSE_FUSE (default 2): with 3 or more levels and at most 16384 rows on level L-2, the two
+ * coarsest levels of the V-cycle (level L-2's residual, restriction, the dense coarsest solve,
+ * prolongation and post-smoothing: five dependent kernels) run as two kernels applying the same
+ * linear map in factored form, x2 = T b + W (Z b) with T = 2S - S A S, W = (I - S A) P and
+ * Z = Ainv R (I - A S) (S the smoother diagonal; T sparse with A's pattern, W and Z dense, formed at
+ * mm_build_poisson).  0: the five kernels everywhere; 1: the fused form in the FP64 and the FP32
+ * solver; 2: fused in the FP64 solver only (measured on the 80 nm cube on GB300: FP64 solve 7 %
+ * faster, FP32 iteration unchanged).  Same V-cycle up to summation order. */
+#define MM_OPT_COARSE_FUSE 9
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* In-solve kernel profile (MM_OPT_PROFILE).  slot = (fp32 * MM_PROF_LEVELS + level) * MM_PROF_KINDS
@@ -256,7 +265,9 @@ int mm_set_option(mm_problem* h, int option, int value);
 #define MM_PROF_SMOOTH0 7       /* level-0 post-smoothing fused with r.z                          */
 #define MM_PROF_SMOOTH 8        /* post-smoothing on a coarse level                              */
 #define MM_PROF_INIT_RESIDUAL 9 /* r = b - A x at the start of a PCG solve                        */
-#define MM_PROF_KINDS 10
+#define MM_PROF_COARSE_A 10     /* fused coarse correction: t = T b and z = Z b (level L-2)        */
+#define MM_PROF_COARSE_B 11     /* fused coarse correction: x2 = t + W z (level L-2)               */
+#define MM_PROF_KINDS 12
 #define MM_PROF_LEVELS 16
 #define MM_PROF_SLOTS (2 * MM_PROF_LEVELS * MM_PROF_KINDS)
 /* Copy the per-slot totals since the last reset: launches, summed device time [ms] and the

@@ -19,7 +19,7 @@ METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2}
 KERNELS = {"spmv_A": 0, "smooth": 1, "energy": 2, "hessian": 3}
 # in-solve profile slots: slot = (fp32 * PROF_LEVELS + level) * len(PROF_KINDS) + kind
 PROF_KINDS = ("pcg_dir", "pcg_step", "vc_residual0", "residual", "restrict", "coarse", "prolong", "smooth0",
-              "smooth", "init_residual")
+              "smooth", "init_residual", "coarse_a", "coarse_b")
 PROF_LEVELS = 16
 PROF_SLOTS = 2 * PROF_LEVELS * len(PROF_KINDS)
 

@@ -105,6 +105,12 @@ struct SolverT {
   cudaGraphExec_t exec = nullptr;
   bool graph_failed = false;
   int64_t iter_launches = 0;          // kernels in one loop trip
+  // fused coarse correction of levels L-2 .. L-1 (x2 = T b + W (Z b)), when eligible
+  bool fused = false;
+  mmk::CsrT<T> Tm{};
+  T *W = nullptr, *Z = nullptr, *tvec = nullptr, *zvec = nullptr;
+  int fn = 0, fc = 0;
+  int64_t Tm_nnz = 0;
   // persistent PCG loop (one cooperative launch per solve)
   mmk::PLev<T>* d_plev = nullptr;     // level views on the device
   mmk::GridBar* d_bar = nullptr;      // barrier state, cleared before each launch
@@ -188,6 +194,7 @@ struct mm_problem {
   bool use_graph = true;
   bool persistent = false;       // MM_OPT_PERSISTENT
   bool pdl = true;               // MM_OPT_PDL
+  int coarse_fuse = 2;           // MM_OPT_COARSE_FUSE
   int persist_bpsm = 0;          // MM_OPT_PERSIST_BPSM (0 = default)
 
   // staging buffers for host-pointer calls
@@ -402,7 +409,9 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
   auto& lv = S.lv;
   const int L = (int)lv.size();
   const double w = sizeof(T);
-  for (int l = 0; l < L - 1; ++l) {
+  const bool fuse = S.fused && (h->coarse_fuse == 1 || (h->coarse_fuse == 2 && sizeof(T) == 8));
+  const int Ld = fuse ? L - 2 : L - 1;  // levels l < Ld compute a residual and restrict it
+  for (int l = 0; l < Ld; ++l) {
     auto& c = lv[l];
     if (l == 0 && in_loop) {
       tagged<T>(h, MM_PROF_VC_RESIDUAL0, 0, mat_bytes(c.A) + 3.0 * w * c.n, [&] {
@@ -414,28 +423,44 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
                 [&] { spmv<1, T>(h, c.A, c.x, l == 0 ? r : c.b, nullptr, c.res, done); });
     }
     auto& nx = lv[l + 1];
-    const bool coarsest = (l + 1 == L - 1);
-    const double rbytes = mat_bytes(c.R) + w * c.n + (coarsest ? 1.0 : 3.0) * w * nx.n;
+    // no pre-smoothing on the coarsest level, nor on level L-2 when its correction is fused
+    const bool no_pre = (l + 1 == L - 1) || (fuse && l + 1 == L - 2);
+    const double rbytes = mat_bytes(c.R) + w * c.n + (no_pre ? 1.0 : 3.0) * w * nx.n;
     tagged<T>(h, MM_PROF_RESTRICT, l, rbytes, [&] {
       if (c.R.tpr == 1) {
-        launch(h, mmk::k_restrict<T>, grid_ilp(nx.n), BS, c.R.s, c.res, nx.b, coarsest ? nullptr : nx.s, nx.x,
+        launch(h, mmk::k_restrict<T>, grid_ilp(nx.n), BS, c.R.s, c.res, nx.b, no_pre ? nullptr : nx.s, nx.x,
                                                                 done);
       } else {
         const int g = grid_rows(nx.n, c.R.tpr);
         TPR_SWITCH(c.R.tpr, (launch(h, mmk::k_restrict_csr<TP, T>, g, BS, c.R.c, c.res, nx.b,
-                                                                          coarsest ? nullptr : nx.s, nx.x, done)));
+                                                                          no_pre ? nullptr : nx.s, nx.x, done)));
       }
       LAUNCH_CHECK();
     });
   }
-  {
+  if (fuse) {
+    auto& c = lv[L - 2];
+    const int n = S.fn, nc = S.fc;
+    const double tbytes = (double)S.Tm.n + 1.0;
+    tagged<T>(h, MM_PROF_COARSE_A, L - 2,
+              4.0 * tbytes + (4.0 + w) * (double)S.Tm_nnz + w * ((double)nc * n + 2.0 * n + nc),
+              [&] {
+                const int gT = grid_rows(n, 32);
+                launch(h, mmk::k_coarse_a<T>, gT + nc, BS, S.Tm, S.Z, nc, c.b, S.tvec, S.zvec, gT, done);
+                LAUNCH_CHECK();
+              });
+    tagged<T>(h, MM_PROF_COARSE_B, L - 2, w * ((double)n * nc + 2.0 * n + nc), [&] {
+      launch(h, mmk::k_coarse_b<T>, grid_rows(n, 32), BS, n, nc, S.W, S.tvec, S.zvec, c.x2, done);
+      LAUNCH_CHECK();
+    });
+  } else {
     auto& c = lv[L - 1];
     tagged<T>(h, MM_PROF_COARSE, L - 1, w * ((double)c.n * c.n + 2.0 * c.n), [&] {
       launch(h, mmk::k_dense_mv<T>, grid_rows(c.n, 32), BS, c.n, S.Ainv, c.b, c.x2, done);
       LAUNCH_CHECK();
     });
   }
-  for (int l = L - 2; l >= 0; --l) {
+  for (int l = (fuse ? L - 3 : L - 2); l >= 0; --l) {
     auto& c = lv[l];
     tagged<T>(h, MM_PROF_PROLONG, l, mat_bytes(c.P) + w * lv[l + 1].n + 2.0 * w * c.n,
               [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
@@ -683,6 +708,15 @@ void launch_persistent(mm_problem* h, SolverT<T>& S) {
   CK(cudaLaunchCooperativeKernel(S.pkern, dim3(S.pgrid), dim3(BS), args, 0, h->st));
   ++h->n_launch;
   CK(cudaMemcpyAsync(S.h_bar, S.d_bar, sizeof(mmk::GridBar), cudaMemcpyDeviceToHost, h->st));
+}
+
+template <class T>
+void drop_graph(SolverT<T>& S) {
+  if (S.exec) cudaGraphExecDestroy(S.exec);
+  if (S.graph) cudaGraphDestroy(S.graph);
+  S.exec = nullptr;
+  S.graph = nullptr;
+  S.graph_failed = false;
 }
 
 // PCG on S.x (initial guess in, solution out) for the right-hand side S.b; stops on the recursive
@@ -1400,6 +1434,67 @@ extern "C" int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const do
   });
 }
 
+// Factored form of the V-cycle's two coarsest levels, formed in FP64 on the host.  With S the smoother
+// diagonal, A, P, R the operators of level L-2 and Ainv the dense inverse of level L-1, the levels
+// L-2 .. L-1 map the restricted residual b to the post-smoothed iterate
+//   x2 = (I - S A) (S + P Ainv R (I - A S)) b + S b = T b + W (Z b),
+//   T = 2S - S A S (A's pattern), W = (I - S A) P (n x nc), Z = Ainv R (I - A S) (nc x n).
+template <class T>
+void build_fused_coarse(mm_problem* h, SolverT<T>& S, int precond_type) {
+  const int L = (int)h->amg_h.size();
+  const mm::AmgLevel& a = h->amg_h[L - 2];
+  const mm::HostCSR &A = a.A, &P = a.P, &R = a.R;
+  const int n = A.n_rows, nc = h->amg_h[L - 1].A.n_rows;
+  std::vector<double> sd(n);
+  for (int i = 0; i < n; ++i) sd[i] = precond_type == MM_PRECOND_AMGCL ? a.spai0[i] : 0.6667 / (a.diag[i] + 1e-30);
+  std::vector<double> tv(A.nnz());
+  for (int i = 0; i < n; ++i) {
+    bool diag = false;
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+      const int j = A.col[k];
+      tv[k] = -sd[i] * A.val[k] * sd[j] + (j == i ? 2.0 * sd[i] : 0.0);
+      diag = diag || j == i;
+    }
+    if (!diag) return;  // a row without a stored diagonal: keep the five-kernel path
+  }
+  std::vector<double> Wd((size_t)n * nc, 0.0), AP((size_t)n * nc, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+      for (int q = P.ptr[A.col[k]]; q < P.ptr[A.col[k] + 1]; ++q) AP[(size_t)i * nc + P.col[q]] += A.val[k] * P.val[q];
+  for (int i = 0; i < n; ++i) {
+    for (int q = P.ptr[i]; q < P.ptr[i + 1]; ++q) Wd[(size_t)i * nc + P.col[q]] += P.val[q];
+    for (int j = 0; j < nc; ++j) Wd[(size_t)i * nc + j] -= sd[i] * AP[(size_t)i * nc + j];
+  }
+  std::vector<double> M((size_t)nc * n, 0.0);  // R (I - A S)
+  for (int r = 0; r < nc; ++r)
+    for (int k = R.ptr[r]; k < R.ptr[r + 1]; ++k) {
+      M[(size_t)r * n + R.col[k]] += R.val[k];
+      const int row = R.col[k];
+      for (int q = A.ptr[row]; q < A.ptr[row + 1]; ++q) M[(size_t)r * n + A.col[q]] -= R.val[k] * A.val[q] * sd[A.col[q]];
+    }
+  const std::vector<double> Ainv = mm::dense_inverse(h->amg_h[L - 1].A);
+  std::vector<double> Zd((size_t)nc * n, 0.0);
+  for (int r = 0; r < nc; ++r)
+    for (int q = 0; q < nc; ++q) {
+      const double c = Ainv[(size_t)r * nc + q];
+      const double* mq = &M[(size_t)q * n];
+      double* zr = &Zd[(size_t)r * n];
+      for (int j = 0; j < n; ++j) zr[j] += c * mq[j];
+    }
+  S.Tm.n = n;
+  S.Tm.ptr = h->upload(A.ptr);
+  S.Tm.col = h->upload(A.col);
+  S.Tm.val = h->upload_as<T>(tv);
+  S.Tm_nnz = A.nnz();
+  S.W = h->upload_as<T>(Wd);
+  S.Z = h->upload_as<T>(Zd);
+  S.tvec = h->alloc<T>(n);
+  S.zvec = h->alloc<T>(nc);
+  S.fn = n;
+  S.fc = nc;
+  S.fused = true;
+}
+
 // Upload the hierarchy in precision T and allocate the solver's vectors.
 template <class T>
 void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, int precond_type) {
@@ -1441,6 +1536,7 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
   S.z = h->alloc<T>(h->N);
   S.p = h->alloc<T>(h->N);
   S.Ap = h->alloc<T>(h->N);
+  if (amg && L >= 3 && h->amg_h[L - 2].A.n_rows <= 16384) build_fused_coarse<T>(h, S, precond_type);
   S.built = true;
 }
 
@@ -2025,21 +2121,20 @@ int mm_set_option(mm_problem* h, int option, int value) {
   }
   if (option == MM_OPT_PDL) {
     if (value != 0 && value != 1) return MM_ERR_ARG;
-    if (h->pdl != (value == 1)) {  // captured loop graphs hold the old launch attribute
-      for (SolverT<double>* S : {&h->s64}) {
-        if (S->exec) cudaGraphExecDestroy(S->exec);
-        if (S->graph) cudaGraphDestroy(S->graph);
-        S->exec = nullptr;
-        S->graph = nullptr;
-        S->graph_failed = false;
-      }
-      if (h->s32.exec) cudaGraphExecDestroy(h->s32.exec);
-      if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
-      h->s32.exec = nullptr;
-      h->s32.graph = nullptr;
-      h->s32.graph_failed = false;
+    if (h->pdl != (value == 1)) {  // captured loop graphs hold the old launches
+      drop_graph(h->s64);
+      drop_graph(h->s32);
     }
     h->pdl = value == 1;
+    return MM_OK;
+  }
+  if (option == MM_OPT_COARSE_FUSE) {
+    if (value < 0 || value > 2) return MM_ERR_ARG;
+    if (h->coarse_fuse != value) {
+      drop_graph(h->s64);
+      drop_graph(h->s32);
+    }
+    h->coarse_fuse = value;
     return MM_OK;
   }
   if (option == MM_OPT_PERSISTENT) {

@@ -580,6 +580,57 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ai
   }
 }
 
+// Fused coarse correction, first phase.  Blocks [0, gT) compute t = T b, one warp per row of T
+// (compressed rows of T = 2S - S A S on level L-2); each block gT + r computes z_r = (Z b)_r for one
+// row of the dense nc x n matrix Z = Ainv R (I - A S) with all its threads (fixed-order block sum).
+// Both read only b, the restricted residual of level L-2.
+template <class T>
+__global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict__ Z, int nc, const T* __restrict__ b,
+                                                 T* __restrict__ t, T* __restrict__ z, int gT,
+                                                 const int* __restrict__ done) {
+  pdl_entry();
+  if (done && *done) return;
+  const int n = Tm.n;
+  if ((int)blockIdx.x < gT) {
+    const int lane = threadIdx.x & 31;
+    for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
+      T acc = T(0);
+      const int e = __ldg(Tm.ptr + row + 1);
+      for (int k = __ldg(Tm.ptr + row) + lane; k < e; k += 32) acc = fmaT<T>(__ldg(Tm.val + k), __ldg(b + __ldg(Tm.col + k)), acc);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) t[row] = acc;
+    }
+  } else {
+    const int r = (int)blockIdx.x - gT;
+    const T* zr = Z + (size_t)r * n;
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < n; k += BS) acc = fma((double)__ldg(zr + k), (double)__ldg(b + k), acc);
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) z[r] = (T)acc;
+  }
+}
+
+// Fused coarse correction, second phase: x2 = t + W z (W dense n x nc, row-major, W = (I - S A) P),
+// one warp per row.  x2 is level L-2's post-smoothed iterate, exactly as the V-cycle's levels
+// L-2 .. L-1 would leave it (same linear map, summed in a different order).
+template <class T>
+__global__ void __launch_bounds__(BS) k_coarse_b(int n, int nc, const T* __restrict__ W, const T* __restrict__ t,
+                                                 const T* __restrict__ z, T* __restrict__ x2,
+                                                 const int* __restrict__ done) {
+  pdl_entry();
+  if (done && *done) return;
+  const int lane = threadIdx.x & 31;
+  for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gridDim.x * (BS / 32)) {
+    const T* wr = W + (size_t)row * nc;
+    T acc = T(0);
+    for (int k = lane; k < nc; k += 32) acc = fmaT<T>(__ldg(wr + k), __ldg(z + k), acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x2[row] = __ldg(t + row) + acc;
+  }
+}
+
 // post-smoothing y = x + s .* (b - A x); with `part` it also reduces b.y into red[R_RZ]
 // (level 0: b = r and y = z)
 template <class T>
