@@ -242,7 +242,9 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * kernel is scheduled while its predecessor drains (every solver kernel waits for its predecessor's
  * results at entry); 0 launches them normally.  Same results either way. */
 #define MM_OPT_PDL 8
-/* MM_OPT_COARSE_FUSE (default 2): with 3 or more levels and at most 16384 rows on level L-2, the two
+/* MM_OPT_COARSE_FUSE (default 2): with 3 or more levels, at most 256 rows on the coarsest level and
+ * at most 4Mi entries in the n(L-2) x n(L-1) dense factors (so that they cost little memory and host
+ * setup time), the two
  * coarsest levels of the V-cycle (level L-2's residual, restriction, the dense coarsest solve,
  * prolongation and post-smoothing: five dependent kernels) run as two kernels applying the same
  * linear map in factored form, x2 = T b + W (Z b) with T = 2S - S A S, W = (I - S A) P and

@@ -1536,7 +1536,11 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
   S.z = h->alloc<T>(h->N);
   S.p = h->alloc<T>(h->N);
   S.Ap = h->alloc<T>(h->N);
-  if (amg && L >= 3 && h->amg_h[L - 2].A.n_rows <= 16384) build_fused_coarse<T>(h, S, precond_type);
+  if (amg && L >= 3) {
+    // only where the dense factors stay small: Z = Ainv M costs nc^2 n host FLOPs, W and Z hold n nc each
+    const double n = h->amg_h[L - 2].A.n_rows, nc = h->amg_h[L - 1].A.n_rows;
+    if (nc <= 256 && n * nc <= 4194304.0) build_fused_coarse<T>(h, S, precond_type);
+  }
   S.built = true;
 }
 

@@ -167,3 +167,58 @@ def tilted_field_direction(tilt_deg: float = 1.0) -> np.ndarray:
     """Unit field direction tilted ``tilt_deg`` from +z in the x-z plane."""
     t = math.radians(tilt_deg)
     return np.array([math.sin(t), 0.0, math.cos(t)], dtype=np.float64)
+
+
+# ------------------------------------------------------------------------------------------------
+# batched particles: voxelised ellipsoids, each in its own graded air box
+# ------------------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Particle:
+    """One tri-axial ellipsoid (semi-axes in nm) and its material."""
+
+    a: float
+    b: float
+    c: float
+    material: Material
+
+
+def random_particles(n: int, seed: int = 0, semi=(5.0, 25.0)) -> list[Particle]:
+    """Semi-axes U(5, 25) nm; easy axis uniform on the sphere; K1 U(1, 5) MJ/m^3; Js U(1.0, 1.6) T;
+    A U(5, 12) pJ/m; from numpy.random.default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a, b, c = rng.uniform(semi[0], semi[1], size=3)
+        v = rng.standard_normal(3)
+        v /= np.linalg.norm(v)
+        mat = Material(Js=float(rng.uniform(1.0, 1.6)), A=float(rng.uniform(5e-12, 12e-12)),
+                       K1=float(rng.uniform(1e6, 5e6)), axis=tuple(float(x) for x in v))
+        out.append(Particle(float(a), float(b), float(c), mat))
+    return out
+
+
+def _graded_cells(L: float, h: float, r: float, box: float) -> int:
+    """Air cells per side so that cells growing by r from h reach the box face."""
+    total = 0.5 * (box - L)
+    return max(1, int(math.ceil(math.log(1.0 + total * (r - 1.0) / (h * r)) / math.log(r))))
+
+
+def ellipsoid_mesh(p: Particle, h: float = 1.5, r: float = 1.2, box_factor: float = 5.0):
+    """(knt, ijk): hexahedra of edge h whose centre lies inside the ellipsoid are the magnet (group 1);
+    the rest of the uniform core and a graded shell (ratio r) up to a cube of edge box_factor * the
+    largest semi-axis are air (group 2).  Every hexahedron is split into six tetrahedra."""
+    box = box_factor * max(p.a, p.b, p.c)
+    axes, ranges = [], []
+    for s in (p.a, p.b, p.c):
+        nc = int(math.ceil(2.0 * s / h))
+        L = nc * h
+        xs, c0, c1 = graded_axis(L, h, r, _graded_cells(L, h, r, box), box)
+        axes.append(xs)
+        ranges.append((c0, c1))
+    xs, ys, zs = axes
+    knt, tets = kuhn_box_mesh(xs, ys, zs)
+    cx, cy, cz = 0.5 * (xs[1:] + xs[:-1]), 0.5 * (ys[1:] + ys[:-1]), 0.5 * (zs[1:] + zs[:-1])
+    Z, Y, X = np.meshgrid(cz, cy, cx, indexing="ij")
+    inside = (X / p.a) ** 2 + (Y / p.b) ** 2 + (Z / p.c) ** 2 <= 1.0
+    mat = np.repeat(np.where(inside.ravel(), 1, 2).astype(np.int32), 6)
+    return knt, np.column_stack([tets, mat]).astype(np.int32)

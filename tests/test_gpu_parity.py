@@ -217,7 +217,12 @@ def test_persistent_loop_matches_graph_loop(cuda_ok, precision):
 def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, precision):
     """The two coarsest levels applied as x2 = T b + W (Z b) against the five level-by-level kernels:
     the same V-cycle (to rounding) and the same solve."""
-    s, p, _ = case("cube40_h2_air200")
+    from mumag_matrixfree2_gb300 import synthetic as syn
+
+    part = syn.random_particles(8, seed=0)[3]  # 110,032 nodes, a 4-level hierarchy (58 coarsest rows)
+    knt, ijk = syn.ellipsoid_mesh(part)
+    A, K1, Js, k, _ = syn.reduced_materials([part.material, syn.AIR])
+    s = fem_utils.prepare(knt, ijk, A, K1, Js, k)
     probs = []
     for fuse in (0, 1):
         prob = fem_utils.make_problem(s)
@@ -225,11 +230,12 @@ def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, prec
         prob.build_poisson(1e-12, "amgcl")
         prob.set_option("coarse_fuse", fuse)
         probs.append(prob)
-    r = np.random.default_rng(41).standard_normal(p.N)
+    assert probs[1].n_levels == 4
+    r = np.random.default_rng(41).standard_normal(s.N)
     z0, z1 = probs[0].precond(r), probs[1].precond(r)
-    assert rel(z1, z0) <= 1e-11
-    m = random_state(p.N, seed=42, amplitude=0.05)
-    U0, it0, rr0, rc0 = probs[0].solve_u(m, np.zeros(p.N), 1e-10)
-    U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(p.N), 1e-10)
+    assert rel(z1, z0) <= (1e-11 if precision == "fp64" else 1e-5)
+    m = random_state(s.N, seed=42, amplitude=0.05)
+    U0, it0, rr0, rc0 = probs[0].solve_u(m, np.zeros(s.N), 1e-10)
+    U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
     assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1
     assert rel(U1, U0) <= 1e-8
