@@ -242,18 +242,26 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * kernel is scheduled while its predecessor drains (every solver kernel waits for its predecessor's
  * results at entry); 0 launches them normally.  Same results either way. */
 #define MM_OPT_PDL 8
-/* MM_OPT_COARSE_FUSE (default 2): with 3 or more levels, at most 256 rows on the coarsest level and
- * at most 4Mi entries in the n(L-2) x n(L-1) dense factors (so that they cost little memory and host
- * setup time), the two
- * coarsest levels of the V-cycle (level L-2's residual, restriction, the dense coarsest solve,
- * prolongation and post-smoothing: five dependent kernels) run as two kernels applying the same
- * linear map in factored form, x2 = T b + W (Z b) with T = 2S - S A S, W = (I - S A) P and
- * Z = Ainv R (I - A S) (S the smoother diagonal; T sparse with A's pattern, W and Z dense, formed at
- * mm_build_poisson).  0: the five kernels everywhere; 1: the fused form in the FP64 and the FP32
- * solver; 2: fused in the FP64 solver only (measured on the 80 nm cube on GB300: FP64 solve 7 %
- * faster, FP32 iteration unchanged).  Same V-cycle up to summation order. */
+/* MM_OPT_COARSE_FUSE (bit mask, default 1): with 3 or more levels, at most 256 rows on the coarsest
+ * level and at most 4Mi entries in the n(L-2) x n(L-1) dense factors (so that they cost little memory
+ * and host setup time), the two coarsest levels of the V-cycle (level L-2's residual, restriction,
+ * the dense coarsest solve, prolongation and post-smoothing: five dependent kernels) run as two
+ * kernels applying the same linear map in factored form, x2 = T b + W (Z b) with T = 2S - S A S,
+ * W = (I - S A) P and Z = Ainv R (I - A S) (S the smoother diagonal; T sparse with A's pattern, W and Z
+ * dense, formed at mm_build_poisson).  Bit 0: in the FP64 solver, bit 1: in the FP32 solver of the
+ * mixed method.  Same V-cycle up to summation order.  (80 nm cube on GB300: the FP64 solve 7 % faster,
+ * the FP32 iteration unchanged; mm_autotune measures it per problem.) */
 #define MM_OPT_COARSE_FUSE 9
 int mm_set_option(mm_problem* h, int option, int value);
+
+/* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,
+ * restrictions, prolongations; both precisions) tries 2, 4, 8, 16 and 32 lanes per row, each timed as
+ * whole V-cycles so that cache state and neighbouring kernels are those of a solve, and keeps the
+ * fastest; then times the V-cycle with and without the fused coarse correction in each solver and
+ * sets MM_OPT_COARSE_FUSE accordingly.  CUDA events on the problem's stream, `reps`
+ * launches per candidate.  A JSON report (candidates, times in microseconds, choices) is written to
+ * `report` (may be NULL; truncated to report_len - 1 characters).  No counterpart in the reference. */
+int mm_autotune(mm_problem* h, int reps, char* report, int report_len);
 
 /* In-solve kernel profile (MM_OPT_PROFILE).  slot = (fp32 * MM_PROF_LEVELS + level) * MM_PROF_KINDS
  * + kind.  No reference counterpart: measurement of this backend's own kernels. */

@@ -85,6 +85,7 @@ SIGNATURES = {
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "mm_autotune": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
     "mm_profile_read": (C.c_int, [_vp, _lp, _dp, _dp]),
     "mm_profile_reset": (C.c_int, [_vp]),
     "mm_last_refinements": (C.c_int, [_vp, _ip]),

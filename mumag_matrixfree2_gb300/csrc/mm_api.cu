@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <stdexcept>
 #include <mutex>
 #include <string>
@@ -194,7 +195,7 @@ struct mm_problem {
   bool use_graph = true;
   bool persistent = false;       // MM_OPT_PERSISTENT
   bool pdl = true;               // MM_OPT_PDL
-  int coarse_fuse = 2;           // MM_OPT_COARSE_FUSE
+  int coarse_fuse = 1;           // MM_OPT_COARSE_FUSE: bit 0 the FP64 solver, bit 1 the FP32 solver
   int persist_bpsm = 0;          // MM_OPT_PERSIST_BPSM (0 = default)
 
   // staging buffers for host-pointer calls
@@ -409,7 +410,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
   auto& lv = S.lv;
   const int L = (int)lv.size();
   const double w = sizeof(T);
-  const bool fuse = S.fused && (h->coarse_fuse == 1 || (h->coarse_fuse == 2 && sizeof(T) == 8));
+  const bool fuse = S.fused && ((h->coarse_fuse >> (sizeof(T) == 8 ? 0 : 1)) & 1);
   const int Ld = fuse ? L - 2 : L - 1;  // levels l < Ld compute a residual and restrict it
   for (int l = 0; l < Ld; ++l) {
     auto& c = lv[l];
@@ -2101,6 +2102,115 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
   });
 }
 
+// ---------------------------------------------------------------------------------------------
+// autotuner: lanes per row of every compressed-row operator, and which solvers use the fused coarse
+// correction, chosen by timing on this GPU (CUDA events on the problem's stream)
+// ---------------------------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+template <class T>
+float time_ms(mm_problem* h, int reps, const std::function<void()>& f) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  f();  // warm-up
+  CK(cudaEventRecord(a, h->st));
+  for (int i = 0; i < reps; ++i) f();
+  CK(cudaEventRecord(b, h->st));
+  CK(cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+// Lanes per row of one compressed-row operator: every candidate is timed in context, as the time of
+// whole V-cycles (back to back, so cache state and neighbouring kernels are those of a solve; an
+// operator timed alone, L2-hot, prefers fewer lanes than it should), and the fastest is kept.
+template <class T>
+void tune_csr(mm_problem* h, SolverT<T>& S, DevMatT<T>& M, int reps, const char* tag, int level, std::string& rep) {
+  if (M.tpr == 1 || M.c.n == 0) return;
+  const int before = M.tpr;
+  int best = before;
+  float best_ms = 1e30f;
+  std::string times;
+  for (int t : {2, 4, 8, 16, 32}) {
+    M.tpr = t;
+    const float ms = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+    times += (times.empty() ? "" : ",") + std::to_string(1e3 * ms);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = t;
+    }
+  }
+  M.tpr = best;
+  rep += std::string(rep.size() > 1 ? "," : "") + "{\"op\":\"" + tag + "\",\"level\":" + std::to_string(level) +
+         ",\"precision\":\"" + (sizeof(T) == 8 ? "fp64" : "fp32") + "\",\"rows\":" + std::to_string(M.c.n) +
+         ",\"nnz\":" + std::to_string(M.nnz) + ",\"heuristic_tpr\":" + std::to_string(before) +
+         ",\"tpr\":" + std::to_string(best) + ",\"vcycle_us\":[" + times + "]}";
+}
+
+template <class T>
+void tune_solver(mm_problem* h, SolverT<T>& S, int reps, std::string& rep) {
+  if (!S.built || !multilevel(h, S)) return;
+  const int L = (int)S.lv.size();
+  for (int l = 0; l < L; ++l) {
+    auto& c = S.lv[l];
+    if (l > 0) tune_csr<T>(h, S, c.A, reps, "A", l, rep);
+    if (l < L - 1) {
+      tune_csr<T>(h, S, c.R, reps, "R", l, rep);
+      tune_csr<T>(h, S, c.P, reps, "P", l, rep);
+    }
+  }
+  drop_graph(S);
+}
+
+// V-cycle time with and without the fused coarse correction in solver S; sets the bit if it wins
+template <class T>
+std::string tune_fuse(mm_problem* h, SolverT<T>& S, int bit, int reps) {
+  if (!S.built || !S.fused || !multilevel(h, S)) return "null";
+  T* r = S.r;
+  T* z = S.z;
+  const int saved = h->coarse_fuse;
+  float ms[2];
+  for (int on = 0; on < 2; ++on) {
+    h->coarse_fuse = on ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+    ms[on] = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, r, z); });
+  }
+  h->coarse_fuse = ms[1] < ms[0] ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+  drop_graph(S);
+  return "{\"unfused_us\":" + std::to_string(1e3 * ms[0]) + ",\"fused_us\":" + std::to_string(1e3 * ms[1]) + "}";
+}
+
+}  // namespace
+
+extern "C" {
+
+int mm_autotune(mm_problem* h, int reps, char* report, int report_len) {
+  if (!h || reps < 1) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    std::string ops = "[";
+    tune_solver<double>(h, h->s64, reps, ops);
+    tune_solver<float>(h, h->s32, reps, ops);
+    ops += "]";
+    const std::string f64 = tune_fuse<double>(h, h->s64, 0, reps);
+    const std::string f32 = tune_fuse<float>(h, h->s32, 1, reps);
+    const std::string rep = "{\"operators\":" + ops + ",\"coarse_fuse\":{\"fp64\":" + f64 + ",\"fp32\":" + f32 +
+                            ",\"chosen\":" + std::to_string(h->coarse_fuse) + "}}";
+    h->sync();
+    if (report && report_len > 0) {
+      const size_t n = std::min(rep.size(), (size_t)report_len - 1);
+      std::memcpy(report, rep.data(), n);
+      report[n] = 0;
+    }
+    return MM_OK;
+  });
+}
+
 int mm_set_option(mm_problem* h, int option, int value) {
   if (!h) return MM_ERR_ARG;
   if (option == MM_OPT_GRAPH) {
@@ -2133,7 +2243,7 @@ int mm_set_option(mm_problem* h, int option, int value) {
     return MM_OK;
   }
   if (option == MM_OPT_COARSE_FUSE) {
-    if (value < 0 || value > 2) return MM_ERR_ARG;
+    if (value < 0 || value > 3) return MM_ERR_ARG;
     if (h->coarse_fuse != value) {
       drop_graph(h->s64);
       drop_graph(h->s32);

@@ -231,6 +231,15 @@ class Problem:
                 "coarse_fuse": 9}
         self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
 
+    def autotune(self, reps: int = 20) -> dict:
+        """Time the launch shapes of the hierarchy's operators and the fused coarse correction on this
+        GPU and keep the fastest (mm_autotune); returns the report."""
+        import json
+
+        buf = C.create_string_buffer(1 << 16)
+        self._check("mm_autotune", lib().mm_autotune(self.h, int(reps), buf, len(buf)))
+        return json.loads(buf.value.decode())
+
     def set_precision(self, precision: str):
         """"fp64" (the reference's plain method) or "mixed"; call before build_poisson()."""
         self.set_option("precision", {"fp64": 0, "mixed": 1}[precision])

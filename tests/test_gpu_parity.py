@@ -224,7 +224,7 @@ def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, prec
     A, K1, Js, k, _ = syn.reduced_materials([part.material, syn.AIR])
     s = fem_utils.prepare(knt, ijk, A, K1, Js, k)
     probs = []
-    for fuse in (0, 1):
+    for fuse in (0, 3):
         prob = fem_utils.make_problem(s)
         prob.set_precision(precision)
         prob.build_poisson(1e-12, "amgcl")
@@ -239,3 +239,19 @@ def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, prec
     U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
     assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1
     assert rel(U1, U0) <= 1e-8
+
+
+def test_autotuner_keeps_results_within_tolerance(cuda_ok):
+    """The autotuner changes launch shapes and the coarse path only: the solve converges to the same
+    potential with the same iterations (+-1), and the report covers every compressed-row operator."""
+    s, p, _ = case("cube40_h2_air200")
+    prob = fem_utils.make_problem(s)
+    prob.set_precision("mixed")
+    prob.build_poisson(1e-12, "amgcl")
+    m = random_state(p.N, seed=51, amplitude=0.05)
+    U0, it0, rr0, _ = prob.solve_u(m, np.zeros(p.N), 1e-10)
+    rep = prob.autotune(reps=5)
+    assert rep["operators"] and all(o["tpr"] in (2, 4, 8, 16, 32) for o in rep["operators"])
+    assert {o["precision"] for o in rep["operators"]} == {"fp64", "fp32"}
+    U1, it1, rr1, rc1 = prob.solve_u(m, np.zeros(p.N), 1e-10)
+    assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1 and rel(U1, U0) <= 1e-8
