@@ -422,3 +422,35 @@ def collect_sweep(prob, ws: WarmStart, m0, h_dir, B_values, params, keep_nodal: 
             nodal.append((mt, Ut))
         info_all.append(info)
     return states, nodal, info_all
+
+
+def time_forward(grid: int = 64, batch: int = 4, reps: int = 10, warmup: int = 3) -> dict:
+    """Forward passes of a freshly initialised network on random input, timed with CUDA events."""
+    import torch
+
+    net = UNet(grid, batch)
+    x = torch.randn(batch, grid ** 3, 4, device="cuda")
+    for _ in range(warmup):
+        net.forward_dev(x, None, batch)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        net.forward_dev(None, None, batch)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flop = batch * sum(2.0 * 27 * ci * co * (grid >> lvl) ** 3 for _, lvl, ci, co, _ in LAYERS)
+    return {"grid": grid, "batch": batch, "ms": ms, "flop": flop, "tflops": flop / (ms * 1e-3) / 1e12}
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="time the warm-start network's forward pass on cuda:0")
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--reps", type=int, default=10)
+    args = ap.parse_args()
+    print(json.dumps(time_forward(args.grid, args.batch, args.reps)))
