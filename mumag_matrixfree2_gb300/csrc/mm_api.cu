@@ -249,17 +249,17 @@ struct mm_problem {
     for (int s = 0; s < ns; ++s) {
       int w = 0;
       for (int r = 32 * s; r < std::min(n, 32 * s + 32); ++r) w = std::max(w, A.ptr[r + 1] - A.ptr[r]);
-      sptr[s + 1] = sptr[s] + 32 * w;
+      sptr[s + 1] = sptr[s] + 64 * ((w + 1) / 2);  // paired entries (mmk::SellT)
     }
     std::vector<int> col(sptr[ns]);
     std::vector<double> val(sptr[ns], 0.0);
     for (int s = 0; s < ns; ++s) {
-      const int w = (sptr[s + 1] - sptr[s]) / 32;
+      const int w2 = (sptr[s + 1] - sptr[s]) / 32;  // stored entries per row (even)
       for (int l = 0; l < 32; ++l) {
         const int r = 32 * s + l;
         const int len = r < n ? A.ptr[r + 1] - A.ptr[r] : 0;
-        for (int k = 0; k < w; ++k) {
-          const size_t at = (size_t)sptr[s] + 32 * k + l;
+        for (int k = 0; k < w2; ++k) {
+          const size_t at = (size_t)sptr[s] + 64 * (k / 2) + 2 * l + (k % 2);
           if (k < len) {
             col[at] = A.col[A.ptr[r] + k];
             val[at] = A.val[A.ptr[r] + k];

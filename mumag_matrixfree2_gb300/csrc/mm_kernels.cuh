@@ -241,7 +241,11 @@ __device__ __forceinline__ double block_total(Acc<T>& acc) {
   return s_out;
 }
 
-// sliced ELL (slice height 32): entry k of row r lives at sptr[r/32] + 32 k + r%32
+// Sliced ELL, slice height 32, entries paired: entry k of row r lives at
+// sptr[r/32] + 64 (k/2) + 2 (r%32) + k%2, so a thread loads the columns and values of two consecutive
+// entries of its row with one 8-byte (columns, FP32 values) or 16-byte (FP64 values) load, and a warp's
+// loads of one pair step are contiguous.  A slice of width w stores 2 ceil(w/2) entries per row; the
+// padding holds value 0 and a valid column.
 template <class T>
 struct SellT {
   int n;
@@ -252,16 +256,28 @@ struct SellT {
 using Sell = SellT<double>;
 
 template <class T>
+struct Pair;
+template <>
+struct Pair<double> {
+  using type = double2;
+};
+template <>
+struct Pair<float> {
+  using type = float2;
+};
+
+template <class T>
 __device__ __forceinline__ T sell_row(const SellT<T>& A, const T* __restrict__ x, int row) {
   const int s = row >> 5;
   const int b0 = __ldg(A.sptr + s);
-  const int w = (__ldg(A.sptr + s + 1) - b0) >> 5;
-  const int base = b0 + (row & 31);
+  const int wp = (__ldg(A.sptr + s + 1) - b0) >> 6;
+  const int base = b0 + 2 * (row & 31);
   T acc = T(0);
-#pragma unroll 4
-  for (int k = 0; k < w; ++k) {
-    const int c = __ldg(A.col + base + 32 * k);
-    acc = fmaT<T>(__ldg(A.val + base + 32 * k), __ldg(x + c), acc);
+  for (int j = 0; j < wp; ++j) {
+    const int2 c = __ldg(reinterpret_cast<const int2*>(A.col + base + 64 * j));
+    const typename Pair<T>::type v = __ldg(reinterpret_cast<const typename Pair<T>::type*>(A.val + base + 64 * j));
+    acc = fmaT<T>(v.x, __ldg(x + c.x), acc);
+    acc = fmaT<T>(v.y, __ldg(x + c.y), acc);
   }
   return acc;
 }
@@ -271,10 +287,9 @@ __device__ __forceinline__ T sell_row(const SellT<T>& A, const T* __restrict__ x
 // one full wave plus a short second one.
 constexpr int ILP = 2;
 
-// Non-zeros of one row loaded together: the column and value loads of KU consecutive entries (of
-// every row a thread holds) are issued before their gathers.  The sum runs over the entries in
-// stored order, one FMA each, so the result does not depend on KU.  A warp's rows share one slice,
-// so the width is warp-uniform.  Measured on the 80 nm cube (GB300): KU = 4 made the PCG iteration
+// Non-zeros per lane loaded together in the compressed-row kernels: the column and value loads of KU
+// entries are issued before their gathers; the sum runs over the entries in stored order, so the
+// result does not depend on KU.  Measured on the 80 nm cube (GB300): KU = 4 made the PCG iteration
 // ~15 % slower than KU = 1 (more registers, fewer resident warps), so 1 is kept.
 constexpr int KU = 1;
 
@@ -286,47 +301,42 @@ __device__ __forceinline__ T ldx(const T* x, int c) {
   else return __ldg(x + c);
 }
 
-template <int R, bool CG, class T, int KU = KU>
+template <int R, bool CG, class T>
 __device__ __forceinline__ void sell_rows_k(const int* __restrict__ sptr, const int* __restrict__ col,
                                             const T* __restrict__ val, int rlim, const T* x, const int (&row)[R],
                                             T (&acc)[R]) {
-  int base[R], w[R];
+  using P2 = typename Pair<T>::type;
+  int base[R], wp[R];
   int wmax = 0;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     acc[q] = T(0);
-    w[q] = 0;
+    wp[q] = 0;
     base[q] = 0;
     if (row[q] < rlim) {
       const int s = row[q] >> 5;
       const int b0 = __ldg(sptr + s);
-      w[q] = (__ldg(sptr + s + 1) - b0) >> 5;
-      base[q] = b0 + (row[q] & 31);
+      wp[q] = (__ldg(sptr + s + 1) - b0) >> 6;
+      base[q] = b0 + 2 * (row[q] & 31);
     }
-    wmax = max(wmax, w[q]);
+    wmax = max(wmax, wp[q]);
   }
-  for (int k = 0; k < wmax; k += KU) {
-    int c[R][KU];
-    T v[R][KU];
+  for (int j = 0; j < wmax; ++j) {
+    int2 c[R];
+    P2 v[R];
 #pragma unroll
     for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int u = 0; u < KU; ++u)
-        if (k + u < w[q]) {
-          c[q][u] = __ldg(col + base[q] + 32 * (k + u));
-          v[q][u] = __ldg(val + base[q] + 32 * (k + u));
-        }
-    T xv[R][KU];
+      if (j < wp[q]) {
+        c[q] = __ldg(reinterpret_cast<const int2*>(col + base[q] + 64 * j));
+        v[q] = __ldg(reinterpret_cast<const P2*>(val + base[q] + 64 * j));
+      }
 #pragma unroll
     for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int u = 0; u < KU; ++u)
-        if (k + u < w[q]) xv[q][u] = ldx<CG>(x, c[q][u]);
-#pragma unroll
-    for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int u = 0; u < KU; ++u)
-        if (k + u < w[q]) acc[q] = fmaT<T>(v[q][u], xv[q][u], acc[q]);
+      if (j < wp[q]) {
+        const T x0 = ldx<CG>(x, c[q].x), x1 = ldx<CG>(x, c[q].y);
+        acc[q] = fmaT<T>(v[q].x, x0, acc[q]);
+        acc[q] = fmaT<T>(v[q].y, x1, acc[q]);
+      }
   }
 }
 

@@ -158,7 +158,7 @@ __device__ __forceinline__ void mat_rows(const MatV<T>& M, const T* x, F&& f) {
       T acc[RPT];
 #pragma unroll
       for (int q = 0; q < RPT; ++q) row[q] = rb + threadIdx.x + q * BS;
-      sell_rows_k<RPT, true, T, KUP>(M.ptr, M.col, M.val, r1, x, row, acc);
+      sell_rows_k<RPT, true, T>(M.ptr, M.col, M.val, r1, x, row, acc);
 #pragma unroll
       for (int q = 0; q < RPT; ++q)
         if (row[q] < r1) f(row[q], acc[q]);
