@@ -38,6 +38,7 @@ extern "C" {
 #define MM_METHOD_PCOHEN_HS 0
 #define MM_METHOD_LBFGS 1
 #define MM_METHOD_WG_NP 2
+#define MM_METHOD_PLBFGS 3 /* preconditioned L-BFGS (src/minimizers.py:1526-1653) */
 
 typedef struct mm_problem mm_problem;
 
@@ -178,6 +179,12 @@ int mm_solve_u(mm_problem* h, const double* m, double* U_inout, double tol, int 
 int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U_inout, double tol, int maxiter,
                    int* iters, double* rel_res);
 
+/* Magnetoelastic anisotropy (src/energy_kernels.py:212-224,319-329,411-426): per element
+ * Kx_Ve = 2 (k1me + k1me_p) Ve / 20 and Ky_Ve = 2 (k1me - k1me_p) Ve / 20 (arrays of n <= n_elems
+ * entries, zero beyond; k1me_p may be NULL) add g_a,x += Kx_Ve (sum_b m_b,x + m_a,x) and likewise y
+ * to the energy gradient and to the local Hessian.  n = 0 removes the term. */
+int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double* k1me_p);
+
 /* Add the multiple of a correction that minimises the energy-norm error of an initial guess:
  * d_U += alpha d_c with alpha = c.(b - A U) / (c.A c), b = D m (never worse than U alone in the A-norm).
  * Used to apply a predicted potential change (the learned warm start) before a solve.  No counterpart
@@ -190,8 +197,8 @@ int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const
 int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec);
 
 /* Minimize the energy for one applied field, m_inout and U_inout updated in place.
- * Replaces make_minimizer(...).minimize (src/minimizers.py:2927-4098) for pcohen_hs, lbfgs and
- * wg_np, and run_cpp_pcohen_hs_minimization (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
+ * Replaces make_minimizer(...).minimize (src/minimizers.py:2927-4098) for pcohen_hs, lbfgs, wg_np
+ * and plbfgs, and run_cpp_pcohen_hs_minimization (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
 int mm_minimize(mm_problem* h, const double* B_ext, double* m_inout, double* U_inout,
                 const mm_min_params* prm, mm_min_info* info);
 

@@ -15,7 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libmumag_cuda.so"
 
 MM_OK, MM_MAXITER, MM_NONFINITE, MM_BREAKDOWN = 0, 1, 2, 3
 PRECOND = {"none": 0, "jacobi": 1, "amg": 2, "amgcl": 3}
-METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2}
+METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2, "plbfgs": 3}
 KERNELS = {"spmv_A": 0, "smooth": 1, "energy": 2, "hessian": 3}
 # in-solve profile slots: slot = (fp32 * PROF_LEVELS + level) * len(PROF_KINDS) + kind
 PROF_KINDS = ("pcg_dir", "pcg_step", "vc_residual0", "residual", "restrict", "coarse", "prolong", "smooth0",
@@ -82,6 +82,7 @@ SIGNATURES = {
     "mm_solve_u_dev": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _ip, _dp]),
     "mm_set_node_weights": (C.c_int, [_vp, _dp, _dp]),
     "mm_scale_correction_dev": (C.c_int, [_vp, _vp, _vp, _vp, _dp]),
+    "mm_set_magnetoelastic": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),

@@ -206,7 +206,7 @@ struct mm_problem {
   double *w_gt = nullptr, *w_gte = nullptr, *w_gprev = nullptr, *w_y = nullptr, *w_d = nullptr,
          *w_dprev = nullptr, *w_H = nullptr, *w_mt = nullptr, *w_Ut = nullptr, *w_gt_trial = nullptr,
          *w_graw = nullptr, *w_r3 = nullptr, *w_z3 = nullptr, *w_p3 = nullptr, *w_Ap3 = nullptr,
-         *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr;
+         *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr, *w_ys = nullptr;
   std::vector<double*> w_S, w_Y;
 
   template <class T>
@@ -916,7 +916,7 @@ void ensure_min_buffers(mm_problem* h, int memory) {
   if (!h->min_ready) {
     double** bufs[] = {&h->w_gt, &h->w_gte, &h->w_gprev, &h->w_y, &h->w_d, &h->w_dprev, &h->w_H, &h->w_mt,
                        &h->w_gt_trial, &h->w_graw, &h->w_r3, &h->w_z3, &h->w_p3, &h->w_Ap3, &h->w_tmp,
-                       &h->w_mprev, &h->w_gtprev};
+                       &h->w_mprev, &h->w_gtprev, &h->w_ys};
     for (double** b : bufs) {
       *b = h->alloc<double>(n3);
       CK(cudaMemsetAsync(*b, 0, n3 * sizeof(double), h->st));
@@ -960,7 +960,8 @@ int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
 }
 
 // Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations
-int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y) {
+int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
+               double reg) {
   mm_problem* h = c.h;
   const int N = c.N, n3 = 3 * N;
   const int ge = grid_elem(N);
@@ -976,7 +977,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   bool done = false;
   const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
   while (it < c.prm->pc_iters && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
-    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, c.prm->pc_reg,
+    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, reg,
                                                                      h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part, R_C)));
     LAUNCH_CHECK();
     const double pAp = h->red(R_C);
@@ -1092,7 +1093,8 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
                  mm_min_info* info) {
   const int N = h->N, n3 = 3 * N;
   const int ge = grid_elem(N);
-  ensure_min_buffers(h, prm->method == MM_METHOD_LBFGS ? std::max(1, prm->memory) : 0);
+  const bool lbfgs = prm->method == MM_METHOD_LBFGS || prm->method == MM_METHOD_PLBFGS;
+  ensure_min_buffers(h, lbfgs ? std::max(1, prm->memory) : 0);
   MinCtx c{h, N, {B[0], B[1], B[2]}, prm->phi_tol > 0 ? prm->phi_tol : std::min(prm->cg_tol, 0.1 * prm->tau_f), prm};
   auto t0 = std::chrono::steady_clock::now();
   double* graw = h->w_graw;
@@ -1128,7 +1130,7 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     double* H = h->w_H;
     if (prm->method == MM_METHOD_PCOHEN_HS) {
       const double pc_tol = prm->pc_auto ? std::min(prm->pc_force_eta, std::pow(gnorm_inf, prm->pc_force_alpha)) : 0.0;
-      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol, h->w_y);
+      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol, h->w_y, prm->pc_reg);
       const double gsm = dev_absmax(h, n3, h->w_y);
       // HS beta
       mmk::k_dot2diff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc,
@@ -1149,6 +1151,40 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       }
       conv_gnorm = gsm;
       gnorm = gsm;
+    } else if (prm->method == MM_METHOD_PLBFGS) {
+      // preconditioned L-BFGS (src/minimizers.py:1526-1653): smoothed gradient y = P^-1 g_tan_ext for
+      // the convergence test and the fallback, two-loop recursion with P^-1 as the initial Hessian
+      solve_Py_g(c, m, graw, h->w_gte, 0.0, h->w_ys, 0.0);
+      const double gsm = dev_absmax(h, n3, h->w_ys);
+      const int n_hist = std::min(hist_it, mem);
+      std::vector<double> alphas(mem, 0.0);
+      double* q = h->w_y;
+      CK(cudaMemcpyAsync(q, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+      for (int i = 0; i < n_hist; ++i) {
+        const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
+        const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
+        LAUNCH_CHECK();
+        alphas[idx] = a;
+      }
+      solve_Py_g(c, m, graw, q, 0.0, h->w_d, prm->pc_reg);
+      for (int i = 0; i < n_hist; ++i) {
+        const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
+        const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], h->w_d);
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, h->w_d);
+        LAUNCH_CHECK();
+      }
+      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_d);
+      LAUNCH_CHECK();
+      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) {
+        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_ys, 0.0, h->w_d);
+        LAUNCH_CHECK();
+      }
+      pg = dev_dot(h, n3, graw, h->w_d);
+      s0 = (it == 0) ? prm->tau0 : 1.0;
+      conv_gnorm = gsm;
+      gnorm = gsm;
+      c.preco += 1;
     } else if (prm->method == MM_METHOD_LBFGS) {
       // two-loop recursion on g_tan_ext (src/minimizers.py:1284-1312)
       const int n_hist = std::min(hist_it, mem);
@@ -1252,7 +1288,7 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       std::swap(h->w_gprev, h->w_gte);
       std::swap(h->w_dprev, h->w_d);
       if (ls.accepted) accept_trial(h, m, U, graw);
-    } else if (prm->method == MM_METHOD_LBFGS) {
+    } else if (lbfgs) {
       const double tau = ls.accepted ? ls.tau : 0.0;
       double* m_new = ls.accepted ? h->w_mt : m;
       double* g_new = ls.accepted ? h->w_gt_trial : graw;
@@ -1980,6 +2016,22 @@ int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U, double tol, in
   return guarded(h, [&] { return solve_dev(h, d_m, d_U, tol, maxiter, iters, rel_res); });
 }
 
+int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double* k1me_p) {
+  if (!h || n < 0 || n > h->E || (n > 0 && !k1me)) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (n == 0) {
+      h->eop.mex = h->eop.mey = nullptr;
+      return MM_OK;
+    }
+    mm::assemble_magnetoelastic(h->eop_h, h->N, h->E, h->conn.data(), h->volume.data(), h->mat_id.data(), n, k1me,
+                                k1me_p);
+    h->eop.mex = h->upload(h->eop_h.mx);
+    h->eop.mey = h->upload(h->eop_h.my);
+    h->sync();
+    return MM_OK;
+  });
+}
+
 int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const double* d_c, double* alpha) {
   if (!h || !d_m || !d_U || !d_c) return MM_ERR_ARG;
   return guarded(h, [&] {
@@ -2015,7 +2067,7 @@ int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* in
 
 int mm_minimize(mm_problem* h, const double* B, double* m, double* U, const mm_min_params* prm, mm_min_info* info) {
   if (!h || !B || !m || !U || !prm) return MM_ERR_ARG;
-  if (prm->method < MM_METHOD_PCOHEN_HS || prm->method > MM_METHOD_WG_NP || prm->max_iter < 0) return MM_ERR_ARG;
+  if (prm->method < MM_METHOD_PCOHEN_HS || prm->method > MM_METHOD_PLBFGS || prm->max_iter < 0) return MM_ERR_ARG;
   return guarded(h, [&] {
     if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
     const size_t n3 = 3 * (size_t)h->N;

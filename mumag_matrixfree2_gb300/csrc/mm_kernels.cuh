@@ -811,6 +811,8 @@ struct EnergyDev {
   const double* dy;
   const double* dz;
   const double* kax;    // (n_mat, 3) easy axes
+  const double* mex;    // magnetoelastic entries on m_x, m_y (null: no magnetoelastic term)
+  const double* mey;
   int single_axis;
   int axis0;            // material whose axis every entry uses when single_axis
 };
@@ -848,6 +850,10 @@ __device__ __forceinline__ void exch_aniso_row(const EnergyDev& op, int r, bool 
       ax += wk * vx + t * kx;
       ay += wk * vy + t * ky;
       az += wk * vz + t * kz;
+      if (op.mex) {
+        ax += op.mex[k] * vx;
+        ay += op.mey[k] * vy;
+      }
     }
   }
   ax = group_sum<TPR>(ax);

@@ -450,6 +450,39 @@ static std::vector<int> aggregate(const HostCSR& A, const std::vector<double>& d
   return agg;
 }
 
+void assemble_magnetoelastic(EnergyOp& op, int N, int E, const int* conn, const double* volume, const int* mat_id,
+                             int n, const double* k1me, const double* k1me_p) {
+  if (n < 0 || n > E) throw std::runtime_error("magnetoelastic arrays longer than the element count");
+  op.mx.assign(op.col.size(), 0.0);
+  op.my.assign(op.col.size(), 0.0);
+  std::vector<int> row_of(N, -1);
+  for (int r = 0; r < op.n_rows; ++r) row_of[op.rows[r]] = r;
+  for (int e = 0; e < n; ++e) {
+    const double kp = k1me_p ? k1me_p[e] : 0.0;
+    const double cx = 2.0 * (k1me[e] + kp) * volume[e] / 20.0;
+    const double cy = 2.0 * (k1me[e] - kp) * volume[e] / 20.0;
+    if (cx == 0.0 && cy == 0.0) continue;
+    const int gk = mat_id[e] - 1;  // entry group of a multi-axis operator
+    for (int a = 0; a < 4; ++a) {
+      const int r = row_of[conn[4 * e + a]];
+      if (r < 0) throw std::runtime_error("magnetoelastic constant on an element outside the magnetic region");
+      const int base = op.ptr[r], len = op.ptr[r + 1] - base;
+      for (int b = 0; b < 4; ++b) {
+        const int cb = conn[4 * e + b];
+        int k = -1;
+        for (int t = 0; t < len; ++t)
+          if (op.col[base + t] == cb && (op.single_axis || op.mat[base + t] == gk)) {
+            k = base + t;
+            break;
+          }
+        if (k < 0) throw std::runtime_error("magnetoelastic entry outside the operator's pattern");
+        op.mx[k] += cx * (a == b ? 2.0 : 1.0);
+        op.my[k] += cy * (a == b ? 2.0 : 1.0);
+      }
+    }
+  }
+}
+
 std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
   std::vector<AmgLevel> levels;
   HostCSR Acur = A0;

@@ -28,6 +28,9 @@ struct EnergyOp {
   int n_mat = 0;
   bool single_axis = true;
   std::vector<double> diag_exchange;  // w_aa per node (N)
+  // magnetoelastic entries (empty when the term is absent): sum_e 2 (k1me +- k1me_p) Ve / 20 (1 + d_ab),
+  // acting on the x (mx) and y (my) components
+  std::vector<double> mx, my;
 };
 
 struct AmgLevel {
@@ -56,6 +59,12 @@ HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, co
 EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, const double* grad_phi,
                          const int* mat_id, int n_mat, const double* A, const double* K1, const double* Js,
                          const double* k_easy);
+
+// Magnetoelastic entries of an assembled operator (src/energy_kernels.py:212-224): per element
+// Kx_Ve = 2 (k1me + k1me_p) Ve / 20, Ky_Ve = 2 (k1me - k1me_p) Ve / 20 (arrays of length n <= E,
+// zero beyond; k1me_p may be null).  Elements with a non-zero constant must belong to the operator.
+void assemble_magnetoelastic(EnergyOp& op, int N, int E, const int* conn, const double* volume, const int* mat_id,
+                             int n, const double* k1me, const double* k1me_p);
 
 std::vector<AmgLevel> build_amg(const HostCSR& A, const AmgParams& prm);
 std::vector<double> dense_inverse(const HostCSR& A);  // row-major n x n; throws on singular

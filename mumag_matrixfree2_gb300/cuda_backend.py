@@ -200,6 +200,22 @@ class Problem:
         return d
 
     # -- minimizer ---------------------------------------------------------------------------------
+    def set_magnetoelastic(self, k1me=None, k1me_p=None):
+        """Per-element magnetoelastic constants (reduced units) as make_energy_kernels takes them
+        (``src/energy_kernels.py:92-93,212-224``); None removes the term."""
+        if k1me is None:
+            self._check("mm_set_magnetoelastic", lib().mm_set_magnetoelastic(self.h, 0, None, None))
+            return
+        a = f64(k1me).reshape(-1)
+        b = None if k1me_p is None else f64(k1me_p).reshape(-1)
+        if b is not None and b.size < a.size:
+            b = np.concatenate([b, np.zeros(a.size - b.size)])
+        n = a.size
+        if b is not None and b.size > n:
+            a = np.concatenate([a, np.zeros(b.size - n)])
+            n = b.size
+        self._check("mm_set_magnetoelastic", lib().mm_set_magnetoelastic(self.h, n, dptr(a), dptr(b)))
+
     def set_node_weights(self, inv_M_rel=None, inv_M_prec=None):
         a = None if inv_M_rel is None else f64(inv_M_rel).reshape(-1)
         b = None if inv_M_prec is None else f64(inv_M_prec).reshape(-1)
@@ -303,7 +319,7 @@ def _digest(*arrays) -> str:
 
 
 def problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy, V_mag=None, M_nodal=None, boundary_mask=None,
-                     n_nodes=None) -> Problem:
+                     n_nodes=None, k1me=None, k1me_p=None) -> Problem:
     """The device problem of a reference-style ``TetGeom`` and material tables (created once).
 
     V_mag and M_nodal default to the reference's definitions (``src/loop.py:864-939``).
@@ -321,7 +337,9 @@ def problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy, V_mag=None, M
         M_nodal = np.bincount(conn.reshape(-1), weights=np.repeat(0.25 * volume * Js[mat_id - 1], 4), minlength=N)
     M_nodal = np.asarray(M_nodal, np.float64).reshape(-1)
     key = _digest(np.asarray(A_lookup), np.asarray(K1_lookup), Js, np.asarray(k_easy), np.array([V_mag]), M_nodal,
-                  None if boundary_mask is None else np.asarray(boundary_mask, np.float64))
+                  None if boundary_mask is None else np.asarray(boundary_mask, np.float64),
+                  None if k1me is None else np.asarray(k1me, np.float64),
+                  None if k1me_p is None else np.asarray(k1me_p, np.float64))
     cache = getattr(geom, "_mm_problems", None)
     if cache is None:
         cache = {}
@@ -337,4 +355,6 @@ def problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy, V_mag=None, M
             gp = np.einsum("eij,aj->eai", JT, ghat)
         cache[key] = Problem(conn, volume, np.asarray(gp, np.float64), mat_id, A_lookup, K1_lookup, Js, k_easy,
                              V_mag, M_nodal, boundary_mask, n_nodes=N)
+        if k1me is not None or k1me_p is not None:
+            cache[key].set_magnetoelastic(np.zeros(1) if k1me is None else k1me, k1me_p)
     return cache[key]

@@ -1,8 +1,8 @@
 """``make_energy_kernels`` with the reference's signature (``src/energy_kernels.py:82-142``), on the GPU.
 
 Both reference modes compute the same operators; here both run the assembled per-row operator of
-libmumag_cuda (``k_energy_grad``, ``k_local_grad``).  ``k1me``/``k1me_p`` (magnetoelastic terms) are
-not part of this backend.
+libmumag_cuda (``k_energy_grad``, ``k_local_grad``), including the per-element magnetoelastic terms
+``k1me``/``k1me_p`` when given (``mm_set_magnetoelastic``).
 """
 
 from __future__ import annotations
@@ -23,9 +23,8 @@ def make_energy_kernels(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_m
     g = (K m + G U + g_z) / V_mag with g_z = -2 M_nodal (B_ext + B_bias) (``:147-180,340-459``).
     m, U may be numpy arrays or CUDA torch tensors (then g is a CUDA tensor).
     """
-    if k1me is not None or k1me_p is not None:
-        raise NotImplementedError("the magnetoelastic terms are not part of the cuda backend")
-    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask)
+    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask,
+                            k1me=k1me, k1me_p=k1me_p)
     bias0 = None if B_bias is None else np.asarray(B_bias, np.float64)
 
     def energy_and_grad(m, U, B_ext, sparse_ops=None):

@@ -1,8 +1,9 @@
 """``make_minimizer`` with the reference's signature (``src/minimizers.py:2927-2963``), on the GPU.
 
-Methods: "pcohen_hs" (the hysteresis loop's default, ``:950-1073``), "lbfgs" (``:1266-1381``) and
-"wg_np" (Barzilai-Borwein, ``:1706-1800``); each field step runs entirely in libmumag_cuda
-(``mm_minimize``).  The other reference methods are not part of this backend.
+Methods: "pcohen_hs" (the hysteresis loop's default, ``:950-1073``), "lbfgs" (``:1266-1381``),
+"wg_np" (Barzilai-Borwein, ``:1706-1800``) and "plbfgs" (preconditioned L-BFGS, ``:1526-1653``); each
+field step runs entirely in libmumag_cuda (``mm_minimize``).  The other reference methods are not
+part of this backend.
 """
 
 from __future__ import annotations
@@ -11,7 +12,7 @@ import numpy as np
 
 from .cuda_backend import MinimizerParams, problem_for_geom
 
-SUPPORTED = ("pcohen_hs", "lbfgs", "wg_np")
+SUPPORTED = ("pcohen_hs", "lbfgs", "wg_np", "plbfgs")
 
 
 def tangent_grad(m, g):

@@ -140,10 +140,31 @@ def _exchange_aniso_contrib(p: Problem, v: np.ndarray) -> np.ndarray:
     return contrib + factor[:, :, None] * k[:, None, :]
 
 
-def energy_and_grad_mf(p: Problem, m, U, B_ext, B_bias=None):
+def _magnetoelastic_contrib(p: Problem, v: np.ndarray, k1me, k1me_p=None) -> np.ndarray:
+    """Per element-vertex magnetoelastic contribution (E,4,3), ``src/energy_kernels.py:212-224,319-329,
+    411-426``: Kx_Ve = 2 (k1me + k1me_p) Ve / 20 and Ky_Ve = 2 (k1me - k1me_p) Ve / 20 per element (the
+    per-element arrays zero-padded to E), g_a,x += Kx_Ve (sum_b v_b,x + v_a,x), likewise y."""
+    E = p.conn.shape[0]
+    kx = np.zeros(E)
+    kx[: len(k1me)] = k1me
+    kp = np.zeros(E)
+    if k1me_p is not None:
+        kp[: len(k1me_p)] = k1me_p
+    Kx_Ve = 2.0 * (kx + kp) * p.volume / 20.0
+    Ky_Ve = 2.0 * (kx - kp) * p.volume / 20.0
+    v_e = v[p.conn]
+    out = np.zeros_like(v_e)
+    out[:, :, 0] = Kx_Ve[:, None] * (v_e[:, :, 0].sum(axis=1, keepdims=True) + v_e[:, :, 0])
+    out[:, :, 1] = Ky_Ve[:, None] * (v_e[:, :, 1].sum(axis=1, keepdims=True) + v_e[:, :, 1])
+    return out
+
+
+def energy_and_grad_mf(p: Problem, m, U, B_ext, B_bias=None, k1me=None, k1me_p=None):
     """Matrix-free energy and gradient, ``src/energy_kernels.py:340-459``."""
     _, _, Js_Ve, _ = _coeffs(p)
     contrib = _exchange_aniso_contrib(p, m)
+    if k1me is not None:
+        contrib = contrib + _magnetoelastic_contrib(p, m, k1me, k1me_p)
     grad_u = np.einsum("ebi,eb->ei", p.grad_phi, U[p.conn])  # :403-407
     contrib = contrib + Js_Ve[:, None, None] * grad_u[:, None, :]
     g_quad = node_sum(p.conn, contrib, p.N)
@@ -154,9 +175,12 @@ def energy_and_grad_mf(p: Problem, m, U, B_ext, B_bias=None):
     return E / p.V_mag, g_total / p.V_mag
 
 
-def local_grad_only_mf(p: Problem, v):
-    """Exchange + anisotropy Hessian action, ``src/energy_kernels.py:272-338``."""
-    return node_sum(p.conn, _exchange_aniso_contrib(p, v), p.N) / p.V_mag
+def local_grad_only_mf(p: Problem, v, k1me=None, k1me_p=None):
+    """Exchange + anisotropy (+ magnetoelastic) Hessian action, ``src/energy_kernels.py:272-338``."""
+    c = _exchange_aniso_contrib(p, v)
+    if k1me is not None:
+        c = c + _magnetoelastic_contrib(p, v, k1me, k1me_p)
+    return node_sum(p.conn, c, p.N) / p.V_mag
 
 
 def exchange_diagonal(p: Problem) -> np.ndarray:

@@ -188,7 +188,7 @@ def minimize(ops: Ops, m0, B, U0, prm: Params, method="pcohen_hs"):
     L = prm.L or N
     st = dict(m=m, U=U, g=g_tan_ext, g_raw=g_raw, y=g_tan_ext, d=-g_tan_ext, E=E, gnorm=gnorm, it=0,
               conv=False, evals=1, preco=0, demag=int(init_demag))
-    if method == "lbfgs":
+    if method in ("lbfgs", "plbfgs"):
         mem = prm.memory
         st.update(g=g_tan, S=np.zeros((mem, N, 3)), Y=np.zeros((mem, N, 3)), rho=np.zeros(mem), hist_it=0)
     if method == "wg_np":
@@ -201,6 +201,8 @@ def minimize(ops: Ops, m0, B, U0, prm: Params, method="pcohen_hs"):
             _lbfgs_step(ops, st, B, prm, phi_tol)
         elif method == "wg_np":
             _wg_np_step(ops, st, B, prm, phi_tol)
+        elif method == "plbfgs":
+            _plbfgs_step(ops, st, B, prm, phi_tol)
         else:
             raise NotImplementedError(method)
     info = dict(iters=st["it"], E=float(st["E"]), gnorm=float(st["gnorm"]), preco_iters=st["preco"],
@@ -283,6 +285,53 @@ def _lbfgs_step(ops, st, B, prm, phi_tol):
         S[idx], Y[idx], rho[idx] = s_new, y_new, 1.0 / (curv + 1e-30)
     st.update(m=m_new, U=U_new, g=g_tan_new, g_raw=g_new, S=S, Y=Y, rho=rho, E=E_new, gnorm=gnorm_inf,
               it=st["it"] + 1, conv=conv, evals=st["evals"] + ev, demag=st["demag"] + dem,
+              hist_it=hit + 1 if ok else hit, tau=tau)
+
+
+def _plbfgs_step(ops, st, B, prm, phi_tol):
+    """Preconditioned L-BFGS, ``src/minimizers.py:1526-1653``: the two-loop recursion's initial Hessian
+    is the inner-PCG solve P^-1 (``solve_Py_g``), convergence uses the smoothed gradient y = P^-1 g_tan_ext,
+    the fallback direction is -y, and the preconditioner count grows by one per iteration."""
+    mem = prm.memory
+    m, U, E_prev, g_raw = st["m"], st["U"], st["E"], st["g_raw"]
+    g_tan_ext = tangent_grad(m, g_raw)
+    y, _ = solve_Py_g(ops, m, g_raw, g_tan_ext, prm.pc_iters, 0.0, 0.0, prm.pc_stagnation_nu)
+    gnorm_smooth = float(np.max(np.abs(y)))
+    S, Y, rho, hit = st["S"], st["Y"], st["rho"], st["hist_it"]
+    n_hist = min(hit, mem)
+    alphas = np.zeros(mem)
+    q = g_tan_ext.copy()
+    for i in range(n_hist):
+        idx = (hit - 1 - i) % mem
+        a = rho[idx] * vdot(S[idx], q)
+        q = q - a * Y[idx]
+        alphas[idx] = a
+    r, _ = solve_Py_g(ops, m, g_raw, q, prm.pc_iters, 0.0, prm.pc_reg, prm.pc_stagnation_nu)
+    for i in range(n_hist):
+        idx = (hit - n_hist + i) % mem
+        b = rho[idx] * vdot(Y[idx], r)
+        r = r + S[idx] * (alphas[idx] - b)
+    d = -r
+    if st["it"] == 0 or vdot(d, g_tan_ext) > 0:
+        d = -y
+    H = np.cross(m, d)
+    pg = vdot(g_raw, d)
+    tau_init = prm.tau0 if st["it"] == 0 else 1.0
+    tau, E_new, g_new, U_new, m_new, ev, dem = armijo_ls(
+        ops, m, pg, H, E_prev, U, g_raw, B, phi_tol, prm.ls_eta1, prm.ls_eta2, prm.ls_C, prm.ls_c, tau_init, 15)
+    conv = check_convergence(st["it"], E_new, E_prev, m, m_new, gnorm_smooth, prm.tau_f, prm.eps_a)
+    s_new = tangent_grad(m_new, d * tau)
+    y_new = tangent_grad(m_new, g_new) - tangent_grad(m_new, g_tan_ext)
+    curv = vdot(y_new, s_new)
+    ok = curv > 1e-12 * vdot(s_new, s_new)
+    idx = hit % mem
+    S = np.stack([tangent_grad(m_new, h) for h in S])
+    Y = np.stack([tangent_grad(m_new, h) for h in Y])
+    rho = rho.copy()
+    if ok:
+        S[idx], Y[idx], rho[idx] = s_new, y_new, 1.0 / (curv + 1e-30)
+    st.update(m=m_new, U=U_new, g_raw=g_new, S=S, Y=Y, rho=rho, E=E_new, gnorm=gnorm_smooth,
+              it=st["it"] + 1, conv=conv, evals=st["evals"] + ev, preco=st["preco"] + 1, demag=st["demag"] + dem,
               hist_it=hit + 1 if ok else hit, tau=tau)
 
 

@@ -143,7 +143,7 @@ def _oracle_ops(p, ops, su):
     )
 
 
-@pytest.mark.parametrize("method", ["pcohen_hs", "lbfgs", "wg_np"])
+@pytest.mark.parametrize("method", ["pcohen_hs", "lbfgs", "wg_np", "plbfgs"])
 def test_minimizer_matches_oracle(cuda_ok, method):
     s, p, _ = case("cube8_h2_air24")
     prob = fem_utils.make_problem(s)
@@ -159,6 +159,8 @@ def test_minimizer_matches_oracle(cuda_ok, method):
     m, U, info = prob.minimize(B, m0, np.zeros(p.N), mp)
     assert info["iters"] == info_ref["iters"]
     assert info["evals"] == info_ref["evals"]
+    if method == "plbfgs":
+        assert info["preco_iters"] == info_ref["preco_iters"] == info["iters"]
     assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
     assert np.max(np.abs(m - m_ref)) <= 1e-7
 
@@ -255,3 +257,31 @@ def test_autotuner_keeps_results_within_tolerance(cuda_ok):
     assert {o["precision"] for o in rep["operators"]} == {"fp64", "fp32"}
     U1, it1, rr1, rc1 = prob.solve_u(m, np.zeros(p.N), 1e-10)
     assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1 and rel(U1, U0) <= 1e-8
+
+
+def test_magnetoelastic_term_matches_oracle(cuda_ok):
+    """Per-element k1me / k1me_p (shorter than E: zero-padded, as the reference pads them) in the
+    energy, gradient and local Hessian, against the matrix-free oracle at the FP64 bar."""
+    from mumag_matrixfree2_gb300.energy_kernels import make_energy_kernels
+
+    s, p, _ = case("cube8_h2_air24")
+    rng = np.random.default_rng(61)
+    mag = np.flatnonzero(s.Js_lookup[s.geom.mat_id - 1] > 0)
+    n = int(mag.max()) + 1
+    k1me = np.zeros(n)
+    k1me[mag] = 0.3 * rng.standard_normal(mag.size)
+    k1me_p = np.zeros(n - 5)
+    k1me_p[mag[mag < n - 5]] = 0.2 * rng.standard_normal(int((mag < n - 5).sum()))
+    eg, _, _, lg = make_energy_kernels(s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, s.V_mag, s.M_nodal,
+                                       k1me=k1me, k1me_p=k1me_p, boundary_mask=s.boundary_mask)
+    m = random_state(p.N, seed=62)
+    U = rng.standard_normal(p.N)
+    B = np.array([0.05, 0.0, -0.2])
+    E, g = eg(m, U, B)
+    E0, g0 = ofem.energy_and_grad_mf(p, m, U, B, k1me=k1me, k1me_p=k1me_p)
+    assert abs(E - E0) <= RTOL * abs(E0) and rel(g, g0) <= RTOL
+    v = rng.standard_normal((p.N, 3))
+    assert rel(lg(v), ofem.local_grad_only_mf(p, v, k1me=k1me, k1me_p=k1me_p)) <= RTOL
+    # the term changes the result (the test is not vacuous)
+    E1, _ = ofem.energy_and_grad_mf(p, m, U, B)
+    assert abs(E1 - E0) > 1e-6 * abs(E0)
