@@ -1,0 +1,62 @@
+"""The reference-style command line (python -m mumag_matrixfree2_gb300.loop): its file readers on the
+CPU and a loop through it on the GPU, against run_hysteresis_loop called directly."""
+
+import numpy as np
+import pytest
+
+from mumag_matrixfree2_gb300 import loop as cli
+from mumag_matrixfree2_gb300 import synthetic as syn
+
+
+def _model(tmp_path):
+    knt, ijk = syn.box_mesh(syn.WORKLOADS["cube8_h2_air24"])
+    base = tmp_path / "cube"
+    np.savez(base.with_suffix(".npz"), knt=knt, ijk=ijk)
+    # theta, phi, K1, K2, Js, A: the magnet (easy axis 0.3 rad off z, in x-z) and the air box
+    base.with_suffix(".krn").write_text("0.3 0.0 4.3e6 0.0 1.61 7.7e-12\n0.0 0.0 0.0 0.0 0.0 0.0\n")
+    base.with_suffix(".p2").write_text(
+        "[mesh]\nsize = 1.0e-9\n[field]\nhx = 0.0\nhy = 0.0\nhz = 1.0\nhstart = 4.0\nhfinal = -4.0\nhstep = 2.0\n"
+        "[initial state]\nmx = 0\nmy = 0\nmz = 1\n[minimizer]\ntol_fun = 1e-8\neps_a = 1e-5\nmethod = pcohen_hs\n")
+    return base
+
+
+def test_krn_and_p2_readers(tmp_path):
+    base = _model(tmp_path)
+    A, K1, Js, k = cli.read_krn(base.with_suffix(".krn"), 2, 1e-9)
+    assert np.allclose(A, [7.7e-12 * 1e18, 0.0]) and np.allclose(Js, [1.61, 0.0]) and np.allclose(K1, [4.3e6, 0])
+    assert np.allclose(k[0], [np.sin(0.3), 0.0, np.cos(0.3)]) and np.allclose(k[1], [0, 0, 1])
+    with pytest.raises(ValueError):
+        cli.read_krn(base.with_suffix(".krn"), 3)
+    p2 = cli.read_p2(base.with_suffix(".p2"))
+    assert p2["mesh_unit"] == 1e-9 and p2["B_start"] == 4.0 and p2["B_end"] == -4.0 and p2["dB"] == 2.0
+    assert np.allclose(p2["h_dir"], [0, 0, 1]) and np.allclose(p2["m0_dir"], [0, 0, 1])
+    assert p2["tau_f"] == 1e-8 and p2["eps_a"] == 1e-5 and p2["method"] == "pcohen_hs"
+
+
+def test_cli_rejects_shell_generation_and_missing_mesh():
+    with pytest.raises(SystemExit):
+        cli.main(["--add-shell", "--mesh", "x.npz"])
+    with pytest.raises(SystemExit):
+        cli.main([])
+
+
+@pytest.mark.gpu
+def test_cli_loop_equals_direct_loop(cuda_ok, tmp_path):
+    from mumag_matrixfree2_gb300 import fem_utils
+    from mumag_matrixfree2_gb300.hysteresis_loop import LoopParams, run_hysteresis_loop
+
+    base = _model(tmp_path)
+    res = cli.main([str(base), "--out-dir", str(tmp_path / "out"), "--eps-a", "1e-6"])
+    assert (tmp_path / "out" / "hysteresis.csv").exists() and (tmp_path / "out" / "hysteresis.mh").exists()
+    # the same loop called directly: CLI value for eps_a wins over the .p2 file
+    knt, ijk = syn.box_mesh(syn.WORKLOADS["cube8_h2_air24"])
+    A, K1, Js, k, Js_ref = syn.reduced_materials(
+        [syn.Material(axis=(np.sin(0.3), 0.0, np.cos(0.3))), syn.AIR])
+    s = fem_utils.prepare(knt, ijk, A, K1, Js, k)
+    prm = LoopParams(h_dir=np.array([0.0, 0, 1]), B_start=4.0 / Js_ref, B_end=-4.0 / Js_ref, dB=2.0 / Js_ref,
+                     loop=False, tau_f=1e-8, eps_a=1e-6, out_dir=str(tmp_path / "direct"), Js_ref=Js_ref)
+    ref = run_hysteresis_loop(knt, s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy,
+                              np.tile([0.0, 0.0, 1.0], (s.N, 1)), prm, s.V_mag, s.node_volumes, s.M_nodal,
+                              boundary_mask=s.boundary_mask)
+    assert res["history"].shape == ref["history"].shape == (5, 6)
+    assert np.allclose(res["history"], ref["history"], rtol=1e-12, atol=1e-12)
