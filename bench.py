@@ -373,9 +373,11 @@ def run_learned(s, prob, pm, a):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     fwd = []
     for _ in range(20):
+        ws.net.sync()
         torch.cuda.synchronize()
         e0.record()
         ws.net.forward_dev(None, None, 1)
+        ws.net.sync()  # the network runs on its own stream: wait for it before the closing event
         e1.record()
         torch.cuda.synchronize()
         fwd.append(e0.elapsed_time(e1))
@@ -419,7 +421,8 @@ def run_learned(s, prob, pm, a):
                         "plain_warm_mixed": mean["ms_base_mx"], "learned_mixed": mean["ms_learn_mx"],
                         "network_and_transfer": mean["ms_net"]},
            "forward": {"ms": fwd_ms, "flop": flops, "tflops": flops / (fwd_ms * 1e-3) / 1e12,
-                       "note": "3x3x3 convolutions, interior voxels only; tcgen05 BF16"}}
+                       "note": "3x3x3 convolutions, interior voxels only; tcgen05 BF16; one CUDA graph, timed "
+                               "with events around the launch and a wait for the network's stream"}}
     if mean["ms_learn_mx"] is not None:
         out["mixed_learned_vs_plain_fp64"] = {
             "solve_time_ratio": mean["ms_base64"] / mean["ms_learn_mx"],

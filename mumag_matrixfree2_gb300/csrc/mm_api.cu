@@ -2041,10 +2041,12 @@ int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const
     enqueue_rhs(h, d_m);                                                      // d_b = D m
     spmv<0, double>(h, A0, d_U, nullptr, nullptr, h->d_out, nullptr);         // A U
     spmv<0, double>(h, A0, d_c, nullptr, nullptr, h->d_r64, nullptr);         // A c
-    const double cb = dev_dot(h, N, d_c, h->d_b);
-    const double cAU = dev_dot(h, N, d_c, h->d_out);
-    const double cAc = dev_dot(h, N, d_c, h->d_r64);
-    const double a = (cAc > 0.0 && std::isfinite(cAc)) ? (cb - cAU) / cAc : 0.0;
+    mmk::k_corr_dots<<<grid_elem(N), BS, 0, h->st>>>(N, d_c, h->d_b, h->d_out, h->d_r64, h->d_sc, h->d_part);
+    LAUNCH_CHECK();
+    CK(cudaMemcpyAsync(&h->h_sc->red[R_A], &h->d_sc->red[R_A], 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    const double num = h->h_sc->red[R_A], cAc = h->h_sc->red[R_B];
+    const double a = (cAc > 0.0 && std::isfinite(cAc)) ? num / cAc : 0.0;
     mmk::k_axpby<<<grid_elem(N), BS, 0, h->st>>>(N, a, d_c, 1.0, d_U);
     LAUNCH_CHECK();
     h->sync();

@@ -1123,6 +1123,18 @@ __global__ void __launch_bounds__(BS) k_absmaxdiff(int n, const double* __restri
 }
 
 // a.(b - c) -> red[R_A] and d.(b - c) -> red[R_B]
+// c.(b - y) -> red[R_A] and c.w -> red[R_B] in one pass (the energy-optimal scaling of a correction c)
+__global__ void __launch_bounds__(BS) k_corr_dots(int n, const double* __restrict__ c, const double* __restrict__ b,
+                                                  const double* __restrict__ y, const double* __restrict__ w,
+                                                  Scalars* sc, double* part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    s1 = fma(c[i], b[i] - y[i], s1);
+    s2 = fma(c[i], w[i], s2);
+  }
+  grid_reduce(s1, s2, sc, part, R_A, R_B);
+}
+
 __global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict__ a, const double* __restrict__ d,
                                                  const double* __restrict__ b, const double* __restrict__ c,
                                                  Scalars* sc, double* part) {

@@ -738,6 +738,9 @@ struct mm_unet {
   float* stage_t = nullptr;    // FP32 [B][G^3] (targets / outputs)
   int* d_err = nullptr;
   int nb_fwd = 0;              // samples of the last forward
+  cudaGraphExec_t fwd_exec[8] = {};   // captured forward passes (batch sizes 1..8), on the in-place input
+  bool fwd_warm = false;              // one forward has run (kernel attributes set) before any capture
+  std::vector<std::pair<const void*, size_t>> attr_done;
   bool train_bias = true;      // false: bias gradients are zero (biases stay as set)
 
   template <class T>
@@ -779,7 +782,19 @@ struct mm_unet {
     const size_t smem = mmn::conv_smem(v.P, cin, nt);
     dim3 grid((unsigned)((v.t1 - v.t0 + 128 * mmn::MT - 1) / (128 * mmn::MT)), (unsigned)(cout / nt), (unsigned)nb);
     conv_dispatch(cin, nt, [&](auto kern) {
-      UCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      // the kernel's shared-memory limit only ever grows (and is not touched during a graph capture
+      // once every size has been seen)
+      size_t* cur = nullptr;
+      for (auto& kv : attr_done)
+        if (kv.first == (const void*)kern) cur = &kv.second;
+      if (!cur) {
+        attr_done.emplace_back((const void*)kern, 0);
+        cur = &attr_done.back().second;
+      }
+      if (smem > *cur) {
+        UCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        *cur = smem;
+      }
       kern<<<grid, 128, smem, st>>>(a);
       UCK(cudaGetLastError());
     });
@@ -1038,6 +1053,8 @@ int mm_unet_create(int grid, int batch, mm_unet** out) {
 int mm_unet_destroy(mm_unet* u) {
   if (!u) return MM_ERR_ARG;
   if (u->st) cudaStreamSynchronize(u->st);
+  for (cudaGraphExec_t e : u->fwd_exec)
+    if (e) cudaGraphExecDestroy(e);
   for (void* q : u->allocs) cudaFree(q);
   if (u->h_lpart) cudaFreeHost(u->h_lpart);
   if (u->st) cudaStreamDestroy(u->st);
@@ -1106,6 +1123,27 @@ int mm_unet_forward_dev(mm_unet* u, const float* d_x, int nb, float* d_y) {
   if (!u || nb < 1 || nb > u->B) return MM_ERR_ARG;
   return uguard(u, [&] {
     const size_t nv = (size_t)nb * u->G * u->G * u->G;
+    if (!d_x && !d_y && nb <= 8) {
+      // in-place input, output left in the network: a CUDA graph of the whole forward, no wait here
+      // (errors are reported by the next call that waits, mm_unet_interp_add_dev or mm_unet_sync)
+      if (!u->fwd_warm) {
+        u->forward(nb);
+        u->check_err();
+        u->fwd_warm = true;
+        return MM_OK;
+      }
+      if (!u->fwd_exec[nb - 1]) {
+        cudaGraph_t g = nullptr;
+        UCK(cudaStreamBeginCapture(u->st, cudaStreamCaptureModeThreadLocal));
+        u->forward(nb);
+        UCK(cudaStreamEndCapture(u->st, &g));
+        UCK(cudaGraphInstantiate(&u->fwd_exec[nb - 1], g, 0));
+        cudaGraphDestroy(g);
+      }
+      UCK(cudaGraphLaunch(u->fwd_exec[nb - 1], u->st));
+      u->nb_fwd = nb;
+      return MM_OK;
+    }
     if (d_x) {
       mmn::k_pack_input<<<grid1d((long long)nv), 256, 0, u->st>>>(d_x, u->vol[0], u->T[T_X], nb);
       UCK(cudaGetLastError());
@@ -1176,7 +1214,7 @@ int mm_unet_interp_add_dev(mm_unet* u, int sample, int n, const int* d_node, con
                                                         scale, d_U);
       UCK(cudaGetLastError());
     }
-    UCK(cudaStreamSynchronize(u->st));
+    u->check_err();
     return MM_OK;
   });
 }

@@ -148,6 +148,10 @@ class UNet:
             self.h, None if x is None else C.c_void_p(x.data_ptr()), nb,
             None if y is None else C.c_void_p(y.data_ptr())))
 
+    def sync(self):
+        """Wait for the network's stream (and report a convolution that gave up waiting)."""
+        self._check("mm_unet_sync", _abi.lib().mm_unet_sync(self.h))
+
     def backward_dev(self, target) -> float:
         loss = C.c_double()
         self._check("mm_unet_backward_dev", _abi.lib().mm_unet_backward_dev(
@@ -430,13 +434,16 @@ def time_forward(grid: int = 64, batch: int = 4, reps: int = 10, warmup: int = 3
 
     net = UNet(grid, batch)
     x = torch.randn(batch, grid ** 3, 4, device="cuda")
-    for _ in range(warmup):
-        net.forward_dev(x, None, batch)
+    net.forward_dev(x, None, batch)
+    for _ in range(warmup):  # the first in-place forwards set the kernels up and capture the graph
+        net.forward_dev(None, None, batch)
+    net.sync()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(reps):
         net.forward_dev(None, None, batch)
+    net.sync()  # the network runs on its own stream: wait for it before the closing event
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
