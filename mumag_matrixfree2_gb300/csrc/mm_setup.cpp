@@ -8,8 +8,30 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 
 namespace mm {
+
+// Host threads of the setup: the machine's hardware threads, at most 16.
+static int setup_threads(int64_t n) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t by_work = std::max<int64_t>(1, n / 4096);
+  return (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), by_work);
+}
+
+// f(t, begin, end) on contiguous chunks of [0, n), one chunk per thread (chunk t of nt in order), so
+// per-chunk outputs concatenated in chunk order equal a serial loop's.  f must not throw.
+template <class F>
+static void parallel_chunks(int64_t n, int nt, F&& f) {
+  if (nt <= 1) {
+    f(0, (int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; ++t) th.emplace_back([&f, t, n, nt] { f(t, n * t / nt, n * (t + 1) / nt); });
+  for (auto& x : th) x.join();
+}
 
 // ---------------------------------------------------------------------------------------------
 // geometry: orientation fix, volume, inv(J)^T and shape-function gradients (src/loop.py:56-102)
@@ -21,10 +43,11 @@ static inline double det3(const double J[3][3]) {
 
 void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn_out, double* volume, double* JinvT,
                   double* grad_phi) {
-  for (int e = 0; e < E; ++e) {
+  for (int64_t k = 0; k < 4 * (int64_t)E; ++k)
+    if (conn_in[k] < 0 || conn_in[k] >= N) throw std::runtime_error("connectivity index out of range");
+  parallel_chunks(E, setup_threads(E), [&](int, int64_t e0, int64_t e1) {
+  for (int e = (int)e0; e < (int)e1; ++e) {
     int c[4] = {conn_in[4 * e], conn_in[4 * e + 1], conn_in[4 * e + 2], conn_in[4 * e + 3]};
-    for (int a = 0; a < 4; ++a)
-      if (c[a] < 0 || c[a] >= N) throw std::runtime_error("connectivity index out of range");
     double J[3][3];
     auto build = [&]() {
       for (int k = 0; k < 3; ++k)
@@ -62,6 +85,7 @@ void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn
       g[3 * 0 + i] = (-T[3 * i + 0] - T[3 * i + 1]) - T[3 * i + 2];
     }
   }
+  });
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -69,23 +93,49 @@ void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn
 // ---------------------------------------------------------------------------------------------
 void boundary_mask(int N, int E, const int* conn, double* mask) {
   static const int fp[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
-  std::vector<std::array<int, 3>> faces((size_t)E * 4);
+  // faces bucketed by their smallest node: a face is on the boundary when its (b, c) pair occurs once
+  // in its bucket
+  std::vector<int64_t> start((size_t)N + 1, 0);
+  auto sorted_face = [&](int e, int f, int& a, int& b, int& c) {
+    int t[3] = {conn[4 * e + fp[f][0]], conn[4 * e + fp[f][1]], conn[4 * e + fp[f][2]]};
+    std::sort(t, t + 3);
+    a = t[0];
+    b = t[1];
+    c = t[2];
+  };
   for (int e = 0; e < E; ++e)
     for (int f = 0; f < 4; ++f) {
-      std::array<int, 3> t = {conn[4 * e + fp[f][0]], conn[4 * e + fp[f][1]], conn[4 * e + fp[f][2]]};
-      std::sort(t.begin(), t.end());
-      faces[(size_t)4 * e + f] = t;
+      int a, b, c;
+      sorted_face(e, f, a, b, c);
+      ++start[(size_t)a + 1];
     }
-  std::sort(faces.begin(), faces.end());
+  for (int i = 0; i < N; ++i) start[i + 1] += start[i];
+  std::vector<int64_t> fill(start.begin(), start.end() - 1);
+  std::vector<std::pair<int, int>> bc((size_t)start[N]);
+  for (int e = 0; e < E; ++e)
+    for (int f = 0; f < 4; ++f) {
+      int a, b, c;
+      sorted_face(e, f, a, b, c);
+      bc[(size_t)fill[a]++] = {b, c};
+    }
+  const int nt = setup_threads(N);
+  std::vector<std::vector<std::array<int, 3>>> found(nt);
+  parallel_chunks(N, nt, [&](int t, int64_t n0, int64_t n1) {
+    for (int64_t a = n0; a < n1; ++a) {
+      auto* p0 = bc.data() + start[a];
+      auto* p1 = bc.data() + start[a + 1];
+      std::sort(p0, p1);
+      for (auto* p = p0; p < p1;) {
+        auto* q = p + 1;
+        while (q < p1 && *q == *p) ++q;
+        if (q - p == 1) found[t].push_back({(int)a, p->first, p->second});
+        p = q;
+      }
+    }
+  });
   for (int i = 0; i < N; ++i) mask[i] = 1.0;
-  size_t i = 0, n = faces.size();
-  while (i < n) {
-    size_t j = i + 1;
-    while (j < n && faces[j] == faces[i]) ++j;
-    if (j - i == 1)
-      for (int k = 0; k < 3; ++k) mask[faces[i][k]] = 0.0;
-    i = j;
-  }
+  for (auto& v : found)
+    for (auto& f : v) mask[f[0]] = mask[f[1]] = mask[f[2]] = 0.0;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -182,39 +232,55 @@ static void drop_zeros(HostCSR& A) {
   A.val.resize(w);
 }
 
+// local index of node i in element e
+static inline int local_index(const int* conn, int e, int i) {
+  return conn[4 * e] == i ? 0 : conn[4 * e + 1] == i ? 1 : conn[4 * e + 2] == i ? 2 : 3;
+}
+
 HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, const double* gp, const double* mask,
                          double reg) {
   NodeElems ne = node_elements(N, E, conn);
   HostCSR A;
   A.n_rows = A.n_cols = N;
   A.ptr.assign(N + 1, 0);
-  std::vector<int> tmp;
-  for (int i = 0; i < N; ++i) {
-    tmp.clear();
-    for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
-      int e = ne.elem[k];
-      for (int b = 0; b < 4; ++b) tmp.push_back(conn[4 * e + b]);
+  const int nt = setup_threads(N);
+  std::vector<std::vector<int>> tcol(nt);
+  parallel_chunks(N, nt, [&](int t, int64_t r0, int64_t r1) {
+    std::vector<int> tmp;
+    for (int i = (int)r0; i < (int)r1; ++i) {
+      tmp.clear();
+      for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
+        int e = ne.elem[k];
+        for (int b = 0; b < 4; ++b) tmp.push_back(conn[4 * e + b]);
+      }
+      tmp.push_back(i);
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      A.ptr[i + 1] = (int)tmp.size();
+      tcol[t].insert(tcol[t].end(), tmp.begin(), tmp.end());
     }
-    tmp.push_back(i);
-    std::sort(tmp.begin(), tmp.end());
-    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-    A.ptr[i + 1] = A.ptr[i] + (int)tmp.size();
-    A.col.insert(A.col.end(), tmp.begin(), tmp.end());
-  }
+  });
+  for (int i = 0; i < N; ++i) A.ptr[i + 1] += A.ptr[i];
+  A.col.reserve(A.ptr[N]);
+  for (auto& v : tcol) A.col.insert(A.col.end(), v.begin(), v.end());
   A.val.assign(A.col.size(), 0.0);
-  // element order accumulation: K_ab = Ve (grad phi_a . grad phi_b)
-  for (int e = 0; e < E; ++e) {
-    const double* g = gp + 12 * e;
-    for (int a = 0; a < 4; ++a) {
-      int r = conn[4 * e + a];
+  // K_ab = sum_e Ve (grad phi_a . grad phi_b): row by row over the row's elements in ascending order,
+  // which is the order an element loop adds them in
+  parallel_chunks(N, nt, [&](int, int64_t r0, int64_t r1) {
+    for (int r = (int)r0; r < (int)r1; ++r) {
       const int* rc = A.col.data() + A.ptr[r];
-      int rn = A.ptr[r + 1] - A.ptr[r];
-      for (int b = 0; b < 4; ++b) {
-        int pos = find_col(rc, rn, conn[4 * e + b]);
-        A.val[A.ptr[r] + pos] += volume[e] * dot3(g + 3 * a, g + 3 * b);
+      const int rn = A.ptr[r + 1] - A.ptr[r];
+      for (int k = ne.ptr[r]; k < ne.ptr[r + 1]; ++k) {
+        const int e = ne.elem[k];
+        const double* g = gp + 12 * e;
+        const int a = local_index(conn, e, r);
+        for (int b = 0; b < 4; ++b) {
+          int pos = find_col(rc, rn, conn[4 * e + b]);
+          A.val[A.ptr[r] + pos] += volume[e] * dot3(g + 3 * a, g + 3 * b);
+        }
       }
     }
-  }
+  });
   if (mask) {
     for (int r = 0; r < N; ++r)
       for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
@@ -255,25 +321,37 @@ EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, co
   }
   NodeElems ne = node_elements(N, E, conn, &use);
   op.diag_exchange.assign(N, 0.0);
-  op.ptr.push_back(0);
-  std::vector<std::pair<int, int>> keys;
-  for (int i = 0; i < N; ++i) {
-    if (ne.ptr[i + 1] == ne.ptr[i]) continue;
-    keys.clear();
-    for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
-      int e = ne.elem[k];
-      int g = op.single_axis ? 0 : mat_id[e] - 1;
-      for (int b = 0; b < 4; ++b) keys.emplace_back(conn[4 * e + b], g);
+  // pattern: per node with used elements, the sorted unique (column, axis group) keys; chunks in parallel
+  const int nt = setup_threads(N);
+  std::vector<int> len(N, -1);
+  std::vector<std::vector<std::pair<int, int>>> tkeys(nt);
+  parallel_chunks(N, nt, [&](int t, int64_t n0, int64_t n1) {
+    std::vector<std::pair<int, int>> keys;
+    for (int i = (int)n0; i < (int)n1; ++i) {
+      if (ne.ptr[i + 1] == ne.ptr[i]) continue;
+      keys.clear();
+      for (int k = ne.ptr[i]; k < ne.ptr[i + 1]; ++k) {
+        int e = ne.elem[k];
+        int g = op.single_axis ? 0 : mat_id[e] - 1;
+        for (int b = 0; b < 4; ++b) keys.emplace_back(conn[4 * e + b], g);
+      }
+      std::sort(keys.begin(), keys.end());
+      keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+      len[i] = (int)keys.size();
+      tkeys[t].insert(tkeys[t].end(), keys.begin(), keys.end());
     }
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-    op.rows.push_back(i);
-    for (auto& kv : keys) {
+  });
+  op.ptr.push_back(0);
+  for (int i = 0; i < N; ++i)
+    if (len[i] >= 0) {
+      op.rows.push_back(i);
+      op.ptr.push_back(op.ptr.back() + len[i]);
+    }
+  for (auto& v : tkeys)
+    for (auto& kv : v) {
       op.col.push_back(kv.first);
       op.mat.push_back(kv.second);
     }
-    op.ptr.push_back((int)op.col.size());
-  }
   op.n_rows = (int)op.rows.size();
   size_t nnz = op.col.size();
   op.w.assign(nnz, 0.0);
@@ -284,44 +362,46 @@ EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, co
   op.dx.assign(nnz, 0.0);
   op.dy.assign(nnz, 0.0);
   op.dz.assign(nnz, 0.0);
-  std::vector<int> row_of(N, -1);
-  for (int r = 0; r < op.n_rows; ++r) row_of[op.rows[r]] = r;
-  for (int e = 0; e < E; ++e) {
-    if (!use[e]) continue;
-    int g = mat_id[e] - 1;
-    int gk = op.single_axis ? 0 : g;
-    const double* G = gp + 12 * e;
-    double cA = 2.0 * Alu[g] * volume[e];
-    double cK = 2.0 * K1lu[g] * volume[e] / 20.0;
-    double cG = 2.0 * Jslu[g] * volume[e] / 4.0;
-    double cD = Jslu[g] * volume[e] / 4.0;
-    for (int a = 0; a < 4; ++a) {
-      int node = conn[4 * e + a];
-      int r = row_of[node];
-      op.diag_exchange[node] += cA * dot3(G + 3 * a, G + 3 * a);
-      int base = op.ptr[r], n = op.ptr[r + 1] - base;
-      for (int b = 0; b < 4; ++b) {
-        int cb = conn[4 * e + b];
-        // entries are sorted by (col, mat): find the matching pair
-        int lo = 0, hi = n;
-        while (lo < hi) {
-          int mid = (lo + hi) / 2;
-          int mc = op.col[base + mid], mg = op.mat[base + mid];
-          if (mc < cb || (mc == cb && mg < gk)) lo = mid + 1;
-          else hi = mid;
+  // values row by row over the row's used elements in ascending order (the order an element loop adds
+  // them in), one row per node, rows in parallel
+  parallel_chunks(op.n_rows, setup_threads(op.n_rows), [&](int, int64_t r0, int64_t r1) {
+    for (int r = (int)r0; r < (int)r1; ++r) {
+      const int node = op.rows[r];
+      const int base = op.ptr[r], n = op.ptr[r + 1] - base;
+      for (int kk = ne.ptr[node]; kk < ne.ptr[node + 1]; ++kk) {
+        const int e = ne.elem[kk];
+        const int g = mat_id[e] - 1;
+        const int gk = op.single_axis ? 0 : g;
+        const double* G = gp + 12 * e;
+        const double cA = 2.0 * Alu[g] * volume[e];
+        const double cK = 2.0 * K1lu[g] * volume[e] / 20.0;
+        const double cG = 2.0 * Jslu[g] * volume[e] / 4.0;
+        const double cD = Jslu[g] * volume[e] / 4.0;
+        const int a = local_index(conn, e, node);
+        op.diag_exchange[node] += cA * dot3(G + 3 * a, G + 3 * a);
+        for (int b = 0; b < 4; ++b) {
+          const int cb = conn[4 * e + b];
+          // entries are sorted by (col, group): find the matching pair
+          int lo = 0, hi = n;
+          while (lo < hi) {
+            int mid = (lo + hi) / 2;
+            int mc = op.col[base + mid], mg = op.mat[base + mid];
+            if (mc < cb || (mc == cb && mg < gk)) lo = mid + 1;
+            else hi = mid;
+          }
+          const int k = base + lo;
+          op.w[k] += cA * dot3(G + 3 * a, G + 3 * b);
+          op.q[k] += cK * (a == b ? 2.0 : 1.0);
+          op.gx[k] += cG * G[3 * b + 0];
+          op.gy[k] += cG * G[3 * b + 1];
+          op.gz[k] += cG * G[3 * b + 2];
+          op.dx[k] += cD * G[3 * a + 0];
+          op.dy[k] += cD * G[3 * a + 1];
+          op.dz[k] += cD * G[3 * a + 2];
         }
-        int k = base + lo;
-        op.w[k] += cA * dot3(G + 3 * a, G + 3 * b);
-        op.q[k] += cK * (a == b ? 2.0 : 1.0);
-        op.gx[k] += cG * G[3 * b + 0];
-        op.gy[k] += cG * G[3 * b + 1];
-        op.gz[k] += cG * G[3 * b + 2];
-        op.dx[k] += cD * G[3 * a + 0];
-        op.dy[k] += cD * G[3 * a + 1];
-        op.dz[k] += cD * G[3 * a + 2];
       }
     }
-  }
+  });
   if (op.single_axis) {
     // all entries refer to the shared axis; remember which material carries it
     for (auto& m : op.mat) m = first < 0 ? 0 : first;
@@ -357,30 +437,47 @@ static HostCSR spgemm(const HostCSR& A, const HostCSR& B) {
   C.n_rows = A.n_rows;
   C.n_cols = B.n_cols;
   C.ptr.assign(C.n_rows + 1, 0);
-  std::vector<double> acc(B.n_cols, 0.0);
-  std::vector<int> mark(B.n_cols, -1), cols;
-  for (int i = 0; i < A.n_rows; ++i) {
-    cols.clear();
-    for (int ka = A.ptr[i]; ka < A.ptr[i + 1]; ++ka) {
-      int k = A.col[ka];
-      double a = A.val[ka];
-      for (int kb = B.ptr[k]; kb < B.ptr[k + 1]; ++kb) {
-        int j = B.col[kb];
-        if (mark[j] != i) {
-          mark[j] = i;
-          acc[j] = 0.0;
-          cols.push_back(j);
+  const int nt = setup_threads(A.n_rows);
+  std::vector<std::vector<int>> tcol(nt), tlen(nt);
+  std::vector<std::vector<double>> tval(nt);
+  // rows in chunks; each row's products are summed in the order of a serial loop
+  parallel_chunks(A.n_rows, nt, [&](int t, int64_t r0, int64_t r1) {
+    std::vector<double> acc(B.n_cols, 0.0);
+    std::vector<int> mark(B.n_cols, -1), cols;
+    for (int i = (int)r0; i < (int)r1; ++i) {
+      cols.clear();
+      for (int ka = A.ptr[i]; ka < A.ptr[i + 1]; ++ka) {
+        int k = A.col[ka];
+        double a = A.val[ka];
+        for (int kb = B.ptr[k]; kb < B.ptr[k + 1]; ++kb) {
+          int j = B.col[kb];
+          if (mark[j] != i) {
+            mark[j] = i;
+            acc[j] = 0.0;
+            cols.push_back(j);
+          }
+          acc[j] += a * B.val[kb];
         }
-        acc[j] += a * B.val[kb];
       }
+      std::sort(cols.begin(), cols.end());
+      int len = 0;
+      for (int j : cols)
+        if (acc[j] != 0.0) {
+          tcol[t].push_back(j);
+          tval[t].push_back(acc[j]);
+          ++len;
+        }
+      tlen[t].push_back(len);
     }
-    std::sort(cols.begin(), cols.end());
-    for (int j : cols)
-      if (acc[j] != 0.0) {
-        C.col.push_back(j);
-        C.val.push_back(acc[j]);
-      }
-    C.ptr[i + 1] = (int)C.col.size();
+  });
+  int r = 0;
+  for (int t = 0; t < nt; ++t) {
+    C.col.insert(C.col.end(), tcol[t].begin(), tcol[t].end());
+    C.val.insert(C.val.end(), tval[t].begin(), tval[t].end());
+    for (int len : tlen[t]) {
+      C.ptr[r + 1] = C.ptr[r] + len;
+      ++r;
+    }
   }
   return C;
 }
