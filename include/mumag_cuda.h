@@ -264,7 +264,7 @@ int mm_set_option(mm_problem* h, int option, int value);
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,
  * restrictions, prolongations; both precisions) tries 2, 4, 8, 16 and 32 lanes per row, each timed as
  * whole V-cycles so that cache state and neighbouring kernels are those of a solve, and keeps the
- * fastest; then times the V-cycle with and without the fused coarse correction in each solver and
+ * fastest when it beats the heuristic's shape by more than 3 %; then times the V-cycle with and without the fused coarse correction in each solver and
  * sets MM_OPT_COARSE_FUSE accordingly.  CUDA events on the problem's stream, `reps`
  * launches per candidate.  A JSON report (candidates, times in microseconds, choices) is written to
  * `report` (may be NULL; truncated to report_len - 1 characters).  No counterpart in the reference. */

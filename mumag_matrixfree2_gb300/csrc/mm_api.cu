@@ -2189,17 +2189,20 @@ void tune_csr(mm_problem* h, SolverT<T>& S, DevMatT<T>& M, int reps, const char*
   if (M.tpr == 1 || M.c.n == 0) return;
   const int before = M.tpr;
   int best = before;
-  float best_ms = 1e30f;
+  float best_ms = 1e30f, before_ms = 1e30f;
   std::string times;
   for (int t : {2, 4, 8, 16, 32}) {
     M.tpr = t;
     const float ms = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
     times += (times.empty() ? "" : ",") + std::to_string(1e3 * ms);
+    if (t == before) before_ms = ms;
     if (ms < best_ms) {
       best_ms = ms;
       best = t;
     }
   }
+  // keep the heuristic's shape unless another is clearly faster (V-cycle times vary by ~1-2 % run to run)
+  if (!(best_ms < 0.97f * before_ms)) best = before;
   M.tpr = best;
   rep += std::string(rep.size() > 1 ? "," : "") + "{\"op\":\"" + tag + "\",\"level\":" + std::to_string(level) +
          ",\"precision\":\"" + (sizeof(T) == 8 ? "fp64" : "fp32") + "\",\"rows\":" + std::to_string(M.c.n) +
