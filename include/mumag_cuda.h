@@ -38,7 +38,21 @@ extern "C" {
 #define MM_METHOD_PCOHEN_HS 0
 #define MM_METHOD_LBFGS 1
 #define MM_METHOD_WG_NP 2
-#define MM_METHOD_PLBFGS 3 /* preconditioned L-BFGS (src/minimizers.py:1526-1653) */
+#define MM_METHOD_PLBFGS 3          /* preconditioned L-BFGS (src/minimizers.py:1526-1653)                */
+#define MM_METHOD_COHEN 4           /* Cohen CG, PR beta, energy-based initial step (:642-720)            */
+#define MM_METHOD_PCG 5             /* preconditioned CG, HS beta, d_prev not re-projected (:828-947)     */
+#define MM_METHOD_PCOHEN 6          /* preconditioned Cohen CG, PR beta (:950-1073, beta_type "pr")       */
+#define MM_METHOD_PCOHEN_EXACT 7    /* as PCOHEN with Cayley transport of d and g (:1081-1200, "pr")      */
+#define MM_METHOD_PCOHEN_HS_EXACT 8 /* as PCOHEN_HS with Cayley transport (:1081-1200, "hs")             */
+#define MM_METHOD_DPLBFGS 9         /* damped preconditioned L-BFGS (:1808-1968)                          */
+#define MM_METHOD_TN_SPLIT 10       /* split truncated Newton, P d = -g_tan_ext (:1437-1517)              */
+#define MM_METHOD_TR 11             /* trust-region Newton-CG on the local Hessian (:1994-2103)           */
+#define MM_METHOD_PTR 12            /* preconditioned trust region on the full Hessian (:2129-2320)       */
+#define MM_METHOD_AAPG 13           /* Anderson-accelerated preconditioned gradient (:2507-2636)          */
+#define MM_METHOD_AAPG_EXACT 14     /* AAPG with Cayley transport of the history (:2395-2504)             */
+#define MM_METHOD_PNAG 15           /* preconditioned Nesterov accelerated gradient (:2715-2803)          */
+#define MM_METHOD_PCOHEN_LBFGS 16   /* Cohen CG over the L-BFGS-smoothed gradient (:2806-2924)            */
+#define MM_METHOD_COUNT 17
 
 typedef struct mm_problem mm_problem;
 
@@ -58,6 +72,10 @@ typedef struct {
   double cg_tol;        /* tolerance of the initial Poisson solve */
   double phi_tol;       /* tolerance of the line-search Poisson solves; <= 0: min(cg_tol, 0.1 tau_f) */
   int cg_maxiter;
+  int tn_iters;         /* inner iterations of TR / PTR; <= 0 means 5                                */
+  double lr;            /* PNAG's initial line-search step; <= 0 means 0.1                           */
+  double mu;            /* PNAG's momentum (0.9 in the reference)                                     */
+  int phi_extrapolate;  /* PNAG: warm-start the look-ahead solve from 2 U - U_prev                    */
 } mm_min_params;
 
 typedef struct {
@@ -196,9 +214,15 @@ int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const
  * src/hysteresis_loop.py:340-353).  Either pointer may be NULL to keep the default. */
 int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec);
 
+/* Per-node bias field (N,3, host) added to the applied field in every energy evaluation of
+ * mm_minimize, as sparse_ops["B_bias"] does in the reference (src/minimizers.py:3444-3445,
+ * src/energy_kernels.py:169-171); NULL removes it. */
+int mm_set_bias_field(mm_problem* h, const double* B_bias);
+
 /* Minimize the energy for one applied field, m_inout and U_inout updated in place.
- * Replaces make_minimizer(...).minimize (src/minimizers.py:2927-4098) for pcohen_hs, lbfgs, wg_np
- * and plbfgs, and run_cpp_pcohen_hs_minimization (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
+ * Replaces make_minimizer(...).minimize (src/minimizers.py:2927-4098) for every method of the
+ * reference's CLI (MM_METHOD_*), and run_cpp_pcohen_hs_minimization
+ * (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
 int mm_minimize(mm_problem* h, const double* B_ext, double* m_inout, double* U_inout,
                 const mm_min_params* prm, mm_min_info* info);
 

@@ -15,7 +15,9 @@ LIB_PATH = Path(__file__).resolve().parent / "libmumag_cuda.so"
 
 MM_OK, MM_MAXITER, MM_NONFINITE, MM_BREAKDOWN = 0, 1, 2, 3
 PRECOND = {"none": 0, "jacobi": 1, "amg": 2, "amgcl": 3}
-METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2, "plbfgs": 3}
+METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2, "plbfgs": 3, "cohen": 4, "pcg": 5, "pcohen": 6, "pcohen_exact": 7,
+           "pcohen_hs_exact": 8, "dplbfgs": 9, "tn_split": 10, "tr": 11, "ptr": 12, "aapg": 13, "aapg_exact": 14,
+           "pnag": 15, "pcohen_lbfgs": 16}
 KERNELS = {"spmv_A": 0, "smooth": 1, "energy": 2, "hessian": 3}
 # in-solve profile slots: slot = (fp32 * PROF_LEVELS + level) * len(PROF_KINDS) + kind
 PROF_KINDS = ("pcg_dir", "pcg_step", "vc_residual0", "residual", "restrict", "coarse", "prolong", "smooth0",
@@ -38,6 +40,7 @@ class MinParams(C.Structure):
         ("ls_eta1", C.c_double), ("ls_eta2", C.c_double), ("ls_C", C.c_double), ("ls_c", C.c_double),
         ("pc_force_eta", C.c_double), ("pc_force_alpha", C.c_double), ("pc_stagnation_nu", C.c_double),
         ("pc_reg", C.c_double), ("cg_tol", C.c_double), ("phi_tol", C.c_double), ("cg_maxiter", C.c_int),
+        ("tn_iters", C.c_int), ("lr", C.c_double), ("mu", C.c_double), ("phi_extrapolate", C.c_int),
     ]
 
 
@@ -81,6 +84,7 @@ SIGNATURES = {
     "mm_solve_u": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_int, _ip, _dp]),
     "mm_solve_u_dev": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _ip, _dp]),
     "mm_set_node_weights": (C.c_int, [_vp, _dp, _dp]),
+    "mm_set_bias_field": (C.c_int, [_vp, _dp]),
     "mm_scale_correction_dev": (C.c_int, [_vp, _vp, _vp, _vp, _dp]),
     "mm_set_magnetoelastic": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),

@@ -206,8 +206,11 @@ struct mm_problem {
   double *w_gt = nullptr, *w_gte = nullptr, *w_gprev = nullptr, *w_y = nullptr, *w_d = nullptr,
          *w_dprev = nullptr, *w_H = nullptr, *w_mt = nullptr, *w_Ut = nullptr, *w_gt_trial = nullptr,
          *w_graw = nullptr, *w_r3 = nullptr, *w_z3 = nullptr, *w_p3 = nullptr, *w_Ap3 = nullptr,
-         *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr, *w_ys = nullptr;
+         *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr, *w_ys = nullptr, *w_x1 = nullptr,
+         *w_x2 = nullptr, *w_x3 = nullptr, *w_x4 = nullptr, *w_U2 = nullptr, *w_U3 = nullptr;
   std::vector<double*> w_S, w_Y;
+  double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
+  double* min_bias_buf = nullptr;  // its storage
 
   template <class T>
   T* alloc(size_t n) {
@@ -916,12 +919,15 @@ void ensure_min_buffers(mm_problem* h, int memory) {
   if (!h->min_ready) {
     double** bufs[] = {&h->w_gt, &h->w_gte, &h->w_gprev, &h->w_y, &h->w_d, &h->w_dprev, &h->w_H, &h->w_mt,
                        &h->w_gt_trial, &h->w_graw, &h->w_r3, &h->w_z3, &h->w_p3, &h->w_Ap3, &h->w_tmp,
-                       &h->w_mprev, &h->w_gtprev, &h->w_ys};
+                       &h->w_mprev, &h->w_gtprev, &h->w_ys, &h->w_x1, &h->w_x2, &h->w_x3, &h->w_x4};
     for (double** b : bufs) {
       *b = h->alloc<double>(n3);
       CK(cudaMemsetAsync(*b, 0, n3 * sizeof(double), h->st));
     }
-    h->w_Ut = h->alloc<double>(h->N);
+    for (double** b : {&h->w_Ut, &h->w_U2, &h->w_U3}) {
+      *b = h->alloc<double>(h->N);
+      CK(cudaMemsetAsync(*b, 0, h->N * sizeof(double), h->st));
+    }
     h->min_ready = true;
   }
   while ((int)h->w_S.size() < memory) {
@@ -947,7 +953,7 @@ double dev_absmax(mm_problem* h, int n, const double* a) {
 
 // energy + gradient of (m, U) into g, E returned
 double eval(MinCtx& c, const double* m, const double* U, double* g) {
-  return energy_dev(c.h, m, U, c.B, c.h->d_bias, g);
+  return energy_dev(c.h, m, U, c.B, c.h->d_min_bias, g);
 }
 
 // solve_U(m, U (warm start, in place), tol) -> iterations
@@ -959,9 +965,12 @@ int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
   return it;
 }
 
-// Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations
+// Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations.
+// max_iter < 0 takes pc_iters, nu < 0 the parameters' stagnation threshold.
 int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
-               double reg) {
+               double reg, int max_iter = -1, double nu = -1.0) {
+  if (max_iter < 0) max_iter = c.prm->pc_iters;
+  if (nu < 0) nu = c.prm->pc_stagnation_nu;
   mm_problem* h = c.h;
   const int N = c.N, n3 = 3 * N;
   const int ge = grid_elem(N);
@@ -976,7 +985,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   int it = 0;
   bool done = false;
   const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
-  while (it < c.prm->pc_iters && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
+  while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
     TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, reg,
                                                                      h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part, R_C)));
     LAUNCH_CHECK();
@@ -984,10 +993,10 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
     const bool neg = pAp <= 0.0;
     const double alpha = rho / (pAp + 1e-30);
     const double dq = 0.5 * alpha * rho;
-    const bool stag = (it > 0) && (dq <= c.prm->pc_stagnation_nu * Q);
+    const bool stag = (it > 0) && (dq <= nu * Q);
     done = neg || stag;
-    mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, alpha, y, h->w_r3, h->w_p3, h->w_Ap3, h->d_inv_M_prec, h->w_z3,
-                                             h->d_sc, h->d_part, R_B, done ? 0 : 1);
+    mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, alpha, alpha, y, h->w_r3, h->w_p3, h->w_Ap3, h->d_inv_M_prec,
+                                             h->w_z3, h->d_sc, h->d_part, R_B, done ? 0 : 1);
     LAUNCH_CHECK();
     const double rho_next = h->red(R_B);
     if (!done) {
@@ -1010,6 +1019,89 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   }
   if (!(dev_dot(h, n3, y, gte) > 1e-12)) {
     CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  }
+  return it;
+}
+
+// out = P v (the extensive local Hessian, src/minimizers.py:396-411); returns v.out
+double apply_P(MinCtx& c, const double* m, const double* gext, const double* v, double reg, double* out) {
+  mm_problem* h = c.h;
+  const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
+  TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, v, reg, h->inv_Vmag, out,
+                                                                   h->d_sc, h->d_part, R_C)));
+  LAUNCH_CHECK();
+  return h->red(R_C);
+}
+
+// sum M_rel a1.b1 and sum M_rel a2.b2
+std::pair<double, double> dev_mdot2(mm_problem* h, const double* a1, const double* b1, const double* a2,
+                                    const double* b2) {
+  mmk::k_mdot2<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, a1, b1, a2, b2, h->d_inv_M_rel, h->d_sc, h->d_part);
+  LAUNCH_CHECK();
+  const double s1 = h->red(R_A);
+  return {s1, h->red(R_B)};
+}
+
+// sum M_rel |y + a p|^2
+double dev_mnorm_axpy(mm_problem* h, const double* y, double a, const double* p) {
+  mmk::k_mnorm_axpy<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, y, a, p, h->d_inv_M_rel, h->d_sc, h->d_part);
+  LAUNCH_CHECK();
+  return h->red(R_C);
+}
+
+// positive root of a x^2 + b x + c = 0 (the step to the trust-region boundary)
+double tr_boundary_step(double a, double b, double c) {
+  return (-b + std::sqrt(std::max(0.0, b * b - 4.0 * a * c))) / (2.0 * a);
+}
+
+// Steihaug-Toint truncated PCG inside the M_rel-norm ball of radius delta (src/minimizers.py:506-592);
+// y = result; returns iterations
+int solve_Py_g_tr(MinCtx& c, const double* m, const double* gext, const double* rhs, double delta, int max_iter,
+                  double tol, double reg, double* y) {
+  mm_problem* h = c.h;
+  const int N = c.N, n3 = 3 * N;
+  const int ge = grid_elem(N);
+  CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
+  CK(cudaMemcpyAsync(h->w_r3, rhs, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
+  LAUNCH_CHECK();
+  CK(cudaMemcpyAsync(h->w_p3, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  double rho = h->red(R_B);
+  const double target = tol * tol * rho;
+  const double d2 = delta * delta;
+  int it = 0;
+  bool done = false;
+  while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
+    const double pAp = apply_P(c, m, gext, h->w_p3, reg, h->w_Ap3);
+    const double alpha = rho / (pAp + 1e-30);
+    const auto pp_yp = dev_mdot2(h, h->w_p3, h->w_p3, y, h->w_p3);
+    const double yy = dev_mdot2(h, y, y, y, y).first;
+    const double a_q = pp_yp.first + 1e-30, b_q = 2.0 * pp_yp.second, c_q = yy - d2;
+    const double alpha_tr = tr_boundary_step(a_q, b_q, c_q);
+    done = (pAp <= 0.0) || (dev_mnorm_axpy(h, y, alpha, h->w_p3) >= d2);
+    mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, done ? alpha_tr : alpha, alpha, y, h->w_r3, h->w_p3, h->w_Ap3,
+                                             h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B, 1);
+    LAUNCH_CHECK();
+    const double rho_next = h->red(R_B);
+    if (!done) {
+      mmk::k_xpay<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
+      LAUNCH_CHECK();
+    }
+    rho = rho_next;
+    ++it;
+  }
+  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, rhs, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
+  LAUNCH_CHECK();
+  const double yn = std::sqrt(dev_dot(h, n3, y, nullptr));
+  const double zn = std::sqrt(dev_dot(h, n3, h->w_z3, nullptr));
+  if (yn > 10.0 * zn) {
+    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, 10.0 * zn / (yn + 1e-30), y);
+    LAUNCH_CHECK();
+  }
+  const double ym = std::sqrt(dev_mdot2(h, y, y, y, y).first + 1e-30);
+  if (ym > delta) {
+    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, delta / ym, y);
+    LAUNCH_CHECK();
   }
   return it;
 }
@@ -1092,12 +1184,26 @@ void accept_trial(mm_problem* h, double*& m, double*& U, double*& graw) {
 int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const mm_min_params* prm,
                  mm_min_info* info) {
   const int N = h->N, n3 = 3 * N;
-  const int ge = grid_elem(N);
-  const bool lbfgs = prm->method == MM_METHOD_LBFGS || prm->method == MM_METHOD_PLBFGS;
+  const int ge = grid_elem(N), g3 = grid_elem(n3);
+  const int meth = prm->method;
+  const bool lbfgs = meth == MM_METHOD_LBFGS || meth == MM_METHOD_PLBFGS || meth == MM_METHOD_DPLBFGS ||
+                     meth == MM_METHOD_PCOHEN_LBFGS;
+  const bool exact = meth == MM_METHOD_PCOHEN_EXACT || meth == MM_METHOD_PCOHEN_HS_EXACT;
+  const bool cg_family = meth == MM_METHOD_PCOHEN_HS || meth == MM_METHOD_PCOHEN || meth == MM_METHOD_PCG;
   ensure_min_buffers(h, lbfgs ? std::max(1, prm->memory) : 0);
   MinCtx c{h, N, {B[0], B[1], B[2]}, prm->phi_tol > 0 ? prm->phi_tol : std::min(prm->cg_tol, 0.1 * prm->tau_f), prm};
+  const int tn_iters = prm->tn_iters > 0 ? prm->tn_iters : 5;
+  const double lr = prm->lr > 0 ? prm->lr : 0.1;
   auto t0 = std::chrono::steady_clock::now();
   double* graw = h->w_graw;
+  auto copy3 = [&](double* dst, const double* src) {
+    CK(cudaMemcpyAsync(dst, src, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  };
+  auto neg3 = [&](double* dst, const double* src) {  // dst = -src
+    mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, src, 0.0, dst);
+    LAUNCH_CHECK();
+  };
+  auto zero3 = [&](double* dst) { CK(cudaMemsetAsync(dst, 0, n3 * sizeof(double), h->st)); };
   mmk::k_normalize<<<ge, BS, 0, h->st>>>(N, m);
   LAUNCH_CHECK();
   c.demag += demag_solve(c, m, U, prm->cg_tol);
@@ -1106,20 +1212,162 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
   LAUNCH_CHECK();
   double gnorm = h->red(R_MAX);
   c.evals = 1;
-  // state: g (previous g_tan_ext or g_tan), y, d
-  CK(cudaMemcpyAsync(h->w_gprev, prm->method == MM_METHOD_PCOHEN_HS ? h->w_gte : h->w_gt, n3 * sizeof(double),
-                     cudaMemcpyDeviceToDevice, h->st));
-  CK(cudaMemcpyAsync(h->w_dprev, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_dprev);
-  LAUNCH_CHECK();
-  CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  // initial state of each method (the reference's init_state_fn, src/minimizers.py:2993-3400):
+  // g_prev in w_gprev, y_prev / z_prev in w_ys, d_prev / p_prev in w_dprev
+  const bool tan_init = meth == MM_METHOD_COHEN || exact;  // these start from g_tan, the others g_tan_ext
+  copy3(h->w_gprev, (cg_family || meth == MM_METHOD_COHEN || meth == MM_METHOD_PCOHEN_LBFGS) ? h->w_gte : h->w_gt);
+  copy3(h->w_ys, tan_init ? h->w_gt : h->w_gte);
+  neg3(h->w_dprev, tan_init ? h->w_gt : h->w_gte);
+  copy3(h->w_mprev, m);
+  copy3(h->w_gtprev, h->w_gt);
+  if (meth == MM_METHOD_PCOHEN_LBFGS) copy3(h->w_x1, h->w_gte);  // z_prev
+  if (exact || meth == MM_METHOD_AAPG || meth == MM_METHOD_AAPG_EXACT) {
+    zero3(h->w_x1);  // H_prev (exact) or F_prev (aapg)
+    zero3(h->w_x2);  // H_prev (aapg_exact)
+  }
+  if (meth == MM_METHOD_PNAG) {
+    zero3(h->w_x4);  // velocity
+    CK(cudaMemcpyAsync(h->w_U3, U, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));  // U_prev
+  }
+  if (meth == MM_METHOD_TN_SPLIT) {
+    // TNState is built without the counters, so they start at zero (src/minimizers.py:3198-3203)
+    c.evals = 0;
+    c.demag = 0;
+  }
+  double tau_prev = exact ? 1.0 : 0.0;
+  double E_last = E;     // cohen: the energy before the previous step
+  double delta = 10.0;   // tr / ptr: trust-region radius
   const int L = prm->L > 0 ? prm->L : N;
   const int mem = std::max(1, prm->memory);
   std::vector<double> rho_h(mem, 0.0);
   int hist_it = 0;
   int it = 0;
   bool conv = false;
+
+  // L-BFGS two-loop recursion on g_tan_ext; `initial(q, out)` applies the initial inverse Hessian
+  auto two_loop = [&](double* out, auto&& initial) {
+    const int n_hist = std::min(hist_it, mem);
+    std::vector<double> alphas(mem, 0.0);
+    double* q = h->w_y;
+    copy3(q, h->w_gte);
+    for (int i = 0; i < n_hist; ++i) {
+      const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
+      const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
+      LAUNCH_CHECK();
+      alphas[idx] = a;
+    }
+    initial(q, out);
+    for (int i = 0; i < n_hist; ++i) {
+      const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
+      const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], out);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, out);
+      LAUNCH_CHECK();
+    }
+  };
+  // initial Hessian of the plain L-BFGS: gamma q .* inv_M_rel, gamma = s.y / y.(y .* inv_M_rel) clipped
+  auto lbfgs_initial = [&](const double* q, double* out, bool clip) {
+    const int last = ((hist_it - 1) % mem + mem) % mem;
+    double gamma = 1.0;
+    if (hist_it > 0) {
+      mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->d_sc, h->d_part, R_B);
+      LAUNCH_CHECK();
+      const double yMy = h->red(R_B);
+      gamma = dev_dot(h, n3, h->w_S[last], h->w_Y[last]) / (yMy + 1e-30);
+    }
+    if (clip) gamma = std::min(std::max(gamma, 1e-3), 1e3);
+    mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, out, h->d_sc, h->d_part, R_B);
+    LAUNCH_CHECK();
+    mmk::k_scale<<<g3, BS, 0, h->st>>>(n3, gamma, out);
+    LAUNCH_CHECK();
+  };
+  // history update at m_new: s = P(d tau), y = P(g_new) - P(g_tan_ext) (optionally replaced by `y_fix`),
+  // all pairs re-projected, the new pair stored if its curvature is positive enough
+  auto hist_update = [&](const double* m_new, const double* g_new, const double* dir, double tau, auto&& y_fix) {
+    double* s_new = h->w_tmp;
+    mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, tau, dir, 0.0, s_new);
+    LAUNCH_CHECK();
+    mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, s_new, s_new);
+    LAUNCH_CHECK();
+    mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, 1.0, g_new, 0.0, h->w_r3);
+    LAUNCH_CHECK();
+    mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_gte, 1.0, h->w_r3);
+    LAUNCH_CHECK();
+    mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_r3, h->w_r3);
+    LAUNCH_CHECK();
+    y_fix(s_new, h->w_r3);
+    const double curv = dev_dot(h, n3, h->w_r3, s_new);
+    const bool ok = curv > 1e-12 * dev_dot(h, n3, s_new, nullptr);
+    for (int i = 0; i < mem; ++i) {
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_S[i], h->w_S[i]);
+      LAUNCH_CHECK();
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_Y[i], h->w_Y[i]);
+      LAUNCH_CHECK();
+    }
+    if (ok) {
+      const int idx = hist_it % mem;
+      copy3(h->w_S[idx], s_new);
+      copy3(h->w_Y[idx], h->w_r3);
+      rho_h[idx] = 1.0 / (curv + 1e-30);
+      ++hist_it;
+    }
+  };
+  auto no_fix = [](double*, double*) {};
+  // d = -y + beta * (P_m) d_prev with the descent safeguard (d = -y when d.g_tan_ext > 0); returns g_raw.d
+  auto direction = [&](const double* y, const double* dprev, double beta, int proj) {
+    mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, y, dprev, beta, h->w_gte, graw, h->w_d, h->d_sc, h->d_part, proj);
+    LAUNCH_CHECK();
+    const double dg = h->red(R_A);
+    double pg = h->red(R_B);
+    if (dg > 0) {
+      neg3(h->w_d, y);
+      pg = dev_dot(h, n3, graw, h->w_d);
+    }
+    return pg;
+  };
+  // d = -a, replaced by -fallback when not a descent direction; returns g_raw.d
+  auto descent_or = [&](const double* a, const double* fallback) {
+    neg3(h->w_d, a);
+    if (dev_dot(h, n3, h->w_d, h->w_gte) > 0) neg3(h->w_d, fallback);
+    return dev_dot(h, n3, graw, h->w_d);
+  };
+  auto pc_tol_of = [&](double gn) {
+    return prm->pc_auto ? std::min(prm->pc_force_eta, std::pow(gn, prm->pc_force_alpha)) : 0.0;
+  };
+  // trust-region trial R(m, m x d, 1), ratio test, radius update, acceptance (src/minimizers.py:2036-2090)
+  auto tr_finish = [&](double pred, double gnorm_inf, int pc_it, int demag_inner) {
+    mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_d, h->w_H);
+    LAUNCH_CHECK();
+    mmk::k_cayley<<<ge, BS, 0, h->st>>>(N, m, h->w_H, 1.0, h->w_mt);
+    LAUNCH_CHECK();
+    CK(cudaMemcpyAsync(h->w_Ut, U, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    const int itd = demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
+    double E_t = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
+    if (!std::isfinite(E_t)) E_t = 1e20;
+    const double rho_tr = (E - E_t) / (pred + 1e-30);
+    const double dnorm = std::sqrt(dev_dot(h, n3, h->w_d, nullptr));
+    const double delta_next = rho_tr < 0.25 ? 0.25 * delta
+                              : (rho_tr > 0.75 && dnorm >= 0.9 * delta) ? std::min(2.0 * delta, 100.0)
+                                                                        : delta;
+    const bool accept = rho_tr > 0.01;
+    double dm = 0.0;
+    if (accept) {
+      mmk::k_absmaxdiff<<<g3, BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
+      LAUNCH_CHECK();
+      dm = h->red(R_MAX);
+    }
+    const double E_next = accept ? E_t : E;
+    conv = check_conv(it, E_next, E, dm, gnorm_inf, prm);
+    if (accept) accept_trial(h, m, U, graw);
+    delta = delta_next;
+    c.evals += 1;
+    c.preco += pc_it;
+    c.demag += demag_inner + itd;
+    E = E_next;
+    gnorm = gnorm_inf;
+    ++it;
+  };
+
   while (!conv && it < prm->max_iter) {
     const double E_prev = E;
     mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->d_sc, h->d_part);
@@ -1128,115 +1376,208 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     double conv_gnorm = gnorm_inf;
     double pg = 0.0, s0 = 1.0;
     double* H = h->w_H;
-    if (prm->method == MM_METHOD_PCOHEN_HS) {
-      const double pc_tol = prm->pc_auto ? std::min(prm->pc_force_eta, std::pow(gnorm_inf, prm->pc_force_alpha)) : 0.0;
-      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol, h->w_y, prm->pc_reg);
+    gnorm = gnorm_inf;
+    if (cg_family) {
+      // preconditioned CG: HS beta (pcohen_hs, pcg) or PR beta (pcohen); pcg keeps d_prev unprojected
+      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm_inf), h->w_y, prm->pc_reg);
       const double gsm = dev_absmax(h, n3, h->w_y);
-      // HS beta
-      mmk::k_dot2diff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc,
-                                                       h->d_part);
+      mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc, h->d_part);
       LAUNCH_CHECK();
       const double num = h->red(R_A);
-      const double den = h->red(R_B) + 1e-30;
+      const double den = (meth == MM_METHOD_PCOHEN ? dev_dot(h, n3, h->w_ys, h->w_gprev) : h->red(R_B)) + 1e-30;
       const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
-      mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_dprev, beta, h->w_gte, graw, h->w_d, h->d_sc,
-                                              h->d_part);
+      pg = direction(h->w_y, h->w_dprev, beta, meth == MM_METHOD_PCG ? 0 : 1);
+      conv_gnorm = gnorm = gsm;
+    } else if (meth == MM_METHOD_COHEN) {
+      // Cohen CG (src/minimizers.py:646-720): y = g_tan, PR beta, energy-based initial step
+      mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_gt, h->w_gt, h->w_gte, h->w_gprev, h->d_sc, h->d_part);
       LAUNCH_CHECK();
-      const double dg = h->red(R_A);
-      pg = h->red(R_B);
-      if (dg > 0) {
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_y, 0.0, h->w_d);
+      const double num = h->red(R_A);
+      const double den = dev_dot(h, n3, h->w_ys, h->w_gprev) + 1e-30;
+      const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
+      pg = direction(h->w_gt, h->w_dprev, beta, 1);
+      double tau_a = 2.0 * (E - E_last) / (-pg + 1e-30);
+      tau_a = std::min(1.0, 1.01 * std::fabs(tau_a));
+      tau_a = std::min(std::max(tau_a, 1e-4), 10.0);
+      s0 = it > 0 ? tau_a : prm->tau0;
+    } else if (exact) {
+      // Cohen CG with Cayley transport of d_prev and g_prev (src/minimizers.py:1093-1200)
+      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm_inf), h->w_y, prm->pc_reg);
+      const double gsm = dev_absmax(h, n3, h->w_y);
+      if (it > 0) {
+        mmk::k_transport<<<ge, BS, 0, h->st>>>(N, h->w_dprev, h->w_x1, tau_prev, h->w_x2);
         LAUNCH_CHECK();
-        pg = dev_dot(h, n3, graw, h->w_d);
+        mmk::k_transport<<<ge, BS, 0, h->st>>>(N, h->w_gprev, h->w_x1, tau_prev, h->w_x3);
+        LAUNCH_CHECK();
+      } else {
+        zero3(h->w_x2);
+        zero3(h->w_x3);
       }
-      conv_gnorm = gsm;
-      gnorm = gsm;
-    } else if (prm->method == MM_METHOD_PLBFGS) {
-      // preconditioned L-BFGS (src/minimizers.py:1526-1653): smoothed gradient y = P^-1 g_tan_ext for
-      // the convergence test and the fallback, two-loop recursion with P^-1 as the initial Hessian
+      mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_x2, h->w_gte, h->w_x3, h->d_sc, h->d_part);
+      LAUNCH_CHECK();
+      const double num = h->red(R_A);
+      const double den =
+          (meth == MM_METHOD_PCOHEN_HS_EXACT ? h->red(R_B) : dev_dot(h, n3, h->w_ys, h->w_x3)) + 1e-30;
+      const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
+      pg = direction(h->w_y, h->w_x2, beta, 0);
+      conv_gnorm = gnorm = gsm;
+    } else if (meth == MM_METHOD_TN_SPLIT) {
+      // split truncated Newton: the Steihaug solve of P d = -g_tan_ext is the step (src/minimizers.py:1448-1517)
+      neg3(h->w_tmp, h->w_gte);
+      c.preco += solve_Py_g(c, m, graw, h->w_tmp, pc_tol_of(gnorm_inf), h->w_d, prm->pc_reg);
+      pg = dev_dot(h, n3, graw, h->w_d);
+      s0 = (it == 0) ? prm->tau0 : 1.0;
+    } else if (meth == MM_METHOD_PLBFGS || meth == MM_METHOD_DPLBFGS) {
+      // preconditioned L-BFGS (src/minimizers.py:1526-1653; damped variant :1820-1968): smoothed gradient
+      // y = P^-1 g_tan_ext for the convergence test and the fallback, P^-1 as the initial Hessian
       solve_Py_g(c, m, graw, h->w_gte, 0.0, h->w_ys, 0.0);
       const double gsm = dev_absmax(h, n3, h->w_ys);
-      const int n_hist = std::min(hist_it, mem);
-      std::vector<double> alphas(mem, 0.0);
-      double* q = h->w_y;
-      CK(cudaMemcpyAsync(q, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-      for (int i = 0; i < n_hist; ++i) {
-        const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
-        const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
-        LAUNCH_CHECK();
-        alphas[idx] = a;
-      }
-      solve_Py_g(c, m, graw, q, 0.0, h->w_d, prm->pc_reg);
-      for (int i = 0; i < n_hist; ++i) {
-        const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
-        const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], h->w_d);
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, h->w_d);
-        LAUNCH_CHECK();
-      }
-      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_d);
+      two_loop(h->w_d, [&](const double* q, double* out) { solve_Py_g(c, m, graw, q, 0.0, out, prm->pc_reg); });
+      mmk::k_scale<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_d);
       LAUNCH_CHECK();
-      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) {
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_ys, 0.0, h->w_d);
-        LAUNCH_CHECK();
-      }
+      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) neg3(h->w_d, h->w_ys);
       pg = dev_dot(h, n3, graw, h->w_d);
       s0 = (it == 0) ? prm->tau0 : 1.0;
-      conv_gnorm = gsm;
-      gnorm = gsm;
-      c.preco += 1;
-    } else if (prm->method == MM_METHOD_LBFGS) {
+      conv_gnorm = gnorm = gsm;
+      c.preco += meth == MM_METHOD_DPLBFGS ? 2 : 1;
+    } else if (meth == MM_METHOD_LBFGS) {
       // two-loop recursion on g_tan_ext (src/minimizers.py:1284-1312)
-      const int n_hist = std::min(hist_it, mem);
-      std::vector<double> alphas(mem, 0.0);
-      double* q = h->w_y;
-      CK(cudaMemcpyAsync(q, h->w_gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-      for (int i = 0; i < n_hist; ++i) {
-        const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
-        const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
-        LAUNCH_CHECK();
-        alphas[idx] = a;
-      }
-      const int last = ((hist_it - 1) % mem + mem) % mem;
-      double gamma = 1.0;
-      if (hist_it > 0) {
-        // y_last . (y_last .* inv_M_rel)
-        mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->d_sc, h->d_part, R_B);
-        LAUNCH_CHECK();
-        const double yMy = h->red(R_B);
-        gamma = dev_dot(h, n3, h->w_S[last], h->w_Y[last]) / (yMy + 1e-30);
-      }
-      gamma = std::min(std::max(gamma, 1e-3), 1e3);
-      // r = gamma q .* inv_M_rel
-      mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, h->w_d, h->d_sc, h->d_part, R_B);
+      two_loop(h->w_d, [&](const double* q, double* out) { lbfgs_initial(q, out, true); });
+      mmk::k_scale<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_d);
       LAUNCH_CHECK();
-      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, gamma, h->w_d);
-      LAUNCH_CHECK();
-      for (int i = 0; i < n_hist; ++i) {
-        const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
-        const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], h->w_d);
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, h->w_d);
-        LAUNCH_CHECK();
-      }
-      mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_d);
-      LAUNCH_CHECK();
-      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) {
-        mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gt, 0.0, h->w_d);
-        LAUNCH_CHECK();
-      }
+      if (it == 0 || dev_dot(h, n3, h->w_d, h->w_gte) > 0) neg3(h->w_d, h->w_gt);
       pg = dev_dot(h, n3, graw, h->w_d);
       s0 = (it == 0) ? prm->tau0 : 1.0;
-      gnorm = gnorm_inf;
+    } else if (meth == MM_METHOD_PCOHEN_LBFGS) {
+      // Cohen CG (PR beta) over the L-BFGS-smoothed gradient z (src/minimizers.py:2816-2924)
+      two_loop(h->w_ys, [&](const double* q, double* out) { lbfgs_initial(q, out, false); });
+      const double gsm = dev_absmax(h, n3, h->w_ys);
+      mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_ys, h->w_ys, h->w_gte, h->w_gprev, h->d_sc, h->d_part);
+      LAUNCH_CHECK();
+      const double num = h->red(R_A);
+      const double den = dev_dot(h, n3, h->w_gprev, h->w_x1) + 1e-30;
+      const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
+      pg = direction(h->w_ys, h->w_dprev, beta, 1);
+      conv_gnorm = gnorm = gsm;
+    } else if (meth == MM_METHOD_AAPG || meth == MM_METHOD_AAPG_EXACT) {
+      // Anderson acceleration of depth one over the previous smoothed gradient (src/minimizers.py:2519-2636),
+      // moved by Cayley transport in the exact variant (:2407-2504)
+      c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm_inf), h->w_y, prm->pc_reg);
+      const double* F_prev = h->w_x1;
+      if (meth == MM_METHOD_AAPG_EXACT && it > 0) {
+        mmk::k_transport<<<ge, BS, 0, h->st>>>(N, h->w_x1, h->w_x2, tau_prev, h->w_x3);
+        LAUNCH_CHECK();
+        F_prev = h->w_x3;
+      }
+      // z_next (w_ys) = z - gamma (z - F_prev) from the third step on, else z
+      copy3(h->w_ys, h->w_y);
+      if (it > 1 || meth == MM_METHOD_AAPG_EXACT) {
+        copy3(h->w_tmp, h->w_y);
+        mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, F_prev, 1.0, h->w_tmp);
+        LAUNCH_CHECK();
+        const double gamma = dev_dot(h, n3, h->w_y, h->w_tmp) / (dev_dot(h, n3, h->w_tmp, nullptr) + 1e-30);
+        if (it > 1) {
+          mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -gamma, h->w_tmp, 1.0, h->w_ys);
+          LAUNCH_CHECK();
+        }
+      }
+      pg = descent_or(h->w_ys, h->w_y);
+      conv_gnorm = gnorm = dev_absmax(h, n3, meth == MM_METHOD_AAPG ? h->w_y : h->w_ys);
+    } else if (meth == MM_METHOD_PNAG) {
+      // Nesterov look-ahead m_look = R(m, -(m x v), mu), smoothed gradient there (src/minimizers.py:2726-2803)
+      const double mu = prm->mu;
+      mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_x4, h->w_x1);
+      LAUNCH_CHECK();
+      mmk::k_cayley<<<ge, BS, 0, h->st>>>(N, m, h->w_x1, -mu, h->w_x2);
+      LAUNCH_CHECK();
+      CK(cudaMemcpyAsync(h->w_U2, U, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+      if (prm->phi_extrapolate && it > 0) {
+        mmk::k_axpby<<<ge, BS, 0, h->st>>>(N, -1.0, h->w_U3, 2.0, h->w_U2);
+        LAUNCH_CHECK();
+      }
+      c.demag += demag_solve(c, h->w_x2, h->w_U2, c.phi_tol);
+      eval(c, h->w_x2, h->w_U2, h->w_x3);
+      c.evals += 1;
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, h->w_x2, h->w_x3, h->w_tmp);
+      LAUNCH_CHECK();
+      c.preco += solve_Py_g(c, h->w_x2, h->w_x3, h->w_tmp, 0.0, h->w_y, prm->pc_reg);
+      conv_gnorm = gnorm = dev_absmax(h, n3, h->w_y);
+      // v_dir = mu P_m(v) - P_m(z)
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m, h->w_x4, h->w_d);
+      LAUNCH_CHECK();
+      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_tmp);
+      LAUNCH_CHECK();
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_tmp, mu, h->w_d);
+      LAUNCH_CHECK();
+      pg = dev_dot(h, n3, graw, h->w_d);
+      s0 = lr;
+    } else if (meth == MM_METHOD_TR) {
+      // trust-region Newton-CG on the local Hessian (src/minimizers.py:2005-2103)
+      neg3(h->w_tmp, h->w_gte);
+      const int pc_it = solve_Py_g_tr(c, m, graw, h->w_tmp, delta, tn_iters, pc_tol_of(gnorm_inf), prm->pc_reg,
+                                      h->w_d);
+      const double dPd = apply_P(c, m, graw, h->w_d, prm->pc_reg, h->w_x1);
+      const double pred = -(dev_dot(h, n3, graw, h->w_d) + 0.5 * dPd);
+      tr_finish(pred, gnorm_inf, pc_it, 0);
+      continue;
+    } else if (meth == MM_METHOD_PTR) {
+      // preconditioned Steihaug CG on the full Hessian; each product solves the Poisson problem of the
+      // direction (src/minimizers.py:2140-2320).  The inner solves use the default stagnation 1e-3.
+      const double pc_tol = pc_tol_of(gnorm_inf);
+      const double zero_B[3] = {0.0, 0.0, 0.0};
+      const double d2 = delta * delta;
+      double *d = h->w_d, *r = h->w_x1, *z = h->w_x2, *p = h->w_x3, *Hp = h->w_x4;
+      zero3(d);
+      copy3(r, h->w_gte);
+      int pc_acc = solve_Py_g(c, m, graw, r, pc_tol, z, prm->pc_reg, -1, 1e-3);
+      neg3(p, z);
+      double rho = dev_dot(h, n3, r, z);
+      double q = 0.0;
+      CK(cudaMemsetAsync(h->w_U3, 0, N * sizeof(double), h->st));
+      int i = 0, dem = 0;
+      bool done = false;
+      while (i < tn_iters && !done && rho > 0.0) {
+        CK(cudaMemcpyAsync(h->w_U2, h->w_U3, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        const int itd = demag_solve(c, p, h->w_U2, c.phi_tol);
+        energy_dev(h, p, h->w_U2, zero_B, h->d_min_bias, h->w_tmp);
+        mmk::k_hess_full<<<ge, BS, 0, h->st>>>(N, m, graw, p, h->w_tmp, Hp, h->d_sc, h->d_part);
+        LAUNCH_CHECK();
+        const double kappa = h->red(R_C);
+        const double alpha = rho / (kappa + 1e-30);
+        const auto pp_dp = dev_mdot2(h, p, p, d, p);
+        const double dd = dev_mdot2(h, d, d, d, d).first;
+        const double alpha_tr = tr_boundary_step(pp_dp.first + 1e-30, 2.0 * pp_dp.second, dd - d2);
+        const bool done_now = (kappa <= 0.0) || (dev_mnorm_axpy(h, d, alpha, p) >= d2);
+        const double af = done_now ? alpha_tr : alpha;
+        q = q + af * dev_dot(h, n3, r, p) + 0.5 * af * af * kappa;
+        mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, af, p, 1.0, d);
+        LAUNCH_CHECK();
+        mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, alpha, Hp, 1.0, r);
+        LAUNCH_CHECK();
+        const int pc_it = solve_Py_g(c, m, graw, r, pc_tol, z, prm->pc_reg, -1, 1e-3);
+        const double rho_next = dev_dot(h, n3, r, z);
+        const double beta = rho_next / (rho + 1e-30);
+        mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, z, beta, p);
+        LAUNCH_CHECK();
+        mmk::k_axpby<<<ge, BS, 0, h->st>>>(N, beta, h->w_U2, 0.0, h->w_U3);
+        LAUNCH_CHECK();
+        done = done || done_now || rho_next < 1e-8 || rho <= 0.0;
+        rho = rho_next;
+        pc_acc += pc_it;
+        dem += itd;
+        ++i;
+      }
+      tr_finish(-q, gnorm_inf, pc_acc, dem);
+      continue;
     } else {  // wg_np: Barzilai-Borwein (src/minimizers.py:1715-1798)
       // s = m - m_prev ; y = g_tan - g_tan_prev
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, m, 0.0, h->w_tmp);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, 1.0, m, 0.0, h->w_tmp);
       LAUNCH_CHECK();
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_mprev, 1.0, h->w_tmp);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_mprev, 1.0, h->w_tmp);
       LAUNCH_CHECK();
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, h->w_gt, 0.0, h->w_y);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, 1.0, h->w_gt, 0.0, h->w_y);
       LAUNCH_CHECK();
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gtprev, 1.0, h->w_y);
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -1.0, h->w_gtprev, 1.0, h->w_y);
       LAUNCH_CHECK();
       const double sty = dev_dot(h, n3, h->w_tmp, h->w_y);
       const double sts = dev_dot(h, n3, h->w_tmp, nullptr);
@@ -1245,10 +1586,8 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       double tau_bb = (it % 2 != 0) ? tau1 : tau2;
       tau_bb = std::min(std::max(std::fabs(tau_bb), 1e-6), 1e3);
       // d = -g_tan so that H = m x d = -(m x z) and pg = g_raw . d
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gt, 0.0, h->w_d);
-      LAUNCH_CHECK();
+      neg3(h->w_d, h->w_gt);
       pg = dev_dot(h, n3, graw, h->w_d);
-      gnorm = gnorm_inf;
       if (it >= prm->wg_gamma) {
         mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_d, H);
         LAUNCH_CHECK();
@@ -1258,12 +1597,12 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
         c.demag += demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
         const double E_new = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
         c.evals += 1;
-        mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
+        mmk::k_absmaxdiff<<<g3, BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
         LAUNCH_CHECK();
         const double dm = h->red(R_MAX);
         conv = check_conv(it, E_new, E_prev, dm, gnorm_inf, prm);
-        CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-        CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        copy3(h->w_mprev, m);
+        copy3(h->w_gtprev, h->w_gt);
         accept_trial(h, m, U, graw);
         E = E_new;
         ++it;
@@ -1275,56 +1614,69 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     LSResult ls = armijo(c, m, pg, H, E_prev, U, s0);
     c.evals += ls.evals;
     c.demag += ls.demag;
+    const double tau = ls.accepted ? ls.tau : 0.0;
+    if (meth == MM_METHOD_DPLBFGS && !ls.accepted) {
+      // m_new = R(m, H, tau) is recomputed by the reference: at tau = 0 that renormalises m
+      mmk::k_cayley<<<ge, BS, 0, h->st>>>(N, m, H, 0.0, h->w_mt);
+      LAUNCH_CHECK();
+    }
+    const bool m_moves = ls.accepted || meth == MM_METHOD_DPLBFGS;
     double dm = 0.0;
-    if (ls.accepted) {
-      mmk::k_absmaxdiff<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
+    if (m_moves) {
+      mmk::k_absmaxdiff<<<g3, BS, 0, h->st>>>(n3, h->w_mt, m, h->d_sc, h->d_part);
       LAUNCH_CHECK();
       dm = h->red(R_MAX);
     }
     const double E_new = ls.accepted ? ls.E : E_prev;
     conv = check_conv(it, E_new, E_prev, dm, conv_gnorm, prm);
-    if (prm->method == MM_METHOD_PCOHEN_HS) {
-      // g_prev <- g_tan_ext, d_prev <- d  (y_prev is not needed by the HS beta)
-      std::swap(h->w_gprev, h->w_gte);
-      std::swap(h->w_dprev, h->w_d);
-      if (ls.accepted) accept_trial(h, m, U, graw);
-    } else if (lbfgs) {
-      const double tau = ls.accepted ? ls.tau : 0.0;
-      double* m_new = ls.accepted ? h->w_mt : m;
-      double* g_new = ls.accepted ? h->w_gt_trial : graw;
-      // s_new = P(m_new, d tau), y_new = P(m_new, g_new) - P(m_new, g_tan_ext)
-      double* s_new = h->w_tmp;
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, tau, h->w_d, 0.0, s_new);
-      LAUNCH_CHECK();
-      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, s_new, s_new);
-      LAUNCH_CHECK();
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, 1.0, g_new, 0.0, h->w_r3);
-      LAUNCH_CHECK();
-      mmk::k_axpby<<<grid_elem(n3), BS, 0, h->st>>>(n3, -1.0, h->w_gte, 1.0, h->w_r3);
-      LAUNCH_CHECK();
-      mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_r3, h->w_r3);
-      LAUNCH_CHECK();
-      const double curv = dev_dot(h, n3, h->w_r3, s_new);
-      const bool ok = curv > 1e-12 * dev_dot(h, n3, s_new, nullptr);
-      for (int i = 0; i < mem; ++i) {
-        mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_S[i], h->w_S[i]);
-        LAUNCH_CHECK();
-        mmk::k_tangent<<<ge, BS, 0, h->st>>>(N, m_new, h->w_Y[i], h->w_Y[i]);
-        LAUNCH_CHECK();
+    if (lbfgs) {
+      const double* m_new = m_moves ? h->w_mt : m;
+      const double* g_new = ls.accepted ? h->w_gt_trial : graw;
+      if (meth == MM_METHOD_DPLBFGS) {
+        // Powell damping against B0 s = P(m_new, g_new) s (src/minimizers.py:1926-1941)
+        hist_update(m_new, g_new, h->w_d, tau, [&](const double* s_k, double* y_k) {
+          const double sBs = apply_P(c, m_new, g_new, s_k, 0.0, h->w_x1);
+          const double sy = dev_dot(h, n3, s_k, y_k);
+          const double theta = sy >= 0.2 * sBs ? 1.0 : 0.8 * sBs / (sBs - sy + 1e-30);
+          mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, 1.0 - theta, h->w_x1, theta, y_k);
+          LAUNCH_CHECK();
+        });
+      } else {
+        hist_update(m_new, g_new, h->w_d, tau, no_fix);
       }
+    }
+    if (cg_family || meth == MM_METHOD_COHEN || exact || meth == MM_METHOD_PCOHEN_LBFGS) {
+      std::swap(h->w_gprev, h->w_gte);  // g_prev <- g_tan_ext
+      std::swap(h->w_dprev, h->w_d);    // d_prev <- d
+    }
+    if (meth == MM_METHOD_PCOHEN || exact) std::swap(h->w_ys, h->w_y);  // y_prev / z_prev <- y / z
+    if (meth == MM_METHOD_COHEN) {
+      std::swap(h->w_ys, h->w_gt);  // y_prev <- g_tan
+      E_last = E_prev;
+    }
+    if (meth == MM_METHOD_PCOHEN_LBFGS) copy3(h->w_x1, h->w_ys);  // z_prev <- z
+    if (exact) {
+      copy3(h->w_x1, H);  // H_prev
+      tau_prev = tau;
+    }
+    if (meth == MM_METHOD_AAPG || meth == MM_METHOD_AAPG_EXACT) {
+      copy3(h->w_x1, h->w_y);  // F_prev <- z
+      if (meth == MM_METHOD_AAPG_EXACT) copy3(h->w_x2, H);
+      tau_prev = tau;
+    }
+    if (meth == MM_METHOD_PNAG) {
+      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, tau, h->w_d, 0.0, h->w_x4);  // v <- tau v_dir
       LAUNCH_CHECK();
-      if (ok) {
-        const int idx = hist_it % mem;
-        CK(cudaMemcpyAsync(h->w_S[idx], s_new, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-        CK(cudaMemcpyAsync(h->w_Y[idx], h->w_r3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-        rho_h[idx] = 1.0 / (curv + 1e-30);
-        ++hist_it;
-      }
-      if (ls.accepted) accept_trial(h, m, U, graw);
-    } else {
-      CK(cudaMemcpyAsync(h->w_mprev, m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-      CK(cudaMemcpyAsync(h->w_gtprev, h->w_gt, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-      if (ls.accepted) accept_trial(h, m, U, graw);
+      CK(cudaMemcpyAsync(h->w_U3, U, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));  // U_prev <- U
+    }
+    if (meth == MM_METHOD_WG_NP) {
+      copy3(h->w_mprev, m);
+      copy3(h->w_gtprev, h->w_gt);
+    }
+    if (ls.accepted) {
+      accept_trial(h, m, U, graw);
+    } else if (meth == MM_METHOD_DPLBFGS) {
+      std::swap(m, h->w_mt);
     }
     E = E_new;
     ++it;
@@ -2055,6 +2407,21 @@ int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const
   });
 }
 
+int mm_set_bias_field(mm_problem* h, const double* B_bias) {
+  if (!h) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!B_bias) {
+      h->d_min_bias = nullptr;  // the buffer stays allocated for a later field
+      return MM_OK;
+    }
+    if (!h->min_bias_buf) h->min_bias_buf = h->alloc<double>(3 * (size_t)h->N);
+    CK(cudaMemcpyAsync(h->min_bias_buf, B_bias, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    h->sync();
+    h->d_min_bias = h->min_bias_buf;
+    return MM_OK;
+  });
+}
+
 int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* inv_M_prec) {
   if (!h) return MM_ERR_ARG;
   return guarded(h, [&] {
@@ -2069,7 +2436,7 @@ int mm_set_node_weights(mm_problem* h, const double* inv_M_rel, const double* in
 
 int mm_minimize(mm_problem* h, const double* B, double* m, double* U, const mm_min_params* prm, mm_min_info* info) {
   if (!h || !B || !m || !U || !prm) return MM_ERR_ARG;
-  if (prm->method < MM_METHOD_PCOHEN_HS || prm->method > MM_METHOD_PLBFGS || prm->max_iter < 0) return MM_ERR_ARG;
+  if (prm->method < 0 || prm->method >= MM_METHOD_COUNT || prm->max_iter < 0) return MM_ERR_ARG;
   return guarded(h, [&] {
     if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
     const size_t n3 = 3 * (size_t)h->N;

@@ -1068,19 +1068,21 @@ __global__ void __launch_bounds__(BS) k_scale3_dot(int N, const double* __restri
   grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// y += a p ; r -= a Ap ; z = r .* w ; r.z -> red[slot]   (inner PCG of the local Hessian)
-__global__ void __launch_bounds__(BS) k_inner_step(int N, double a, double* __restrict__ y, double* __restrict__ r,
-                                                   const double* __restrict__ p, const double* __restrict__ Ap,
-                                                   const double* __restrict__ w, double* __restrict__ z, Scalars* sc,
-                                                   double* part, int slot, int update) {
+// y += ay p ; r -= ar Ap ; z = r .* w ; r.z -> red[slot]   (inner PCG of the local Hessian; the
+// trust-region variant moves y by the boundary step ay and r by the Newton step ar)
+__global__ void __launch_bounds__(BS) k_inner_step(int N, double ay, double ar, double* __restrict__ y,
+                                                   double* __restrict__ r, const double* __restrict__ p,
+                                                   const double* __restrict__ Ap, const double* __restrict__ w,
+                                                   double* __restrict__ z, Scalars* sc, double* part, int slot,
+                                                   int update) {
   double d = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double s = w[i];
     for (int c = 0; c < 3; ++c) {
       double rc = r[3 * i + c];
       if (update) {
-        y[3 * i + c] = y[3 * i + c] + a * p[3 * i + c];
-        rc = rc - a * Ap[3 * i + c];
+        y[3 * i + c] = y[3 * i + c] + ay * p[3 * i + c];
+        rc = rc - ar * Ap[3 * i + c];
         r[3 * i + c] = rc;
       }
       const double zc = rc * s;
@@ -1147,15 +1149,15 @@ __global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict
   grid_reduce(s1, s2, sc, part, R_A, R_B);
 }
 
-// d = -y + beta * P_m(d_prev); d.gte -> red[R_A]; g_raw.d -> red[R_B]
+// d = -y + beta * P_m(d_prev) (d_prev itself when proj == 0); d.gte -> red[R_A]; g_raw.d -> red[R_B]
 __global__ void __launch_bounds__(BS) k_direction(int N, const double* __restrict__ m, const double* __restrict__ y,
                                                   const double* __restrict__ dprev, double beta,
                                                   const double* __restrict__ gte, const double* __restrict__ graw,
-                                                  double* __restrict__ d, Scalars* sc, double* part) {
+                                                  double* __restrict__ d, Scalars* sc, double* part, int proj) {
   double s1 = 0.0, s2 = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
-    const double a = m0 * dprev[3 * i] + m1 * dprev[3 * i + 1] + m2 * dprev[3 * i + 2];
+    const double a = proj ? m0 * dprev[3 * i] + m1 * dprev[3 * i + 1] + m2 * dprev[3 * i + 2] : 0.0;
     const double dp0 = dprev[3 * i] - a * m0, dp1 = dprev[3 * i + 1] - a * m1, dp2 = dprev[3 * i + 2] - a * m2;
     const double d0 = -y[3 * i] + beta * dp0, d1 = -y[3 * i + 1] + beta * dp1, d2 = -y[3 * i + 2] + beta * dp2;
     d[3 * i] = d0;
@@ -1177,6 +1179,75 @@ __global__ void __launch_bounds__(BS) k_cross(int N, const double* __restrict__ 
     H[3 * i + 1] = m2 * d0 - m0 * d2;
     H[3 * i + 2] = m0 * d1 - m1 * d0;
   }
+}
+
+// Cayley transport of a tangent vector: out = ((1 - k.k) v + 2 k x v + 2 (k.v) k) / (1 + k.k), k = tau H / 2
+// (src/minimizers.py:82-91); out may alias v
+__global__ void __launch_bounds__(BS) k_transport(int N, const double* v, const double* __restrict__ H, double tau,
+                                                  double* out) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double k0 = 0.5 * tau * H[3 * i], k1 = 0.5 * tau * H[3 * i + 1], k2 = 0.5 * tau * H[3 * i + 2];
+    const double v0 = v[3 * i], v1 = v[3 * i + 1], v2 = v[3 * i + 2];
+    const double kk = k0 * k0 + k1 * k1 + k2 * k2;
+    const double den = 1.0 + kk;
+    const double kv0 = k1 * v2 - k2 * v1, kv1 = k2 * v0 - k0 * v2, kv2 = k0 * v1 - k1 * v0;
+    const double kd = k0 * v0 + k1 * v1 + k2 * v2;
+    out[3 * i] = ((1.0 - kk) * v0 + 2.0 * kv0 + 2.0 * kd * k0) / den;
+    out[3 * i + 1] = ((1.0 - kk) * v1 + 2.0 * kv1 + 2.0 * kd * k1) / den;
+    out[3 * i + 2] = ((1.0 - kk) * v2 + 2.0 * kv2 + 2.0 * kd * k2) / den;
+  }
+}
+
+// M_rel-weighted inner products, M_rel = 1 / inv_M_rel where inv_M_rel > 1e-20 (else 0):
+// sum M a1.b1 -> red[R_A], sum M a2.b2 -> red[R_B]
+__global__ void __launch_bounds__(BS) k_mdot2(int N, const double* __restrict__ a1, const double* __restrict__ b1,
+                                              const double* __restrict__ a2, const double* __restrict__ b2,
+                                              const double* __restrict__ imr, Scalars* sc, double* part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double w = imr[i] > 1e-20 ? 1.0 / imr[i] : 0.0;
+    s1 += w * (a1[3 * i] * b1[3 * i] + a1[3 * i + 1] * b1[3 * i + 1] + a1[3 * i + 2] * b1[3 * i + 2]);
+    s2 += w * (a2[3 * i] * b2[3 * i] + a2[3 * i + 1] * b2[3 * i + 1] + a2[3 * i + 2] * b2[3 * i + 2]);
+  }
+  grid_reduce(s1, s2, sc, part, R_A, R_B);
+}
+
+// sum M_rel |y + a p|^2 -> red[R_C]
+__global__ void __launch_bounds__(BS) k_mnorm_axpy(int N, const double* __restrict__ y, double a,
+                                                   const double* __restrict__ p, const double* __restrict__ imr,
+                                                   Scalars* sc, double* part) {
+  double s = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double w = imr[i] > 1e-20 ? 1.0 / imr[i] : 0.0;
+    const double u0 = y[3 * i] + a * p[3 * i], u1 = y[3 * i + 1] + a * p[3 * i + 1], u2 = y[3 * i + 2] + a * p[3 * i + 2];
+    s += w * (u0 * u0 + u1 * u1 + u2 * u2);
+  }
+  grid_reduce(s, 0.0, sc, part, R_C);
+}
+
+// Riemannian Hessian action from the full gradient operator: out = Cv - ((v.g) m + (m.g) v + (m.Cv) m)
+// per node (src/minimizers.py:2155-2162); v.out -> red[R_C]
+__global__ void __launch_bounds__(BS) k_hess_full(int N, const double* __restrict__ m, const double* __restrict__ g,
+                                                  const double* __restrict__ v, const double* __restrict__ Cv,
+                                                  double* __restrict__ out, Scalars* sc, double* part) {
+  double s = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
+    const double v0 = v[3 * i], v1 = v[3 * i + 1], v2 = v[3 * i + 2];
+    const double g0 = g[3 * i], g1 = g[3 * i + 1], g2 = g[3 * i + 2];
+    const double c0 = Cv[3 * i], c1 = Cv[3 * i + 1], c2 = Cv[3 * i + 2];
+    const double mg = m0 * g0 + m1 * g1 + m2 * g2;
+    const double vg = v0 * g0 + v1 * g1 + v2 * g2;
+    const double mc = m0 * c0 + m1 * c1 + m2 * c2;
+    const double o0 = c0 - (vg * m0 + mg * v0 + mc * m0);
+    const double o1 = c1 - (vg * m1 + mg * v1 + mc * m1);
+    const double o2 = c2 - (vg * m2 + mg * v2 + mc * m2);
+    out[3 * i] = o0;
+    out[3 * i + 1] = o1;
+    out[3 * i + 2] = o2;
+    s += v0 * o0 + v1 * o1 + v2 * o2;
+  }
+  grid_reduce(s, 0.0, sc, part, R_C);
 }
 
 }  // namespace mmk

@@ -47,6 +47,10 @@ class MinimizerParams:
     cg_tol: float = 1e-8
     phi_tol: float | None = None
     cg_maxiter: int = 2000
+    tn_iters: int = 5
+    lr: float = 0.1
+    mu: float = 0.9
+    phi_extrapolate: bool = True
 
     def to_c(self) -> _abi.MinParams:
         if self.method not in _abi.METHODS:
@@ -59,7 +63,9 @@ class MinimizerParams:
             tau0=self.tau0, ls_eta1=self.ls_eta1, ls_eta2=self.ls_eta2, ls_C=self.ls_C, ls_c=self.ls_c,
             pc_force_eta=self.pc_force_eta, pc_force_alpha=self.pc_force_alpha,
             pc_stagnation_nu=self.pc_stagnation_nu, pc_reg=self.pc_reg, cg_tol=self.cg_tol,
-            phi_tol=-1.0 if self.phi_tol is None else float(self.phi_tol), cg_maxiter=int(self.cg_maxiter))
+            phi_tol=-1.0 if self.phi_tol is None else float(self.phi_tol), cg_maxiter=int(self.cg_maxiter),
+            tn_iters=int(self.tn_iters), lr=float(self.lr), mu=float(self.mu),
+            phi_extrapolate=1 if self.phi_extrapolate else 0)
 
 
 class Problem:
@@ -220,6 +226,12 @@ class Problem:
         a = None if inv_M_rel is None else f64(inv_M_rel).reshape(-1)
         b = None if inv_M_prec is None else f64(inv_M_prec).reshape(-1)
         self._check("mm_set_node_weights", lib().mm_set_node_weights(self.h, dptr(a), dptr(b)))
+
+    def set_bias_field(self, B_bias=None):
+        """Per-node bias field (N,3) added to B_ext in every energy evaluation of minimize (the
+        reference's sparse_ops["B_bias"]); None removes it."""
+        b = None if B_bias is None else f64(B_bias, (self.N, 3))
+        self._check("mm_set_bias_field", lib().mm_set_bias_field(self.h, dptr(b)))
 
     def minimize(self, B_ext, m0, U0, params: MinimizerParams):
         if not self.poisson_built:

@@ -153,7 +153,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                            mode=mode, precision=precision)
     minimize = make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, node_volumes, M_nodal,
                               solve_U, params.cg_tol, method=params.method, memory=params.memory,
-                              boundary_mask=boundary_mask)
+                              boundary_mask=boundary_mask, B_bias=B_bias)
     m = np.asarray(m0, np.float64)
     avg = NodalAverages(geom.conn, geom.volume, geom.mat_id, Js_lookup, m.shape[0])
     m = m / np.linalg.norm(m, axis=1, keepdims=True)
@@ -169,7 +169,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                               ls_c=params.ls_c, pc_iters=params.pc_iters, pc_auto=params.pc_auto,
                               pc_force_eta=params.pc_force_eta, pc_force_alpha=params.pc_force_alpha,
                               pc_stagnation_nu=params.pc_stagnation_nu, memory=params.memory, pc_reg=params.pc_reg,
-                              wg_gamma=params.wg_gamma, L=params.L, verbose=params.verbose)
+                              wg_gamma=params.wg_gamma, L=params.L, tn_iters=params.tn_iters, lr=params.lr,
+                              mu=params.mu, phi_extrapolate=params.phi_extrapolate, verbose=params.verbose)
         dt = time.perf_counter() - t0
         J = avg.J_parallel(m, h)
         mx, my, mz = avg.m_avg(m)

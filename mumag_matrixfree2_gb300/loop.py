@@ -5,7 +5,7 @@
 
 Same inputs and outputs as the reference: an NPZ mesh (``knt``, ``ijk`` with an optional material
 column), a MaMMoS ``.krn`` file (theta, phi, K1, K2, Js, A per material group), an optional ``.p2``
-file whose [mesh], [field], [initial state] and [minimizer] entries override the defaults, fields in
+file whose [mesh], [field], [initial state], [minimizer] and [poisson] entries override the defaults, fields in
 Tesla, and the CSV / ``.mh`` files of ``run_hysteresis_loop`` in ``--out-dir``.  Values given on the
 command line win over the ``.p2`` file, which wins over the defaults (``src/loop.py:940-1062``).
 
@@ -23,6 +23,8 @@ from pathlib import Path
 import numpy as np
 
 MU0 = 4e-7 * np.pi
+METHODS = ("cohen", "pcg", "pcohen", "pcohen_hs", "pcohen_exact", "pcohen_hs_exact", "lbfgs", "plbfgs", "dplbfgs",
+           "tn_split", "wg_np", "tr", "aapg", "aapg_exact", "pnag", "pcohen_lbfgs", "ptr")
 
 
 def read_krn(path, G: int, mesh_unit: float = 1e-9):
@@ -38,8 +40,10 @@ def read_krn(path, G: int, mesh_unit: float = 1e-9):
 
 def read_p2(path) -> dict:
     """Overrides from a .p2 file ([mesh] size; [field] h or hx/hy/hz, hstart, hfinal, hstep, mfinal,
-    mstep, loop; [initial state] mx/my/mz; [minimizer] tol_fun, eps_a, max_iter, tau0, method,
-    pc_iters), as ``src/loop.py:174-288`` reads it.  Fields stay in Tesla."""
+    mstep, loop, bias_type, bias_strength; [initial state] mx/my/mz; [minimizer] tol_fun, eps_a,
+    max_iter, tau0, method, pc_iters, pc_auto, pc_force_eta, pc_force_alpha, pc_stagnation_nu, memory,
+    tn_iters, lr, mu, pc_reg, wg_gamma, phi_extrapolate; [poisson] cg_maxiter, cg_tol, reg), as
+    ``src/loop.py:174-288`` reads it.  Fields stay in Tesla."""
     cp = configparser.ConfigParser()
     cp.read(path)
     out: dict = {}
@@ -56,11 +60,13 @@ def read_p2(path) -> dict:
         if h is not None:
             out["h_dir"] = h / (np.linalg.norm(h) + 1e-30)
         for key, name in (("hstart", "B_start"), ("hfinal", "B_end"), ("hstep", "dB"), ("mfinal", "mfinal"),
-                          ("mstep", "mstep")):
+                          ("mstep", "mstep"), ("bias_strength", "bias_strength")):
             if key in f:
                 out[name] = float(f[key])
         if "loop" in f:
             out["loop"] = f.getboolean("loop")
+        if "bias_type" in f:
+            out["bias_type"] = str(f["bias_type"])
     if "initial state" in cp:
         s = cp["initial state"]
         if all(k in s for k in ("mx", "my", "mz")):
@@ -69,10 +75,45 @@ def read_p2(path) -> dict:
     if "minimizer" in cp:
         mn = cp["minimizer"]
         for key, name, typ in (("tol_fun", "tau_f", float), ("eps_a", "eps_a", float), ("max_iter", "max_iter", int),
-                               ("tau0", "tau0", float), ("method", "method", str), ("pc_iters", "pc_iters", int)):
+                               ("tau0", "tau0", float), ("method", "method", str), ("pc_iters", "pc_iters", int),
+                               ("pc_force_eta", "pc_force_eta", float), ("pc_force_alpha", "pc_force_alpha", float),
+                               ("pc_stagnation_nu", "pc_stagnation_nu", float), ("memory", "memory", int),
+                               ("tn_iters", "tn_iters", int), ("lr", "lr", float), ("mu", "mu", float),
+                               ("pc_reg", "pc_reg", float), ("wg_gamma", "wg_gamma", int)):
             if key in mn:
                 out[name] = typ(mn[key])
+        for key in ("pc_auto", "phi_extrapolate"):
+            if key in mn:
+                out[key] = mn.getboolean(key)
+    if "poisson" in cp:
+        po = cp["poisson"]
+        for key, name, typ in (("cg_maxiter", "cg_maxiter", int), ("cg_tol", "cg_tol", float),
+                               ("reg", "poisson_reg", float)):
+            if key in po:
+                out[name] = typ(po[key])
     return out
+
+
+def bias_field(knt, conn, mat_id, bias_type, strength) -> np.ndarray | None:
+    """Per-node symmetry-breaking field (``src/loop.py:1064-1083``): "circular" is the unit azimuthal
+    field (-y, x) / |(x, y)| around the centre of the magnet's nodes, "random" unit vectors from
+    numpy's default_rng(42); both scaled by ``strength`` (reduced units)."""
+    if bias_type is None:
+        return None
+    B = np.zeros((knt.shape[0], 3))
+    if bias_type == "circular":
+        mag = np.unique(conn[mat_id == 1])
+        if mag.size > 0:
+            xy = knt - np.mean(knt[mag], axis=0)
+            nr = np.sqrt(xy[:, 1] ** 2 + xy[:, 0] ** 2) + 1e-30
+            B[:, 0] = -xy[:, 1] / nr
+            B[:, 1] = xy[:, 0] / nr
+    elif bias_type == "random":
+        B = np.random.default_rng(42).standard_normal((knt.shape[0], 3))
+        B /= np.linalg.norm(B, axis=1, keepdims=True) + 1e-30
+    else:
+        raise ValueError(f"bias type {bias_type!r} (circular or random)")
+    return B * strength
 
 
 def parser() -> argparse.ArgumentParser:
@@ -94,9 +135,23 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--tau-f", type=float, default=1e-8)
     ap.add_argument("--eps-a", type=float, default=1e-12)
     ap.add_argument("--tau0", type=float, default=1e-2)
-    ap.add_argument("--method", default="pcohen_hs", choices=["pcohen_hs", "lbfgs", "wg_np", "plbfgs"])
+    ap.add_argument("--bias-type", default=None, choices=["circular", "random"])
+    ap.add_argument("--bias-strength", type=float, default=0.0)
+    ap.add_argument("--method", default="pcohen_hs", choices=list(METHODS))
     ap.add_argument("--pc-iters", type=int, default=10)
+    ap.add_argument("--pc-auto", action="store_true", default=True)
+    ap.add_argument("--pc-no-auto", action="store_false", dest="pc_auto")
+    ap.add_argument("--pc-force-eta", type=float, default=0.5)
+    ap.add_argument("--pc-force-alpha", type=float, default=0.5)
+    ap.add_argument("--pc-stagnation-nu", type=float, default=0.01)
     ap.add_argument("--memory", type=int, default=5)
+    ap.add_argument("--tn-iters", type=int, default=5)
+    ap.add_argument("--lr", type=float, default=0.1)
+    ap.add_argument("--mu", type=float, default=0.9)
+    ap.add_argument("--pc-reg", type=float, default=0.0)
+    ap.add_argument("--wg-gamma", type=int, default=5)
+    ap.add_argument("--phi-extrapolate", action="store_true", default=True)
+    ap.add_argument("--no-phi-extrapolate", action="store_false", dest="phi_extrapolate")
     ap.add_argument("--m0-dir", type=str, default="0,0,1")
     ap.add_argument("--out-dir", default="hyst_out")
     ap.add_argument("--verbose", action="store_true")
@@ -158,7 +213,11 @@ def main(argv=None) -> dict:
     prm = dict(h_dir=np.array([float(x) for x in args.h_dir.split(",")]), B_start=args.B_start, B_end=args.B_end,
                dB=args.dB, max_iter=args.max_iter, tau_f=args.tau_f, eps_a=args.eps_a, tau0=args.tau0,
                method=args.method, pc_iters=args.pc_iters, memory=args.memory, cg_tol=args.cg_tol,
-               cg_maxiter=args.cg_maxiter, poisson_reg=args.poisson_reg, loop=False, mfinal=None, mstep=None)
+               cg_maxiter=args.cg_maxiter, poisson_reg=args.poisson_reg, loop=False, mfinal=None, mstep=None,
+               pc_auto=args.pc_auto, pc_force_eta=args.pc_force_eta, pc_force_alpha=args.pc_force_alpha,
+               pc_stagnation_nu=args.pc_stagnation_nu, tn_iters=args.tn_iters, lr=args.lr, mu=args.mu,
+               pc_reg=args.pc_reg, wg_gamma=args.wg_gamma, phi_extrapolate=args.phi_extrapolate,
+               bias_type=args.bias_type, bias_strength=args.bias_strength)
     m0_dir = np.array([float(x) for x in args.m0_dir.split(",")])
     for key, val in p2.items():
         if key == "m0_dir":
@@ -171,8 +230,9 @@ def main(argv=None) -> dict:
             prm[key] = prm[key] / Js_ref
     params = LoopParams(**prm, out_dir=args.out_dir, verbose=args.verbose, Js_ref=Js_ref)
     m0 = np.tile(m0_dir / np.linalg.norm(m0_dir), (s.N, 1))
+    B_bias = bias_field(s.knt, s.geom.conn, s.geom.mat_id, params.bias_type, params.bias_strength)
     return run_hysteresis_loop(knt, s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, m0, params, s.V_mag,
-                               s.node_volumes, s.M_nodal, boundary_mask=s.boundary_mask,
+                               s.node_volumes, s.M_nodal, B_bias=B_bias, boundary_mask=s.boundary_mask,
                                precond_type=args.precond_type, mode=args.operator_mode, precision=args.precision)
 
 

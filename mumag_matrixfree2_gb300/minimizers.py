@@ -1,9 +1,12 @@
 """``make_minimizer`` with the reference's signature (``src/minimizers.py:2927-2963``), on the GPU.
 
-Methods: "pcohen_hs" (the hysteresis loop's default, ``:950-1073``), "lbfgs" (``:1266-1381``),
-"wg_np" (Barzilai-Borwein, ``:1706-1800``) and "plbfgs" (preconditioned L-BFGS, ``:1526-1653``); each
-field step runs entirely in libmumag_cuda (``mm_minimize``).  The other reference methods are not
-part of this backend.
+Every method of the reference's command line runs on the GPU (``mm_minimize``): the preconditioned CG
+family "pcohen_hs" (the hysteresis loop's default, ``:950-1073``), "pcohen", "pcg" (``:828-947``),
+"cohen" (``:642-720``), "pcohen_exact" / "pcohen_hs_exact" (Cayley transport, ``:1081-1200``); the
+quasi-Newton family "lbfgs" (``:1266-1381``), "plbfgs" (``:1526-1653``), "dplbfgs" (``:1808-1968``),
+"pcohen_lbfgs" (``:2806-2924``); "wg_np" (Barzilai-Borwein, ``:1706-1800``); the Newton family
+"tn_split" (``:1437-1517``), "tr" and "ptr" (trust regions, ``:1994-2320``); "aapg" / "aapg_exact"
+(Anderson acceleration, ``:2395-2636``) and "pnag" (Nesterov, ``:2715-2803``).
 """
 
 from __future__ import annotations
@@ -12,7 +15,8 @@ import numpy as np
 
 from .cuda_backend import MinimizerParams, problem_for_geom
 
-SUPPORTED = ("pcohen_hs", "lbfgs", "wg_np", "plbfgs")
+SUPPORTED = ("pcohen_hs", "lbfgs", "wg_np", "plbfgs", "cohen", "pcg", "pcohen", "pcohen_exact", "pcohen_hs_exact",
+             "dplbfgs", "tn_split", "tr", "ptr", "aapg", "aapg_exact", "pnag", "pcohen_lbfgs")
 
 
 def tangent_grad(m, g):
@@ -33,13 +37,13 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
     """Return minimize(m0, B_ext, **params) -> (m, U, info) running each field step on the GPU."""
     if method not in SUPPORTED:
         raise NotImplementedError(f"method {method!r} is not part of the cuda backend (available: {SUPPORTED})")
-    if kwargs.get("k1me") is not None:
-        raise NotImplementedError("the magnetoelastic terms are not part of the cuda backend")
     sp = getattr(solve_U, "problem", None)
     boundary_mask = kwargs.get("boundary_mask")
     if boundary_mask is None and sp is not None and sp.has_mask:
         boundary_mask = sp.mask_host
-    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask)
+    # the magnetoelastic constants reach the energy operator as make_energy_kernels' keywords do
+    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask,
+                            k1me=kwargs.get("k1me"), k1me_p=kwargs.get("k1me_p"))
     if not prob.poisson_built:
         if sp is not None:
             if sp.precision != "fp64":
@@ -54,8 +58,8 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
         sparse_ops = params.get("sparse_ops") or {}
         if sparse_ops.get("inv_M_rel") is not None or sparse_ops.get("inv_M_prec") is not None:
             prob.set_node_weights(sparse_ops.get("inv_M_rel"), sparse_ops.get("inv_M_prec"))
-        if B_bias is not None and np.any(np.asarray(B_bias) != 0):
-            raise NotImplementedError("a per-node bias field is evaluated by make_energy_kernels, not by minimize")
+        bias = sparse_ops.get("B_bias", B_bias)
+        prob.set_bias_field(None if bias is None else np.broadcast_to(np.asarray(bias, np.float64), (prob.N, 3)))
         tau_f = float(params.get("tau_f", 1e-6))
         prm = MinimizerParams(
             method=method, max_iter=int(params.get("max_iter", 2000)), tau_f=tau_f,
@@ -69,7 +73,9 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
             memory=int(params.get("memory", memory)), wg_gamma=int(params.get("wg_gamma", 2)),
             L=params.get("L"), cg_tol=float(cg_tol),
             phi_tol=float(params["phi_tol"]) if "phi_tol" in params else float(min(cg_tol, 0.1 * tau_f)),
-            cg_maxiter=int(params.get("cg_maxiter", 2000)))
+            cg_maxiter=int(params.get("cg_maxiter", 2000)), tn_iters=int(params.get("tn_iters", 5)),
+            lr=float(params.get("lr", 0.1)), mu=float(params.get("mu", 0.9)),
+            phi_extrapolate=bool(params.get("phi_extrapolate", False)))
         U0 = params.get("U0")
         if U0 is None:
             U0 = np.zeros(prob.N)

@@ -132,10 +132,10 @@ def test_maxiter_is_reported(cuda_ok):
     assert it == 2 and rc == 1 and rr > 1e-14
 
 
-def _oracle_ops(p, ops, su):
+def _oracle_ops(p, ops, su, bias=None):
     d = ofem.exchange_diagonal(p)
     return omin.Ops(
-        energy_and_grad=lambda m, U, B: ofem.energy_and_grad_asm(p, ops, m, U, B),
+        energy_and_grad=lambda m, U, B: ofem.energy_and_grad_asm(p, ops, m, U, B, bias),
         local_grad_only=lambda v: ofem.local_grad_only_asm(p, ops, v),
         solve_U=lambda m, x0, tol: su(m, x0, tol, return_info=True),
         inv_M_rel=np.where(p.M_nodal > 1e-20, p.V_mag / np.where(p.M_nodal > 0, p.M_nodal, 1), 0.0)[:, None],
@@ -143,8 +143,10 @@ def _oracle_ops(p, ops, su):
     )
 
 
-@pytest.mark.parametrize("method", ["pcohen_hs", "lbfgs", "wg_np", "plbfgs"])
+@pytest.mark.parametrize("method", omin.METHODS)
 def test_minimizer_matches_oracle(cuda_ok, method):
+    """Every minimizer of the reference's command line: same iterations, energy evaluations and
+    inner (preconditioner) iterations as the oracle, same energy and state."""
     s, p, _ = case("cube8_h2_air24")
     prob = fem_utils.make_problem(s)
     prob.build_poisson(1e-12, "amgcl")
@@ -159,8 +161,34 @@ def test_minimizer_matches_oracle(cuda_ok, method):
     m, U, info = prob.minimize(B, m0, np.zeros(p.N), mp)
     assert info["iters"] == info_ref["iters"]
     assert info["evals"] == info_ref["evals"]
+    assert info["preco_iters"] == info_ref["preco_iters"]
     if method == "plbfgs":
-        assert info["preco_iters"] == info_ref["preco_iters"] == info["iters"]
+        assert info["preco_iters"] == info["iters"]
+    assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
+    assert np.max(np.abs(m - m_ref)) <= 1e-7
+
+
+@pytest.mark.parametrize("method", ["pcohen_hs", "ptr"])
+def test_minimizer_with_bias_field_matches_oracle(cuda_ok, method):
+    """A per-node bias field (sparse_ops["B_bias"]) enters every energy evaluation of the step,
+    including the full-Hessian products of the preconditioned trust region."""
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    ops = ofem.assembled_operators(p)
+    su = opo.SolveU(p, ops, cg_tol=1e-10)
+    bias = 0.05 * np.random.default_rng(4).standard_normal((p.N, 3))
+    O = _oracle_ops(p, ops, su, bias)
+    m0 = random_state(p.N, seed=16, amplitude=0.2)
+    B = np.array([0.0, 0.0, -0.3])
+    prm = omin.Params(max_iter=8, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+    m_ref, _, info_ref = omin.minimize(O, m0, B, np.zeros(p.N), prm, method)
+    prob.set_bias_field(bias)
+    m, _, info = prob.minimize(B, m0, np.zeros(p.N), MinimizerParams(method=method, max_iter=8, tau_f=1e-8, eps_a=1e-6,
+                                                                     cg_tol=1e-10))
+    prob.set_bias_field(None)
+    assert (info["iters"], info["evals"], info["preco_iters"]) == (info_ref["iters"], info_ref["evals"],
+                                                                  info_ref["preco_iters"])
     assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
     assert np.max(np.abs(m - m_ref)) <= 1e-7
 

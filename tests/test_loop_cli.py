@@ -33,6 +33,33 @@ def test_krn_and_p2_readers(tmp_path):
     assert p2["tau_f"] == 1e-8 and p2["eps_a"] == 1e-5 and p2["method"] == "pcohen_hs"
 
 
+def test_minimizer_options_and_bias_field(tmp_path):
+    """Every method of the reference's --method list parses; the minimizer and bias entries of a .p2
+    file are read; the circular bias field is the unit azimuthal field around the magnet's centre."""
+    for method in cli.METHODS:
+        assert cli.parser().parse_args(["m", "--method", method]).method == method
+    a = cli.parser().parse_args(["m", "--pc-no-auto", "--no-phi-extrapolate", "--tn-iters", "7", "--lr", "0.5",
+                                 "--mu", "0.8", "--bias-type", "random", "--bias-strength", "0.02"])
+    assert (a.pc_auto, a.phi_extrapolate, a.tn_iters, a.lr, a.mu, a.bias_type, a.bias_strength) == \
+        (False, False, 7, 0.5, 0.8, "random", 0.02)
+    p2 = tmp_path / "x.p2"
+    p2.write_text("[field]\nbias_type = circular\nbias_strength = 0.01\n[minimizer]\nmethod = ptr\ntn_iters = 3\n"
+                  "pc_auto = false\nmu = 0.7\nphi_extrapolate = no\n[poisson]\ncg_tol = 1e-9\nreg = 1e-11\n")
+    o = cli.read_p2(p2)
+    assert o == {"bias_type": "circular", "bias_strength": 0.01, "method": "ptr", "tn_iters": 3, "pc_auto": False,
+                 "mu": 0.7, "phi_extrapolate": False, "cg_tol": 1e-9, "poisson_reg": 1e-11}
+    knt = np.array([[0.0, 0, 0], [2, 0, 0], [0, 2, 0], [0, 0, 2], [5, 5, 5], [1, 3, 0]])
+    conn = np.array([[0, 1, 2, 3], [1, 2, 3, 4]])
+    B = cli.bias_field(knt, conn, np.array([1, 2]), "circular", 0.5)
+    c = knt[:4].mean(axis=0)
+    for i in range(6):
+        x, y = knt[i, 0] - c[0], knt[i, 1] - c[1]
+        assert np.allclose(B[i], 0.5 * np.array([-y, x, 0.0]) / (np.hypot(x, y) + 1e-30))
+    R = cli.bias_field(knt, conn, np.array([1, 2]), "random", 2.0)
+    assert np.allclose(np.linalg.norm(R, axis=1), 2.0)
+    assert cli.bias_field(knt, conn, np.array([1, 2]), None, 1.0) is None
+
+
 def test_cli_rejects_shell_generation_and_missing_mesh():
     with pytest.raises(SystemExit):
         cli.main(["--add-shell", "--mesh", "x.npz"])

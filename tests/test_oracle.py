@@ -174,7 +174,7 @@ def test_oracle_minimizer_decreases_energy():
     )
     m0 = syn.initial_state(p.N, amplitude=0.2)
     B = np.array([0.0, 0.0, -0.5])
-    for method in ["pcohen_hs", "lbfgs", "wg_np", "plbfgs"]:
+    for method in omin.METHODS:
         prm = omin.Params(max_iter=30, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
         U0, _, _ = su(m0, np.zeros(p.N), 1e-10, return_info=True)
         E0, _ = O.energy_and_grad(m0, U0, B)
