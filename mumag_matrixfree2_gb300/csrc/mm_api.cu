@@ -220,14 +220,14 @@ struct mm_problem {
     allocs.push_back(p);
     return (T*)p;
   }
-  template <class T>
-  T* upload(const std::vector<T>& v) {
+  template <class T, class Alloc>
+  T* upload(const std::vector<T, Alloc>& v) {
     T* p = alloc<T>(v.size());
     if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
   }
-  template <class T>
-  T* upload_as(const std::vector<double>& v) {
+  template <class T, class Alloc>
+  T* upload_as(const std::vector<double, Alloc>& v) {
     std::vector<T> t(v.begin(), v.end());
     return upload(t);
   }

@@ -33,6 +33,17 @@ static void parallel_chunks(int64_t n, int nt, F&& f) {
   for (auto& x : th) x.join();
 }
 
+// out = the concatenation of parts (in order), each part copied by its own thread
+template <class V, class P>
+static void concat_parallel(const std::vector<P>& parts, V& out) {
+  std::vector<size_t> off(parts.size() + 1, 0);
+  for (size_t t = 0; t < parts.size(); ++t) off[t + 1] = off[t] + parts[t].size();
+  out.resize(off.back());
+  parallel_chunks((int64_t)parts.size(), (int)parts.size(), [&](int, int64_t t0, int64_t t1) {
+    for (int64_t t = t0; t < t1; ++t) std::copy(parts[t].begin(), parts[t].end(), out.begin() + off[t]);
+  });
+}
+
 // ---------------------------------------------------------------------------------------------
 // geometry: orientation fix, volume, inv(J)^T and shape-function gradients (src/loop.py:56-102)
 // ---------------------------------------------------------------------------------------------
@@ -95,29 +106,38 @@ void boundary_mask(int N, int E, const int* conn, double* mask) {
   static const int fp[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
   // faces bucketed by their smallest node: a face is on the boundary when its (b, c) pair occurs once
   // in its bucket
+  // (bucket fill in parallel with relaxed atomics; every bucket is sorted before it is read, so the
+  // result does not depend on the thread schedule)
   std::vector<int64_t> start((size_t)N + 1, 0);
-  auto sorted_face = [&](int e, int f, int& a, int& b, int& c) {
-    int t[3] = {conn[4 * e + fp[f][0]], conn[4 * e + fp[f][1]], conn[4 * e + fp[f][2]]};
-    std::sort(t, t + 3);
-    a = t[0];
-    b = t[1];
-    c = t[2];
+  auto sorted_face = [&](int64_t e, int f, int& a, int& b, int& c) {
+    int x = conn[4 * e + fp[f][0]], y = conn[4 * e + fp[f][1]], z = conn[4 * e + fp[f][2]];
+    if (x > y) std::swap(x, y);
+    if (y > z) std::swap(y, z);
+    if (x > y) std::swap(x, y);
+    a = x;
+    b = y;
+    c = z;
   };
-  for (int e = 0; e < E; ++e)
-    for (int f = 0; f < 4; ++f) {
-      int a, b, c;
-      sorted_face(e, f, a, b, c);
-      ++start[(size_t)a + 1];
-    }
+  const int nte = setup_threads(E);
+  parallel_chunks(E, nte, [&](int, int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; ++e)
+      for (int f = 0; f < 4; ++f) {
+        int a, b, c;
+        sorted_face(e, f, a, b, c);
+        __atomic_fetch_add(&start[(size_t)a + 1], (int64_t)1, __ATOMIC_RELAXED);
+      }
+  });
   for (int i = 0; i < N; ++i) start[i + 1] += start[i];
   std::vector<int64_t> fill(start.begin(), start.end() - 1);
   std::vector<std::pair<int, int>> bc((size_t)start[N]);
-  for (int e = 0; e < E; ++e)
-    for (int f = 0; f < 4; ++f) {
-      int a, b, c;
-      sorted_face(e, f, a, b, c);
-      bc[(size_t)fill[a]++] = {b, c};
-    }
+  parallel_chunks(E, nte, [&](int, int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; ++e)
+      for (int f = 0; f < 4; ++f) {
+        int a, b, c;
+        sorted_face(e, f, a, b, c);
+        bc[(size_t)__atomic_fetch_add(&fill[a], (int64_t)1, __ATOMIC_RELAXED)] = {b, c};
+      }
+  });
   const int nt = setup_threads(N);
   std::vector<std::vector<std::array<int, 3>>> found(nt);
   parallel_chunks(N, nt, [&](int t, int64_t n0, int64_t n1) {
@@ -190,20 +210,32 @@ struct NodeElems {
   std::vector<int> ptr, elem;
 };
 
+// Node -> element lists, each in ascending element order (the order an element loop visits them):
+// counts and slots taken with relaxed atomics over element chunks in parallel, then every node's list
+// sorted, so the result does not depend on the thread schedule.
 static NodeElems node_elements(int N, int E, const int* conn, const std::vector<char>* use = nullptr) {
   NodeElems ne;
   ne.ptr.assign(N + 1, 0);
-  for (int e = 0; e < E; ++e) {
-    if (use && !(*use)[e]) continue;
-    for (int a = 0; a < 4; ++a) ne.ptr[conn[4 * e + a] + 1]++;
-  }
+  const int nte = setup_threads(E);
+  int* cnt = ne.ptr.data() + 1;
+  parallel_chunks(E, nte, [&](int, int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; ++e) {
+      if (use && !(*use)[e]) continue;
+      for (int a = 0; a < 4; ++a) __atomic_fetch_add(&cnt[conn[4 * e + a]], 1, __ATOMIC_RELAXED);
+    }
+  });
   for (int i = 0; i < N; ++i) ne.ptr[i + 1] += ne.ptr[i];
   ne.elem.resize(ne.ptr[N]);
   std::vector<int> fill(ne.ptr.begin(), ne.ptr.end() - 1);
-  for (int e = 0; e < E; ++e) {
-    if (use && !(*use)[e]) continue;
-    for (int a = 0; a < 4; ++a) ne.elem[fill[conn[4 * e + a]]++] = e;
-  }
+  parallel_chunks(E, nte, [&](int, int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; ++e) {
+      if (use && !(*use)[e]) continue;
+      for (int a = 0; a < 4; ++a) ne.elem[__atomic_fetch_add(&fill[conn[4 * e + a]], 1, __ATOMIC_RELAXED)] = (int)e;
+    }
+  });
+  parallel_chunks(N, setup_threads(N), [&](int, int64_t n0, int64_t n1) {
+    for (int64_t i = n0; i < n1; ++i) std::sort(ne.elem.begin() + ne.ptr[i], ne.elem.begin() + ne.ptr[i + 1]);
+  });
   return ne;
 }
 
@@ -261,15 +293,15 @@ HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, co
     }
   });
   for (int i = 0; i < N; ++i) A.ptr[i + 1] += A.ptr[i];
-  A.col.reserve(A.ptr[N]);
-  for (auto& v : tcol) A.col.insert(A.col.end(), v.begin(), v.end());
-  A.val.assign(A.col.size(), 0.0);
+  concat_parallel(tcol, A.col);
+  A.val.resize(A.col.size());
   // K_ab = sum_e Ve (grad phi_a . grad phi_b): row by row over the row's elements in ascending order,
   // which is the order an element loop adds them in
   parallel_chunks(N, nt, [&](int, int64_t r0, int64_t r1) {
     for (int r = (int)r0; r < (int)r1; ++r) {
       const int* rc = A.col.data() + A.ptr[r];
       const int rn = A.ptr[r + 1] - A.ptr[r];
+      std::fill(A.val.begin() + A.ptr[r], A.val.begin() + A.ptr[r + 1], 0.0);
       for (int k = ne.ptr[r]; k < ne.ptr[r + 1]; ++k) {
         const int e = ne.elem[k];
         const double* g = gp + 12 * e;
@@ -347,27 +379,30 @@ EnergyOp assemble_energy(int N, int E, const int* conn, const double* volume, co
       op.rows.push_back(i);
       op.ptr.push_back(op.ptr.back() + len[i]);
     }
-  for (auto& v : tkeys)
-    for (auto& kv : v) {
-      op.col.push_back(kv.first);
-      op.mat.push_back(kv.second);
-    }
+  {
+    std::vector<size_t> off(nt + 1, 0);
+    for (int t = 0; t < nt; ++t) off[t + 1] = off[t] + tkeys[t].size();
+    op.col.resize(off[nt]);
+    op.mat.resize(off[nt]);
+    parallel_chunks(nt, nt, [&](int, int64_t t0, int64_t t1) {
+      for (int64_t t = t0; t < t1; ++t)
+        for (size_t k = 0; k < tkeys[t].size(); ++k) {
+          op.col[off[t] + k] = tkeys[t][k].first;
+          op.mat[off[t] + k] = tkeys[t][k].second;
+        }
+    });
+  }
   op.n_rows = (int)op.rows.size();
   size_t nnz = op.col.size();
-  op.w.assign(nnz, 0.0);
-  op.q.assign(nnz, 0.0);
-  op.gx.assign(nnz, 0.0);
-  op.gy.assign(nnz, 0.0);
-  op.gz.assign(nnz, 0.0);
-  op.dx.assign(nnz, 0.0);
-  op.dy.assign(nnz, 0.0);
-  op.dz.assign(nnz, 0.0);
+  for (dvec* v : {&op.w, &op.q, &op.gx, &op.gy, &op.gz, &op.dx, &op.dy, &op.dz}) v->resize(nnz);
   // values row by row over the row's used elements in ascending order (the order an element loop adds
   // them in), one row per node, rows in parallel
   parallel_chunks(op.n_rows, setup_threads(op.n_rows), [&](int, int64_t r0, int64_t r1) {
     for (int r = (int)r0; r < (int)r1; ++r) {
       const int node = op.rows[r];
       const int base = op.ptr[r], n = op.ptr[r + 1] - base;
+      for (dvec* v : {&op.w, &op.q, &op.gx, &op.gy, &op.gz, &op.dx, &op.dy, &op.dz})
+        std::fill(v->begin() + base, v->begin() + base + n, 0.0);
       for (int kk = ne.ptr[node]; kk < ne.ptr[node + 1]; ++kk) {
         const int e = ne.elem[kk];
         const int g = mat_id[e] - 1;
@@ -471,32 +506,35 @@ static HostCSR spgemm(const HostCSR& A, const HostCSR& B) {
     }
   });
   int r = 0;
-  for (int t = 0; t < nt; ++t) {
-    C.col.insert(C.col.end(), tcol[t].begin(), tcol[t].end());
-    C.val.insert(C.val.end(), tval[t].begin(), tval[t].end());
+  for (int t = 0; t < nt; ++t)
     for (int len : tlen[t]) {
       C.ptr[r + 1] = C.ptr[r] + len;
       ++r;
     }
-  }
+  concat_parallel(tcol, C.col);
+  concat_parallel(tval, C.val);
   return C;
 }
 
 static std::vector<double> diag_of(const HostCSR& A) {
   std::vector<double> d(A.n_rows, 0.0);
-  for (int r = 0; r < A.n_rows; ++r)
-    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
-      if (A.col[k] == r) d[r] = A.val[k];
+  parallel_chunks(A.n_rows, setup_threads(A.n_rows), [&](int, int64_t r0, int64_t r1) {
+    for (int64_t r = r0; r < r1; ++r)
+      for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k)
+        if (A.col[k] == r) d[r] = A.val[k];
+  });
   return d;
 }
 
 static std::vector<double> spai0_of(const HostCSR& A, const std::vector<double>& d) {
   std::vector<double> s(A.n_rows);
-  for (int r = 0; r < A.n_rows; ++r) {
-    double ss = 0.0;
-    for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) ss += A.val[k] * A.val[k];
-    s[r] = d[r] / (ss + 1e-30);
-  }
+  parallel_chunks(A.n_rows, setup_threads(A.n_rows), [&](int, int64_t r0, int64_t r1) {
+    for (int64_t r = r0; r < r1; ++r) {
+      double ss = 0.0;
+      for (int k = A.ptr[r]; k < A.ptr[r + 1]; ++k) ss += A.val[k] * A.val[k];
+      s[r] = d[r] / (ss + 1e-30);
+    }
+  });
   return s;
 }
 
@@ -582,14 +620,16 @@ void assemble_magnetoelastic(EnergyOp& op, int N, int E, const int* conn, const 
 
 std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
   std::vector<AmgLevel> levels;
-  HostCSR Acur = A0;
+  levels.reserve(prm.max_levels);
+  HostCSR next = A0;
   double theta = prm.theta0;
   while (true) {
-    AmgLevel L;
-    L.A = Acur;
+    levels.emplace_back();
+    AmgLevel& L = levels.back();
+    L.A = std::move(next);
+    const HostCSR& Acur = L.A;
     L.diag = diag_of(Acur);
     L.spai0 = spai0_of(Acur, L.diag);
-    levels.push_back(L);
     int n = Acur.n_rows;
     if (n <= prm.max_coarse || (int)levels.size() >= prm.max_levels) break;
     int nagg = 0;
@@ -647,11 +687,10 @@ std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
     }
     HostCSR R = transpose(P);
     HostCSR RA = spgemm(R, Acur);
-    HostCSR Ac = spgemm(RA, P);
-    levels.back().P = P;
-    levels.back().R = R;
-    levels.back().agg = agg;
-    Acur = Ac;
+    next = spgemm(RA, P);
+    L.P = std::move(P);
+    L.R = std::move(R);
+    L.agg = std::move(agg);
     theta *= 0.5;
   }
   return levels;

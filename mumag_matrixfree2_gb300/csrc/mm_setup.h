@@ -3,14 +3,41 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 namespace mm {
 
+// Allocator whose resize() leaves new elements uninitialised: the large setup arrays are then first
+// written (and their pages first touched) by the threads that fill them, in parallel.
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <class U>
+  UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <class U, class... Args>
+  void construct(U* p, Args&&... args) {
+    ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+  }
+};
+using dvec = std::vector<double, UninitAlloc<double>>;
+using ivec = std::vector<int, UninitAlloc<int>>;
+
 struct HostCSR {
   int n_rows = 0, n_cols = 0;
-  std::vector<int> ptr, col;
-  std::vector<double> val;
+  std::vector<int> ptr;
+  ivec col;
+  dvec val;
   int64_t nnz() const { return ptr.empty() ? 0 : ptr.back(); }
 };
 
@@ -23,14 +50,15 @@ struct HostCSR {
 //   D   = sum_e Js_e Ve / 4 * grad(phi_a)                            (demag source, b_a += D . m_b)
 struct EnergyOp {
   int n_rows = 0;
-  std::vector<int> rows, ptr, col, mat;
-  std::vector<double> w, q, gx, gy, gz, dx, dy, dz;
+  std::vector<int> rows, ptr;
+  ivec col, mat;
+  dvec w, q, gx, gy, gz, dx, dy, dz;
   int n_mat = 0;
   bool single_axis = true;
   std::vector<double> diag_exchange;  // w_aa per node (N)
   // magnetoelastic entries (empty when the term is absent): sum_e 2 (k1me +- k1me_p) Ve / 20 (1 + d_ab),
   // acting on the x (mx) and y (my) components
-  std::vector<double> mx, my;
+  dvec mx, my;
 };
 
 struct AmgLevel {

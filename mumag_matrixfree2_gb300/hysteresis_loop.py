@@ -14,6 +14,7 @@ from typing import Any
 
 import numpy as np
 
+from .cuda_backend import problem_for_geom
 from .minimizers import make_minimizer
 from .poisson_solve import make_solve_U
 from .synthetic import field_values
@@ -148,9 +149,12 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     h = np.array([float(x) for x in params.h_dir.split(",")]) if isinstance(params.h_dir, str) else \
         np.asarray(params.h_dir, np.float64)
     h = h / (np.linalg.norm(h) + 1e-30)
+    # one device problem for the solver and the minimizer: the energy operator and the hierarchy are
+    # built once (make_minimizer finds this problem in the geometry's cache)
+    prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask)
     solve_U = make_solve_U(geom, Js_lookup, precond_type=precond_type, cg_maxiter=params.cg_maxiter,
                            cg_tol=params.cg_tol, poisson_reg=params.poisson_reg, boundary_mask=boundary_mask,
-                           mode=mode, precision=precision)
+                           mode=mode, precision=precision, problem=prob)
     minimize = make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, node_volumes, M_nodal,
                               solve_U, params.cg_tol, method=params.method, memory=params.memory,
                               boundary_mask=boundary_mask, B_bias=B_bias)
