@@ -1,8 +1,8 @@
 """Field sweep with the reference's interface (``src/hysteresis_loop.py:34-657``) on the GPU backend.
 
 Every field step is one ``minimize`` call that runs entirely in libmumag_cuda; the host computes the
-volume-averaged polarisation and writes the reference's CSV and .mh formats.  VTU snapshots are
-I/O outside the hot path and are not written here.
+volume-averaged polarisation and writes the reference's CSV, .mh and VTU snapshot files
+(``io_utils``) with the reference's snapshot rule (``:585-640``).
 """
 
 from __future__ import annotations
@@ -14,6 +14,7 @@ from typing import Any
 
 import numpy as np
 
+from . import io_utils
 from .cuda_backend import problem_for_geom
 from .minimizers import make_minimizer
 from .poisson_solve import make_solve_U
@@ -145,7 +146,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     csv_path = out_dir / params.csv_name
     if write_files:
         out_dir.mkdir(parents=True, exist_ok=True)
-        csv_path.write_text("config,B_ext_T,J_par_T,E,gnorm\n", encoding="utf-8")
+        io_utils.write_hysteresis_header(csv_path)
     h = np.array([float(x) for x in params.h_dir.split(",")]) if isinstance(params.h_dir, str) else \
         np.asarray(params.h_dir, np.float64)
     h = h / (np.linalg.norm(h) + 1e-30)
@@ -187,13 +188,25 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
         total["preco"] += info["preco_iters"]
         total["evals"] += info["evals"]
         total["demag"] += info["demag_iters"]
-        if J_last is None or (params.mstep is not None and abs(J - J_last) >= params.mstep):
+        # a state is saved on the first step, then when J moved by mstep or, without mstep, every
+        # snapshot_every steps; each save after the first starts a new configuration index
+        if J_last is None:
+            save = True
+        elif params.mstep is not None:
+            save = abs(J - J_last) >= params.mstep
+        else:
+            save = params.snapshot_every > 0 and step_idx % params.snapshot_every == 0
+        if save:
             if J_last is not None:
                 config_idx += 1
             J_last = J
+            if write_files and params.snapshot_every > 0:
+                io_utils.write_vtu_tetra(out_dir / io_utils.snapshot_name(config_idx, B_t), points,
+                                         np.asarray(geom.conn), point_data={"m": m.astype(np.float32),
+                                                                            "U": U.astype(np.float32)},
+                                         cell_data={"mat_id": np.asarray(geom.mat_id).astype(np.int32)})
         if write_files:
-            with csv_path.open("a", encoding="utf-8") as f:
-                f.write(f"{config_idx},{B_t:.9e},{J_t:.9e},{info['E']:.9e},{info['gnorm']:.9e}\n")
+            io_utils.append_hysteresis_row(csv_path, config_idx, B_t, J_t, float(info["E"]), float(info["gnorm"]))
         print(f"step {step_idx:05d}  B={B_t:+.6e} T  J_par={J_t:+.6e} T  E={info['E']:.6e}  t={dt:.3f}s  "
               f"it={info['iters']}  t/it={dt / max(1, info['iters']):.3e}s  nf={info['evals']}  "
               f"icg_amg={info['demag_iters']}")
@@ -205,8 +218,6 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
           f"Total Poisson (demag) iterations: {total['demag']}")
     hist = np.array(history)
     if write_files:
-        with open(out_dir / "hysteresis.mh", "w") as f:
-            f.write("# B_ext [T]  J_parallel [T]  mx  my  mz  E [J/m^3] \n")
-            np.savetxt(f, hist, fmt="%.9e")
+        io_utils.write_mh(out_dir / "hysteresis", hist)
     return {"out_dir": str(out_dir), "csv_path": str(csv_path), "last_m": m, "last_U": U, "history": hist,
             "steps": steps, "totals": total}

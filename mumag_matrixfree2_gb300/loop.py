@@ -154,6 +154,7 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--no-phi-extrapolate", action="store_false", dest="phi_extrapolate")
     ap.add_argument("--m0-dir", type=str, default="0,0,1")
     ap.add_argument("--out-dir", default="hyst_out")
+    ap.add_argument("--snapshot-every", type=int, default=1, help="VTU snapshot every N steps (0: none)")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="demag solve precision of this backend (mixed: FP32 inside FP64 refinement)")
@@ -228,7 +229,8 @@ def main(argv=None) -> dict:
     for key in ("B_start", "B_end", "dB", "mfinal", "mstep"):  # Tesla -> reduced units
         if prm[key] is not None:
             prm[key] = prm[key] / Js_ref
-    params = LoopParams(**prm, out_dir=args.out_dir, verbose=args.verbose, Js_ref=Js_ref)
+    params = LoopParams(**prm, out_dir=args.out_dir, verbose=args.verbose, Js_ref=Js_ref,
+                        snapshot_every=args.snapshot_every)
     m0 = np.tile(m0_dir / np.linalg.norm(m0_dir), (s.N, 1))
     B_bias = bias_field(s.knt, s.geom.conn, s.geom.mat_id, params.bias_type, params.bias_strength)
     return run_hysteresis_loop(knt, s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, m0, params, s.V_mag,

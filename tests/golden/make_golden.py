@@ -10,7 +10,10 @@ from the reference, which import with numpy/scipy only, and stores their outputs
 * ``grid_box_*.npz``: ``mesh_backend_grid_box`` for three boxes (knt, ijk); the 20 nm box also
   records whether it equals the reference's test mesh ``tests/single_solid.npz``;
 * ``morton_*.npz``: ``reorder_mesh(..., target="gpu")`` of a graded box mesh and of a grid box
-  (knt, ijk, node_perm, inv_node_perm) together with the input mesh.
+  (knt, ijk, node_perm, inv_node_perm) together with the input mesh;
+* ``io_state.vtu``, ``io_records.mh``, ``io_hysteresis.csv`` and their inputs ``io_inputs.npz``: the
+  reference's ``src/io_utils.py`` writers (VTU snapshot with float32 m and U and int32 mat_id, the
+  .mh history, the CSV header and rows) on seeded data.
 """
 
 import sys
@@ -25,6 +28,7 @@ sys.path.insert(0, str(HERE.parent.parent))
 
 def main(ref_root: str) -> None:
     sys.path.insert(0, str(Path(ref_root) / "src"))
+    import io_utils as ref_io  # noqa: E402
     import mesh as ref_mesh  # noqa: E402
     import reorder_mesh as ref_reorder  # noqa: E402
 
@@ -57,6 +61,26 @@ def main(ref_root: str) -> None:
             np.savez_compressed(HERE / name, knt_in=knt, ijk_in=ijk, knt=out["knt"], ijk=out["ijk"],
                                 node_perm=out["node_perm"], inv_node_perm=out["inv_node_perm"])
         print("wrote", name)
+
+    rng = np.random.default_rng(7)
+    knt, ijk = ref_mesh.mesh_backend_grid_box((8.0, 6.0, 4.0), ex, ey, ez, 2.0, False)
+    m = rng.standard_normal((knt.shape[0], 3))
+    m /= np.linalg.norm(m, axis=1, keepdims=True)
+    U = rng.standard_normal(knt.shape[0])
+    mat_id = rng.integers(1, 3, ijk.shape[0]).astype(np.int32)
+    records = rng.standard_normal((7, 6))
+    rows = [(i, float(rng.standard_normal()), float(rng.standard_normal()), float(rng.standard_normal()),
+             float(abs(rng.standard_normal()))) for i in range(4)]
+    np.savez_compressed(HERE / "io_inputs.npz", knt=knt, conn=ijk[:, :4], m=m, U=U, mat_id=mat_id, records=records,
+                        rows=np.array(rows))
+    ref_io.write_vtu_tetra(HERE / "io_state.vtu", knt, ijk[:, :4],
+                           point_data={"m": m.astype(np.float32), "U": U.astype(np.float32)},
+                           cell_data={"mat_id": mat_id})
+    ref_io.write_mh(HERE / "io_records", records)
+    ref_io.write_hysteresis_header(HERE / "io_hysteresis.csv")
+    for r in rows:
+        ref_io.append_hysteresis_row(HERE / "io_hysteresis.csv", int(r[0]), r[1], r[2], r[3], r[4])
+    print("wrote io_state.vtu, io_records.mh, io_hysteresis.csv")
 
 
 if __name__ == "__main__":

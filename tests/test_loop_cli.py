@@ -87,3 +87,8 @@ def test_cli_loop_equals_direct_loop(cuda_ok, tmp_path):
                               boundary_mask=s.boundary_mask)
     assert res["history"].shape == ref["history"].shape == (5, 6)
     assert np.allclose(res["history"], ref["history"], rtol=1e-12, atol=1e-12)
+    # without mstep every step is a saved configuration: one VTU snapshot each, config = step
+    snaps = sorted((tmp_path / "out").glob("state_cfg*.vtu"))
+    assert len(snaps) == 5 and snaps[0].name.startswith("state_cfg00000_B+4.0000e+00T")
+    cfg = np.loadtxt(tmp_path / "out" / "hysteresis.csv", delimiter=",", skiprows=1)[:, 0]
+    assert np.array_equal(cfg, np.arange(5))
