@@ -173,6 +173,7 @@ def _explicit(ap, argv) -> set:
 def main(argv=None) -> dict:
     from . import fem_utils
     from .hysteresis_loop import LoopParams, run_hysteresis_loop
+    from .io_utils import write_mh
 
     argv = list(sys.argv[1:] if argv is None else argv)
     ap = parser()
@@ -233,9 +234,19 @@ def main(argv=None) -> dict:
                         snapshot_every=args.snapshot_every)
     m0 = np.tile(m0_dir / np.linalg.norm(m0_dir), (s.N, 1))
     B_bias = bias_field(s.knt, s.geom.conn, s.geom.mat_id, params.bias_type, params.bias_strength)
-    return run_hysteresis_loop(knt, s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, m0, params, s.V_mag,
-                               s.node_volumes, s.M_nodal, B_bias=B_bias, boundary_mask=s.boundary_mask,
-                               precond_type=args.precond_type, mode=args.operator_mode, precision=args.precision)
+    res = run_hysteresis_loop(knt, s.geom, s.A_lookup, s.K1_lookup, s.Js_lookup, s.k_easy, m0, params, s.V_mag,
+                              s.node_volumes, s.M_nodal, B_bias=B_bias, boundary_mask=s.boundary_mask,
+                              precond_type=args.precond_type, mode=args.operator_mode, precision=args.precision)
+    # the mammos-mumag history file is named after the model (src/loop.py:1248-1251)
+    mh_name = Path(args.modelname).name if args.modelname else "hysteresis"
+    write_mh(Path(args.out_dir) / mh_name, res["history"])
+    print(f"[ok] Wrote mammos-mumag compatibility file: {Path(args.out_dir) / mh_name}.mh")
+    try:
+        import mammos_entity  # noqa: F401
+    except ImportError:
+        # src/io_utils.py:271-300 skips the mammos_entity CSV the same way when the package is absent
+        print("[warning] mammos_entity not found, skipping CSV conversion")
+    return res
 
 
 if __name__ == "__main__":

@@ -75,6 +75,7 @@ def test_cli_loop_equals_direct_loop(cuda_ok, tmp_path):
     base = _model(tmp_path)
     res = cli.main([str(base), "--out-dir", str(tmp_path / "out"), "--eps-a", "1e-6"])
     assert (tmp_path / "out" / "hysteresis.csv").exists() and (tmp_path / "out" / "hysteresis.mh").exists()
+    assert (tmp_path / "out" / "cube.mh").read_text() == (tmp_path / "out" / "hysteresis.mh").read_text()
     # the same loop called directly: CLI value for eps_a wins over the .p2 file
     knt, ijk = syn.box_mesh(syn.WORKLOADS["cube8_h2_air24"])
     A, K1, Js, k, Js_ref = syn.reduced_materials(
