@@ -576,7 +576,10 @@ def run_ours(a):
                        "level_sizes": [int(x["A"].shape[0]) for x in lv],
                        "pcg_iters_per_solve": its[0], "rel_res": max(rrs), "setup_s": setup_s,
                        "autotune": {"seconds": tune_s, "operators_tuned": len(tune["operators"]),
-                                    "coarse_fuse": tune["coarse_fuse"]["chosen"]},
+                                    "coarse_fuse": tune["coarse_fuse"]["chosen"],
+                                    "shapes": {f"{o['op']}{o['level']}_{o['precision']}":
+                                               ("sell" if o["tpr"] == 1 else f"csr{o['tpr']}")
+                                               for o in tune["operators"]}},
                        "l2": "256 MiB buffer written between timed solves (outside the solve events)",
                        "timing": "sum of per-solve CUDA events on the problem's stream ("
                                  + ("host-polled PCG loop)" if a.no_graph else "CUDA-graph PCG loop)"),

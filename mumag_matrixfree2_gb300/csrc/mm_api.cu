@@ -231,6 +231,9 @@ struct mm_problem {
     std::vector<T> t(v.begin(), v.end());
     return upload(t);
   }
+  // Compressed rows get the sliced-ELL copy as well (both are small below 64Ki rows), so that the
+  // autotuner can also try one thread per row: no shuffle reductions, whose FP64 adds take a third
+  // of the FP64 pipe in the lanes-per-row kernels.
   template <class T>
   DevMatT<T> upload_mat(const mm::HostCSR& A, bool force_sell = false) {
     const int tpr = force_sell ? 1 : choose_tpr(A.n_rows, A.nnz());
@@ -242,10 +245,14 @@ struct mm_problem {
       d.c.ptr = upload(A.ptr);
       d.c.col = upload(A.col);
       d.c.val = upload_as<T>(A.val);
-      d.s.n = A.n_rows;
       d.stored = A.nnz();
-      return d;
     }
+    upload_sell<T>(A, d);
+    return d;
+  }
+  // sliced ELL (mmk::SellT): slices of 32 rows, entries paired, padding with value 0 and a valid column
+  template <class T>
+  void upload_sell(const mm::HostCSR& A, DevMatT<T>& d) {
     const int n = A.n_rows;
     const int ns = (n + 31) / 32;
     std::vector<int> sptr(ns + 1, 0);
@@ -277,8 +284,7 @@ struct mm_problem {
     d.s.sptr = upload(sptr);
     d.s.col = upload(col);
     d.s.val = upload_as<T>(val);
-    d.stored = sptr[ns];
-    return d;
+    if (d.tpr == 1) d.stored = sptr[ns];
   }
   double red(int slot) {
     CK(cudaMemcpyAsync(&h_sc->red[slot], &d_sc->red[slot], sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -2553,12 +2559,12 @@ float time_ms(mm_problem* h, int reps, const std::function<void()>& f) {
 // operator timed alone, L2-hot, prefers fewer lanes than it should), and the fastest is kept.
 template <class T>
 void tune_csr(mm_problem* h, SolverT<T>& S, DevMatT<T>& M, int reps, const char* tag, int level, std::string& rep) {
-  if (M.tpr == 1 || M.c.n == 0) return;
+  if (M.c.n == 0) return;  // sliced ELL only (level 0)
   const int before = M.tpr;
   int best = before;
   float best_ms = 1e30f, before_ms = 1e30f;
   std::string times;
-  for (int t : {2, 4, 8, 16, 32}) {
+  for (int t : {1, 2, 4, 8, 16, 32}) {
     M.tpr = t;
     const float ms = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
     times += (times.empty() ? "" : ",") + std::to_string(1e3 * ms);
