@@ -208,6 +208,10 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
  * Used to apply a predicted potential change (the learned warm start) before a solve.  No counterpart
  * in the reference.  alpha may be NULL. */
 int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const double* d_c, double* alpha);
+/* The same correction queued on the problem's stream after the work already queued on `after` (a
+ * cudaStream_t, e.g. the network's from mm_unet_predict_dev; NULL = the legacy default stream), with
+ * alpha computed and applied on the device: no host wait, so the next solve follows directly. */
+int mm_scale_correction_async(mm_problem* h, void* after, const double* d_m, double* d_U, const double* d_c);
 
 /* Override the node weights of the minimizers (default: inv_M_rel = V_mag / M_nodal where
  * M_nodal > 1e-20 else 0; inv_M_prec = 1/d where d > 1e-20 else 1, d the exchange diagonal,
@@ -371,6 +375,16 @@ int mm_unet_interp_add_dev(mm_unet* u, int sample, int n, const int* d_node, con
 int mm_unet_tensor_info(int which, int* level, int* channels);
 int mm_unet_read_tensor(mm_unet* u, int which, int grad, int sample, float* out);
 int mm_unet_sync(mm_unet* u);
+/* The in-solve prediction without a host wait (no counterpart in the reference): the network's stream
+ * first waits for the work queued on `after` (a cudaStream_t; NULL = the legacy default stream), then
+ * voxelises (f3a - f3b, f1) into sample 0 as mm_unet_voxelise_dev does (f3b may be NULL), runs the
+ * forward graph, zeroes d_out[0..n_out) and adds the prediction at the grid's nodes as
+ * mm_unet_interp_add_dev does.  *stream_out (may be NULL) receives the network's stream so that a
+ * consumer can queue after it; convolution errors are reported by the next waiting call. */
+int mm_unet_predict_dev(mm_unet* u, void* after, int sample, int n_vox, const int* d_idx4, const float* d_w4,
+                        const double* d_f3a, const double* d_f3b, const double* d_f1, double scale3, double scale1,
+                        int n, const int* d_node, const int* d_idx8, const float* d_w8, double scale, int n_out,
+                        double* d_out, void** stream_out);
 
 /* Wait for the problem's stream. */
 int mm_sync(mm_problem* h);

@@ -85,6 +85,7 @@ SIGNATURES = {
     "mm_solve_u_dev": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _ip, _dp]),
     "mm_set_node_weights": (C.c_int, [_vp, _dp, _dp]),
     "mm_set_bias_field": (C.c_int, [_vp, _dp]),
+    "mm_scale_correction_async": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "mm_scale_correction_dev": (C.c_int, [_vp, _vp, _vp, _vp, _dp]),
     "mm_set_magnetoelastic": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
@@ -116,6 +117,8 @@ SIGNATURES = {
     "mm_unet_tensor_info": (C.c_int, [C.c_int, _ip, _ip]),
     "mm_unet_read_tensor": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
     "mm_unet_sync": (C.c_int, [_vp]),
+    "mm_unet_predict_dev": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
+                                      C.c_int, _vp, _vp, _vp, C.c_double, C.c_int, _vp, C.POINTER(_vp)]),
 }
 
 _lib = None

@@ -211,6 +211,7 @@ struct mm_problem {
   std::vector<double*> w_S, w_Y;
   double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
   double* min_bias_buf = nullptr;  // its storage
+  cudaEvent_t ev_after = nullptr;  // ordering point taken on another stream (mm_scale_correction_async)
 
   template <class T>
   T* alloc(size_t n) {
@@ -2201,6 +2202,7 @@ int mm_destroy(mm_problem* h) {
   if (h->s32.h_bar) cudaFreeHost(h->s32.h_bar);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->ev_after) cudaEventDestroy(h->ev_after);
   for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -2409,6 +2411,26 @@ int mm_scale_correction_dev(mm_problem* h, const double* d_m, double* d_U, const
     LAUNCH_CHECK();
     h->sync();
     if (alpha) *alpha = a;
+    return MM_OK;
+  });
+}
+
+int mm_scale_correction_async(mm_problem* h, void* after, const double* d_m, double* d_U, const double* d_c) {
+  if (!h || !d_m || !d_U || !d_c) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    const int N = h->N;
+    const auto& A0 = h->s64.lv[0].A;
+    if (!h->ev_after) CK(cudaEventCreateWithFlags(&h->ev_after, cudaEventDisableTiming));
+    CK(cudaEventRecord(h->ev_after, (cudaStream_t)after));
+    CK(cudaStreamWaitEvent(h->st, h->ev_after, 0));
+    enqueue_rhs(h, d_m);                                                      // d_b = D m
+    spmv<0, double>(h, A0, d_U, nullptr, nullptr, h->d_out, nullptr);         // A U
+    spmv<0, double>(h, A0, d_c, nullptr, nullptr, h->d_r64, nullptr);         // A c
+    mmk::k_corr_dots<<<grid_elem(N), BS, 0, h->st>>>(N, d_c, h->d_b, h->d_out, h->d_r64, h->d_sc, h->d_part);
+    LAUNCH_CHECK();
+    mmk::k_axpy_ratio<<<grid_elem(N), BS, 0, h->st>>>(N, d_c, d_U, h->d_sc);
+    LAUNCH_CHECK();
     return MM_OK;
   });
 }

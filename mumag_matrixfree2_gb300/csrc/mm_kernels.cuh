@@ -1250,4 +1250,14 @@ __global__ void __launch_bounds__(BS) k_hess_full(int N, const double* __restric
   grid_reduce(s, 0.0, sc, part, R_C);
 }
 
+// y += a x with a = red[R_A] / red[R_B] (0 unless the denominator is positive and finite), the
+// scaling computed on the device; a -> red[R_C]
+__global__ void __launch_bounds__(BS) k_axpy_ratio(int n, const double* __restrict__ x, double* __restrict__ y,
+                                                   Scalars* sc) {
+  const double num = sc->red[R_A], den = sc->red[R_B];
+  const double a = (den > 0.0 && isfinite(den)) ? num / den : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc->red[R_C] = a;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * x[i] + y[i];
+}
+
 }  // namespace mmk

@@ -598,8 +598,9 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, size_t n, f
 // mesh -> grid: channel c of voxel v = sum_k w[v][k] f_c(node idx[v][k]) * scale_c (4 nodes; idx < 0
 // ends the list), written as chunk 0 of sample `sample` (channels 0..2 from a (N,3) field, 3 from a
 // scalar field)
-__global__ void k_voxelise(const int* idx, const float* w, int nv, const double* f3, const double* f1, double s3,
-                           double s1, Vol v, uint4* x, int sample) {
+// f3b (may be null) is subtracted from f3 node by node (the state change m_new - m_old)
+__global__ void k_voxelise(const int* idx, const float* w, int nv, const double* f3, const double* f3b,
+                           const double* f1, double s3, double s1, Vol v, uint4* x, int sample) {
   const int G = v.G;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
     double acc[4] = {0, 0, 0, 0};
@@ -608,9 +609,10 @@ __global__ void k_voxelise(const int* idx, const float* w, int nv, const double*
       const int nd = idx[4 * i + k];
       if (nd >= 0) {
         const double wk = w[4 * i + k];
-        acc[0] += wk * f3[3 * (size_t)nd];
-        acc[1] += wk * f3[3 * (size_t)nd + 1];
-        acc[2] += wk * f3[3 * (size_t)nd + 2];
+        const size_t o = 3 * (size_t)nd;
+        acc[0] += wk * (f3b ? f3[o] - f3b[o] : f3[o]);
+        acc[1] += wk * (f3b ? f3[o + 1] - f3b[o + 1] : f3[o + 1]);
+        acc[2] += wk * (f3b ? f3[o + 2] - f3b[o + 2] : f3[o + 2]);
         acc[3] += wk * f1[nd];
       }
     }
@@ -740,6 +742,7 @@ struct mm_unet {
   int nb_fwd = 0;              // samples of the last forward
   cudaGraphExec_t fwd_exec[8] = {};   // captured forward passes (batch sizes 1..8), on the in-place input
   bool fwd_warm = false;              // one forward has run (kernel attributes set) before any capture
+  cudaEvent_t ev_after = nullptr;     // ordering point taken on a caller's stream (mm_unet_predict_dev)
   std::vector<std::pair<const void*, size_t>> attr_done;
   bool train_bias = true;      // false: bias gradients are zero (biases stay as set)
 
@@ -1057,6 +1060,7 @@ int mm_unet_destroy(mm_unet* u) {
     if (e) cudaGraphExecDestroy(e);
   for (void* q : u->allocs) cudaFree(q);
   if (u->h_lpart) cudaFreeHost(u->h_lpart);
+  if (u->ev_after) cudaEventDestroy(u->ev_after);
   if (u->st) cudaStreamDestroy(u->st);
   delete u;
   return MM_OK;
@@ -1119,29 +1123,34 @@ int mm_unet_forward(mm_unet* u, const float* x, int nb, float* y) {
   });
 }
 
+// The forward on the in-place input as one CUDA graph (captured at the second call for each batch
+// size), without a wait; errors are reported by the next call that waits.
+static void forward_graph(mm_unet* u, int nb) {
+  if (!u->fwd_warm) {
+    u->forward(nb);
+    u->check_err();
+    u->fwd_warm = true;
+    return;
+  }
+  if (!u->fwd_exec[nb - 1]) {
+    cudaGraph_t g = nullptr;
+    UCK(cudaStreamBeginCapture(u->st, cudaStreamCaptureModeThreadLocal));
+    u->forward(nb);
+    UCK(cudaStreamEndCapture(u->st, &g));
+    UCK(cudaGraphInstantiate(&u->fwd_exec[nb - 1], g, 0));
+    cudaGraphDestroy(g);
+  }
+  UCK(cudaGraphLaunch(u->fwd_exec[nb - 1], u->st));
+  u->nb_fwd = nb;
+}
+
 int mm_unet_forward_dev(mm_unet* u, const float* d_x, int nb, float* d_y) {
   if (!u || nb < 1 || nb > u->B) return MM_ERR_ARG;
   return uguard(u, [&] {
     const size_t nv = (size_t)nb * u->G * u->G * u->G;
     if (!d_x && !d_y && nb <= 8) {
-      // in-place input, output left in the network: a CUDA graph of the whole forward, no wait here
-      // (errors are reported by the next call that waits, mm_unet_interp_add_dev or mm_unet_sync)
-      if (!u->fwd_warm) {
-        u->forward(nb);
-        u->check_err();
-        u->fwd_warm = true;
-        return MM_OK;
-      }
-      if (!u->fwd_exec[nb - 1]) {
-        cudaGraph_t g = nullptr;
-        UCK(cudaStreamBeginCapture(u->st, cudaStreamCaptureModeThreadLocal));
-        u->forward(nb);
-        UCK(cudaStreamEndCapture(u->st, &g));
-        UCK(cudaGraphInstantiate(&u->fwd_exec[nb - 1], g, 0));
-        cudaGraphDestroy(g);
-      }
-      UCK(cudaGraphLaunch(u->fwd_exec[nb - 1], u->st));
-      u->nb_fwd = nb;
+      // in-place input, output left in the network (errors: mm_unet_interp_add_dev or mm_unet_sync)
+      forward_graph(u, nb);
       return MM_OK;
     }
     if (d_x) {
@@ -1197,8 +1206,8 @@ int mm_unet_voxelise_dev(mm_unet* u, int sample, int n_vox, const int* d_idx4, c
   if (!u || sample < 0 || sample >= u->B || n_vox != u->G * u->G * u->G || !d_idx4 || !d_w4 || !d_f3 || !d_f1)
     return MM_ERR_ARG;
   return uguard(u, [&] {
-    mmn::k_voxelise<<<grid1d(n_vox), 256, 0, u->st>>>(d_idx4, d_w4, n_vox, d_f3, d_f1, scale3, scale1, u->vol[0],
-                                                       u->T[T_X], sample);
+    mmn::k_voxelise<<<grid1d(n_vox), 256, 0, u->st>>>(d_idx4, d_w4, n_vox, d_f3, nullptr, d_f1, scale3, scale1,
+                                                       u->vol[0], u->T[T_X], sample);
     UCK(cudaGetLastError());
     return MM_OK;
   });
@@ -1240,6 +1249,32 @@ int mm_unet_read_tensor(mm_unet* u, int which, int grad, int sample, float* out)
     UCK(cudaStreamSynchronize(u->st));
     UCK(cudaFree(d));
     u->allocs.pop_back();
+    return MM_OK;
+  });
+}
+
+int mm_unet_predict_dev(mm_unet* u, void* after, int sample, int n_vox, const int* d_idx4, const float* d_w4,
+                        const double* d_f3a, const double* d_f3b, const double* d_f1, double scale3, double scale1,
+                        int n, const int* d_node, const int* d_idx8, const float* d_w8, double scale, int n_out,
+                        double* d_out, void** stream_out) {
+  if (!u || sample != 0 || n_vox != u->G * u->G * u->G || !d_idx4 || !d_w4 || !d_f3a || !d_f1 || n < 0 ||
+      n_out < 0 || (n > 0 && (!d_node || !d_idx8 || !d_w8)) || (n_out > 0 && !d_out))
+    return MM_ERR_ARG;
+  return uguard(u, [&] {
+    if (!u->ev_after) UCK(cudaEventCreateWithFlags(&u->ev_after, cudaEventDisableTiming));
+    UCK(cudaEventRecord(u->ev_after, (cudaStream_t)after));
+    UCK(cudaStreamWaitEvent(u->st, u->ev_after, 0));
+    mmn::k_voxelise<<<grid1d(n_vox), 256, 0, u->st>>>(d_idx4, d_w4, n_vox, d_f3a, d_f3b, d_f1, scale3, scale1,
+                                                       u->vol[0], u->T[T_X], 0);
+    UCK(cudaGetLastError());
+    forward_graph(u, 1);
+    if (n_out > 0) UCK(cudaMemsetAsync(d_out, 0, (size_t)n_out * sizeof(double), u->st));
+    if (n > 0) {
+      mmn::k_interp_add<<<grid1d(n), 256, 0, u->st>>>(d_node, d_idx8, d_w8, n, u->T[T_OUT], u->vol[0], 2, 0, scale,
+                                                        d_out);
+      UCK(cudaGetLastError());
+    }
+    if (stream_out) *stream_out = (void*)u->st;
     return MM_OK;
   });
 }

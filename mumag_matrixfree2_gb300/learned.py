@@ -319,6 +319,7 @@ class WarmStart:
         self._x = torch.zeros((batch, self.V, 4), dtype=torch.float32, device=dev)
         self._t = torch.zeros((batch, self.V), dtype=torch.float32, device=dev)
         self._y = torch.zeros((batch, self.V), dtype=torch.float32, device=dev)
+        self._c = torch.zeros(self.N, dtype=torch.float64, device=dev)  # the nodal prediction (no-wait path)
 
     def _vox(self, f):
         if f.dim() == 1:
@@ -383,13 +384,28 @@ class WarmStart:
         U[self.k_nodes.long()] += (true[self.k_idx8.long()] * self.k_w8.double()).sum(1)
         return U
 
-    def apply(self, m_new, m_old, U, prob=None):
+    def apply(self, m_new, m_old, U, prob=None, wait: bool = True):
         """U += the predicted potential change of m_old -> m_new (CUDA float64 tensors; U in place),
         entirely on the device: voxelise dm and U, run the network, interpolate to the nodes.  With
         the solver's `prob`, the prediction c is added as alpha c with alpha = c.(b - A U) / (c.A c)
         (the multiple that minimises the energy-norm error), so a poor prediction cannot hurt.
-        Returns alpha (1.0 without `prob`)."""
+        Returns alpha (1.0 without `prob`).
+
+        wait=False (with `prob`): the whole chain is queued without a host wait - the network's stream
+        waits for the caller's current stream, the problem's stream for the network's, alpha is
+        computed on the device - so the next solve on `prob` follows directly; returns None."""
         L = _abi.lib()
+        if not wait and prob is not None:
+            vp = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+            st = C.c_void_p()
+            after = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+            self.net._check("mm_unet_predict_dev", L.mm_unet_predict_dev(
+                self.net.h, after, 0, self.V, vp(self.k_idx4), vp(self.k_w4), vp(m_new), vp(m_old), vp(U), 1.0,
+                float(self.c_U), int(self.k_nodes.numel()), vp(self.k_nodes), vp(self.k_idx8), vp(self.k_w8), 1.0,
+                self.N, vp(self._c), C.byref(st)))
+            prob._check("mm_scale_correction_async", L.mm_scale_correction_async(prob.h, st, vp(m_new), vp(U),
+                                                                                  vp(self._c)))
+            return None
         dm = m_new - m_old
         c = self.torch.zeros_like(U)
         self.torch.cuda.current_stream().synchronize()  # dm, U and c are ready before the network's stream reads them

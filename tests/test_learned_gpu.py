@@ -193,3 +193,27 @@ def test_trained_warm_start_saves_pcg_iterations(sweeps):
         base += it0
         learn += it1
     assert learn < base, (learn, base)
+
+
+def test_no_wait_apply_equals_waiting_apply(sweeps):
+    """The queued chain (network stream after the caller's stream, scaled correction on the problem's
+    stream after the network's, alpha on the device) gives the waiting path's corrected U and the same
+    PCG iterations; the correction's alpha is the one the waiting path returns."""
+    prob, ws, train, pairs, ev, nodal = sweeps
+    for k in (3, 9):
+        (ma, Ua), (mb, _) = nodal[k], nodal[k + 1]
+        x1 = Ua.clone()
+        a1 = ws.apply(mb, ma, x1, prob)
+        x2 = Ua.clone()
+        assert ws.apply(mb, ma, x2, prob, wait=False) is None
+        prob.sync()  # before torch reads x2
+        ws.net.sync()
+        d = (x1 - x2).abs().max().item()
+        assert d <= 1e-12 * max(1.0, x1.abs().max().item()), d
+        # the solve queued right behind the correction on the problem's stream
+        x3 = Ua.clone()
+        ws.apply(mb, ma, x3, prob, wait=False)
+        _, it3, rr3, rc3 = prob.solve_u(mb, x3, 1e-10)
+        _, it1, rr1, rc1 = prob.solve_u(mb, x1, 1e-10)
+        assert rc1 == rc3 == 0 and it1 == it3 and rr3 <= 1e-10
+        assert a1 > 0
