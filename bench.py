@@ -328,6 +328,7 @@ def run_loop(s, m0, precision, dB_T):
     J = hist[:, 1]
     sw = int(np.argmax(J < 0)) if np.any(J < 0) else -1
     return {"loop_s": tot["time"], "wall_with_setup_s": wall, "field_steps": len(hist),
+            "demag_solve_device_s": tot["demag_time"], "demag_solve_host_s": tot["demag_wall_time"],
             "minimizer_iters": tot["iters"], "energy_evals": tot["evals"], "demag_pcg_iters": tot["demag"],
             "preconditioner_iters": tot["preco"], "switch_step": sw, "switch_B_T": float(hist[sw, 0]) if sw >= 0 else None,
             "Hc_T": coercive_field(hist[:, 0], hist[:, 1]), "_J": J}

@@ -82,6 +82,8 @@ typedef struct {
   int iters, evals, preco_iters, demag_iters;
   double E, gnorm, seconds;
   int status;
+  double demag_seconds;       /* device time of the demag solves (CUDA events around each)            */
+  double demag_wall_seconds;  /* host time spent in the demag solve calls (the rest is the minimizer's) */
 } mm_min_info;
 
 /* ---- setup helpers ------------------------------------------------------------------------ */

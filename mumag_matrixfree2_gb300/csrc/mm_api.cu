@@ -170,6 +170,9 @@ struct mm_problem {
   mm::EnergyOp eop_h;
   mmk::EnergyDev eop{};
   int eop_tpr = 8;
+  mmk::EnergySell eops{};          // the energy operator in sliced-ELL order (the kernels' layout)
+  std::vector<int64_t> eops_pos;   // sliced position of every compressed-row entry
+  int64_t eops_stored = 0;
   double* d_Mn = nullptr;
   double* d_inv_M_rel = nullptr;
   double* d_inv_M_prec = nullptr;
@@ -231,6 +234,58 @@ struct mm_problem {
   T* upload_as(const std::vector<double, Alloc>& v) {
     std::vector<T> t(v.begin(), v.end());
     return upload(t);
+  }
+  // a per-entry array of the energy operator in sliced order (padding entries `pad`)
+  template <class T, class V>
+  T* upload_eop_sell(const V& a, T pad) {
+    std::vector<T> out((size_t)eops_stored, pad);
+    for (size_t k = 0; k < eops_pos.size(); ++k) out[eops_pos[k]] = (T)a[k];
+    return upload(out);
+  }
+  // the energy operator's sliced-ELL copy (slices of 32 magnetic rows, width = the slice's longest
+  // row; padding entries: zero values, the row's own node as column)
+  void upload_eop_sell_all() {
+    const mm::EnergyOp& o = eop_h;
+    const int n = o.n_rows, ns = (n + 31) / 32;
+    std::vector<int> sptr(ns + 1, 0);
+    for (int sl = 0; sl < ns; ++sl) {
+      int w = 0;
+      for (int r = 32 * sl; r < std::min(n, 32 * sl + 32); ++r) w = std::max(w, o.ptr[r + 1] - o.ptr[r]);
+      sptr[sl + 1] = sptr[sl] + 32 * w;
+    }
+    eops_stored = sptr[ns];
+    eops_pos.assign(o.col.size(), 0);
+    std::vector<int> col((size_t)eops_stored, 0);
+    for (int r = 0; r < n; ++r) {
+      const int sl = r / 32, l = r % 32, w = (sptr[sl + 1] - sptr[sl]) / 32, len = o.ptr[r + 1] - o.ptr[r];
+      for (int k = 0; k < w; ++k) {
+        const int64_t at = (int64_t)sptr[sl] + 32 * k + l;
+        if (k < len) {
+          eops_pos[o.ptr[r] + k] = at;
+          col[at] = o.col[o.ptr[r] + k];
+        } else {
+          col[at] = o.rows[r];
+        }
+      }
+    }
+    mmk::EnergySell& d = eops;
+    d.n_rows = n;
+    d.rows = eop.rows;
+    d.sptr = upload(sptr);
+    d.col = upload(col);
+    d.mat = upload_eop_sell<int>(o.mat, 0);
+    d.w = upload_eop_sell<double>(o.w, 0.0);
+    d.q = upload_eop_sell<double>(o.q, 0.0);
+    d.gx = upload_eop_sell<double>(o.gx, 0.0);
+    d.gy = upload_eop_sell<double>(o.gy, 0.0);
+    d.gz = upload_eop_sell<double>(o.gz, 0.0);
+    d.dx = upload_eop_sell<double>(o.dx, 0.0);
+    d.dy = upload_eop_sell<double>(o.dy, 0.0);
+    d.dz = upload_eop_sell<double>(o.dz, 0.0);
+    d.kax = eop.kax;
+    d.mex = d.mey = nullptr;
+    d.single_axis = eop.single_axis;
+    d.axis0 = eop.axis0;
   }
   // Compressed rows get the sliced-ELL copy as well (both are small below 64Ki rows), so that the
   // autotuner can also try one thread per row: no shuffle reductions, whose FP64 adds take a third
@@ -786,8 +841,7 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
 void enqueue_rhs(mm_problem* h, const double* m) {
   const int N = h->N;
   if (!h->has_mask) CK(cudaMemsetAsync(h->d_b, 0, N * sizeof(double), h->st));
-  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_rhs<TP><<<g, BS, 0, h->st>>>(h->eop, m, h->d_b)));
+  mmk::k_rhs_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, m, h->d_b);
   LAUNCH_CHECK();
   dot(h, N, h->d_b, nullptr, R_BB0);
 }
@@ -873,17 +927,14 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
 
 double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
                   double* d_g) {
-  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<TP><<<g, BS, 0, h->st>>>(h->eop, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
-                                                                      d_bias, h->inv_Vmag, d_g, h->d_sc,
-                                                                      h->d_part)));
+  mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
+                                                                     d_bias, h->inv_Vmag, d_g, h->d_sc, h->d_part);
   LAUNCH_CHECK();
   return 0.5 * h->red(R_E) * h->inv_Vmag;
 }
 
 void local_grad_dev(mm_problem* h, const double* d_v, double* d_out) {
-  const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_local_grad<TP><<<g, BS, 0, h->st>>>(h->eop, d_v, h->inv_Vmag, d_out)));
+  mmk::k_local_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, d_v, h->inv_Vmag, d_out);
   LAUNCH_CHECK();
 }
 
@@ -919,6 +970,7 @@ struct MinCtx {
   double phi_tol;
   const mm_min_params* prm;
   int demag = 0, evals = 0, preco = 0;
+  double demag_ms = 0.0, demag_wall = 0.0;  // device and host time of the demag solves
 };
 
 void ensure_min_buffers(mm_problem* h, int memory) {
@@ -968,7 +1020,10 @@ int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
   int it = 0;
   double rr = 0.0;
   const int cg_maxiter = c.prm->cg_maxiter > 0 ? c.prm->cg_maxiter : 2000;
+  const auto t0 = std::chrono::steady_clock::now();
   solve_dev(c.h, m, U, tol, cg_maxiter, &it, &rr);
+  c.demag_wall += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  c.demag_ms += c.h->last_solve_ms;
   return it;
 }
 
@@ -991,10 +1046,10 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   double Q = 0.0;
   int it = 0;
   bool done = false;
-  const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
+  const int gP = grid_elem(h->eops.n_rows);
   while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
-    TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, h->w_p3, reg,
-                                                                     h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part, R_C)));
+    mmk::k_apply_P_s<<<gP, BS, 0, h->st>>>(h->eops, m, gext, h->w_p3, reg, h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part,
+                                           R_C);
     LAUNCH_CHECK();
     const double pAp = h->red(R_C);
     const bool neg = pAp <= 0.0;
@@ -1033,9 +1088,8 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
 // out = P v (the extensive local Hessian, src/minimizers.py:396-411); returns v.out
 double apply_P(MinCtx& c, const double* m, const double* gext, const double* v, double reg, double* out) {
   mm_problem* h = c.h;
-  const int gP = grid_rows(h->eop.n_rows, h->eop_tpr);
-  TPR_SWITCH(h->eop_tpr, (mmk::k_apply_P<TP><<<gP, BS, 0, h->st>>>(h->eop, m, gext, v, reg, h->inv_Vmag, out,
-                                                                   h->d_sc, h->d_part, R_C)));
+  mmk::k_apply_P_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, m, gext, v, reg, h->inv_Vmag, out, h->d_sc,
+                                                                 h->d_part, R_C);
   LAUNCH_CHECK();
   return h->red(R_C);
 }
@@ -1700,6 +1754,8 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     info->gnorm = gnorm;
     info->seconds = std::chrono::duration<double>(t1 - t0).count();
     info->status = (it >= prm->max_iter && !conv) ? MM_MAXITER : MM_OK;
+    info->demag_seconds = 1e-3 * c.demag_ms;
+    info->demag_wall_seconds = c.demag_wall;
   }
   return std::isfinite(E) ? MM_OK : MM_NONFINITE;
 }
@@ -2144,6 +2200,7 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     d.single_axis = o.single_axis ? 1 : 0;
     d.axis0 = o.mat.empty() ? 0 : o.mat[0];
     h->eop_tpr = pick_tpr((int64_t)o.col.size(), std::max(1, o.n_rows));
+    h->upload_eop_sell_all();
     h->d_Mn = h->upload(std::vector<double>(M_nodal, M_nodal + N));
     // default node weights (src/hysteresis_loop.py:340-353)
     std::vector<double> imr(N), imp(N), dex(N);
@@ -2381,12 +2438,15 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
   return guarded(h, [&] {
     if (n == 0) {
       h->eop.mex = h->eop.mey = nullptr;
+      h->eops.mex = h->eops.mey = nullptr;
       return MM_OK;
     }
     mm::assemble_magnetoelastic(h->eop_h, h->N, h->E, h->conn.data(), h->volume.data(), h->mat_id.data(), n, k1me,
                                 k1me_p);
     h->eop.mex = h->upload(h->eop_h.mx);
     h->eop.mey = h->upload(h->eop_h.my);
+    h->eops.mex = h->upload_eop_sell<double>(h->eop_h.mx, 0.0);
+    h->eops.mey = h->upload_eop_sell<double>(h->eop_h.my, 0.0);
     h->sync();
     return MM_OK;
   });
@@ -2507,10 +2567,9 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
                                                                 nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
-        const int g = grid_rows(h->eop.n_rows, h->eop_tpr);
-        TPR_SWITCH(h->eop_tpr, (mmk::k_energy_grad<TP><<<g, BS, 0, h->st>>>(h->eop, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
-                                                                            1.0, nullptr, h->inv_Vmag, h->d_g,
-                                                                            h->d_sc, h->d_part)));
+        mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
+                                                                           1.0, nullptr, h->inv_Vmag, h->d_g, h->d_sc,
+                                                                           h->d_part);
         LAUNCH_CHECK();
       } else {
         local_grad_dev(h, h->d_m, h->d_out);

@@ -984,6 +984,180 @@ __global__ void __launch_bounds__(BS) k_rhs(EnergyDev op, const double* __restri
 }
 
 // ------------------------------------------------------------------------------------------
+// The energy operator in sliced-ELL order, one thread per magnetic row.  On this part a warp-wide
+// FP64 instruction costs 16 SM cycles whatever its active lanes, so the lanes-per-row kernels above
+// spend most of their FP64 issue on idle lanes, shuffle reductions and a one-lane epilogue; here
+// every FP64 instruction does useful work for 32 rows and the loads are coalesced across the warp.
+// ------------------------------------------------------------------------------------------
+// Slices of 32 rows: entry k of lane l of slice s at sptr[s] + 32 k + l; padding entries carry zero
+// values and the row's own node as column (the per-node arrays are only read, never indexed out of
+// range).
+struct EnergySell {
+  int n_rows;
+  const int* rows;
+  const int* sptr;
+  const int* col;
+  const int* mat;
+  const double* w;
+  const double* q;
+  const double* gx;
+  const double* gy;
+  const double* gz;
+  const double* dx;
+  const double* dy;
+  const double* dz;
+  const double* kax;
+  const double* mex;  // null: no magnetoelastic term
+  const double* mey;
+  int single_axis;
+  int axis0;
+};
+
+// (exchange + anisotropy + magnetoelastic) v on row r: sum_k w v_j - q (k.v_j) k (+ mex v_j,x, mey v_j,y);
+// with a single easy axis the anisotropy sum is accumulated as a scalar and applied once
+__device__ __forceinline__ void exch_aniso_sell(const EnergySell& op, int r, const double* __restrict__ v,
+                                                double& ax, double& ay, double& az) {
+  const int s = r >> 5, l = r & 31;
+  const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+  ax = ay = az = 0.0;
+  if (op.single_axis) {
+    const double kx = op.kax[3 * op.axis0], ky = op.kax[3 * op.axis0 + 1], kz = op.kax[3 * op.axis0 + 2];
+    double t = 0.0;
+#pragma unroll 3
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const int j = __ldg(op.col + at);
+      const double vx = __ldg(v + 3 * j), vy = __ldg(v + 3 * j + 1), vz = __ldg(v + 3 * j + 2);
+      const double wk = __ldg(op.w + at);
+      ax = fma(wk, vx, ax);
+      ay = fma(wk, vy, ay);
+      az = fma(wk, vz, az);
+      t = fma(__ldg(op.q + at), fma(kz, vz, fma(ky, vy, kx * vx)), t);
+      if (op.mex) {
+        ax = fma(__ldg(op.mex + at), vx, ax);
+        ay = fma(__ldg(op.mey + at), vy, ay);
+      }
+    }
+    ax = fma(-t, kx, ax);
+    ay = fma(-t, ky, ay);
+    az = fma(-t, kz, az);
+  } else {
+#pragma unroll 2
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const int j = __ldg(op.col + at);
+      const int g = __ldg(op.mat + at);
+      const double kx = op.kax[3 * g], ky = op.kax[3 * g + 1], kz = op.kax[3 * g + 2];
+      const double vx = __ldg(v + 3 * j), vy = __ldg(v + 3 * j + 1), vz = __ldg(v + 3 * j + 2);
+      const double wk = __ldg(op.w + at);
+      const double t = -__ldg(op.q + at) * fma(kz, vz, fma(ky, vy, kx * vx));
+      ax = fma(t, kx, fma(wk, vx, ax));
+      ay = fma(t, ky, fma(wk, vy, ay));
+      az = fma(t, kz, fma(wk, vz, az));
+      if (op.mex) {
+        ax = fma(__ldg(op.mex + at), vx, ax);
+        ay = fma(__ldg(op.mey + at), vy, ay);
+      }
+    }
+  }
+}
+
+// as k_energy_grad, sliced layout
+__global__ void __launch_bounds__(BS) k_energy_grad_s(EnergySell op, const double* __restrict__ m,
+                                                      const double* __restrict__ U, const double* __restrict__ Mn,
+                                                      double Bx, double By, double Bz,
+                                                      const double* __restrict__ Bbias, double inv_Vmag,
+                                                      double* __restrict__ g, Scalars* sc, double* part) {
+  double en = 0.0;
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    double ax, ay, az;
+    exch_aniso_sell(op, r, m, ax, ay, az);
+    const int s = r >> 5, l = r & 31;
+    const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+    double ux = 0, uy = 0, uz = 0;
+#pragma unroll 3
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const double u = __ldg(U + __ldg(op.col + at));
+      ux = fma(__ldg(op.gx + at), u, ux);
+      uy = fma(__ldg(op.gy + at), u, uy);
+      uz = fma(__ldg(op.gz + at), u, uz);
+    }
+    const int a = __ldg(op.rows + r);
+    double bx = Bx, by = By, bz = Bz;
+    if (Bbias) {
+      bx += Bbias[3 * a];
+      by += Bbias[3 * a + 1];
+      bz += Bbias[3 * a + 2];
+    }
+    const double mn = -2.0 * Mn[a];
+    const double zx = mn * bx, zy = mn * by, zz = mn * bz;
+    const double gx = (ax + ux) + zx, gy = (ay + uy) + zy, gz = (az + uz) + zz;
+    en += m[3 * a] * (gx + zx) + m[3 * a + 1] * (gy + zy) + m[3 * a + 2] * (gz + zz);
+    g[3 * a] = gx * inv_Vmag;
+    g[3 * a + 1] = gy * inv_Vmag;
+    g[3 * a + 2] = gz * inv_Vmag;
+  }
+  grid_reduce(en, 0.0, sc, part, R_E);
+}
+
+// as k_local_grad, sliced layout
+__global__ void __launch_bounds__(BS) k_local_grad_s(EnergySell op, const double* __restrict__ v, double inv_Vmag,
+                                                     double* __restrict__ out) {
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    double ax, ay, az;
+    exch_aniso_sell(op, r, v, ax, ay, az);
+    const int a = __ldg(op.rows + r);
+    out[3 * a] = ax * inv_Vmag;
+    out[3 * a + 1] = ay * inv_Vmag;
+    out[3 * a + 2] = az * inv_Vmag;
+  }
+}
+
+// as k_apply_P, sliced layout
+__global__ void __launch_bounds__(BS) k_apply_P_s(EnergySell op, const double* __restrict__ m,
+                                                  const double* __restrict__ gext, const double* __restrict__ p,
+                                                  double reg, double inv_Vmag, double* __restrict__ Ap, Scalars* sc,
+                                                  double* part, int slot) {
+  double d = 0.0;
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    double ax, ay, az;
+    exch_aniso_sell(op, r, p, ax, ay, az);
+    const int a = __ldg(op.rows + r);
+    const double cx = ax * inv_Vmag, cy = ay * inv_Vmag, cz = az * inv_Vmag;
+    const double mx = m[3 * a], my = m[3 * a + 1], mz = m[3 * a + 2];
+    const double mc = mx * cx + my * cy + mz * cz;
+    const double mg = mx * gext[3 * a] + my * gext[3 * a + 1] + mz * gext[3 * a + 2];
+    const double px = p[3 * a], py = p[3 * a + 1], pz = p[3 * a + 2];
+    const double ox = cx - mc * mx - mg * px + reg * px;
+    const double oy = cy - mc * my - mg * py + reg * py;
+    const double oz = cz - mc * mz - mg * pz + reg * pz;
+    Ap[3 * a] = ox;
+    Ap[3 * a + 1] = oy;
+    Ap[3 * a + 2] = oz;
+    d += px * ox + py * oy + pz * oz;
+  }
+  grid_reduce(d, 0.0, sc, part, slot);
+}
+
+// as k_rhs, sliced layout: b = D m on the magnetic rows
+__global__ void __launch_bounds__(BS) k_rhs_s(EnergySell op, const double* __restrict__ m, double* __restrict__ b) {
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    const int s = r >> 5, l = r & 31;
+    const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+    double acc = 0.0;
+#pragma unroll 3
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const int j = __ldg(op.col + at);
+      acc += __ldg(op.dx + at) * __ldg(m + 3 * j) + __ldg(op.dy + at) * __ldg(m + 3 * j + 1) +
+             __ldg(op.dz + at) * __ldg(m + 3 * j + 2);
+    }
+    b[__ldg(op.rows + r)] = acc;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // minimizer vector kernels (3-vectors per node, xyz interleaved)
 // ------------------------------------------------------------------------------------------
 // g_tan = P_m(g .* inv_M_rel), g_tan_ext = P_m(g); max |g_tan| -> red[R_MAX]
@@ -1028,17 +1202,19 @@ __global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double k0 = 0.5 * tau * H[3 * i], k1 = 0.5 * tau * H[3 * i + 1], k2 = 0.5 * tau * H[3 * i + 2];
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
+    // FP64 division and square root are long instruction sequences on this part's narrow FP64 pipe:
+    // one reciprocal of (1 + k.k) and one of the norm instead of six divisions
     const double kk = k0 * k0 + k1 * k1 + k2 * k2;
-    const double den = 1.0 + kk;
+    const double iden = 1.0 / (1.0 + kk);
     const double km0 = k1 * m2 - k2 * m1, km1 = k2 * m0 - k0 * m2, km2 = k0 * m1 - k1 * m0;
     const double kd = k0 * m0 + k1 * m1 + k2 * m2;
-    const double n0 = ((1.0 - kk) * m0 + 2.0 * km0 + 2.0 * kd * k0) / den;
-    const double n1 = ((1.0 - kk) * m1 + 2.0 * km1 + 2.0 * kd * k1) / den;
-    const double n2 = ((1.0 - kk) * m2 + 2.0 * km2 + 2.0 * kd * k2) / den;
-    const double nr = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-    out[3 * i] = n0 / nr;
-    out[3 * i + 1] = n1 / nr;
-    out[3 * i + 2] = n2 / nr;
+    const double n0 = ((1.0 - kk) * m0 + 2.0 * km0 + 2.0 * kd * k0) * iden;
+    const double n1 = ((1.0 - kk) * m1 + 2.0 * km1 + 2.0 * kd * k1) * iden;
+    const double n2 = ((1.0 - kk) * m2 + 2.0 * km2 + 2.0 * kd * k2) * iden;
+    const double inr = 1.0 / sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    out[3 * i] = n0 * inr;
+    out[3 * i + 1] = n1 * inr;
+    out[3 * i + 2] = n2 * inr;
   }
 }
 
@@ -1046,10 +1222,10 @@ __global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__
 __global__ void __launch_bounds__(BS) k_normalize(int N, double* __restrict__ m) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double a = m[3 * i], b = m[3 * i + 1], c = m[3 * i + 2];
-    const double nr = sqrt(a * a + b * b + c * c);
-    m[3 * i] = a / nr;
-    m[3 * i + 1] = b / nr;
-    m[3 * i + 2] = c / nr;
+    const double inr = 1.0 / sqrt(a * a + b * b + c * c);
+    m[3 * i] = a * inr;
+    m[3 * i + 1] = b * inr;
+    m[3 * i + 2] = c * inr;
   }
 }
 
@@ -1189,12 +1365,12 @@ __global__ void __launch_bounds__(BS) k_transport(int N, const double* v, const 
     const double k0 = 0.5 * tau * H[3 * i], k1 = 0.5 * tau * H[3 * i + 1], k2 = 0.5 * tau * H[3 * i + 2];
     const double v0 = v[3 * i], v1 = v[3 * i + 1], v2 = v[3 * i + 2];
     const double kk = k0 * k0 + k1 * k1 + k2 * k2;
-    const double den = 1.0 + kk;
+    const double iden = 1.0 / (1.0 + kk);
     const double kv0 = k1 * v2 - k2 * v1, kv1 = k2 * v0 - k0 * v2, kv2 = k0 * v1 - k1 * v0;
     const double kd = k0 * v0 + k1 * v1 + k2 * v2;
-    out[3 * i] = ((1.0 - kk) * v0 + 2.0 * kv0 + 2.0 * kd * k0) / den;
-    out[3 * i + 1] = ((1.0 - kk) * v1 + 2.0 * kv1 + 2.0 * kd * k1) / den;
-    out[3 * i + 2] = ((1.0 - kk) * v2 + 2.0 * kv2 + 2.0 * kd * k2) / den;
+    out[3 * i] = ((1.0 - kk) * v0 + 2.0 * kv0 + 2.0 * kd * k0) * iden;
+    out[3 * i + 1] = ((1.0 - kk) * v1 + 2.0 * kv1 + 2.0 * kd * k1) * iden;
+    out[3 * i + 2] = ((1.0 - kk) * v2 + 2.0 * kv2 + 2.0 * kd * k2) * iden;
   }
 }
 

@@ -244,7 +244,8 @@ class Problem:
         self._check("mm_minimize", lib().mm_minimize(self.h, dptr(B), dptr(m), dptr(U), C.byref(prm), C.byref(info)))
         return m, U, dict(iters=info.iters, evals=info.evals, preco_iters=info.preco_iters,
                           demag_iters=info.demag_iters, E=info.E, gnorm=info.gnorm, time=info.seconds,
-                          status=info.status)
+                          status=info.status, demag_time=info.demag_seconds,
+                          demag_wall_time=info.demag_wall_seconds)
 
     def time_kernel(self, kernel: str, reps: int = 20):
         """(mean ms per launch with L2 flushed before each, algorithmic bytes per launch)."""

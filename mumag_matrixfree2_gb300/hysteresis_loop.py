@@ -166,7 +166,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     B_vals = field_values(params.B_start, params.B_end, params.dB, params.loop)
     history, steps = [], []
     config_idx, J_last = 0, None
-    total = dict(time=0.0, iters=0, preco=0, evals=0, demag=0)
+    total = dict(time=0.0, iters=0, preco=0, evals=0, demag=0, demag_time=0.0, demag_wall_time=0.0)
     for step_idx, Bmag in enumerate(B_vals):
         t0 = time.perf_counter()
         m, U, info = minimize(m, Bmag * h, U0=U, max_iter=params.max_iter, tau_f=params.tau_f, eps_a=params.eps_a,
@@ -188,6 +188,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
         total["preco"] += info["preco_iters"]
         total["evals"] += info["evals"]
         total["demag"] += info["demag_iters"]
+        total["demag_time"] += info.get("demag_time", 0.0)
+        total["demag_wall_time"] += info.get("demag_wall_time", 0.0)
         # a state is saved on the first step, then when J moved by mstep or, without mstep, every
         # snapshot_every steps; each save after the first starts a new configuration index
         if J_last is None:
