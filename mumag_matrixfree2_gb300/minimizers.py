@@ -90,3 +90,57 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
 
     minimize.problem = prob
     return minimize
+
+
+def time_field_steps(workload: str = "cube80_h1.6_air200", method: str = "pcohen_hs", first: int = 120,
+                     steps: int = 15, precision: str = "fp64") -> dict:
+    """Minimize the field steps first .. first+steps-1 of the +8 T -> -8 T sweep (0.1 T, tilted 1 deg)
+    of a synthetic cube workload, after three warm-up steps from the first fields; the timed steps
+    run inside the NVTX range "steps" so that a profiler can select exactly their launches.  Returns
+    the host time and the minimizer's counters, with the demag solves' share."""
+    import time
+
+    import torch
+
+    from . import fem_utils
+    from . import synthetic as syn
+
+    knt, ijk = syn.box_mesh(syn.WORKLOADS[workload])
+    A, K1, Js, k, Js_ref = syn.reduced_materials([syn.Material(), syn.AIR])
+    s = fem_utils.prepare(knt, ijk, A, K1, Js, k)
+    prob = fem_utils.make_problem(s)
+    prob.set_precision(precision)
+    prob.build_poisson(1e-12, "amgcl")
+    prob.autotune(20)
+    h = syn.tilted_field_direction(1.0)
+    m, U = syn.initial_state(s.N, seed=0), np.zeros(s.N)
+    prm = MinimizerParams(method=method, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10)
+    Bs = syn.field_values(8.0 / Js_ref, -8.0 / Js_ref, 0.1 / Js_ref)
+    for B in Bs[:3]:
+        m, U, _ = prob.minimize(B * h, m, U, prm)
+    tot = dict(seconds=0.0, demag_device_s=0.0, demag_host_s=0.0, iters=0, evals=0, preco_iters=0, demag_iters=0)
+    torch.cuda.nvtx.range_push("steps")
+    for B in Bs[first:first + steps]:
+        t = time.perf_counter()
+        m, U, info = prob.minimize(B * h, m, U, prm)
+        tot["seconds"] += time.perf_counter() - t
+        tot["demag_device_s"] += info["demag_time"]
+        tot["demag_host_s"] += info["demag_wall_time"]
+        for key in ("iters", "evals", "preco_iters", "demag_iters"):
+            tot[key] += info[key]
+    torch.cuda.nvtx.range_pop()
+    return tot
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="time field steps of the GPU minimizer on a synthetic cube")
+    ap.add_argument("--workload", default="cube80_h1.6_air200")
+    ap.add_argument("--method", default="pcohen_hs", choices=SUPPORTED)
+    ap.add_argument("--first", type=int, default=120)
+    ap.add_argument("--steps", type=int, default=15)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    a = ap.parse_args()
+    print(json.dumps(time_field_steps(a.workload, a.method, a.first, a.steps, a.precision)))
