@@ -347,6 +347,12 @@ struct mm_problem {
     CK(cudaStreamSynchronize(st));
     return h_sc->red[slot];
   }
+  // `count` consecutive reduction slots from `first` with one copy and one wait
+  const double* red_n(int first, int count) {
+    CK(cudaMemcpyAsync(&h_sc->red[first], &d_sc->red[first], count * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return &h_sc->red[first];
+  }
   void sync() { CK(cudaStreamSynchronize(st)); }
   cudaEvent_t prof_event() {
     if (prof_used == prof_pool.size()) {
@@ -1069,17 +1075,20 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
     Q = Q + dq;
     ++it;
   }
-  // fallback direction, clipping, descent check
-  // z_fb = gte .* inv_M_prec  (into w_z3)
-  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
+  // fallback direction z_fb = gte .* inv_M_prec (into w_z3), clipping, descent check: |y|^2, |z_fb|^2
+  // and y.gte from one pass and one wait
+  mmk::k_fallback_dots<<<ge, BS, 0, h->st>>>(N, y, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  const double yn = std::sqrt(dev_dot(h, n3, y, nullptr));
-  const double zn = std::sqrt(dev_dot(h, n3, h->w_z3, nullptr));
+  const double* f = h->red_n(R_A, 3);
+  const double yn = std::sqrt(f[0]), zn = std::sqrt(f[1]);
+  double yg = f[2];
   if (yn > 10.0 * zn) {
-    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, 10.0 * zn / (yn + 1e-30), y);
+    const double c = 10.0 * zn / (yn + 1e-30);
+    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, c, y);
     LAUNCH_CHECK();
+    yg = dev_dot(h, n3, y, gte);  // the clipped direction's slope, as the unfused test computed it
   }
-  if (!(dev_dot(h, n3, y, gte) > 1e-12)) {
+  if (!(yg > 1e-12)) {
     CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   }
   return it;
@@ -1099,8 +1108,8 @@ std::pair<double, double> dev_mdot2(mm_problem* h, const double* a1, const doubl
                                     const double* b2) {
   mmk::k_mdot2<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, a1, b1, a2, b2, h->d_inv_M_rel, h->d_sc, h->d_part);
   LAUNCH_CHECK();
-  const double s1 = h->red(R_A);
-  return {s1, h->red(R_B)};
+  const double* v = h->red_n(R_A, 2);
+  return {v[0], v[1]};
 }
 
 // sum M_rel |y + a p|^2
@@ -1378,8 +1387,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
   auto direction = [&](const double* y, const double* dprev, double beta, int proj) {
     mmk::k_direction<<<ge, BS, 0, h->st>>>(N, m, y, dprev, beta, h->w_gte, graw, h->w_d, h->d_sc, h->d_part, proj);
     LAUNCH_CHECK();
-    const double dg = h->red(R_A);
-    double pg = h->red(R_B);
+    const double* ab = h->red_n(R_A, 2);
+    const double dg = ab[0];
+    double pg = ab[1];
     if (dg > 0) {
       neg3(h->w_d, y);
       pg = dev_dot(h, n3, graw, h->w_d);
@@ -1444,8 +1454,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       const double gsm = dev_absmax(h, n3, h->w_y);
       mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc, h->d_part);
       LAUNCH_CHECK();
-      const double num = h->red(R_A);
-      const double den = (meth == MM_METHOD_PCOHEN ? dev_dot(h, n3, h->w_ys, h->w_gprev) : h->red(R_B)) + 1e-30;
+      const double* ab = h->red_n(R_A, 2);
+      const double num = ab[0];
+      const double den = (meth == MM_METHOD_PCOHEN ? dev_dot(h, n3, h->w_ys, h->w_gprev) : ab[1]) + 1e-30;
       const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
       pg = direction(h->w_y, h->w_dprev, beta, meth == MM_METHOD_PCG ? 0 : 1);
       conv_gnorm = gnorm = gsm;
@@ -1476,9 +1487,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       }
       mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_x2, h->w_gte, h->w_x3, h->d_sc, h->d_part);
       LAUNCH_CHECK();
-      const double num = h->red(R_A);
-      const double den =
-          (meth == MM_METHOD_PCOHEN_HS_EXACT ? h->red(R_B) : dev_dot(h, n3, h->w_ys, h->w_x3)) + 1e-30;
+      const double* ab = h->red_n(R_A, 2);
+      const double num = ab[0];
+      const double den = (meth == MM_METHOD_PCOHEN_HS_EXACT ? ab[1] : dev_dot(h, n3, h->w_ys, h->w_x3)) + 1e-30;
       const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
       pg = direction(h->w_y, h->w_x2, beta, 0);
       conv_gnorm = gnorm = gsm;

@@ -1436,4 +1436,25 @@ __global__ void __launch_bounds__(BS) k_axpy_ratio(int n, const double* __restri
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * x[i] + y[i];
 }
 
+// z = g .* w (per node); |y|^2 -> red[R_A], |z|^2 -> red[R_B], y.g -> red[R_C] (the inner solve's
+// fallback direction, clipping and descent test in one pass)
+__global__ void __launch_bounds__(BS) k_fallback_dots(int N, const double* __restrict__ y,
+                                                      const double* __restrict__ g, const double* __restrict__ w,
+                                                      double* __restrict__ z, Scalars* sc, double* part) {
+  double yy = 0.0, zz = 0.0, yg = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double s = w[i];
+    for (int c = 0; c < 3; ++c) {
+      const double gc = g[3 * i + c], yc = y[3 * i + c];
+      const double zc = gc * s;
+      z[3 * i + c] = zc;
+      yy += yc * yc;
+      zz += zc * zc;
+      yg += yc * gc;
+    }
+  }
+  grid_reduce(yy, zz, sc, part, R_A, R_B);
+  grid_reduce(yg, 0.0, sc, part, R_C);
+}
+
 }  // namespace mmk
