@@ -253,6 +253,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 #define MM_OPT_PRECISION 2
 #define MM_PRECISION_FP64 0
 #define MM_PRECISION_MIXED 1
+/* MM_PRECISION_FP32_PRECOND: the FP64 PCG of the plain method (iterate, residual, directions, the
+ * products with the finest operator and every inner product in FP64, the same stopping test), with
+ * the V-cycle preconditioner applied in FP32 on a copy of the hierarchy. */
+#define MM_PRECISION_FP32_PRECOND 2
 /* MM_OPT_MIXED_ETA_E6: relative residual reduction asked of each FP32 correction solve, in units of
  * 1e-6 (default 10, i.e. 1e-5). */
 #define MM_OPT_MIXED_ETA_E6 3

@@ -43,8 +43,8 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
     A, K1, Js, k, Js_ref = syn.reduced_materials([p.material, syn.AIR])
     s = fem_utils.prepare(knt, ijk, A, K1, Js, k)
     prob = fem_utils.make_problem(s)
-    if precision == "mixed":
-        prob.set_precision("mixed")
+    if precision != "fp64":
+        prob.set_precision(precision)
     prob.build_poisson(1e-12, "amgcl")
     avg = NodalAverages(s.geom.conn, s.geom.volume, s.geom.mat_id, s.Js_lookup, s.N)
     prm = params or MinimizerParams(method="pcohen_hs", tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10)

@@ -185,7 +185,8 @@ struct mm_problem {
   std::vector<mm::AmgLevel> amg_h;
   SolverT<double> s64;           // plain FP64 method (and the outer residual of the mixed one)
   SolverT<float> s32;            // inner solves of the mixed-precision method
-  bool mixed = false;            // MM_OPT_PRECISION
+  bool mixed = false;            // MM_OPT_PRECISION = MM_PRECISION_MIXED
+  bool fp32_precond = false;     // MM_OPT_PRECISION = MM_PRECISION_FP32_PRECOND
   double mixed_eta = 1e-5;       // relative reduction asked of each inner FP32 solve
   int mixed_max_outer = 12;
   int last_outer = 0;            // refinement steps of the last mixed solve
@@ -222,6 +223,9 @@ struct mm_problem {
     if (n == 0) n = 1;
     CK(cudaMalloc(&p, n * sizeof(T)));
     allocs.push_back(p);
+    // zeroed: reused device memory can hold any bit pattern (a NaN in an FP32 view of old FP64 data),
+    // and a vector read once with a zero factor (the first direction's beta p) must not carry it in
+    CK(cudaMemset(p, 0, n * sizeof(T)));
     return (T*)p;
   }
   template <class T, class Alloc>
@@ -477,7 +481,9 @@ double mat_bytes(const DevMatT<T>& M) {
 // in_loop: the level-0 residual is skipped once the solve has converged.
 // ---------------------------------------------------------------------------------------------
 template <class T>
-void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop, const int* done) {
+void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop, const int* done,
+                    mmk::Scalars* scal = nullptr) {
+  mmk::Scalars* const sc = scal ? scal : S.sc;  // the PCG's scalars (another solver's with the FP32 preconditioner)
   auto& lv = S.lv;
   const int L = (int)lv.size();
   const double w = sizeof(T);
@@ -487,7 +493,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     auto& c = lv[l];
     if (l == 0 && in_loop) {
       tagged<T>(h, MM_PROF_VC_RESIDUAL0, 0, mat_bytes(c.A) + 3.0 * w * c.n, [&] {
-        launch(h, mmk::k_vc_residual0<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.res, S.sc);
+        launch(h, mmk::k_vc_residual0<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.res, sc);
         LAUNCH_CHECK();
       });
     } else {
@@ -538,7 +544,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
               [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
     if (l == 0) {
       tagged<T>(h, MM_PROF_SMOOTH0, 0, mat_bytes(c.A) + 4.0 * w * c.n, [&] {
-        launch(h, mmk::k_smooth_dot<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.s, z, S.sc, h->d_part, done);
+        launch(h, mmk::k_smooth_dot<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.s, z, sc, h->d_part, done);
         LAUNCH_CHECK();
       });
     } else {
@@ -611,8 +617,8 @@ void enqueue_iteration(mm_problem* h, SolverT<T>& S) {
 
 // Build the loop graph: WHILE (condition) { iteration; k_set_cond }.  Returns false when the
 // driver cannot build conditional graphs (the host-polled loop is used then).
-template <class T>
-bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
+template <class T, class Iter>
+bool build_loop_graph(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
   if (S.exec) return true;
   if (S.graph_failed) return false;
   cudaGraph_t g = nullptr;
@@ -636,7 +642,7 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
     if (ok) {
       const int64_t saved = h->n_launch;
       try {
-        enqueue_iteration<T>(h, S);
+        iteration();
         launch(h, mmk::k_set_cond, 1, 32, hnd, S.sc);
       } catch (const Fail&) {
         ok = false;
@@ -659,6 +665,10 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
   S.graph = g;
   S.exec = ex;
   return true;
+}
+template <class T>
+bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
+  return build_loop_graph(h, S, [&] { enqueue_iteration<T>(h, S); });
 }
 
 template <class T>
@@ -843,6 +853,69 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
 }
 
+// FP64 PCG preconditioned by the FP32 V-cycle (MM_PRECISION_FP32_PRECOND): x, r, p, A p, the
+// products with A0 and every inner product in FP64; the V-cycle on the FP32 copy of the hierarchy,
+// from fl32(r) (its level-0 pre-smoothing fused into the step) to z, widened for the next direction.
+// The scalars of the iteration are the FP64 solver's.
+void enqueue_iteration_mp(mm_problem* h) {
+  auto& S = h->s64;
+  auto& F = h->s32;
+  const int N = h->N;
+  auto& l0 = S.lv[0];
+  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * 8.0 * N, [&] {
+    launch(h, mmk::k_pcg_dir<double>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+    LAUNCH_CHECK();
+  });
+  tagged<double>(h, MM_PROF_PCG_STEP, 0, 6.0 * 8.0 * N + 3.0 * 4.0 * N, [&] {
+    launch(h, mmk::k_pcg_step_mp, grid_ilp(N), BS, N, S.x, S.r, S.p, S.Ap, F.lv[0].s, F.r, F.lv[0].x, S.sc,
+           h->d_part);
+    LAUNCH_CHECK();
+  });
+  enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc);
+  launch(h, mmk::k_widen, grid_elem(N), BS, N, F.z, S.z, &S.sc->done);
+  LAUNCH_CHECK();
+}
+
+void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
+  auto& S = h->s64;
+  auto& F = h->s32;
+  const int N = h->N;
+  dotT<double>(h, N, S.b, (const double*)nullptr, S.sc, R_BB);
+  launch(h, mmk::k_pcg_init_scalars, 1, 32, S.sc, tol, maxiter);
+  LAUNCH_CHECK();
+  auto& l0 = S.lv[0];
+  tagged<double>(h, MM_PROF_INIT_RESIDUAL, 0, mat_bytes(l0.A) + 3.0 * 8.0 * N, [&] {
+    launch(h, mmk::k_init_residual<double>, grid_ilp(N), BS, l0.A.s, S.x, S.b, S.r, (const double*)nullptr,
+           l0.x, S.sc, h->d_part);
+    LAUNCH_CHECK();
+  });
+  launch(h, mmk::k_split_mp, grid_elem(N), BS, N, S.r, F.lv[0].s, F.r, F.lv[0].x);
+  LAUNCH_CHECK();
+  enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc);
+  launch(h, mmk::k_widen, grid_elem(N), BS, N, F.z, S.z, (const int*)nullptr);
+  LAUNCH_CHECK();
+  const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
+  if (graph) {
+    CK(cudaGraphLaunch(S.exec, h->st));
+  } else {
+    // host-polled: read `done` every fourth iteration (every step when profiling)
+    const int every = h->prof ? 1 : 4;
+    for (int i = 0;; ++i) {
+      enqueue_iteration_mp(h);
+      if ((i + 1) % every == 0) {
+        CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+        h->sync();
+        if (h->h_sc->done || i > maxiter + 8) break;
+      }
+    }
+  }
+  CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+  h->sync();
+  if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
+  if (iters) *iters = h->h_sc->it;
+  if (r2_out) *r2_out = h->h_sc->red[R_R2];
+}
+
 // b = D m on device (magnetic rows), b.b -> red[R_BB0]
 void enqueue_rhs(mm_problem* h, const double* m) {
   const int N = h->N;
@@ -911,6 +984,9 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   if (h->mixed && h->s32.built) {
     run_mixed(h, tol, maxiter, &it, &r2);
     tol2_ref = tol * tol * h->red(R_BB);
+  } else if (h->fp32_precond && h->s32.built && multilevel(h, h->s32)) {
+    run_pcg_mp(h, tol, maxiter, &it, &r2);
+    tol2_ref = h->h_sc->tol2;
   } else {
     run_pcg<double>(h, h->s64, tol, maxiter, &it, &r2);
     tol2_ref = h->h_sc->tol2;
@@ -2302,7 +2378,7 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
     h->s64.b = h->d_b;
     h->s64.x = h->d_x;
     h->s64.sc = h->d_sc;
-    if (h->mixed) {
+    if (h->mixed || h->fp32_precond) {
       build_solver<float>(h, h->s32, A, amg, precond_type);
       h->s32.b = h->d_r32;
       h->s32.x = h->d_d32;
@@ -2741,8 +2817,10 @@ int mm_set_option(mm_problem* h, int option, int value) {
   }
   if (option == MM_OPT_PRECISION) {
     if (h->poisson_built) return MM_ERR_STATE;  // the FP32 hierarchy is built by mm_build_poisson
-    if (value != MM_PRECISION_FP64 && value != MM_PRECISION_MIXED) return MM_ERR_ARG;
+    if (value != MM_PRECISION_FP64 && value != MM_PRECISION_MIXED && value != MM_PRECISION_FP32_PRECOND)
+      return MM_ERR_ARG;
     h->mixed = value == MM_PRECISION_MIXED;
+    h->fp32_precond = value == MM_PRECISION_FP32_PRECOND;
     return MM_OK;
   }
   if (option == MM_OPT_GRID_CAP) {

@@ -498,8 +498,9 @@ __global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict_
     for (int q = 0; q < ILP; ++q) {
       const int i = row[q];
       if (i >= A.n) continue;
-      const T pn = z[i] + beta * p[i];
-      const T apn = az[q] + beta * Ap[i];
+      // first direction (beta = 0): p = z, Ap = A z, whatever p and Ap held before
+      const T pn = beta != T(0) ? z[i] + beta * p[i] : z[i];
+      const T apn = beta != T(0) ? az[q] + beta * Ap[i] : az[q];
       p[i] = pn;
       Ap[i] = apn;
       acc.add(pn, apn);
@@ -532,6 +533,54 @@ __global__ void __launch_bounds__(BS) k_pcg_step(int n, T* __restrict__ x, T* __
     }
   }
   grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
+}
+
+// FP64 PCG preconditioned by the FP32 V-cycle: x += alpha p ; r -= alpha Ap (FP64) ; r.r -> red[R_R2] ;
+// r32 = fl32(r) and xv = s0 .* r32, the FP32 V-cycle's input and its level-0 pre-smoothing
+__global__ void __launch_bounds__(BS) k_pcg_step_mp(int n, double* __restrict__ x, double* __restrict__ r,
+                                                    const double* __restrict__ p, const double* __restrict__ Ap,
+                                                    const float* __restrict__ s0, float* __restrict__ r32,
+                                                    float* __restrict__ xv, Scalars* sc, double* part) {
+  pdl_entry();
+  if (sc->done) return;
+  const double alpha = sc->alpha;
+  Acc<double> acc;
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= n) continue;
+      x[i] = x[i] + alpha * p[i];
+      const double ri = r[i] - alpha * Ap[i];
+      r[i] = ri;
+      acc.add(ri, ri);
+      const float rf = (float)ri;
+      r32[i] = rf;
+      xv[i] = s0[i] * rf;
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
+}
+
+// r32 = fl32(r), xv = s0 .* r32 (before the first V-cycle of a solve)
+__global__ void __launch_bounds__(BS) k_split_mp(int n, const double* __restrict__ r, const float* __restrict__ s0,
+                                                 float* __restrict__ r32, float* __restrict__ xv) {
+  pdl_entry();
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    const float rf = (float)r[i];
+    r32[i] = rf;
+    xv[i] = s0[i] * rf;
+  }
+}
+
+// z = fl64(z32), skipped once the solve has converged
+__global__ void __launch_bounds__(BS) k_widen(int n, const float* __restrict__ z32, double* __restrict__ z,
+                                              const int* __restrict__ done) {
+  pdl_entry();
+  if (done && *done) return;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) z[i] = (double)z32[i];
 }
 
 // level-0 residual res = r - A xv (skipped once the solve has converged)

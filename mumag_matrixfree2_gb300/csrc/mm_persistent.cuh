@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(BS, MINB) k_pcg_persistent(PcgArgs<T> a) {
       const T bt = (T)beta;
       Acc<T> acc;
       mat_rows<RPT, T>(A0, a.z, [&](int i, T az) {
-        const T pn = __ldcg(a.z + i) + bt * a.p[i];
-        const T apn = az + bt * a.Ap[i];
+        const T pn = bt != T(0) ? __ldcg(a.z + i) + bt * a.p[i] : __ldcg(a.z + i);
+        const T apn = bt != T(0) ? az + bt * a.Ap[i] : az;
         a.p[i] = pn;
         a.Ap[i] = apn;
         acc.add(pn, apn);

@@ -270,8 +270,10 @@ class Problem:
         return json.loads(buf.value.decode())
 
     def set_precision(self, precision: str):
-        """"fp64" (the reference's plain method) or "mixed"; call before build_poisson()."""
-        self.set_option("precision", {"fp64": 0, "mixed": 1}[precision])
+        """"fp64" (the reference's plain method), "mixed" (FP32 correction solves inside FP64 iterative
+        refinement) or "fp32_precond" (the FP64 PCG with the V-cycle applied in FP32); call before
+        build_poisson()."""
+        self.set_option("precision", {"fp64": 0, "mixed": 1, "fp32_precond": 2}[precision])
         self.precision = precision
 
     def profile(self, reset: bool = False) -> list[dict]:

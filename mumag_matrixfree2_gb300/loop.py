@@ -156,7 +156,7 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--out-dir", default="hyst_out")
     ap.add_argument("--snapshot-every", type=int, default=1, help="VTU snapshot every N steps (0: none)")
     ap.add_argument("--verbose", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"],
                     help="demag solve precision of this backend (mixed: FP32 inside FP64 refinement)")
     return ap
 

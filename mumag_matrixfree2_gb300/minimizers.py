@@ -141,6 +141,6 @@ if __name__ == "__main__":
     ap.add_argument("--method", default="pcohen_hs", choices=SUPPORTED)
     ap.add_argument("--first", type=int, default=120)
     ap.add_argument("--steps", type=int, default=15)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"])
     a = ap.parse_args()
     print(json.dumps(time_field_steps(a.workload, a.method, a.first, a.steps, a.precision)))

@@ -214,6 +214,36 @@ def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     assert rel(U32, U64) <= 1e-8
 
 
+@pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
+def test_fp32_preconditioner_keeps_the_fp64_pcg(cuda_ok, name):
+    """The FP64 PCG with the V-cycle applied in FP32: the stopping test is the plain method's (recursive
+    FP64 residual), the true FP64 residual meets the tolerance, the iterations stay within one of the
+    FP64 preconditioner's and the potential matches the plain solve to the tolerance."""
+    s, p, _ = case(name)
+    plain = fem_utils.make_problem(s)
+    plain.build_poisson(1e-12, "amgcl")
+    pc = fem_utils.make_problem(s)
+    pc.set_precision("fp32_precond")
+    pc.build_poisson(1e-12, "amgcl")
+    ops = opo.SolveU(p, ofem.assembled_operators(p, parts=("A", "D")), cg_tol=1e-10)
+    for seed, x0 in ((31, None), (32, "warm")):
+        m = random_state(p.N, seed=seed, amplitude=0.05)
+        U0 = np.zeros(p.N) if x0 is None else plain.solve_u(random_state(p.N, seed=seed + 10, amplitude=0.05),
+                                                            np.zeros(p.N), 1e-10)[0]
+        U64, it64, rr64, _ = plain.solve_u(m, U0.copy(), 1e-10)
+        Upc, itpc, rrpc, rc = pc.solve_u(m, U0.copy(), 1e-10)
+        assert rc == 0 and rrpc <= 1e-10 and abs(itpc - it64) <= 1, (itpc, it64)
+        b = ops.rhs(m)
+        true_rr = np.linalg.norm(b - ops.apply_A(Upc)) / np.linalg.norm(b)
+        assert true_rr <= 1.5e-10
+        assert rel(Upc, U64) <= 1e-8
+    pc.set_option("graph", 0)  # the host-polled loop: same iterations
+    m = random_state(p.N, seed=31, amplitude=0.05)
+    _, it_h, rr_h, rc_h = pc.solve_u(m, np.zeros(p.N), 1e-10)
+    _, it_g, _, _ = plain.solve_u(m, np.zeros(p.N), 1e-10)
+    assert rc_h == 0 and rr_h <= 1e-10 and abs(it_h - it_g) <= 1
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_persistent_loop_matches_graph_loop(cuda_ok, precision):
     """The one-launch PCG loop (grid barriers between the phases) against the graph of separate
@@ -313,3 +343,25 @@ def test_magnetoelastic_term_matches_oracle(cuda_ok):
     # the term changes the result (the test is not vacuous)
     E1, _ = ofem.energy_and_grad_mf(p, m, U, B)
     assert abs(E1 - E0) > 1e-6 * abs(E0)
+
+
+def test_solves_on_reused_device_memory(cuda_ok):
+    """Problems created after others were destroyed get device memory that held old data (an FP32 view
+    of FP64 values can be NaN).  Every precision and loop form still converges to the plain solve:
+    buffers are zeroed when allocated and the first PCG direction ignores the previous one."""
+    s, p, _ = case("cube40_h2_air200")
+    m = random_state(p.N, seed=31, amplitude=0.05)
+    ref = None
+    for prec in ("fp64", "fp32_precond", "mixed"):
+        for graph in (1, 0):
+            pr = fem_utils.make_problem(s)
+            if prec != "fp64":
+                pr.set_precision(prec)
+            pr.set_option("graph", graph)
+            pr.build_poisson(1e-12, "amgcl")
+            U, it, rr, rc = pr.solve_u(m, np.zeros(p.N), 1e-10)
+            assert rc == 0 and rr <= 1e-10 and it < 40, (prec, graph, it, rr, rc)
+            if ref is None:
+                ref = U
+            assert rel(U, ref) <= 1e-8
+            del pr
