@@ -224,8 +224,11 @@ struct mm_problem {
     CK(cudaMalloc(&p, n * sizeof(T)));
     allocs.push_back(p);
     // zeroed: reused device memory can hold any bit pattern (a NaN in an FP32 view of old FP64 data),
-    // and a vector read once with a zero factor (the first direction's beta p) must not carry it in
-    CK(cudaMemset(p, 0, n * sizeof(T)));
+    // and a vector read once with a zero factor (the first direction's beta p) must not carry it in.
+    // On the problem's own stream, ahead of any copy into the buffer (that stream does not order with
+    // the legacy default stream).
+    if (!st) throw Fail{MM_ERR_CUDA, "device allocation before the problem's stream exists"};
+    CK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
     return (T*)p;
   }
   template <class T, class Alloc>
@@ -855,15 +858,15 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
 
 // FP64 PCG preconditioned by the FP32 V-cycle (MM_PRECISION_FP32_PRECOND): x, r, p, A p, the
 // products with A0 and every inner product in FP64; the V-cycle on the FP32 copy of the hierarchy,
-// from fl32(r) (its level-0 pre-smoothing fused into the step) to z, widened for the next direction.
-// The scalars of the iteration are the FP64 solver's.
+// from fl32(r) (its level-0 pre-smoothing fused into the step) to z in FP32.
+// The scalars of the iteration are the FP64 solver's; the direction update reads z in FP32.
 void enqueue_iteration_mp(mm_problem* h) {
   auto& S = h->s64;
   auto& F = h->s32;
   const int N = h->N;
   auto& l0 = S.lv[0];
-  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * 8.0 * N, [&] {
-    launch(h, mmk::k_pcg_dir<double>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 4.0 * 8.0 * N + 4.0 * N, [&] {
+    launch(h, mmk::k_pcg_dir_mp, grid_ilp(N), BS, l0.A.s, F.z, S.p, S.Ap, S.sc, h->d_part);
     LAUNCH_CHECK();
   });
   tagged<double>(h, MM_PROF_PCG_STEP, 0, 6.0 * 8.0 * N + 3.0 * 4.0 * N, [&] {
@@ -872,8 +875,6 @@ void enqueue_iteration_mp(mm_problem* h) {
     LAUNCH_CHECK();
   });
   enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc);
-  launch(h, mmk::k_widen, grid_elem(N), BS, N, F.z, S.z, &S.sc->done);
-  LAUNCH_CHECK();
 }
 
 void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
@@ -892,8 +893,6 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
   launch(h, mmk::k_split_mp, grid_elem(N), BS, N, S.r, F.lv[0].s, F.r, F.lv[0].x);
   LAUNCH_CHECK();
   enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc);
-  launch(h, mmk::k_widen, grid_elem(N), BS, N, F.z, S.z, (const int*)nullptr);
-  LAUNCH_CHECK();
   const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));

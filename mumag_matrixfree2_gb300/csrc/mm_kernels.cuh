@@ -301,9 +301,9 @@ __device__ __forceinline__ T ldx(const T* x, int c) {
   else return __ldg(x + c);
 }
 
-template <int R, bool CG, class T>
+template <int R, bool CG, class T, class TX = T>
 __device__ __forceinline__ void sell_rows_k(const int* __restrict__ sptr, const int* __restrict__ col,
-                                            const T* __restrict__ val, int rlim, const T* x, const int (&row)[R],
+                                            const T* __restrict__ val, int rlim, const TX* x, const int (&row)[R],
                                             T (&acc)[R]) {
   using P2 = typename Pair<T>::type;
   int base[R], wp[R];
@@ -333,7 +333,7 @@ __device__ __forceinline__ void sell_rows_k(const int* __restrict__ sptr, const 
 #pragma unroll
     for (int q = 0; q < R; ++q)
       if (j < wp[q]) {
-        const T x0 = ldx<CG>(x, c[q].x), x1 = ldx<CG>(x, c[q].y);
+        const T x0 = (T)ldx<CG>(x, c[q].x), x1 = (T)ldx<CG>(x, c[q].y);
         acc[q] = fmaT<T>(v[q].x, x0, acc[q]);
         acc[q] = fmaT<T>(v[q].y, x1, acc[q]);
       }
@@ -344,6 +344,11 @@ template <class T>
 __device__ __forceinline__ void sell_rows(const SellT<T>& A, const T* __restrict__ x, const int (&row)[ILP],
                                           T (&acc)[ILP]) {
   sell_rows_k<ILP, false, T>(A.sptr, A.col, A.val, A.n, x, row, acc);
+}
+// FP64 operator on an FP32 vector (widened exactly on load)
+__device__ __forceinline__ void sell_rows_w(const SellT<double>& A, const float* __restrict__ x, const int (&row)[ILP],
+                                            double (&acc)[ILP]) {
+  sell_rows_k<ILP, false, double, float>(A.sptr, A.col, A.val, A.n, x, row, acc);
 }
 
 // row indices of thread threadIdx.x in the block-stride step starting at rb
@@ -564,6 +569,35 @@ __global__ void __launch_bounds__(BS) k_pcg_step_mp(int n, double* __restrict__ 
   grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
 
+// k_pcg_dir with the FP32 preconditioned residual z (widened exactly on load): y = A z ;
+// p = z + beta p ; Ap = y + beta Ap ; p.Ap -> red[R_PAP], all in FP64
+__global__ void __launch_bounds__(BS) k_pcg_dir_mp(SellT<double> A, const float* __restrict__ z,
+                                                   double* __restrict__ p, double* __restrict__ Ap, Scalars* sc,
+                                                   double* part) {
+  pdl_entry();
+  if (sc->done) return;
+  const double beta = sc->beta;
+  Acc<double> acc;
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    double az[ILP];
+    rows_of(rb, row);
+    sell_rows_w(A, z, row, az);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const double zi = (double)z[i];
+      const double pn = beta != 0.0 ? zi + beta * p[i] : zi;
+      const double apn = beta != 0.0 ? az[q] + beta * Ap[i] : az[q];
+      p[i] = pn;
+      Ap[i] = apn;
+      acc.add(pn, apn);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_PAP, -1, POST_PAP);
+}
+
 // r32 = fl32(r), xv = s0 .* r32 (before the first V-cycle of a solve)
 __global__ void __launch_bounds__(BS) k_split_mp(int n, const double* __restrict__ r, const float* __restrict__ s0,
                                                  float* __restrict__ r32, float* __restrict__ xv) {
@@ -573,14 +607,6 @@ __global__ void __launch_bounds__(BS) k_split_mp(int n, const double* __restrict
     r32[i] = rf;
     xv[i] = s0[i] * rf;
   }
-}
-
-// z = fl64(z32), skipped once the solve has converged
-__global__ void __launch_bounds__(BS) k_widen(int n, const float* __restrict__ z32, double* __restrict__ z,
-                                              const int* __restrict__ done) {
-  pdl_entry();
-  if (done && *done) return;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) z[i] = (double)z32[i];
 }
 
 // level-0 residual res = r - A xv (skipped once the solve has converged)
