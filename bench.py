@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--batch-particles", type=int, default=64,
                     help="particles of the batched leg (256 in the full workload; 0 skips the leg)")
     ap.add_argument("--batch-workers", type=int, default=16, help="host threads of the batched leg")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"],
+                    help="solver of the main timed solves (fp64: the headline plain method; the others for "
+                         "profiling their kernels)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm worker processes (0: all cores)")
@@ -480,6 +483,8 @@ def run_ours(a):
     t0 = time.perf_counter()
     s = fem_utils.prepare(knt, ijk, *mats)
     prob = fem_utils.make_problem(s)
+    if a.precision != "fp64":
+        prob.set_precision(a.precision)
     n_levels = prob.build_poisson(1e-12, "amgcl")
     setup_s = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -620,7 +625,7 @@ def run_ours(a):
             "warmup": a.warmup, "ms_per_step": 1000.0 * t_dev / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": value / PUBLISHED_SOLVES_PER_S, "dtype": "f64", "data": "synthetic",
             "config": {"workload": a.workload, "nodes": N, "tets": int(len(ijk)), "tol": a.tol,
-                       "precond": "SA-AMG V(1,1) SPAI0", "amg_levels": n_levels,
+                       "precond": "SA-AMG V(1,1) SPAI0", "solver_precision": a.precision, "amg_levels": n_levels,
                        "level_sizes": [int(x["A"].shape[0]) for x in lv],
                        "pcg_iters_per_solve": its[0], "rel_res": max(rrs), "setup_s": setup_s,
                        "autotune": {"seconds": tune_s, "operators_tuned": len(tune["operators"]),

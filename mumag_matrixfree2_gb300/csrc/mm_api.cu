@@ -485,7 +485,7 @@ double mat_bytes(const DevMatT<T>& M) {
 // ---------------------------------------------------------------------------------------------
 template <class T>
 void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop, const int* done,
-                    mmk::Scalars* scal = nullptr) {
+                    mmk::Scalars* scal = nullptr, double* z64 = nullptr) {
   mmk::Scalars* const sc = scal ? scal : S.sc;  // the PCG's scalars (another solver's with the FP32 preconditioner)
   auto& lv = S.lv;
   const int L = (int)lv.size();
@@ -547,7 +547,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
               [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
     if (l == 0) {
       tagged<T>(h, MM_PROF_SMOOTH0, 0, mat_bytes(c.A) + 4.0 * w * c.n, [&] {
-        launch(h, mmk::k_smooth_dot<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.s, z, sc, h->d_part, done);
+        launch(h, mmk::k_smooth_dot<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.s, z, sc, h->d_part, done, z64);
         LAUNCH_CHECK();
       });
     } else {
@@ -859,14 +859,15 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
 // FP64 PCG preconditioned by the FP32 V-cycle (MM_PRECISION_FP32_PRECOND): x, r, p, A p, the
 // products with A0 and every inner product in FP64; the V-cycle on the FP32 copy of the hierarchy,
 // from fl32(r) (its level-0 pre-smoothing fused into the step) to z in FP32.
-// The scalars of the iteration are the FP64 solver's; the direction update reads z in FP32.
+// The scalars of the iteration are the FP64 solver's; the last V-cycle kernel also writes z in FP64
+// (one conversion per row there, not one per stored entry in the FP64 product with A0).
 void enqueue_iteration_mp(mm_problem* h) {
   auto& S = h->s64;
   auto& F = h->s32;
   const int N = h->N;
   auto& l0 = S.lv[0];
-  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 4.0 * 8.0 * N + 4.0 * N, [&] {
-    launch(h, mmk::k_pcg_dir_mp, grid_ilp(N), BS, l0.A.s, F.z, S.p, S.Ap, S.sc, h->d_part);
+  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * 8.0 * N, [&] {
+    launch(h, mmk::k_pcg_dir<double>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
     LAUNCH_CHECK();
   });
   tagged<double>(h, MM_PROF_PCG_STEP, 0, 6.0 * 8.0 * N + 3.0 * 4.0 * N, [&] {
@@ -874,7 +875,7 @@ void enqueue_iteration_mp(mm_problem* h) {
            h->d_part);
     LAUNCH_CHECK();
   });
-  enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc);
+  enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc, S.z);
 }
 
 void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
@@ -892,7 +893,7 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
   });
   launch(h, mmk::k_split_mp, grid_elem(N), BS, N, S.r, F.lv[0].s, F.r, F.lv[0].x);
   LAUNCH_CHECK();
-  enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc);
+  enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc, S.z);
   const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
@@ -2650,7 +2651,7 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
       } else if (kernel == MM_KERNEL_SMOOTH) {
         const double* s = l0->s ? l0->s : h->d_U;
         launch(h, mmk::k_smooth_dot<double>, grid_ilp(l0->n), BS, l0->A.s, h->d_U, h->d_b, s, h->d_out, h->d_sc, h->d_part,
-                                                                nullptr);
+                                                                nullptr, (double*)nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
         mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,

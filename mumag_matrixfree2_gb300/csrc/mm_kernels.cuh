@@ -345,12 +345,6 @@ __device__ __forceinline__ void sell_rows(const SellT<T>& A, const T* __restrict
                                           T (&acc)[ILP]) {
   sell_rows_k<ILP, false, T>(A.sptr, A.col, A.val, A.n, x, row, acc);
 }
-// FP64 operator on an FP32 vector (widened exactly on load)
-__device__ __forceinline__ void sell_rows_w(const SellT<double>& A, const float* __restrict__ x, const int (&row)[ILP],
-                                            double (&acc)[ILP]) {
-  sell_rows_k<ILP, false, double, float>(A.sptr, A.col, A.val, A.n, x, row, acc);
-}
-
 // row indices of thread threadIdx.x in the block-stride step starting at rb
 __device__ __forceinline__ void rows_of(int rb, int (&row)[ILP]) {
 #pragma unroll
@@ -569,35 +563,6 @@ __global__ void __launch_bounds__(BS) k_pcg_step_mp(int n, double* __restrict__ 
   grid_finish(block_total(acc), 0.0, sc, part, R_R2, -1, POST_R2_STEP);
 }
 
-// k_pcg_dir with the FP32 preconditioned residual z (widened exactly on load): y = A z ;
-// p = z + beta p ; Ap = y + beta Ap ; p.Ap -> red[R_PAP], all in FP64
-__global__ void __launch_bounds__(BS) k_pcg_dir_mp(SellT<double> A, const float* __restrict__ z,
-                                                   double* __restrict__ p, double* __restrict__ Ap, Scalars* sc,
-                                                   double* part) {
-  pdl_entry();
-  if (sc->done) return;
-  const double beta = sc->beta;
-  Acc<double> acc;
-  ROW_LOOP(A.n) {
-    int row[ILP];
-    double az[ILP];
-    rows_of(rb, row);
-    sell_rows_w(A, z, row, az);
-#pragma unroll
-    for (int q = 0; q < ILP; ++q) {
-      const int i = row[q];
-      if (i >= A.n) continue;
-      const double zi = (double)z[i];
-      const double pn = beta != 0.0 ? zi + beta * p[i] : zi;
-      const double apn = beta != 0.0 ? az[q] + beta * Ap[i] : az[q];
-      p[i] = pn;
-      Ap[i] = apn;
-      acc.add(pn, apn);
-    }
-  }
-  grid_finish(block_total(acc), 0.0, sc, part, R_PAP, -1, POST_PAP);
-}
-
 // r32 = fl32(r), xv = s0 .* r32 (before the first V-cycle of a solve)
 __global__ void __launch_bounds__(BS) k_split_mp(int n, const double* __restrict__ r, const float* __restrict__ s0,
                                                  float* __restrict__ r32, float* __restrict__ xv) {
@@ -719,9 +684,12 @@ __global__ void __launch_bounds__(BS) k_coarse_b(int n, int nc, const T* __restr
 // post-smoothing y = x + s .* (b - A x); with `part` it also reduces b.y into red[R_RZ]
 // (level 0: b = r and y = z)
 template <class T>
+// y64 (may be null): y also widened to FP64 (the FP32 preconditioner's output for the FP64 PCG: N
+// conversions here instead of one per stored entry in the next FP64 product)
 __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                    const T* __restrict__ s, T* __restrict__ y, Scalars* sc,
-                                                   double* part, const int* __restrict__ done) {
+                                                   double* part, const int* __restrict__ done,
+                                                   double* __restrict__ y64) {
   pdl_entry();
   if (done && *done) return;
   Acc<T> acc;
@@ -736,6 +704,7 @@ __global__ void __launch_bounds__(BS) k_smooth_dot(SellT<T> A, const T* __restri
       if (i >= A.n) continue;
       const T yi = x[i] + s[i] * (b[i] - ax[q]);
       y[i] = yi;
+      if (y64) y64[i] = (double)yi;
       acc.add(b[i], yi);
     }
   }
