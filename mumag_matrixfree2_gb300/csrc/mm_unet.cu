@@ -729,6 +729,10 @@ struct mm_unet {
   int adam_t = 0;
   uint4* wk[MM_UNET_LAYERS] = {};
   uint4* wkT[MM_UNET_LAYERS] = {};
+  // Layers whose forward grid would cover few CTAs (the coarse levels of a small grid) run with
+  // 16-channel N tiles from a second weight copy: 4x the CTAs, each issuing a quarter of the MMA
+  // work, the same accumulation order per output (identical results).
+  uint4* wk16[MM_UNET_LAYERS] = {};
   uint4* T[T_COUNT] = {};
   uint4* dT[T_COUNT] = {};
   float* part = nullptr;
@@ -770,11 +774,12 @@ struct mm_unet {
     const LayerDef& d = DEFS[l];
     const int cin = transposed ? d.cout : d.cin;
     const int cout = transposed ? d.cin : d.cout;
-    const int nt = nt_of(cout);
+    const bool n16 = !transposed && wk16[l];
+    const int nt = n16 ? 16 : nt_of(cout);
     const mmn::Vol& v = vol[d.level];
     mmn::ConvArgs a{};
     a.in = in;
-    a.wk = transposed ? wkT[l] : wk[l];
+    a.wk = transposed ? wkT[l] : (n16 ? wk16[l] : wk[l]);
     a.bias = transposed ? nullptr : p + boff[l];
     a.out = out;
     a.v = v;
@@ -864,6 +869,10 @@ struct mm_unet {
       const int nt2 = (d.cin / nt_of(d.cin)) * (d.cout / 16) * 54 * nt_of(d.cin);
       mmn::k_prep_weights<<<grid1d(nt2), 256, 0, st>>>(p + woff[l], d.cin, d.cout, nt_of(d.cin), 1, wkT[l]);
       UCK(cudaGetLastError());
+      if (wk16[l]) {
+        mmn::k_prep_weights<<<grid1d(nf), 256, 0, st>>>(p + woff[l], d.cin, d.cout, 16, 0, wk16[l]);
+        UCK(cudaGetLastError());
+      }
     }
   }
 
@@ -1011,6 +1020,11 @@ int mm_unet_create(int grid, int batch, mm_unet** out) {
     for (int l = 0; l < MM_UNET_LAYERS; ++l) {
       u->wk[l] = u->alloc<uint4>((size_t)27 * 2 * DEFS[l].cin / 16 * DEFS[l].cout);
       u->wkT[l] = u->alloc<uint4>((size_t)27 * 2 * DEFS[l].cout / 16 * DEFS[l].cin);
+      // fewer than half an SM's worth of CTAs per sample with the default N tile: also keep N = 16
+      const mmn::Vol& v = u->vol[DEFS[l].level];
+      const int tiles = (v.t1 - v.t0 + 128 * mmn::MT - 1) / (128 * mmn::MT);
+      if (DEFS[l].cout > 16 && tiles * (DEFS[l].cout / nt_of(DEFS[l].cout)) < 76)
+        u->wk16[l] = u->alloc<uint4>((size_t)27 * 2 * DEFS[l].cin / 16 * DEFS[l].cout);
     }
     for (int t = 0; t < T_COUNT; ++t) {
       u->T[t] = u->tensor(TDEF[t][0], TDEF[t][1]);
