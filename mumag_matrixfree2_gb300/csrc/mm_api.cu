@@ -294,9 +294,9 @@ struct mm_problem {
     d.single_axis = eop.single_axis;
     d.axis0 = eop.axis0;
   }
-  // Compressed rows get the sliced-ELL copy as well (both are small below 64Ki rows), so that the
-  // autotuner can also try one thread per row: no shuffle reductions, whose FP64 adds take a third
-  // of the FP64 pipe in the lanes-per-row kernels.
+  // Compressed rows (below 64Ki rows) get a sliced-ELL copy when the autotuner asks for one: one
+  // thread per row has no shuffle reductions, whose FP64 adds take a third of the FP64 pipe in the
+  // lanes-per-row kernels.
   template <class T>
   DevMatT<T> upload_mat(const mm::HostCSR& A, bool force_sell = false) {
     const int tpr = force_sell ? 1 : choose_tpr(A.n_rows, A.nnz());
@@ -309,6 +309,8 @@ struct mm_problem {
       d.c.col = upload(A.col);
       d.c.val = upload_as<T>(A.val);
       d.stored = A.nnz();
+      d.s.n = A.n_rows;
+      return d;
     }
     upload_sell<T>(A, d);
     return d;
@@ -2726,8 +2728,10 @@ float time_ms(mm_problem* h, int reps, const std::function<void()>& f) {
 // whole V-cycles (back to back, so cache state and neighbouring kernels are those of a solve; an
 // operator timed alone, L2-hot, prefers fewer lanes than it should), and the fastest is kept.
 template <class T>
-void tune_csr(mm_problem* h, SolverT<T>& S, DevMatT<T>& M, int reps, const char* tag, int level, std::string& rep) {
+void tune_csr(mm_problem* h, SolverT<T>& S, DevMatT<T>& M, const mm::HostCSR& host, int reps, const char* tag,
+              int level, std::string& rep) {
   if (M.c.n == 0) return;  // sliced ELL only (level 0)
+  if (!M.s.sptr) h->upload_sell<T>(host, M);  // the one-thread-per-row candidate
   const int before = M.tpr;
   int best = before;
   float best_ms = 1e30f, before_ms = 1e30f;
@@ -2757,10 +2761,10 @@ void tune_solver(mm_problem* h, SolverT<T>& S, int reps, std::string& rep) {
   const int L = (int)S.lv.size();
   for (int l = 0; l < L; ++l) {
     auto& c = S.lv[l];
-    if (l > 0) tune_csr<T>(h, S, c.A, reps, "A", l, rep);
+    if (l > 0) tune_csr<T>(h, S, c.A, h->amg_h[l].A, reps, "A", l, rep);
     if (l < L - 1) {
-      tune_csr<T>(h, S, c.R, reps, "R", l, rep);
-      tune_csr<T>(h, S, c.P, reps, "P", l, rep);
+      tune_csr<T>(h, S, c.R, h->amg_h[l].R, reps, "R", l, rep);
+      tune_csr<T>(h, S, c.P, h->amg_h[l].P, reps, "P", l, rep);
     }
   }
   drop_graph(S);
