@@ -146,6 +146,7 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--pc-stagnation-nu", type=float, default=0.01)
     ap.add_argument("--memory", type=int, default=5)
     ap.add_argument("--tn-iters", type=int, default=5)
+    ap.add_argument("--L", type=int, default=None, help="CG restart period (default: the number of nodes)")
     ap.add_argument("--lr", type=float, default=0.1)
     ap.add_argument("--mu", type=float, default=0.9)
     ap.add_argument("--pc-reg", type=float, default=0.0)
@@ -156,6 +157,34 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--out-dir", default="hyst_out")
     ap.add_argument("--snapshot-every", type=int, default=1, help="VTU snapshot every N steps (0: none)")
     ap.add_argument("--verbose", action="store_true")
+    # accepted so that the reference's command lines run unchanged; this backend has a single path for
+    # each of them (assembled operators on the GPU, one device, no shell generation)
+    compat = ap.add_argument_group("accepted for compatibility, no effect")
+    compat.add_argument("--geom-backend", default="stored_JinvT", choices=["stored_JinvT", "stored_grad_phi", "on_the_fly"])
+    compat.add_argument("--chunk-elems", type=int, default=200_000)
+    compat.add_argument("--cpu-spmv-backend", default="persistent_mkl",
+                        choices=["persistent_mkl", "dot_product_mkl", "scipy", "jax_default", "custom_jax", "mkl_ffi"])
+    compat.add_argument("--poisson-solver", default="auto", choices=["auto", "jax", "pardiso", "jax_mkl"])
+    compat.add_argument("--tau-min", type=float, default=1e-6)
+    compat.add_argument("--tau-max", type=float, default=1.0)
+    compat.add_argument("--wg-threshold", type=float, default=1e-6)
+    compat.add_argument("--cpp-mkl", action=argparse.BooleanOptionalAction, default=None)
+    compat.add_argument("--data-parallel", action="store_true")
+    compat.add_argument("--benchmark", action="store_true")
+    shell = ap.add_argument_group("shell generation (with --add-shell, which this backend refuses)")
+    shell.add_argument("--shell-type", default="hull", choices=["triangles", "hull"])
+    shell.add_argument("--layers", type=int, default=None)
+    shell.add_argument("--K", type=float, default=1.5)
+    shell.add_argument("--KL", type=float, default=10.0)
+    shell.add_argument("--auto-layers", action="store_true")
+    shell.add_argument("--beta", type=float, default=1.0)
+    shell.add_argument("--center", default="0,0,0")
+    shell.add_argument("--h0", type=float, default=None)
+    shell.add_argument("--hmax", type=float, default=None)
+    shell.add_argument("--minratio", type=float, default=1.4)
+    shell.add_argument("--max-steiner", type=int, default=None)
+    shell.add_argument("--no-exact", action="store_true")
+    shell.add_argument("--shell-verbose", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"],
                     help="demag solve precision of this backend (mixed: FP32 inside FP64 refinement)")
     return ap
@@ -219,7 +248,7 @@ def main(argv=None) -> dict:
                pc_auto=args.pc_auto, pc_force_eta=args.pc_force_eta, pc_force_alpha=args.pc_force_alpha,
                pc_stagnation_nu=args.pc_stagnation_nu, tn_iters=args.tn_iters, lr=args.lr, mu=args.mu,
                pc_reg=args.pc_reg, wg_gamma=args.wg_gamma, phi_extrapolate=args.phi_extrapolate,
-               bias_type=args.bias_type, bias_strength=args.bias_strength)
+               bias_type=args.bias_type, bias_strength=args.bias_strength, L=args.L)
     m0_dir = np.array([float(x) for x in args.m0_dir.split(",")])
     for key, val in p2.items():
         if key == "m0_dir":

@@ -60,6 +60,28 @@ def test_minimizer_options_and_bias_field(tmp_path):
     assert cli.bias_field(knt, conn, np.array([1, 2]), None, 1.0) is None
 
 
+# every option of the reference's command line (src/loop.py:338-740)
+REFERENCE_OPTIONS = (
+    "--B-end", "--B-start", "--K", "--KL", "--L", "--add-shell", "--auto-layers", "--benchmark", "--beta",
+    "--bias-strength", "--bias-type", "--center", "--cg-maxiter", "--cg-tol", "--chunk-elems", "--cpp-mkl",
+    "--cpu-spmv-backend", "--dB", "--data-parallel", "--eps-a", "--geom-backend", "--h-dir", "--h0", "--hmax",
+    "--layers", "--lr", "--m0-dir", "--materials", "--max-iter", "--max-steiner", "--memory", "--mesh", "--method",
+    "--minratio", "--mu", "--no-exact", "--no-phi-extrapolate", "--operator-mode", "--out-dir", "--pc-auto",
+    "--pc-force-alpha", "--pc-force-eta", "--pc-iters", "--pc-no-auto", "--pc-reg", "--pc-stagnation-nu",
+    "--phi-extrapolate", "--poisson-reg", "--poisson-solver", "--precond-type", "--shell-type", "--shell-verbose",
+    "--snapshot-every", "--tau-f", "--tau-max", "--tau-min", "--tau0", "--tn-iters", "--verbose", "--wg-gamma",
+    "--wg-threshold")
+
+
+def test_every_reference_option_is_accepted():
+    opts = set()
+    for act in cli.parser()._actions:
+        opts.update(act.option_strings)
+    assert not set(REFERENCE_OPTIONS) - opts
+    a = cli.parser().parse_args(["m", "--L", "40", "--no-cpp-mkl", "--geom-backend", "on_the_fly"])
+    assert a.L == 40 and a.cpp_mkl is False
+
+
 def test_cli_rejects_shell_generation_and_missing_mesh():
     with pytest.raises(SystemExit):
         cli.main(["--add-shell", "--mesh", "x.npz"])
