@@ -156,8 +156,9 @@ class Problem:
         self._check("mm_rhs", lib().mm_rhs(self.h, dptr(m), dptr(b), C.byref(bb)))
         return b, bb.value
 
-    def solve_u(self, m, x0, tol, maxiter=2000):
-        """(U, iterations, rel_res, status).  Torch CUDA tensors are solved in place, without copies."""
+    def solve_u(self, m, x0, tol, maxiter=2000, out=None):
+        """(U, iterations, rel_res, status).  Torch CUDA tensors are solved in place, without copies.
+        Host arrays: `out` (a float64 (N,) array, e.g. in pinned memory) receives U, starting from x0."""
         it, rr = C.c_int(), C.c_double()
         if _is_torch_cuda(m):
             U = x0 if _is_torch_cuda(x0) else None
@@ -168,7 +169,14 @@ class Problem:
                                                                     C.byref(it), C.byref(rr)))
             return U, it.value, rr.value, rc
         m = f64(m, (self.N, 3))
-        U = f64(x0).reshape(-1).copy()
+        if out is None:
+            U = f64(x0).reshape(-1).copy()
+        else:
+            if out.dtype != np.float64 or out.shape != (self.N,) or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float64 array of shape (N,)")
+            U = out
+            if x0 is not out:
+                np.copyto(U, np.asarray(x0, np.float64).reshape(-1))
         rc = self._check("mm_solve_u", lib().mm_solve_u(self.h, dptr(m), dptr(U), float(tol), int(maxiter),
                                                         C.byref(it), C.byref(rr)))
         return U, it.value, rr.value, rc
