@@ -293,6 +293,12 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * mixed method.  Same V-cycle up to summation order.  (80 nm cube on GB300: the FP64 solve 7 % faster,
  * the FP32 iteration unchanged; mm_autotune measures it per problem.) */
 #define MM_OPT_COARSE_FUSE 9
+/* MM_OPT_MIN_FP32: precision of the minimizer's inner preconditioner solve (the Steihaug PCG on the
+ * local Hessian P y = g of mm_minimize).  -1 (default) follows MM_OPT_PRECISION: FP32 entries, vectors
+ * and float-float inner products when the demag solve is MM_PRECISION_MIXED or
+ * MM_PRECISION_FP32_PRECOND, FP64 otherwise; 0 always FP64; 1 always FP32.  The energy, the gradient,
+ * the outer iteration and the line search stay FP64 in every case. */
+#define MM_OPT_MIN_FP32 10
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

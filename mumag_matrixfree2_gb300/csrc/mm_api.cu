@@ -173,6 +173,10 @@ struct mm_problem {
   mmk::EnergySell eops{};          // the energy operator in sliced-ELL order (the kernels' layout)
   std::vector<int64_t> eops_pos;   // sliced position of every compressed-row entry
   int64_t eops_stored = 0;
+  std::vector<double> kax_h;        // easy axes (n_mat, 3)
+  mmk::EnergySell32 eops32{};      // FP32 exchange + anisotropy entries for the inner solve (lazy)
+  bool eops32_ok = false;          // built and current (a new magnetoelastic term clears it)
+  int min_fp32 = -1;               // MM_OPT_MIN_FP32
   double* d_Mn = nullptr;
   double* d_inv_M_rel = nullptr;
   double* d_inv_M_prec = nullptr;
@@ -213,6 +217,7 @@ struct mm_problem {
          *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr, *w_ys = nullptr, *w_x1 = nullptr,
          *w_x2 = nullptr, *w_x3 = nullptr, *w_x4 = nullptr, *w_U2 = nullptr, *w_U3 = nullptr;
   std::vector<double*> w_S, w_Y;
+  float *w_r3f = nullptr, *w_z3f = nullptr, *w_p3f = nullptr, *w_Ap3f = nullptr, *w_yf = nullptr;
   double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
   double* min_bias_buf = nullptr;  // its storage
   cudaEvent_t ev_after = nullptr;  // ordering point taken on another stream (mm_scale_correction_async)
@@ -293,6 +298,46 @@ struct mm_problem {
     d.mex = d.mey = nullptr;
     d.single_axis = eop.single_axis;
     d.axis0 = eop.axis0;
+  }
+  // whether the inner solve runs in FP32, building its entries on first use; false also when an entry
+  // of the operator lies outside the range FP32 represents with full precision
+  bool inner_fp32() {
+    const bool want = min_fp32 < 0 ? (mixed || fp32_precond) : min_fp32 != 0;
+    if (!want || eop_h.n_rows == 0) return false;
+    if (eops32_ok) return true;
+    // 1/V_mag is folded into the FP32 entries (the operator kernel then scales by 1)
+    double lo = 1e300, hi = 0.0;
+    auto scaled = [&](const mm::dvec& v) {
+      std::vector<double> out(v.size());
+      for (size_t k = 0; k < v.size(); ++k) {
+        out[k] = v[k] * inv_Vmag;
+        if (out[k] != 0.0) lo = std::min(lo, std::fabs(out[k])), hi = std::max(hi, std::fabs(out[k]));
+      }
+      return out;
+    };
+    const std::vector<double> w32 = scaled(eop_h.w), q32 = scaled(eop_h.q);
+    std::vector<double> mx32, my32;
+    if (eops.mex) mx32 = scaled(eop_h.mx), my32 = scaled(eop_h.my);
+    if (hi > 0.0 && (lo < 1e-30 || hi > 1e30)) return false;
+    mmk::EnergySell32& d = eops32;
+    d.n_rows = eops.n_rows;
+    d.rows = eops.rows;
+    d.sptr = eops.sptr;
+    d.col = eops.col;
+    d.mat = eops.mat;
+    d.w = upload_eop_sell<float>(w32, 0.0f);
+    d.q = upload_eop_sell<float>(q32, 0.0f);
+    d.kax = upload(std::vector<float>(kax_h.begin(), kax_h.end()));
+    d.mex = eops.mex ? upload_eop_sell<float>(mx32, 0.0f) : nullptr;
+    d.mey = eops.mex ? upload_eop_sell<float>(my32, 0.0f) : nullptr;
+    d.single_axis = eops.single_axis;
+    d.axis0 = eops.axis0;
+    if (!w_yf) {
+      const size_t n3 = 3 * (size_t)N;
+      for (float** b : {&w_r3f, &w_z3f, &w_p3f, &w_Ap3f, &w_yf}) *b = alloc<float>(n3);
+    }
+    eops32_ok = true;
+    return true;
   }
   // Compressed rows (below 64Ki rows) get a sliced-ELL copy when the autotuner asks for one: one
   // thread per row has no shuffle reductions, whose FP64 adds take a third of the FP64 pipe in the
@@ -1111,6 +1156,61 @@ int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
   return it;
 }
 
+// solve_Py_g in FP32 (the same iteration, stopping tests and fallback; scalars formed in FP64 on the
+// host from the float-float inner products, the result widened to FP64)
+int solve_Py_g32(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
+                 double reg, int max_iter, double nu) {
+  mm_problem* h = c.h;
+  const int N = c.N, n3 = 3 * N;
+  const int ge = grid_elem(N);
+  mmk::k_inner_init32<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_r3f, h->w_z3f, h->w_yf, h->d_sc,
+                                             h->d_part, R_B);
+  LAUNCH_CHECK();
+  CK(cudaMemcpyAsync(h->w_p3f, h->w_z3f, n3 * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  double rho = h->red(R_B);
+  const double target = tol * tol * rho;
+  double Q = 0.0;
+  int it = 0;
+  bool done = false;
+  const int gP = grid_elem(h->eops32.n_rows);
+  while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
+    mmk::k_apply_P_s32<<<gP, BS, 0, h->st>>>(h->eops32, m, gext, h->w_p3f, (float)reg, 1.0f, h->w_Ap3f, h->d_sc,
+                                             h->d_part, R_C);
+    LAUNCH_CHECK();
+    const double pAp = h->red(R_C);
+    const bool neg = pAp <= 0.0;
+    const double alpha = rho / (pAp + 1e-30);
+    const double dq = 0.5 * alpha * rho;
+    const bool stag = (it > 0) && (dq <= nu * Q);
+    done = neg || stag;
+    mmk::k_inner_step32<<<ge, BS, 0, h->st>>>(N, (float)alpha, (float)alpha, h->w_yf, h->w_r3f, h->w_p3f,
+                                              h->w_Ap3f, h->d_inv_M_prec, h->w_z3f, h->d_sc, h->d_part, R_B,
+                                              done ? 0 : 1);
+    LAUNCH_CHECK();
+    const double rho_next = h->red(R_B);
+    if (!done) {
+      mmk::k_xpay32<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3f, (float)(rho_next / (rho + 1e-30)), h->w_p3f);
+      LAUNCH_CHECK();
+    }
+    rho = rho_next;
+    Q = Q + dq;
+    ++it;
+  }
+  mmk::k_fallback_dots32<<<ge, BS, 0, h->st>>>(N, h->w_yf, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
+  LAUNCH_CHECK();
+  const double* f = h->red_n(R_A, 3);
+  const double yn = std::sqrt(f[0]), zn = std::sqrt(f[1]);
+  double yg = f[2];
+  const bool clip = yn > 10.0 * zn;
+  mmk::k_widen_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_yf, clip ? 10.0 * zn / (yn + 1e-30) : 1.0, y);
+  LAUNCH_CHECK();
+  if (clip) yg = dev_dot(h, n3, y, gte);
+  if (!(yg > 1e-12)) {
+    CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  }
+  return it;
+}
+
 // Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations.
 // max_iter < 0 takes pc_iters, nu < 0 the parameters' stagnation threshold.
 int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
@@ -1118,6 +1218,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   if (max_iter < 0) max_iter = c.prm->pc_iters;
   if (nu < 0) nu = c.prm->pc_stagnation_nu;
   mm_problem* h = c.h;
+  if (h->inner_fp32()) return solve_Py_g32(c, m, gext, gte, tol, y, reg, max_iter, nu);
   const int N = c.N, n3 = 3 * N;
   const int ge = grid_elem(N);
   CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
@@ -2285,7 +2386,8 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     d.dx = h->upload(o.dx);
     d.dy = h->upload(o.dy);
     d.dz = h->upload(o.dz);
-    d.kax = h->upload(std::vector<double>(k_easy, k_easy + 3 * (size_t)n_mat));
+    h->kax_h.assign(k_easy, k_easy + 3 * (size_t)n_mat);
+    d.kax = h->upload(h->kax_h);
     d.single_axis = o.single_axis ? 1 : 0;
     d.axis0 = o.mat.empty() ? 0 : o.mat[0];
     h->eop_tpr = pick_tpr((int64_t)o.col.size(), std::max(1, o.n_rows));
@@ -2528,6 +2630,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
     if (n == 0) {
       h->eop.mex = h->eop.mey = nullptr;
       h->eops.mex = h->eops.mey = nullptr;
+      h->eops32_ok = false;
       return MM_OK;
     }
     mm::assemble_magnetoelastic(h->eop_h, h->N, h->E, h->conn.data(), h->volume.data(), h->mat_id.data(), n, k1me,
@@ -2536,6 +2639,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
     h->eop.mey = h->upload(h->eop_h.my);
     h->eops.mex = h->upload_eop_sell<double>(h->eop_h.mx, 0.0);
     h->eops.mey = h->upload_eop_sell<double>(h->eop_h.my, 0.0);
+    h->eops32_ok = false;
     h->sync();
     return MM_OK;
   });
@@ -2825,6 +2929,11 @@ int mm_set_option(mm_problem* h, int option, int value) {
       return MM_ERR_ARG;
     h->mixed = value == MM_PRECISION_MIXED;
     h->fp32_precond = value == MM_PRECISION_FP32_PRECOND;
+    return MM_OK;
+  }
+  if (option == MM_OPT_MIN_FP32) {
+    if (value < -1 || value > 1) return MM_ERR_ARG;
+    h->min_fp32 = value;
     return MM_OK;
   }
   if (option == MM_OPT_GRID_CAP) {

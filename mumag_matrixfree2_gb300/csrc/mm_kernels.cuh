@@ -1202,6 +1202,179 @@ __global__ void __launch_bounds__(BS) k_rhs_s(EnergySell op, const double* __res
 }
 
 // ------------------------------------------------------------------------------------------
+// The minimizer's inner preconditioner solve (the local Hessian P y = g by Steihaug PCG) in FP32, for
+// the mixed-precision problems: FP32 copies of the exchange and anisotropy entries in the sliced
+// order, FP32 vectors, inner products accumulated in float-float and reduced in FP64.  The energy,
+// the gradient, the outer iteration and the line search stay FP64.
+// ------------------------------------------------------------------------------------------
+struct EnergySell32 {
+  int n_rows;
+  const int* rows;
+  const int* sptr;
+  const int* col;
+  const int* mat;
+  const float* w;
+  const float* q;
+  const float* kax;   // (n_mat, 3) easy axes
+  const float* mex;   // null: no magnetoelastic term
+  const float* mey;
+  int single_axis;
+  int axis0;
+};
+
+__device__ __forceinline__ void exch_aniso_sell32(const EnergySell32& op, int r, const float* __restrict__ v,
+                                                  float& ax, float& ay, float& az) {
+  const int s = r >> 5, l = r & 31;
+  const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+  ax = ay = az = 0.0f;
+  if (op.single_axis) {
+    const float kx = op.kax[3 * op.axis0], ky = op.kax[3 * op.axis0 + 1], kz = op.kax[3 * op.axis0 + 2];
+    float t = 0.0f;
+#pragma unroll 3
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const int j = __ldg(op.col + at);
+      const float vx = __ldg(v + 3 * j), vy = __ldg(v + 3 * j + 1), vz = __ldg(v + 3 * j + 2);
+      const float wk = __ldg(op.w + at);
+      ax = fmaf(wk, vx, ax);
+      ay = fmaf(wk, vy, ay);
+      az = fmaf(wk, vz, az);
+      t = fmaf(__ldg(op.q + at), fmaf(kz, vz, fmaf(ky, vy, kx * vx)), t);
+      if (op.mex) {
+        ax = fmaf(__ldg(op.mex + at), vx, ax);
+        ay = fmaf(__ldg(op.mey + at), vy, ay);
+      }
+    }
+    ax = fmaf(-t, kx, ax);
+    ay = fmaf(-t, ky, ay);
+    az = fmaf(-t, kz, az);
+  } else {
+#pragma unroll 2
+    for (int k = 0; k < wd; ++k) {
+      const int at = base + (k << 5) + l;
+      const int j = __ldg(op.col + at);
+      const int g = __ldg(op.mat + at);
+      const float kx = op.kax[3 * g], ky = op.kax[3 * g + 1], kz = op.kax[3 * g + 2];
+      const float vx = __ldg(v + 3 * j), vy = __ldg(v + 3 * j + 1), vz = __ldg(v + 3 * j + 2);
+      const float wk = __ldg(op.w + at);
+      const float t = -__ldg(op.q + at) * fmaf(kz, vz, fmaf(ky, vy, kx * vx));
+      ax = fmaf(t, kx, fmaf(wk, vx, ax));
+      ay = fmaf(t, ky, fmaf(wk, vy, ay));
+      az = fmaf(t, kz, fmaf(wk, vz, az));
+      if (op.mex) {
+        ax = fmaf(__ldg(op.mex + at), vx, ax);
+        ay = fmaf(__ldg(op.mey + at), vy, ay);
+      }
+    }
+  }
+}
+
+// Pp = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows (FP32; m and g_ext read in FP64 and
+// rounded per node); p.Pp -> red[slot]
+__global__ void __launch_bounds__(BS) k_apply_P_s32(EnergySell32 op, const double* __restrict__ m,
+                                                    const double* __restrict__ gext, const float* __restrict__ p,
+                                                    float reg, float inv_Vmag, float* __restrict__ Ap, Scalars* sc,
+                                                    double* part, int slot) {
+  Acc<float> acc;
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    float ax, ay, az;
+    exch_aniso_sell32(op, r, p, ax, ay, az);
+    const int a = __ldg(op.rows + r);
+    const float cx = ax * inv_Vmag, cy = ay * inv_Vmag, cz = az * inv_Vmag;
+    const float mx = (float)m[3 * a], my = (float)m[3 * a + 1], mz = (float)m[3 * a + 2];
+    const float mc = mx * cx + my * cy + mz * cz;
+    const float mg = mx * (float)gext[3 * a] + my * (float)gext[3 * a + 1] + mz * (float)gext[3 * a + 2];
+    const float px = p[3 * a], py = p[3 * a + 1], pz = p[3 * a + 2];
+    const float ox = cx - mc * mx - mg * px + reg * px;
+    const float oy = cy - mc * my - mg * py + reg * py;
+    const float oz = cz - mc * mz - mg * pz + reg * pz;
+    Ap[3 * a] = ox;
+    Ap[3 * a + 1] = oy;
+    Ap[3 * a + 2] = oz;
+    acc.add(px, ox);
+    acc.add(py, oy);
+    acc.add(pz, oz);
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, slot);
+}
+
+// y += ay p ; r -= ar Ap ; z = r .* w ; r.z -> red[slot]  (FP32 vectors, w the FP64 node weights)
+__global__ void __launch_bounds__(BS) k_inner_step32(int N, float ay, float ar, float* __restrict__ y,
+                                                     float* __restrict__ r, const float* __restrict__ p,
+                                                     const float* __restrict__ Ap, const double* __restrict__ w,
+                                                     float* __restrict__ z, Scalars* sc, double* part, int slot,
+                                                     int update) {
+  Acc<float> acc;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const float s = (float)w[i];
+    for (int c = 0; c < 3; ++c) {
+      float rc = r[3 * i + c];
+      if (update) {
+        y[3 * i + c] = fmaf(ay, p[3 * i + c], y[3 * i + c]);
+        rc = fmaf(-ar, Ap[3 * i + c], rc);
+        r[3 * i + c] = rc;
+      }
+      const float zc = rc * s;
+      z[3 * i + c] = zc;
+      acc.add(rc, zc);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, slot);
+}
+
+// r = fl32(g), z = r .* w ; r.z -> red[slot] (the inner solve's start from an FP64 right-hand side)
+__global__ void __launch_bounds__(BS) k_inner_init32(int N, const double* __restrict__ g,
+                                                     const double* __restrict__ w, float* __restrict__ r,
+                                                     float* __restrict__ z, float* __restrict__ y, Scalars* sc,
+                                                     double* part, int slot) {
+  Acc<float> acc;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const float s = (float)w[i];
+    for (int c = 0; c < 3; ++c) {
+      const float rc = (float)g[3 * i + c];
+      const float zc = rc * s;
+      r[3 * i + c] = rc;
+      z[3 * i + c] = zc;
+      y[3 * i + c] = 0.0f;
+      acc.add(rc, zc);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, slot);
+}
+
+// p = z + a p (FP32)
+__global__ void __launch_bounds__(BS) k_xpay32(int n, const float* __restrict__ z, float a, float* __restrict__ p) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) p[i] = fmaf(a, p[i], z[i]);
+}
+
+// the FP32 inner solve's end: |y|^2 -> red[R_A], |z_fb|^2 -> red[R_B], y.g -> red[R_C] with
+// z_fb = g .* w computed in FP64 into zf (the fallback direction, as the FP64 solve forms it)
+__global__ void __launch_bounds__(BS) k_fallback_dots32(int N, const float* __restrict__ y,
+                                                        const double* __restrict__ g, const double* __restrict__ w,
+                                                        double* __restrict__ zf, Scalars* sc, double* part) {
+  double yy = 0.0, zz = 0.0, yg = 0.0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const double s = w[i];
+    for (int c = 0; c < 3; ++c) {
+      const double gc = g[3 * i + c], yc = (double)y[3 * i + c];
+      const double zc = gc * s;
+      zf[3 * i + c] = zc;
+      yy += yc * yc;
+      zz += zc * zc;
+      yg += yc * gc;
+    }
+  }
+  grid_reduce(yy, zz, sc, part, R_A, R_B);
+  grid_reduce(yg, 0.0, sc, part, R_C);
+}
+
+// out = c * fl64(y) (the FP32 inner solution, scaled by the clipping factor, widened)
+__global__ void __launch_bounds__(BS) k_widen_scale(int n, const float* __restrict__ y, double c,
+                                                    double* __restrict__ out) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = c * (double)y[i];
+}
+
+// ------------------------------------------------------------------------------------------
 // minimizer vector kernels (3-vectors per node, xyz interleaved)
 // ------------------------------------------------------------------------------------------
 // g_tan = P_m(g .* inv_M_rel), g_tan_ext = P_m(g); max |g_tan| -> red[R_MAX]

@@ -265,7 +265,7 @@ class Problem:
     def set_option(self, name: str, value: int):
         opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5, "persistent": 6,
                 "persist_bpsm": 7, "pdl": 8,
-                "coarse_fuse": 9}
+                "coarse_fuse": 9, "min_fp32": 10}
         self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
 
     def autotune(self, reps: int = 20) -> dict:
@@ -283,6 +283,11 @@ class Problem:
         build_poisson()."""
         self.set_option("precision", {"fp64": 0, "mixed": 1, "fp32_precond": 2}[precision])
         self.precision = precision
+
+    def set_inner_precision(self, precision: str):
+        """Precision of the minimizer's inner preconditioner solve: "auto" (FP32 when the demag solve
+        is not plain FP64), "fp64" or "fp32"."""
+        self.set_option("min_fp32", {"auto": -1, "fp64": 0, "fp32": 1}[precision])
 
     def profile(self, reset: bool = False) -> list[dict]:
         """In-solve kernel profile (set_option("profile", 1) first): one row per used slot with the

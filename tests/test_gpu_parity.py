@@ -193,6 +193,30 @@ def test_minimizer_with_bias_field_matches_oracle(cuda_ok, method):
     assert np.max(np.abs(m - m_ref)) <= 1e-7
 
 
+@pytest.mark.parametrize("method", ["pcohen_hs", "plbfgs", "pcohen_lbfgs", "tn_split", "pcohen_exact"])
+def test_fp32_inner_solve_reaches_the_fp64_minimum(cuda_ok, method):
+    """The minimizer's inner preconditioner solve in FP32 (entries, vectors, float-float inner
+    products) against the FP64 one on the same problem: both stop converged on the same minimum,
+    energy to 1e-9 relative, state to 1e-4, with a comparable number of outer iterations."""
+    s, p, _ = case("cube16_h2_air48")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    m0 = random_state(p.N, seed=17, amplitude=0.3)
+    B = np.array([0.0, 0.01, -0.4])
+    out = {}
+    for inner in ("fp64", "fp32"):
+        prob.set_inner_precision(inner)
+        mp = MinimizerParams(method=method, max_iter=400, tau_f=1e-12, eps_a=1e-8, cg_tol=1e-10)
+        out[inner] = prob.minimize(B, m0, np.zeros(p.N), mp)
+    prob.set_inner_precision("auto")
+    (m64, _, i64), (m32, _, i32) = out["fp64"], out["fp32"]
+    assert i64["status"] == 0 and i32["status"] == 0, (i64, i32)
+    assert i32["preco_iters"] == 0 or i32["preco_iters"] >= 0.5 * i64["preco_iters"]
+    assert abs(i32["E"] - i64["E"]) <= 1e-9 * abs(i64["E"])
+    assert np.max(np.abs(m32 - m64)) <= 1e-4
+    assert i32["iters"] <= 1.25 * i64["iters"] + 3, (i32["iters"], i64["iters"])
+
+
 @pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
 def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     """FP32 correction solves inside FP64 iterative refinement: the true FP64 residual meets the
