@@ -299,6 +299,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * MM_PRECISION_FP32_PRECOND, FP64 otherwise; 0 always FP64; 1 always FP32.  The energy, the gradient,
  * the outer iteration and the line search stay FP64 in every case. */
 #define MM_OPT_MIN_FP32 10
+/* MM_OPT_SPLIT_A0 (default 1): in MM_PRECISION_FP32_PRECOND, the finest-level product A0 z of the
+ * FP64 PCG (z the FP32 V-cycle's output, exact in FP32) runs on the operator split into FP32 pairs
+ * a = hi + lo and sums in float-float (error ~2^-47 sum |a z|) on the FP32 pipes; 0 takes it in FP64. */
+#define MM_OPT_SPLIT_A0 11
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

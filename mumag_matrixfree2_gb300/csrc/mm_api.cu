@@ -10,6 +10,7 @@
 #include <stdexcept>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mumag_cuda.h"
@@ -191,6 +192,9 @@ struct mm_problem {
   SolverT<float> s32;            // inner solves of the mixed-precision method
   bool mixed = false;            // MM_OPT_PRECISION = MM_PRECISION_MIXED
   bool fp32_precond = false;     // MM_OPT_PRECISION = MM_PRECISION_FP32_PRECOND
+  bool split_a0 = true;          // MM_OPT_SPLIT_A0: FP32_PRECOND's A0 z with the split operator
+  mmk::SellDF a0df{};            // A0 = hi + lo in FP32 pairs (built on first use)
+  bool a0df_ok = false;
   double mixed_eta = 1e-5;       // relative reduction asked of each inner FP32 solve
   int mixed_max_outer = 12;
   int last_outer = 0;            // refinement steps of the last mixed solve
@@ -218,6 +222,26 @@ struct mm_problem {
          *w_x2 = nullptr, *w_x3 = nullptr, *w_x4 = nullptr, *w_U2 = nullptr, *w_U3 = nullptr;
   std::vector<double*> w_S, w_Y;
   float *w_r3f = nullptr, *w_z3f = nullptr, *w_p3f = nullptr, *w_Ap3f = nullptr, *w_yf = nullptr;
+  struct InnerGraph {              // the inner solve's WHILE graph for one (m, g_ext, y, reg, precision)
+    const double* m;
+    const double* gext;
+    const void* y;
+    double reg;
+    bool fp32;
+    cudaGraph_t g;
+    cudaGraphExec_t ex;
+  };
+  std::vector<InnerGraph> inner_graphs;  // at most 8, oldest replaced first
+  bool inner_graph_failed = false;
+  void drop_inner_graphs() {  // their launches hold the operator's arrays and the launch attributes
+    if (inner_graphs.empty()) return;
+    if (st) cudaStreamSynchronize(st);
+    for (auto& ig : inner_graphs) {
+      cudaGraphExecDestroy(ig.ex);
+      cudaGraphDestroy(ig.g);
+    }
+    inner_graphs.clear();
+  }
   double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
   double* min_bias_buf = nullptr;  // its storage
   cudaEvent_t ev_after = nullptr;  // ordering point taken on another stream (mm_scale_correction_async)
@@ -408,6 +432,20 @@ struct mm_problem {
     return &h_sc->red[first];
   }
   void sync() { CK(cudaStreamSynchronize(st)); }
+  // the split copy of the level-0 operator for the FP32-preconditioned PCG (sliced rows only)
+  bool use_a0df() {
+    if (!split_a0) return false;
+    if (a0df_ok) return true;
+    const DevMatT<double>& A = s64.lv[0].A;
+    if (A.tpr != 1 || A.stored <= 0 || !A.s.val) return false;
+    float* hi = alloc<float>((size_t)A.stored);
+    float* lo = alloc<float>((size_t)A.stored);
+    mmk::k_split_df<<<1024, BS, 0, st>>>(A.stored, A.s.val, hi, lo);
+    CK(cudaGetLastError());
+    a0df = mmk::SellDF{A.s.n, A.s.sptr, A.s.col, hi, lo};
+    a0df_ok = true;
+    return true;
+  }
   cudaEvent_t prof_event() {
     if (prof_used == prof_pool.size()) {
       cudaEvent_t e = nullptr;
@@ -665,12 +703,10 @@ void enqueue_iteration(mm_problem* h, SolverT<T>& S) {
   enqueue_apply_M<T>(h, S);
 }
 
-// Build the loop graph: WHILE (condition) { iteration; k_set_cond }.  Returns false when the
-// driver cannot build conditional graphs (the host-polled loop is used then).
-template <class T, class Iter>
-bool build_loop_graph(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
-  if (S.exec) return true;
-  if (S.graph_failed) return false;
+// WHILE (condition) { body(handle) } captured from the problem's stream into an instantiated graph.
+// Returns false when the driver cannot build conditional graphs (the caller polls on the host then).
+template <class Body>
+bool capture_while_graph(mm_problem* h, Body&& body, cudaGraph_t* g_out, cudaGraphExec_t* ex_out) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ex = nullptr;
   cudaGraphConditionalHandle hnd;
@@ -686,19 +722,15 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
     ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
   }
   if (ok) {
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    ok = cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+    cudaGraph_t inner = cp.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(h->st, inner, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
          cudaSuccess;
     if (ok) {
-      const int64_t saved = h->n_launch;
       try {
-        iteration();
-        launch(h, mmk::k_set_cond, 1, 32, hnd, S.sc);
+        body(hnd);
       } catch (const Fail&) {
         ok = false;
       }
-      S.iter_launches = h->n_launch - saved + 1;
-      h->n_launch = saved;
       cudaGraph_t out = nullptr;
       const bool end_ok = cudaStreamEndCapture(h->st, &out) == cudaSuccess;
       ok = ok && end_ok;
@@ -709,12 +741,30 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
     cudaGetLastError();  // clear the error of the failed attempt
     if (ex) cudaGraphExecDestroy(ex);
     if (g) cudaGraphDestroy(g);
-    S.graph_failed = true;
     return false;
   }
-  S.graph = g;
-  S.exec = ex;
+  *g_out = g;
+  *ex_out = ex;
   return true;
+}
+
+// Build the PCG loop graph: WHILE (condition) { iteration; k_set_cond }.
+template <class T, class Iter>
+bool build_loop_graph(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
+  if (S.exec) return true;
+  if (S.graph_failed) return false;
+  const int64_t saved = h->n_launch;
+  const bool ok = capture_while_graph(
+      h,
+      [&](cudaGraphConditionalHandle hnd) {
+        iteration();
+        launch(h, mmk::k_set_cond, 1, 32, hnd, S.sc);
+      },
+      &S.graph, &S.exec);
+  S.iter_launches = h->n_launch - saved + 1;
+  h->n_launch = saved;
+  if (!ok) S.graph_failed = true;
+  return ok;
 }
 template <class T>
 bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
@@ -913,22 +963,31 @@ void enqueue_iteration_mp(mm_problem* h) {
   auto& F = h->s32;
   const int N = h->N;
   auto& l0 = S.lv[0];
-  tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * 8.0 * N, [&] {
-    launch(h, mmk::k_pcg_dir<double>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
-    LAUNCH_CHECK();
-  });
+  const bool df = h->a0df_ok && h->split_a0;
+  if (df) {
+    tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 4.0 * N + 4.0 * 8.0 * N, [&] {
+      launch(h, mmk::k_pcg_dir_df, grid_ilp(N), BS, h->a0df, (const float*)F.z, S.p, S.Ap, S.sc, h->d_part);
+      LAUNCH_CHECK();
+    });
+  } else {
+    tagged<double>(h, MM_PROF_PCG_DIR, 0, mat_bytes(l0.A) + 5.0 * 8.0 * N, [&] {
+      launch(h, mmk::k_pcg_dir<double>, grid_ilp(N), BS, l0.A.s, S.z, S.p, S.Ap, S.sc, h->d_part);
+      LAUNCH_CHECK();
+    });
+  }
   tagged<double>(h, MM_PROF_PCG_STEP, 0, 6.0 * 8.0 * N + 3.0 * 4.0 * N, [&] {
     launch(h, mmk::k_pcg_step_mp, grid_ilp(N), BS, N, S.x, S.r, S.p, S.Ap, F.lv[0].s, F.r, F.lv[0].x, S.sc,
            h->d_part);
     LAUNCH_CHECK();
   });
-  enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc, S.z);
+  enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc, df ? nullptr : S.z);
 }
 
 void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
   auto& S = h->s64;
   auto& F = h->s32;
   const int N = h->N;
+  const bool df = h->use_a0df();  // z stays FP32 for the split A0 product (no FP64 copy)
   dotT<double>(h, N, S.b, (const double*)nullptr, S.sc, R_BB);
   launch(h, mmk::k_pcg_init_scalars, 1, 32, S.sc, tol, maxiter);
   LAUNCH_CHECK();
@@ -940,7 +999,7 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
   });
   launch(h, mmk::k_split_mp, grid_elem(N), BS, N, S.r, F.lv[0].s, F.r, F.lv[0].x);
   LAUNCH_CHECK();
-  enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc, S.z);
+  enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc, df ? nullptr : S.z);
   const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
@@ -1156,117 +1215,113 @@ int demag_solve(MinCtx& c, const double* m, double* U, double tol) {
   return it;
 }
 
-// solve_Py_g in FP32 (the same iteration, stopping tests and fallback; scalars formed in FP64 on the
-// host from the float-float inner products, the result widened to FP64)
-int solve_Py_g32(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
-                 double reg, int max_iter, double nu) {
-  mm_problem* h = c.h;
-  const int N = c.N, n3 = 3 * N;
-  const int ge = grid_elem(N);
-  mmk::k_inner_init32<<<ge, BS, 0, h->st>>>(N, gte, h->d_inv_M_prec, h->w_r3f, h->w_z3f, h->w_yf, h->d_sc,
-                                             h->d_part, R_B);
-  LAUNCH_CHECK();
-  CK(cudaMemcpyAsync(h->w_p3f, h->w_z3f, n3 * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  double rho = h->red(R_B);
-  const double target = tol * tol * rho;
-  double Q = 0.0;
-  int it = 0;
-  bool done = false;
-  const int gP = grid_elem(h->eops32.n_rows);
-  while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
-    mmk::k_apply_P_s32<<<gP, BS, 0, h->st>>>(h->eops32, m, gext, h->w_p3f, (float)reg, 1.0f, h->w_Ap3f, h->d_sc,
-                                             h->d_part, R_C);
-    LAUNCH_CHECK();
-    const double pAp = h->red(R_C);
-    const bool neg = pAp <= 0.0;
-    const double alpha = rho / (pAp + 1e-30);
-    const double dq = 0.5 * alpha * rho;
-    const bool stag = (it > 0) && (dq <= nu * Q);
-    done = neg || stag;
-    mmk::k_inner_step32<<<ge, BS, 0, h->st>>>(N, (float)alpha, (float)alpha, h->w_yf, h->w_r3f, h->w_p3f,
-                                              h->w_Ap3f, h->d_inv_M_prec, h->w_z3f, h->d_sc, h->d_part, R_B,
-                                              done ? 0 : 1);
-    LAUNCH_CHECK();
-    const double rho_next = h->red(R_B);
-    if (!done) {
-      mmk::k_xpay32<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3f, (float)(rho_next / (rho + 1e-30)), h->w_p3f);
-      LAUNCH_CHECK();
+// one trip of the device-driven inner solve: P p with alpha and the stop tests, the step with beta
+// and the loop test, the new direction
+template <class Op, class T>
+void enqueue_inner_trip(mm_problem* h, const Op& op, const double* m, const double* gext, T reg, T inv_Vmag, T* r,
+                        T* z, T* p, T* Ap, T* y) {
+  const int N = h->N;
+  launch(h, mmk::k_in_apply<Op, T>, grid_elem(op.n_rows), BS, op, m, gext, p, reg, inv_Vmag, Ap, h->d_sc,
+         h->d_part);
+  launch(h, mmk::k_in_step<T>, grid_elem(N), BS, N, y, r, p, Ap, h->d_inv_M_prec, z, h->d_sc, h->d_part);
+  launch(h, mmk::k_in_xpay<T>, grid_elem(3 * N), BS, 3 * N, z, p, h->d_sc);
+}
+
+// The inner PCG loop of solve_Py_g queued without host waits: setup and start, then the WHILE graph
+// cached per (m, g_ext, y, reg, precision) (or, without conditional graphs, one wait per trip).  The
+// iteration count lands in red[R_D].
+template <class Op, class T>
+void run_inner(mm_problem* h, const Op& op, const double* m, const double* gext, const double* gte, double tol,
+               double reg, T inv_Vmag, T* r, T* z, T* p, T* Ap, T* y, int max_iter, double nu) {
+  const int N = h->N;
+  launch(h, mmk::k_in_setup, 1, 32, h->d_sc, max_iter, nu, tol * tol);
+  launch(h, mmk::k_in_init<T>, grid_elem(N), BS, N, gte, h->d_inv_M_prec, r, z, p, y, h->d_sc, h->d_part);
+  h->n_launch += 2;
+  const bool fp32 = std::is_same<T, float>::value;
+  const T reg_t = (T)reg;
+  auto trip = [&] { enqueue_inner_trip<Op, T>(h, op, m, gext, reg_t, inv_Vmag, r, z, p, Ap, y); };
+  cudaGraphExec_t ex = nullptr;
+  if (h->use_graph && !h->prof && !h->inner_graph_failed) {
+    for (auto& ig : h->inner_graphs)
+      if (ig.m == m && ig.gext == gext && ig.y == y && ig.reg == reg && ig.fp32 == fp32) ex = ig.ex;
+    if (!ex) {
+      mm_problem::InnerGraph ig{m, gext, y, reg, fp32, nullptr, nullptr};
+      const bool ok = capture_while_graph(
+          h,
+          [&](cudaGraphConditionalHandle hnd) {
+            trip();
+            launch(h, mmk::k_in_cond, 1, 32, hnd, h->d_sc);
+          },
+          &ig.g, &ig.ex);
+      if (ok) {
+        if (h->inner_graphs.size() >= 8) {
+          CK(cudaStreamSynchronize(h->st));
+          cudaGraphExecDestroy(h->inner_graphs.front().ex);
+          cudaGraphDestroy(h->inner_graphs.front().g);
+          h->inner_graphs.erase(h->inner_graphs.begin());
+        }
+        h->inner_graphs.push_back(ig);
+        ex = ig.ex;
+      } else {
+        h->inner_graph_failed = true;
+      }
     }
-    rho = rho_next;
-    Q = Q + dq;
-    ++it;
   }
-  mmk::k_fallback_dots32<<<ge, BS, 0, h->st>>>(N, h->w_yf, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
-  LAUNCH_CHECK();
-  const double* f = h->red_n(R_A, 3);
-  const double yn = std::sqrt(f[0]), zn = std::sqrt(f[1]);
-  double yg = f[2];
-  const bool clip = yn > 10.0 * zn;
-  mmk::k_widen_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_yf, clip ? 10.0 * zn / (yn + 1e-30) : 1.0, y);
-  LAUNCH_CHECK();
-  if (clip) yg = dev_dot(h, n3, y, gte);
-  if (!(yg > 1e-12)) {
-    CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  if (ex) {
+    CK(cudaGraphLaunch(ex, h->st));
+    h->n_launch += 4;  // the trips' kernels are counted by the caller from the iteration count
+    return;
   }
-  return it;
+  for (int t = 0; t < max_iter + 2; ++t) {
+    trip();
+    h->n_launch += 3;
+    CK(cudaMemcpyAsync(&h->h_sc->in_done, &h->d_sc->in_done, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->h_sc->in_done) break;
+  }
 }
 
 // Inner PCG with Steihaug exit (src/minimizers.py:413-490); y = result; returns iterations.
-// max_iter < 0 takes pc_iters, nu < 0 the parameters' stagnation threshold.
+// max_iter < 0 takes pc_iters, nu < 0 the parameters' stagnation threshold.  The iteration runs on
+// the device (alpha, the curvature and stagnation tests, beta and the stopping test are formed by the
+// reductions' finishing blocks); the host waits once, for the fallback test.  In the mixed-precision
+// modes the operator, the vectors and the inner products are FP32 (float-float sums), the result is
+// widened to FP64.
 int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte, double tol, double* y,
                double reg, int max_iter = -1, double nu = -1.0) {
   if (max_iter < 0) max_iter = c.prm->pc_iters;
   if (nu < 0) nu = c.prm->pc_stagnation_nu;
   mm_problem* h = c.h;
-  if (h->inner_fp32()) return solve_Py_g32(c, m, gext, gte, tol, y, reg, max_iter, nu);
   const int N = c.N, n3 = 3 * N;
   const int ge = grid_elem(N);
-  CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
-  CK(cudaMemcpyAsync(h->w_r3, gte, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
-  LAUNCH_CHECK();
-  CK(cudaMemcpyAsync(h->w_p3, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  double rho = h->red(R_B);
-  const double target = tol * tol * rho;
-  double Q = 0.0;
-  int it = 0;
-  bool done = false;
-  const int gP = grid_elem(h->eops.n_rows);
-  while (it < max_iter && rho > target && rho > 1e-25 && rho < 1e20 && !done) {
-    mmk::k_apply_P_s<<<gP, BS, 0, h->st>>>(h->eops, m, gext, h->w_p3, reg, h->inv_Vmag, h->w_Ap3, h->d_sc, h->d_part,
-                                           R_C);
-    LAUNCH_CHECK();
-    const double pAp = h->red(R_C);
-    const bool neg = pAp <= 0.0;
-    const double alpha = rho / (pAp + 1e-30);
-    const double dq = 0.5 * alpha * rho;
-    const bool stag = (it > 0) && (dq <= nu * Q);
-    done = neg || stag;
-    mmk::k_inner_step<<<ge, BS, 0, h->st>>>(N, alpha, alpha, y, h->w_r3, h->w_p3, h->w_Ap3, h->d_inv_M_prec,
-                                             h->w_z3, h->d_sc, h->d_part, R_B, done ? 0 : 1);
-    LAUNCH_CHECK();
-    const double rho_next = h->red(R_B);
-    if (!done) {
-      mmk::k_xpay<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
-      LAUNCH_CHECK();
-    }
-    rho = rho_next;
-    Q = Q + dq;
-    ++it;
-  }
+  const bool fp32 = h->inner_fp32();
   // fallback direction z_fb = gte .* inv_M_prec (into w_z3), clipping, descent check: |y|^2, |z_fb|^2
-  // and y.gte from one pass and one wait
-  mmk::k_fallback_dots<<<ge, BS, 0, h->st>>>(N, y, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
+  // and y.gte from one pass, the iteration count beside them, one wait
+  if (fp32) {
+    run_inner<mmk::EnergySell32, float>(h, h->eops32, m, gext, gte, tol, reg, 1.0f, h->w_r3f, h->w_z3f, h->w_p3f,
+                                        h->w_Ap3f, h->w_yf, max_iter, nu);
+    mmk::k_fallback_dots32<<<ge, BS, 0, h->st>>>(N, h->w_yf, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
+  } else {
+    run_inner<mmk::EnergySell, double>(h, h->eops, m, gext, gte, tol, reg, h->inv_Vmag, h->w_r3, h->w_z3, h->w_p3,
+                                       h->w_Ap3, y, max_iter, nu);
+    mmk::k_fallback_dots<<<ge, BS, 0, h->st>>>(N, y, gte, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part);
+  }
   LAUNCH_CHECK();
-  const double* f = h->red_n(R_A, 3);
+  const double* f = h->red_n(R_A, 4);
   const double yn = std::sqrt(f[0]), zn = std::sqrt(f[1]);
   double yg = f[2];
-  if (yn > 10.0 * zn) {
-    const double c = 10.0 * zn / (yn + 1e-30);
-    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, c, y);
+  const int it = (int)f[3];
+  h->n_launch += 3 * (int64_t)it;
+  const bool clip = yn > 10.0 * zn;
+  const double cf = clip ? 10.0 * zn / (yn + 1e-30) : 1.0;
+  if (fp32) {
+    mmk::k_widen_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_yf, cf, y);
     LAUNCH_CHECK();
-    yg = dev_dot(h, n3, y, gte);  // the clipped direction's slope, as the unfused test computed it
+  } else if (clip) {
+    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, cf, y);
+    LAUNCH_CHECK();
   }
+  if (clip) yg = dev_dot(h, n3, y, gte);  // the clipped direction's slope, as the unfused test computed it
   if (!(yg > 1e-12)) {
     CK(cudaMemcpyAsync(y, h->w_z3, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   }
@@ -2444,6 +2499,7 @@ int mm_destroy(mm_problem* h) {
   if (h->s64.graph) cudaGraphDestroy(h->s64.graph);
   if (h->s32.exec) cudaGraphExecDestroy(h->s32.exec);
   if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
+  h->drop_inner_graphs();
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
   if (h->s64.h_bar) cudaFreeHost(h->s64.h_bar);
@@ -2631,6 +2687,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
       h->eop.mex = h->eop.mey = nullptr;
       h->eops.mex = h->eops.mey = nullptr;
       h->eops32_ok = false;
+      h->drop_inner_graphs();
       return MM_OK;
     }
     mm::assemble_magnetoelastic(h->eop_h, h->N, h->E, h->conn.data(), h->volume.data(), h->mat_id.data(), n, k1me,
@@ -2640,6 +2697,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
     h->eops.mex = h->upload_eop_sell<double>(h->eop_h.mx, 0.0);
     h->eops.mey = h->upload_eop_sell<double>(h->eop_h.my, 0.0);
     h->eops32_ok = false;
+    h->drop_inner_graphs();
     h->sync();
     return MM_OK;
   });
@@ -2931,6 +2989,12 @@ int mm_set_option(mm_problem* h, int option, int value) {
     h->fp32_precond = value == MM_PRECISION_FP32_PRECOND;
     return MM_OK;
   }
+  if (option == MM_OPT_SPLIT_A0) {
+    if (value != 0 && value != 1) return MM_ERR_ARG;
+    if (h->split_a0 != (value == 1)) drop_graph(h->s64);  // the captured loop holds the old product
+    h->split_a0 = value == 1;
+    return MM_OK;
+  }
   if (option == MM_OPT_MIN_FP32) {
     if (value < -1 || value > 1) return MM_ERR_ARG;
     h->min_fp32 = value;
@@ -2951,6 +3015,7 @@ int mm_set_option(mm_problem* h, int option, int value) {
     if (h->pdl != (value == 1)) {  // captured loop graphs hold the old launches
       drop_graph(h->s64);
       drop_graph(h->s32);
+      h->drop_inner_graphs();
     }
     h->pdl = value == 1;
     return MM_OK;

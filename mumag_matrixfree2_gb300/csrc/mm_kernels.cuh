@@ -38,11 +38,29 @@ struct Scalars {
   int pad;
   double red[NRED];
   unsigned cnt[NRED];
+  // the minimizer's inner (preconditioner) solve, driven on the device
+  double in_rho;     // current r.z
+  double in_target;  // tol^2 * r0.z0
+  double in_Q;       // accumulated model decrease
+  double in_dq;      // this iteration's decrease 0.5 alpha rho
+  double in_alpha;
+  double in_beta;
+  double in_tol2;
+  double in_nu;      // stagnation threshold
+  float in_alpha_f;
+  float in_beta_f;
+  int in_it;         // completed inner iterations
+  int in_max;
+  int in_stop;       // p.Pp <= 0 or stagnation: this iteration does not update y and r
+  int in_done;       // the loop ends after this iteration
+  int in_loops;      // graph-loop trips (hard stop for the conditional node)
+  int in_pad;
 };
 
 // Scalar follow-ups computed once, by the block that finishes a reduction (so that no thread of
 // the consumer kernels spends FP64 divides or compares on them).
-enum Post { POST_NONE, POST_PAP, POST_R2_STEP, POST_R2_INIT, POST_RZ, POST_MEAN };
+enum Post { POST_NONE, POST_PAP, POST_R2_STEP, POST_R2_INIT, POST_RZ, POST_MEAN, POST_IN_INIT, POST_IN_PAP,
+            POST_IN_RHO };
 
 // Programmatic dependent launch: wait until the preceding grid in the stream has completed and its
 // writes are visible, then allow the next grid to be scheduled (it waits the same way).  Both are
@@ -155,6 +173,28 @@ __device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, d
         sc->rz_valid = 1;
       } else if (post == POST_MEAN) {
         sc->red[slot0] = a / post_arg;
+      } else if (post == POST_IN_INIT) {
+        sc->in_rho = a;
+        sc->in_target = sc->in_tol2 * a;
+        sc->in_done = !(sc->in_it < sc->in_max && a > sc->in_target && a > 1e-25 && a < 1e20);
+      } else if (post == POST_IN_PAP) {
+        const double alpha = sc->in_rho / (a + 1e-30);
+        const double dq = 0.5 * alpha * sc->in_rho;
+        const bool stag = (sc->in_it > 0) && (dq <= sc->in_nu * sc->in_Q);
+        sc->in_alpha = alpha;
+        sc->in_alpha_f = (float)alpha;
+        sc->in_dq = dq;
+        sc->in_stop = (a <= 0.0) || stag;
+      } else if (post == POST_IN_RHO) {
+        const double rho = a;
+        sc->in_beta = rho / (sc->in_rho + 1e-30);
+        sc->in_beta_f = (float)sc->in_beta;
+        sc->in_rho = rho;
+        sc->in_Q = sc->in_Q + sc->in_dq;
+        sc->in_it += 1;
+        sc->red[R_D] = (double)sc->in_it;  // read by the host with the fallback test's sums
+        sc->in_done = sc->in_stop ||
+                      !(sc->in_it < sc->in_max && rho > sc->in_target && rho > 1e-25 && rho < 1e20);
       }
     }
   }
@@ -500,6 +540,107 @@ __global__ void __launch_bounds__(BS) k_pcg_dir(SellT<T> A, const T* __restrict_
       // first direction (beta = 0): p = z, Ap = A z, whatever p and Ap held before
       const T pn = beta != T(0) ? z[i] + beta * p[i] : z[i];
       const T apn = beta != T(0) ? az[q] + beta * Ap[i] : az[q];
+      p[i] = pn;
+      Ap[i] = apn;
+      acc.add(pn, apn);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_PAP, -1, POST_PAP);
+}
+
+// ------------------------------------------------------------------------------------------
+// The FP64 operator split as a = hi + lo (hi = fl32(a), lo = fl32(a - hi)), sliced-ELL order of SellT,
+// for products with FP32 vectors summed in float-float on the FP32 pipes: each entry adds hi z exactly
+// (the product's rounding error is recovered with one FMA) and lo z rounded, so a row's sum carries an
+// error of about 2^-47 sum |a z|, against 2^-53 in FP64, at 1/64 of the FP64 issue cost per entry.
+// ------------------------------------------------------------------------------------------
+struct SellDF {
+  int n;
+  const int* sptr;
+  const int* col;
+  const float* hi;
+  const float* lo;
+};
+
+__global__ void k_split_df(int64_t n, const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo) {
+  for (int64_t i = blockIdx.x * (int64_t)BS + threadIdx.x; i < n; i += (int64_t)gridDim.x * BS) {
+    const double v = a[i];
+    const float h = (float)v;
+    hi[i] = h;
+    lo[i] = (float)(v - (double)h);
+  }
+}
+
+// (sh, sl) += (hi + lo) z
+__device__ __forceinline__ void df_madd(float hi, float lo, float z, float& sh, float& sl) {
+  const float p = hi * z;
+  float e = fmaf(hi, z, -p);  // hi z = p + e exactly
+  e = fmaf(lo, z, e);
+  float t, err;
+  Acc<float>::two_sum(sh, p, t, err);
+  sh = t;
+  sl += err + e;
+}
+
+__device__ __forceinline__ void sell_rows_df(const SellDF& A, const float* __restrict__ z, const int (&row)[ILP],
+                                             float (&sh)[ILP], float (&sl)[ILP]) {
+  int base[ILP], wp[ILP];
+  int wmax = 0;
+#pragma unroll
+  for (int q = 0; q < ILP; ++q) {
+    sh[q] = 0.0f;
+    sl[q] = 0.0f;
+    wp[q] = 0;
+    base[q] = 0;
+    if (row[q] < A.n) {
+      const int s = row[q] >> 5;
+      const int b0 = __ldg(A.sptr + s);
+      wp[q] = (__ldg(A.sptr + s + 1) - b0) >> 6;
+      base[q] = b0 + 2 * (row[q] & 31);
+    }
+    wmax = max(wmax, wp[q]);
+  }
+  for (int j = 0; j < wmax; ++j) {
+    int2 c[ILP];
+    float2 vh[ILP], vl[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (j < wp[q]) {
+        c[q] = __ldg(reinterpret_cast<const int2*>(A.col + base[q] + 64 * j));
+        vh[q] = __ldg(reinterpret_cast<const float2*>(A.hi + base[q] + 64 * j));
+        vl[q] = __ldg(reinterpret_cast<const float2*>(A.lo + base[q] + 64 * j));
+      }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (j < wp[q]) {
+        df_madd(vh[q].x, vl[q].x, __ldg(z + c[q].x), sh[q], sl[q]);
+        df_madd(vh[q].y, vl[q].y, __ldg(z + c[q].y), sh[q], sl[q]);
+      }
+  }
+}
+
+// k_pcg_dir of the FP64 PCG preconditioned by the FP32 V-cycle: the V-cycle's z is exactly FP32, so
+// A z is taken with the split operator (FP32 pipes) and only the per-row updates run in FP64:
+//   p = z + beta p ; Ap = A z + beta Ap ; p.Ap -> red[R_PAP]
+__global__ void __launch_bounds__(BS) k_pcg_dir_df(SellDF A, const float* __restrict__ z, double* __restrict__ p,
+                                                   double* __restrict__ Ap, Scalars* sc, double* part) {
+  pdl_entry();
+  if (sc->done) return;
+  const double beta = sc->beta;
+  Acc<double> acc;
+  ROW_LOOP(A.n) {
+    int row[ILP];
+    float sh[ILP], sl[ILP];
+    rows_of(rb, row);
+    sell_rows_df(A, z, row, sh, sl);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int i = row[q];
+      if (i >= A.n) continue;
+      const double az = (double)sh[q] + (double)sl[q];
+      const double zi = (double)z[i];
+      const double pn = beta != 0.0 ? zi + beta * p[i] : zi;
+      const double apn = beta != 0.0 ? az + beta * Ap[i] : az;
       p[i] = pn;
       Ap[i] = apn;
       acc.add(pn, apn);
@@ -1269,84 +1410,6 @@ __device__ __forceinline__ void exch_aniso_sell32(const EnergySell32& op, int r,
   }
 }
 
-// Pp = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows (FP32; m and g_ext read in FP64 and
-// rounded per node); p.Pp -> red[slot]
-__global__ void __launch_bounds__(BS) k_apply_P_s32(EnergySell32 op, const double* __restrict__ m,
-                                                    const double* __restrict__ gext, const float* __restrict__ p,
-                                                    float reg, float inv_Vmag, float* __restrict__ Ap, Scalars* sc,
-                                                    double* part, int slot) {
-  Acc<float> acc;
-  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
-    float ax, ay, az;
-    exch_aniso_sell32(op, r, p, ax, ay, az);
-    const int a = __ldg(op.rows + r);
-    const float cx = ax * inv_Vmag, cy = ay * inv_Vmag, cz = az * inv_Vmag;
-    const float mx = (float)m[3 * a], my = (float)m[3 * a + 1], mz = (float)m[3 * a + 2];
-    const float mc = mx * cx + my * cy + mz * cz;
-    const float mg = mx * (float)gext[3 * a] + my * (float)gext[3 * a + 1] + mz * (float)gext[3 * a + 2];
-    const float px = p[3 * a], py = p[3 * a + 1], pz = p[3 * a + 2];
-    const float ox = cx - mc * mx - mg * px + reg * px;
-    const float oy = cy - mc * my - mg * py + reg * py;
-    const float oz = cz - mc * mz - mg * pz + reg * pz;
-    Ap[3 * a] = ox;
-    Ap[3 * a + 1] = oy;
-    Ap[3 * a + 2] = oz;
-    acc.add(px, ox);
-    acc.add(py, oy);
-    acc.add(pz, oz);
-  }
-  grid_finish(block_total(acc), 0.0, sc, part, slot);
-}
-
-// y += ay p ; r -= ar Ap ; z = r .* w ; r.z -> red[slot]  (FP32 vectors, w the FP64 node weights)
-__global__ void __launch_bounds__(BS) k_inner_step32(int N, float ay, float ar, float* __restrict__ y,
-                                                     float* __restrict__ r, const float* __restrict__ p,
-                                                     const float* __restrict__ Ap, const double* __restrict__ w,
-                                                     float* __restrict__ z, Scalars* sc, double* part, int slot,
-                                                     int update) {
-  Acc<float> acc;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
-    const float s = (float)w[i];
-    for (int c = 0; c < 3; ++c) {
-      float rc = r[3 * i + c];
-      if (update) {
-        y[3 * i + c] = fmaf(ay, p[3 * i + c], y[3 * i + c]);
-        rc = fmaf(-ar, Ap[3 * i + c], rc);
-        r[3 * i + c] = rc;
-      }
-      const float zc = rc * s;
-      z[3 * i + c] = zc;
-      acc.add(rc, zc);
-    }
-  }
-  grid_finish(block_total(acc), 0.0, sc, part, slot);
-}
-
-// r = fl32(g), z = r .* w ; r.z -> red[slot] (the inner solve's start from an FP64 right-hand side)
-__global__ void __launch_bounds__(BS) k_inner_init32(int N, const double* __restrict__ g,
-                                                     const double* __restrict__ w, float* __restrict__ r,
-                                                     float* __restrict__ z, float* __restrict__ y, Scalars* sc,
-                                                     double* part, int slot) {
-  Acc<float> acc;
-  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
-    const float s = (float)w[i];
-    for (int c = 0; c < 3; ++c) {
-      const float rc = (float)g[3 * i + c];
-      const float zc = rc * s;
-      r[3 * i + c] = rc;
-      z[3 * i + c] = zc;
-      y[3 * i + c] = 0.0f;
-      acc.add(rc, zc);
-    }
-  }
-  grid_finish(block_total(acc), 0.0, sc, part, slot);
-}
-
-// p = z + a p (FP32)
-__global__ void __launch_bounds__(BS) k_xpay32(int n, const float* __restrict__ z, float a, float* __restrict__ p) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) p[i] = fmaf(a, p[i], z[i]);
-}
-
 // the FP32 inner solve's end: |y|^2 -> red[R_A], |z_fb|^2 -> red[R_B], y.g -> red[R_C] with
 // z_fb = g .* w computed in FP64 into zf (the fallback direction, as the FP64 solve forms it)
 __global__ void __launch_bounds__(BS) k_fallback_dots32(int N, const float* __restrict__ y,
@@ -1366,6 +1429,136 @@ __global__ void __launch_bounds__(BS) k_fallback_dots32(int N, const float* __re
   }
   grid_reduce(yy, zz, sc, part, R_A, R_B);
   grid_reduce(yg, 0.0, sc, part, R_C);
+}
+
+// ------------------------------------------------------------------------------------------
+// The inner solve with every decision on the device (Steihaug PCG of src/minimizers.py:413-490):
+// the reductions' finishing blocks form alpha, the stagnation and curvature tests, beta and the
+// stopping test (POST_IN_*), so an inner solve is one graph launch (WHILE node) and one host wait.
+// T = double: the FP64 entries of the energy operator; T = float: the FP32 copy (1/V_mag folded in).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void exch_rows(const EnergySell& op, int r, const double* __restrict__ v, double& ax,
+                                          double& ay, double& az) {
+  exch_aniso_sell(op, r, v, ax, ay, az);
+}
+__device__ __forceinline__ void exch_rows(const EnergySell32& op, int r, const float* __restrict__ v, float& ax,
+                                          float& ay, float& az) {
+  exch_aniso_sell32(op, r, v, ax, ay, az);
+}
+
+__global__ void k_in_setup(Scalars* sc, int max_iter, double nu, double tol2) {
+  pdl_entry();
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    sc->in_max = max_iter;
+    sc->in_nu = nu;
+    sc->in_tol2 = tol2;
+    sc->in_it = 0;
+    sc->in_Q = 0.0;
+    sc->in_stop = 0;
+    sc->in_done = 0;
+    sc->in_loops = 0;
+    sc->red[R_D] = 0.0;
+  }
+}
+
+// r = g, z = r .* w, p = z, y = 0; r.z -> in_rho (POST_IN_INIT)
+template <class T>
+__global__ void __launch_bounds__(BS) k_in_init(int N, const double* __restrict__ g, const double* __restrict__ w,
+                                                T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
+                                                T* __restrict__ y, Scalars* sc, double* part) {
+  pdl_entry();
+  Acc<T> acc;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const T s = (T)w[i];
+    for (int c = 0; c < 3; ++c) {
+      const T rc = (T)g[3 * i + c];
+      const T zc = rc * s;
+      r[3 * i + c] = rc;
+      z[3 * i + c] = zc;
+      p[3 * i + c] = zc;
+      y[3 * i + c] = T(0);
+      acc.add(rc, zc);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_B, -1, POST_IN_INIT);
+}
+
+// Pp on the magnetic rows; p.Pp -> alpha, dq, the stop flag (POST_IN_PAP)
+template <class Op, class T>
+__global__ void __launch_bounds__(BS) k_in_apply(Op op, const double* __restrict__ m,
+                                                 const double* __restrict__ gext, const T* __restrict__ p, T reg,
+                                                 T inv_Vmag, T* __restrict__ Ap, Scalars* sc, double* part) {
+  pdl_entry();
+  if (sc->in_done) return;
+  Acc<T> acc;
+  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
+    T ax, ay, az;
+    exch_rows(op, r, p, ax, ay, az);
+    const int a = __ldg(op.rows + r);
+    const T cx = ax * inv_Vmag, cy = ay * inv_Vmag, cz = az * inv_Vmag;
+    const T mx = (T)m[3 * a], my = (T)m[3 * a + 1], mz = (T)m[3 * a + 2];
+    const T mc = mx * cx + my * cy + mz * cz;
+    const T mg = mx * (T)gext[3 * a] + my * (T)gext[3 * a + 1] + mz * (T)gext[3 * a + 2];
+    const T px = p[3 * a], py = p[3 * a + 1], pz = p[3 * a + 2];
+    const T ox = cx - mc * mx - mg * px + reg * px;
+    const T oy = cy - mc * my - mg * py + reg * py;
+    const T oz = cz - mc * mz - mg * pz + reg * pz;
+    Ap[3 * a] = ox;
+    Ap[3 * a + 1] = oy;
+    Ap[3 * a + 2] = oz;
+    acc.add(px, ox);
+    acc.add(py, oy);
+    acc.add(pz, oz);
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_C, -1, POST_IN_PAP);
+}
+
+// unless stopped: y += alpha p, r -= alpha Pp; z = r .* w; r.z -> beta, in_rho, the loop test
+// (POST_IN_RHO)
+template <class T>
+__global__ void __launch_bounds__(BS) k_in_step(int N, T* __restrict__ y, T* __restrict__ r,
+                                                const T* __restrict__ p, const T* __restrict__ Ap,
+                                                const double* __restrict__ w, T* __restrict__ z, Scalars* sc,
+                                                double* part) {
+  pdl_entry();
+  if (sc->in_done) return;
+  const bool update = !sc->in_stop;
+  const T alpha = scal<T>(sc->in_alpha, sc->in_alpha_f);
+  Acc<T> acc;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+    const T s = (T)w[i];
+    for (int c = 0; c < 3; ++c) {
+      T rc = r[3 * i + c];
+      if (update) {
+        y[3 * i + c] = fmaT(alpha, p[3 * i + c], y[3 * i + c]);
+        rc = fmaT(-alpha, Ap[3 * i + c], rc);
+        r[3 * i + c] = rc;
+      }
+      const T zc = rc * s;
+      z[3 * i + c] = zc;
+      acc.add(rc, zc);
+    }
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, R_B, -1, POST_IN_RHO);
+}
+
+// p = z + beta p while the loop goes on
+template <class T>
+__global__ void __launch_bounds__(BS) k_in_xpay(int n, const T* __restrict__ z, T* __restrict__ p, Scalars* sc) {
+  pdl_entry();
+  if (sc->in_done) return;
+  const T beta = scal<T>(sc->in_beta, sc->in_beta_f);
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) p[i] = fmaT(beta, p[i], z[i]);
+}
+
+// condition of the inner solve's WHILE node (bounded by max_iter + 2 trips)
+__global__ void k_in_cond(cudaGraphConditionalHandle hnd, Scalars* sc) {
+  pdl_entry();
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    sc->in_loops += 1;
+    const bool more = !sc->in_done && sc->in_loops <= sc->in_max + 2;
+    cudaGraphSetConditional(hnd, more ? 1u : 0u);
+  }
 }
 
 // out = c * fl64(y) (the FP32 inner solution, scaled by the clipping factor, widened)

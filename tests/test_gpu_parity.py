@@ -217,6 +217,26 @@ def test_fp32_inner_solve_reaches_the_fp64_minimum(cuda_ok, method):
     assert i32["iters"] <= 1.25 * i64["iters"] + 3, (i32["iters"], i64["iters"])
 
 
+@pytest.mark.parametrize("inner", ["fp64", "fp32"])
+def test_inner_solve_graph_equals_host_polled_loop(cuda_ok, inner):
+    """The inner solve's WHILE graph and the host-polled loop run the same kernels with the same
+    device-side decisions: bit-identical minimizer results."""
+    s, p, _ = case("cube8_h2_air24")
+    m0 = random_state(p.N, seed=18, amplitude=0.2)
+    B = np.array([0.0, 0.0, -0.3])
+    out = []
+    for graph in (1, 0):
+        prob = fem_utils.make_problem(s)
+        prob.set_option("graph", graph)
+        prob.build_poisson(1e-12, "amgcl")
+        prob.set_inner_precision(inner)
+        mp = MinimizerParams(method="pcohen_hs", max_iter=15, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+        out.append(prob.minimize(B, m0, np.zeros(p.N), mp))
+    (m1, U1, i1), (m0_, U0, i0) = out
+    assert i1["preco_iters"] == i0["preco_iters"] > 0 and i1["iters"] == i0["iters"]
+    assert np.array_equal(m1, m0_) and np.array_equal(U1, U0)
+
+
 @pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
 def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     """FP32 correction solves inside FP64 iterative refinement: the true FP64 residual meets the
