@@ -49,6 +49,11 @@ int g_elem_cap = MAXG;
 inline int grid_elem(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + BS - 1) / BS, g_elem_cap));
 }
+// Blocks of the minimizer's vector kernels (FP64 block reductions): about four per SM with several
+// elements per thread, so that the FP64 shuffle trees (a warp-wide FP64 add holds the SM's FP64 pipe
+// for 16 cycles) stay a small part of the launch.  Set from the device's SM count at problem creation.
+int g_vec_cap = 608;
+inline int grid_vec(int64_t n) { return std::min(grid_elem(n), g_vec_cap); }
 // grid of the kernels that keep mmk::ILP rows per thread in flight
 inline int grid_ilp(int64_t n) {
   const int64_t per = (int64_t)BS * mmk::ILP;
@@ -525,7 +530,7 @@ void spmv(mm_problem* h, const DevMatT<T>& A, const T* x, const T* b, const T* s
 
 template <class T>
 void dotT(mm_problem* h, int n, const T* x, const T* y, mmk::Scalars* sc, int slot, int post = mmk::POST_NONE) {
-  launch(h, mmk::k_dot<T>, grid_ilp(n), BS, n, x, y, sc, h->d_part, slot, post);
+  launch(h, mmk::k_dot<T>, std::min(grid_ilp(n), g_vec_cap), BS, n, x, y, sc, h->d_part, slot, post);
   LAUNCH_CHECK();
 }
 
@@ -1193,7 +1198,7 @@ double dev_dot(mm_problem* h, int n, const double* a, const double* b) {
 }
 
 double dev_absmax(mm_problem* h, int n, const double* a) {
-  mmk::k_absmax<<<grid_elem(n), BS, 0, h->st>>>(n, a, h->d_sc, h->d_part);
+  mmk::k_absmax<<<grid_vec(n), BS, 0, h->st>>>(n, a, h->d_sc, h->d_part);
   LAUNCH_CHECK();
   return h->red(R_MAX);
 }
@@ -1221,10 +1226,10 @@ template <class Op, class T>
 void enqueue_inner_trip(mm_problem* h, const Op& op, const double* m, const double* gext, T reg, T inv_Vmag, T* r,
                         T* z, T* p, T* Ap, T* y) {
   const int N = h->N;
-  launch(h, mmk::k_in_apply<Op, T>, grid_elem(op.n_rows), BS, op, m, gext, p, reg, inv_Vmag, Ap, h->d_sc,
+  launch(h, mmk::k_in_apply<Op, T>, grid_vec(op.n_rows), BS, op, m, gext, p, reg, inv_Vmag, Ap, h->d_sc,
          h->d_part);
-  launch(h, mmk::k_in_step<T>, grid_elem(N), BS, N, y, r, p, Ap, h->d_inv_M_prec, z, h->d_sc, h->d_part);
-  launch(h, mmk::k_in_xpay<T>, grid_elem(3 * N), BS, 3 * N, z, p, h->d_sc);
+  launch(h, mmk::k_in_step<T>, grid_vec(N), BS, N, y, r, p, Ap, h->d_inv_M_prec, z, h->d_sc, h->d_part);
+  launch(h, mmk::k_in_xpay<T>, grid_vec(3 * N), BS, 3 * N, z, p, h->d_sc);
 }
 
 // The inner PCG loop of solve_Py_g queued without host waits: setup and start, then the WHILE graph
@@ -1235,7 +1240,7 @@ void run_inner(mm_problem* h, const Op& op, const double* m, const double* gext,
                double reg, T inv_Vmag, T* r, T* z, T* p, T* Ap, T* y, int max_iter, double nu) {
   const int N = h->N;
   launch(h, mmk::k_in_setup, 1, 32, h->d_sc, max_iter, nu, tol * tol);
-  launch(h, mmk::k_in_init<T>, grid_elem(N), BS, N, gte, h->d_inv_M_prec, r, z, p, y, h->d_sc, h->d_part);
+  launch(h, mmk::k_in_init<T>, grid_vec(N), BS, N, gte, h->d_inv_M_prec, r, z, p, y, h->d_sc, h->d_part);
   h->n_launch += 2;
   const bool fp32 = std::is_same<T, float>::value;
   const T reg_t = (T)reg;
@@ -1293,7 +1298,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   if (nu < 0) nu = c.prm->pc_stagnation_nu;
   mm_problem* h = c.h;
   const int N = c.N, n3 = 3 * N;
-  const int ge = grid_elem(N);
+  const int ge = grid_vec(N);
   const bool fp32 = h->inner_fp32();
   // fallback direction z_fb = gte .* inv_M_prec (into w_z3), clipping, descent check: |y|^2, |z_fb|^2
   // and y.gte from one pass, the iteration count beside them, one wait
@@ -1315,10 +1320,10 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
   const bool clip = yn > 10.0 * zn;
   const double cf = clip ? 10.0 * zn / (yn + 1e-30) : 1.0;
   if (fp32) {
-    mmk::k_widen_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_yf, cf, y);
+    mmk::k_widen_scale<<<grid_vec(n3), BS, 0, h->st>>>(n3, h->w_yf, cf, y);
     LAUNCH_CHECK();
   } else if (clip) {
-    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, cf, y);
+    mmk::k_scale<<<grid_vec(n3), BS, 0, h->st>>>(n3, cf, y);
     LAUNCH_CHECK();
   }
   if (clip) yg = dev_dot(h, n3, y, gte);  // the clipped direction's slope, as the unfused test computed it
@@ -1331,7 +1336,7 @@ int solve_Py_g(MinCtx& c, const double* m, const double* gext, const double* gte
 // out = P v (the extensive local Hessian, src/minimizers.py:396-411); returns v.out
 double apply_P(MinCtx& c, const double* m, const double* gext, const double* v, double reg, double* out) {
   mm_problem* h = c.h;
-  mmk::k_apply_P_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, m, gext, v, reg, h->inv_Vmag, out, h->d_sc,
+  mmk::k_apply_P_s<<<grid_vec(h->eops.n_rows), BS, 0, h->st>>>(h->eops, m, gext, v, reg, h->inv_Vmag, out, h->d_sc,
                                                                  h->d_part, R_C);
   LAUNCH_CHECK();
   return h->red(R_C);
@@ -1340,7 +1345,7 @@ double apply_P(MinCtx& c, const double* m, const double* gext, const double* v, 
 // sum M_rel a1.b1 and sum M_rel a2.b2
 std::pair<double, double> dev_mdot2(mm_problem* h, const double* a1, const double* b1, const double* a2,
                                     const double* b2) {
-  mmk::k_mdot2<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, a1, b1, a2, b2, h->d_inv_M_rel, h->d_sc, h->d_part);
+  mmk::k_mdot2<<<grid_vec(h->N), BS, 0, h->st>>>(h->N, a1, b1, a2, b2, h->d_inv_M_rel, h->d_sc, h->d_part);
   LAUNCH_CHECK();
   const double* v = h->red_n(R_A, 2);
   return {v[0], v[1]};
@@ -1348,7 +1353,7 @@ std::pair<double, double> dev_mdot2(mm_problem* h, const double* a1, const doubl
 
 // sum M_rel |y + a p|^2
 double dev_mnorm_axpy(mm_problem* h, const double* y, double a, const double* p) {
-  mmk::k_mnorm_axpy<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, y, a, p, h->d_inv_M_rel, h->d_sc, h->d_part);
+  mmk::k_mnorm_axpy<<<grid_vec(h->N), BS, 0, h->st>>>(h->N, y, a, p, h->d_inv_M_rel, h->d_sc, h->d_part);
   LAUNCH_CHECK();
   return h->red(R_C);
 }
@@ -1364,7 +1369,7 @@ int solve_Py_g_tr(MinCtx& c, const double* m, const double* gext, const double* 
                   double tol, double reg, double* y) {
   mm_problem* h = c.h;
   const int N = c.N, n3 = 3 * N;
-  const int ge = grid_elem(N);
+  const int ge = grid_vec(N);
   CK(cudaMemsetAsync(y, 0, n3 * sizeof(double), h->st));
   CK(cudaMemcpyAsync(h->w_r3, rhs, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_r3, h->d_inv_M_prec, h->w_z3, h->d_sc, h->d_part, R_B);
@@ -1388,7 +1393,7 @@ int solve_Py_g_tr(MinCtx& c, const double* m, const double* gext, const double* 
     LAUNCH_CHECK();
     const double rho_next = h->red(R_B);
     if (!done) {
-      mmk::k_xpay<<<grid_elem(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
+      mmk::k_xpay<<<grid_vec(n3), BS, 0, h->st>>>(n3, h->w_z3, rho_next / (rho + 1e-30), h->w_p3);
       LAUNCH_CHECK();
     }
     rho = rho_next;
@@ -1399,12 +1404,12 @@ int solve_Py_g_tr(MinCtx& c, const double* m, const double* gext, const double* 
   const double yn = std::sqrt(dev_dot(h, n3, y, nullptr));
   const double zn = std::sqrt(dev_dot(h, n3, h->w_z3, nullptr));
   if (yn > 10.0 * zn) {
-    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, 10.0 * zn / (yn + 1e-30), y);
+    mmk::k_scale<<<grid_vec(n3), BS, 0, h->st>>>(n3, 10.0 * zn / (yn + 1e-30), y);
     LAUNCH_CHECK();
   }
   const double ym = std::sqrt(dev_mdot2(h, y, y, y, y).first + 1e-30);
   if (ym > delta) {
-    mmk::k_scale<<<grid_elem(n3), BS, 0, h->st>>>(n3, delta / ym, y);
+    mmk::k_scale<<<grid_vec(n3), BS, 0, h->st>>>(n3, delta / ym, y);
     LAUNCH_CHECK();
   }
   return it;
@@ -1426,7 +1431,7 @@ LSResult armijo(MinCtx& c, const double* m, double pg, const double* H, double E
   if (pg >= 0) return res;
   CK(cudaMemcpyAsync(h->w_Ut, U_base, N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   auto D = [&](double s, double& E_t) {
-    mmk::k_cayley<<<grid_elem(N), BS, 0, h->st>>>(N, m, H, s, h->w_mt);
+    mmk::k_cayley<<<grid_vec(N), BS, 0, h->st>>>(N, m, H, s, h->w_mt);
     LAUNCH_CHECK();
     res.demag += demag_solve(c, h->w_mt, h->w_Ut, c.phi_tol);
     E_t = eval(c, h->w_mt, h->w_Ut, h->w_gt_trial);
@@ -1488,7 +1493,7 @@ void accept_trial(mm_problem* h, double*& m, double*& U, double*& graw) {
 int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const mm_min_params* prm,
                  mm_min_info* info) {
   const int N = h->N, n3 = 3 * N;
-  const int ge = grid_elem(N), g3 = grid_elem(n3);
+  const int ge = grid_vec(N), g3 = grid_vec(n3);
   const int meth = prm->method;
   const bool lbfgs = meth == MM_METHOD_LBFGS || meth == MM_METHOD_PLBFGS || meth == MM_METHOD_DPLBFGS ||
                      meth == MM_METHOD_PCOHEN_LBFGS;
@@ -2416,6 +2421,12 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     h->V_mag = V_mag;
     h->inv_Vmag = 1.0 / V_mag;
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    {
+      int dev = 0, sms = 0;
+      CK(cudaGetDevice(&dev));
+      CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      if (sms > 0) g_vec_cap = std::min(4 * sms, MAXG);
+    }
     CK(cudaEventCreate(&h->ev0));
     CK(cudaEventCreate(&h->ev1));
     h->conn.assign(conn, conn + 4 * (size_t)E);

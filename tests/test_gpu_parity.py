@@ -168,6 +168,29 @@ def test_minimizer_matches_oracle(cuda_ok, method):
     assert np.max(np.abs(m - m_ref)) <= 1e-7
 
 
+@pytest.mark.parametrize("pc_iters", [0, 1, 3])
+def test_inner_iteration_cap_matches_oracle(cuda_ok, pc_iters):
+    """The device-driven inner solve at small iteration caps (0: the loop body never updates, the
+    fallback direction is taken): same counts, energy and state as the oracle."""
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    ops = ofem.assembled_operators(p)
+    su = opo.SolveU(p, ops, cg_tol=1e-10)
+    O = _oracle_ops(p, ops, su)
+    m0 = random_state(p.N, seed=19, amplitude=0.2)
+    B = np.array([0.0, 0.0, -0.3])
+    prm = omin.Params(max_iter=10, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=pc_iters)
+    m_ref, _, info_ref = omin.minimize(O, m0, B, np.zeros(p.N), prm, "pcohen_hs")
+    mp = MinimizerParams(method="pcohen_hs", max_iter=10, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=pc_iters)
+    m, _, info = prob.minimize(B, m0, np.zeros(p.N), mp)
+    assert (info["iters"], info["evals"], info["preco_iters"]) == (info_ref["iters"], info_ref["evals"],
+                                                                  info_ref["preco_iters"])
+    assert info["preco_iters"] <= pc_iters * info["iters"]
+    assert abs(info["E"] - info_ref["E"]) <= 1e-9 * abs(info_ref["E"])
+    assert np.max(np.abs(m - m_ref)) <= 1e-7
+
+
 @pytest.mark.parametrize("method", ["pcohen_hs", "ptr"])
 def test_minimizer_with_bias_field_matches_oracle(cuda_ok, method):
     """A per-node bias field (sparse_ops["B_bias"]) enters every energy evaluation of the step,
