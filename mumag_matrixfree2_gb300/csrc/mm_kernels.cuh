@@ -14,6 +14,7 @@
 
 #include <cuda/atomic>
 #include <cuda_runtime.h>
+#include <type_traits>
 #include <stdint.h>
 
 namespace mmk {
@@ -86,20 +87,26 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
-// Sum (or max) over the block; the result is returned to every thread.
+// Sum (or max) over the block; the result is returned to every thread.  Transposed: the first warp
+// folds the block's 256 values eight to a lane, then one shuffle tree, i.e. 12 warp-wide FP64
+// instructions per block instead of a tree in every warp (48); a warp-wide FP64 add holds the SM's
+// FP64 pipe for 16 cycles on this part, so the trees were a visible share of the FP64 kernels.
 template <bool MAX>
 __device__ __forceinline__ double block_reduce(double v) {
-  __shared__ double s_red[BS / 32];
+  __shared__ double s_red[BS];
   __shared__ double s_out;
-  v = MAX ? warp_max(v) : warp_sum(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();  // the previous reduction of this block has read s_red and s_out
+  s_red[threadIdx.x] = v;
   __syncthreads();
-  if (lane == 0) s_red[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    double t = lane < BS / 32 ? s_red[lane] : 0.0;
+  if (threadIdx.x < 32) {
+    double t = s_red[threadIdx.x];
+#pragma unroll
+    for (int k = 1; k < BS / 32; ++k) {
+      const double u = s_red[threadIdx.x + 32 * k];
+      t = MAX ? fmax(t, u) : t + u;
+    }
     t = MAX ? warp_max(t) : warp_sum(t);
-    if (lane == 0) s_out = t;
+    if (threadIdx.x == 0) s_out = t;
   }
   __syncthreads();
   return s_out;
@@ -261,24 +268,29 @@ __device__ __forceinline__ double scal<double>(double d, float) { return d; }
 template <>
 __device__ __forceinline__ float scal<float>(double, float f) { return f; }
 
-// Block total of an accumulator, returned to every thread (FP64 only across the warp leaders).
+// Block total of an accumulator, returned to every thread (FP64 only across the warp leaders; an
+// FP64 accumulator takes the transposed block reduction).
 template <class T>
 __device__ __forceinline__ double block_total(Acc<T>& acc) {
-  __shared__ double s_w[BS / 32];
-  __shared__ double s_out;
-  const double w = acc.warp_total();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) s_w[wid] = w;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
+  if constexpr (std::is_same<T, double>::value) {
+    return block_reduce<false>(acc.s);
+  } else {
+    __shared__ double s_w[BS / 32];
+    __shared__ double s_out;
+    const double w = acc.warp_total();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) s_w[wid] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
 #pragma unroll
-    for (int i = 0; i < BS / 32; ++i) t += s_w[i];
-    s_out = t;
+      for (int i = 0; i < BS / 32; ++i) t += s_w[i];
+      s_out = t;
+    }
+    __syncthreads();
+    return s_out;
   }
-  __syncthreads();
-  return s_out;
 }
 
 // Sliced ELL, slice height 32, entries paired: entry k of row r lives at
