@@ -519,7 +519,7 @@ def run_ours(a):
     # U every step
     m_host = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     m_host[:] = m0
-    zero = np.zeros(N)
+    zero = torch.zeros(N, dtype=torch.float64, pin_memory=True).numpy()
     U_host = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     barrier(ws)
     torch.cuda.synchronize()

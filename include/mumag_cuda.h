@@ -198,6 +198,10 @@ int mm_solve_u(mm_problem* h, const double* m, double* U_inout, double tol, int 
                double* rel_res);
 int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U_inout, double tol, int maxiter,
                    int* iters, double* rel_res);
+/* As mm_solve_u with the warm start x0 left untouched and U written to U_out (host arrays; solve_U's
+ * (m, x0) -> U of src/poisson_solve.py:748-771 without a host-side copy of x0). */
+int mm_solve_u_x0(mm_problem* h, const double* m, const double* x0, double* U_out, double tol, int maxiter,
+                  int* iters, double* rel_res);
 
 /* Magnetoelastic anisotropy (src/energy_kernels.py:212-224,319-329,411-426): per element
  * Kx_Ve = 2 (k1me + k1me_p) Ve / 20 and Ky_Ve = 2 (k1me - k1me_p) Ve / 20 (arrays of n <= n_elems

@@ -84,6 +84,7 @@ SIGNATURES = {
     "mm_precond": (C.c_int, [_vp, _dp, _dp]),
     "mm_solve_u": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_int, _ip, _dp]),
     "mm_solve_u_dev": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _ip, _dp]),
+    "mm_solve_u_x0": (C.c_int, [_vp, _dp, _dp, _dp, C.c_double, C.c_int, _ip, _dp]),
     "mm_set_node_weights": (C.c_int, [_vp, _dp, _dp]),
     "mm_set_bias_field": (C.c_int, [_vp, _dp]),
     "mm_scale_correction_async": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),

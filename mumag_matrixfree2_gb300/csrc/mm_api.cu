@@ -2685,6 +2685,19 @@ int mm_solve_u(mm_problem* h, const double* m, double* U, double tol, int maxite
   });
 }
 
+int mm_solve_u_x0(mm_problem* h, const double* m, const double* x0, double* U_out, double tol, int maxiter,
+                  int* iters, double* rel_res) {
+  if (!h || !m || !x0 || !U_out || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_U, x0, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    const int rc = solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res);
+    CK(cudaMemcpyAsync(U_out, h->d_U, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    return rc;
+  });
+}
+
 int mm_solve_u_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters,
                    double* rel_res) {
   if (!h || !d_m || !d_U || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;

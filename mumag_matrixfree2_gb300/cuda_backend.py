@@ -175,8 +175,13 @@ class Problem:
             if out.dtype != np.float64 or out.shape != (self.N,) or not out.flags.c_contiguous:
                 raise ValueError("out must be a contiguous float64 array of shape (N,)")
             U = out
-            if x0 is not out:
-                np.copyto(U, np.asarray(x0, np.float64).reshape(-1))
+            if x0 is not out:  # x0 goes to the device as it is; U lands in `out`
+                x0 = f64(x0).reshape(-1)
+                if x0.shape != (self.N,):
+                    raise ValueError("x0 must have N entries")
+                rc = self._check("mm_solve_u_x0", lib().mm_solve_u_x0(self.h, dptr(m), dptr(x0), dptr(U), float(tol),
+                                                                      int(maxiter), C.byref(it), C.byref(rr)))
+                return U, it.value, rr.value, rc
         rc = self._check("mm_solve_u", lib().mm_solve_u(self.h, dptr(m), dptr(U), float(tol), int(maxiter),
                                                         C.byref(it), C.byref(rr)))
         return U, it.value, rr.value, rc

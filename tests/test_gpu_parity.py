@@ -112,6 +112,27 @@ def test_solve_cfg_mesh_and_determinism(cuda_ok):
     assert it1 == it2 and np.array_equal(U1, U2)  # fixed grids and fixed reduction trees
 
 
+def test_solve_into_out_leaves_x0_untouched(cuda_ok):
+    """solve_u(m, x0, tol, out=U): x0 is read on the device as it is (not modified), U lands in `out`,
+    identical to the in-place host solve and to the device solve."""
+    import torch
+
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    m = random_state(p.N, seed=23, amplitude=0.2)
+    x0 = 0.01 * np.random.default_rng(24).standard_normal(p.N)
+    x0_copy = x0.copy()
+    out = torch.empty(p.N, dtype=torch.float64, pin_memory=True).numpy()
+    U1, it1, rr1, rc1 = prob.solve_u(m, x0, 1e-10, out=out)
+    assert U1 is out and np.array_equal(x0, x0_copy)
+    U2, it2, rr2, rc2 = prob.solve_u(m, x0, 1e-10)
+    assert rc1 == rc2 == 0 and it1 == it2 and np.array_equal(U1, U2)
+    Ud = torch.from_numpy(x0.copy()).cuda()
+    _, it3, _, _ = prob.solve_u(torch.from_numpy(m).cuda(), Ud, 1e-10)
+    assert it3 == it1 and np.array_equal(Ud.cpu().numpy(), U1)
+
+
 def test_solve_without_mask_projects_the_mean(cuda_ok):
     s, p, _ = case("cube8_h2_air24", with_boundary=False)
     prob = fem_utils.make_problem(s)
