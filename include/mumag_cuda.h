@@ -235,6 +235,10 @@ int mm_set_bias_field(mm_problem* h, const double* B_bias);
  * (src/cpp/cpp_mkl_minimizer.cpp:542-763). */
 int mm_minimize(mm_problem* h, const double* B_ext, double* m_inout, double* U_inout,
                 const mm_min_params* prm, mm_min_info* info);
+/* As mm_minimize with the state in device memory (d_m_inout (N,3), d_U_inout (N)), updated in place:
+ * a field sweep keeps m and U on the GPU between field steps (B_ext stays a host array of 3). */
+int mm_minimize_dev(mm_problem* h, const double* B_ext, double* d_m_inout, double* d_U_inout,
+                    const mm_min_params* prm, mm_min_info* info);
 
 /* Time one hot kernel in isolation: `reps` launches on the problem's stream, each preceded by a
  * write of a buffer larger than L2 (so every launch streams its operands from HBM), timed with CUDA

@@ -91,6 +91,7 @@ SIGNATURES = {
     "mm_scale_correction_dev": (C.c_int, [_vp, _vp, _vp, _vp, _dp]),
     "mm_set_magnetoelastic": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "mm_minimize": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
+    "mm_minimize_dev": (C.c_int, [_vp, _dp, _vp, _vp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
     "mm_autotune": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),

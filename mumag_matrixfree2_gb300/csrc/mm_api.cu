@@ -2819,6 +2819,29 @@ int mm_minimize(mm_problem* h, const double* B, double* m, double* U, const mm_m
   });
 }
 
+int mm_minimize_dev(mm_problem* h, const double* B, double* d_m, double* d_U, const mm_min_params* prm,
+                    mm_min_info* info) {
+  if (!h || !B || !d_m || !d_U || !prm) return MM_ERR_ARG;
+  if (prm->method < 0 || prm->method >= MM_METHOD_COUNT || prm->max_iter < 0) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called first"};
+    const size_t n3 = 3 * (size_t)h->N;
+    // the minimizer swaps its state with its trial buffers, so it runs on the problem's own buffers;
+    // the caller's arrays are copied in and out on the device
+    CK(cudaMemcpyAsync(h->d_m, d_m, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_U, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    double* dm = h->d_m;
+    double* dU = h->d_U;
+    const int rc = minimize_dev(h, B, dm, dU, prm, info);
+    CK(cudaMemcpyAsync(d_m, dm, n3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(d_U, dU, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    h->sync();
+    h->d_m = dm;
+    h->d_U = dU;
+    return rc;
+  });
+}
+
 int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* bytes) {
   if (!h || reps <= 0 || kernel < MM_KERNEL_SPMV_A || kernel > MM_KERNEL_HESSIAN) return MM_ERR_ARG;
   return guarded(h, [&] {

@@ -250,11 +250,27 @@ class Problem:
         if not self.poisson_built:
             raise RuntimeError("build_poisson() must be called before minimize()")
         B = f64(B_ext).reshape(3)
-        m = f64(m0, (self.N, 3)).copy()
-        U = f64(U0).reshape(-1).copy()
         info = _abi.MinInfo()
         prm = params.to_c()
-        self._check("mm_minimize", lib().mm_minimize(self.h, dptr(B), dptr(m), dptr(U), C.byref(prm), C.byref(info)))
+        if _is_torch_cuda(m0):
+            # device-resident state (a field sweep keeps m and U on the GPU): updated in place
+            import torch
+
+            m, U = m0, U0
+            if not _is_torch_cuda(U):
+                raise TypeError("U0 must be a CUDA tensor when m0 is one")
+            if (m.dtype != torch.float64 or U.dtype != torch.float64 or not m.is_contiguous()
+                    or not U.is_contiguous() or m.numel() != 3 * self.N or U.numel() != self.N):
+                raise ValueError("m0 (N,3) and U0 (N,) must be contiguous float64 CUDA tensors")
+            torch.cuda.current_stream().synchronize()  # the caller's writes are complete
+            self._check("mm_minimize_dev", lib().mm_minimize_dev(self.h, dptr(B), C.c_void_p(m.data_ptr()),
+                                                                 C.c_void_p(U.data_ptr()), C.byref(prm),
+                                                                 C.byref(info)))
+        else:
+            m = f64(m0, (self.N, 3)).copy()
+            U = f64(U0).reshape(-1).copy()
+            self._check("mm_minimize", lib().mm_minimize(self.h, dptr(B), dptr(m), dptr(U), C.byref(prm),
+                                                         C.byref(info)))
         return m, U, dict(iters=info.iters, evals=info.evals, preco_iters=info.preco_iters,
                           demag_iters=info.demag_iters, E=info.E, gnorm=info.gnorm, time=info.seconds,
                           status=info.status, demag_time=info.demag_seconds,

@@ -131,6 +131,19 @@ class NodalAverages:
         return self.wm @ m
 
 
+def _torch_cuda():
+    """torch when a CUDA device is present (the loop then keeps its state on the GPU), else None."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    return torch if torch.cuda.is_available() else None
+
+
+def _host(a) -> np.ndarray:
+    return a.cpu().numpy() if hasattr(a, "cpu") else np.asarray(a)
+
+
 def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, m0, params: LoopParams, V_mag,
                         node_volumes, M_nodal, B_bias=None, precond_type: str = "amgcl", order: int = 3,
                         energy_assembly: str = "segment_sum", grad_backend: str = "stored_grad_phi",
@@ -163,6 +176,15 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     avg = NodalAverages(geom.conn, geom.volume, geom.mat_id, Js_lookup, m.shape[0])
     m = m / np.linalg.norm(m, axis=1, keepdims=True)
     U = np.zeros(m.shape[0])
+    # m and U stay on the GPU between field steps (no host round trip of the state per step); the
+    # two averages are taken there and only their values come back
+    torch = _torch_cuda()
+    if torch is not None:
+        m = torch.from_numpy(np.ascontiguousarray(m)).cuda()
+        U = torch.zeros(m.shape[0], dtype=torch.float64, device="cuda")
+        wJ_d = torch.from_numpy(avg.wJ).cuda()
+        wm_d = torch.from_numpy(avg.wm).cuda()
+        h_d = torch.from_numpy(h).cuda()
     B_vals = field_values(params.B_start, params.B_end, params.dB, params.loop)
     history, steps = [], []
     config_idx, J_last = 0, None
@@ -177,8 +199,12 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                               wg_gamma=params.wg_gamma, L=params.L, tn_iters=params.tn_iters, lr=params.lr,
                               mu=params.mu, phi_extrapolate=params.phi_extrapolate, verbose=params.verbose)
         dt = time.perf_counter() - t0
-        J = avg.J_parallel(m, h)
-        mx, my, mz = avg.m_avg(m)
+        if torch is not None:
+            J = float((wJ_d @ m) @ h_d)
+            mx, my, mz = (wm_d @ m).cpu().numpy()
+        else:
+            J = avg.J_parallel(m, h)
+            mx, my, mz = avg.m_avg(m)
         B_t, J_t = float(Bmag) * params.Js_ref, J * params.Js_ref
         E_si = info["E"] * params.Js_ref**2 / (2.0 * 4e-7 * np.pi)
         history.append([B_t, J_t, mx, my, mz, E_si])
@@ -204,8 +230,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
             J_last = J
             if write_files and params.snapshot_every > 0:
                 io_utils.write_vtu_tetra(out_dir / io_utils.snapshot_name(config_idx, B_t), points,
-                                         np.asarray(geom.conn), point_data={"m": m.astype(np.float32),
-                                                                            "U": U.astype(np.float32)},
+                                         np.asarray(geom.conn), point_data={"m": _host(m).astype(np.float32),
+                                                                            "U": _host(U).astype(np.float32)},
                                          cell_data={"mat_id": np.asarray(geom.mat_id).astype(np.int32)})
         if write_files:
             io_utils.append_hysteresis_row(csv_path, config_idx, B_t, J_t, float(info["E"]), float(info["gnorm"]))
@@ -221,5 +247,5 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     hist = np.array(history)
     if write_files:
         io_utils.write_mh(out_dir / "hysteresis", hist)
-    return {"out_dir": str(out_dir), "csv_path": str(csv_path), "last_m": m, "last_U": U, "history": hist,
+    return {"out_dir": str(out_dir), "csv_path": str(csv_path), "last_m": _host(m), "last_U": _host(U), "history": hist,
             "steps": steps, "totals": total}

@@ -77,8 +77,8 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
             lr=float(params.get("lr", 0.1)), mu=float(params.get("mu", 0.9)),
             phi_extrapolate=bool(params.get("phi_extrapolate", False)))
         U0 = params.get("U0")
-        if U0 is None:
-            U0 = np.zeros(prob.N)
+        if U0 is None:  # a device-resident m (torch CUDA tensor) gets a device U
+            U0 = m0.new_zeros(prob.N) if hasattr(m0, "new_zeros") else np.zeros(prob.N)
         m, U, info = prob.minimize(B_ext, m0, U0, prm)
         if params.get("verbose", True):
             print(f"          number of iterations   : {info['iters']}")

@@ -189,6 +189,27 @@ def test_minimizer_matches_oracle(cuda_ok, method):
     assert np.max(np.abs(m - m_ref)) <= 1e-7
 
 
+def test_device_resident_minimize_equals_host_minimize(cuda_ok):
+    """minimize with m and U as CUDA tensors (mm_minimize_dev, updated in place) runs the same
+    iteration as with host arrays: bit-identical state and counts."""
+    import torch
+
+    s, p, _ = case("cube8_h2_air24")
+    prob = fem_utils.make_problem(s)
+    prob.build_poisson(1e-12, "amgcl")
+    m0 = random_state(p.N, seed=25, amplitude=0.2)
+    B = np.array([0.0, 0.0, -0.3])
+    mp = MinimizerParams(method="pcohen_hs", max_iter=15, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+    m1, U1, i1 = prob.minimize(B, m0, np.zeros(p.N), mp)
+    md = torch.from_numpy(m0.copy()).cuda()
+    Ud = torch.zeros(p.N, dtype=torch.float64, device="cuda")
+    m2, U2, i2 = prob.minimize(B, md, Ud, mp)
+    assert m2 is md and U2 is Ud
+    assert (i1["iters"], i1["evals"], i1["preco_iters"], i1["demag_iters"]) == \
+        (i2["iters"], i2["evals"], i2["preco_iters"], i2["demag_iters"])
+    assert np.array_equal(m2.cpu().numpy(), m1) and np.array_equal(U2.cpu().numpy(), U1)
+
+
 @pytest.mark.parametrize("pc_iters", [0, 1, 3])
 def test_inner_iteration_cap_matches_oracle(cuda_ok, pc_iters):
     """The device-driven inner solve at small iteration caps (0: the loop body never updates, the
@@ -306,7 +327,8 @@ def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
 def test_fp32_preconditioner_keeps_the_fp64_pcg(cuda_ok, name):
     """The FP64 PCG with the V-cycle applied in FP32: the stopping test is the plain method's (recursive
     FP64 residual), the true FP64 residual meets the tolerance, the iterations stay within one of the
-    FP64 preconditioner's and the potential matches the plain solve to the tolerance."""
+    FP64 preconditioner's and the potential matches the plain solve to the tolerance; the split
+    finest-level product agrees with the FP64 one."""
     s, p, _ = case(name)
     plain = fem_utils.make_problem(s)
     plain.build_poisson(1e-12, "amgcl")
@@ -330,6 +352,14 @@ def test_fp32_preconditioner_keeps_the_fp64_pcg(cuda_ok, name):
     _, it_h, rr_h, rc_h = pc.solve_u(m, np.zeros(p.N), 1e-10)
     _, it_g, _, _ = plain.solve_u(m, np.zeros(p.N), 1e-10)
     assert rc_h == 0 and rr_h <= 1e-10 and abs(it_h - it_g) <= 1
+    # the finest-level product in FP64 instead of the FP32-split operator: same iterations, the
+    # potentials agree to the split's rounding (~2^-47 relative per product)
+    U_split, it_split, _, _ = pc.solve_u(m, np.zeros(p.N), 1e-10)
+    pc.set_option("split_a0", 0)
+    U_f64, it_f64, rr_f64, rc_f64 = pc.solve_u(m, np.zeros(p.N), 1e-10)
+    pc.set_option("split_a0", 1)
+    assert rc_f64 == 0 and rr_f64 <= 1e-10 and it_f64 == it_split
+    assert rel(U_split, U_f64) <= 1e-11
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
