@@ -906,10 +906,27 @@ void drop_graph(SolverT<T>& S) {
   S.graph_failed = false;
 }
 
+// A PCG solve whose final scalars copy is queued but not yet waited for (solve_dev waits once, after
+// its own follow-up work, and then reads them with finish_pcg).
+struct PcgPending {
+  SolverT<double>* S = nullptr;
+  bool graph = false;
+  bool persist = false;
+};
+
+void finish_pcg(mm_problem* h, const PcgPending& pend, int* iters, double* r2_out) {
+  if (pend.persist && pend.S->h_bar->err != 0)
+    throw Fail{MM_ERR_CUDA, "persistent PCG: a grid-barrier wait ran out (blocks not co-resident?)"};
+  if (pend.graph) h->n_launch += (int64_t)h->h_sc->loops * pend.S->iter_launches;
+  if (iters) *iters = h->h_sc->it;
+  if (r2_out) *r2_out = h->h_sc->red[R_R2];
+}
+
 // PCG on S.x (initial guess in, solution out) for the right-hand side S.b; stops on the recursive
 // residual r.r <= tol^2 b.b or maxiter (src/poisson_solve.py:422-478).  Returns iterations and r.r.
 template <class T>
-void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out) {
+void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out,
+             PcgPending* pend = nullptr) {
   const int N = h->N;
   dotT<T>(h, N, S.b, (const T*)nullptr, S.sc, R_BB);
   launch(h, mmk::k_pcg_init_scalars, 1, 32, S.sc, tol, maxiter);
@@ -950,6 +967,12 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
     }
   }
   CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+  if constexpr (std::is_same<T, double>::value) {
+    if (pend) {
+      *pend = PcgPending{&S, graph, persist};
+      return;
+    }
+  }
   h->sync();
   if (persist && S.h_bar->err != 0)
     throw Fail{MM_ERR_CUDA, "persistent PCG: a grid-barrier wait ran out (blocks not co-resident?)"};
@@ -988,7 +1011,7 @@ void enqueue_iteration_mp(mm_problem* h) {
   enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc, df ? nullptr : S.z);
 }
 
-void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out) {
+void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out, PcgPending* pend = nullptr) {
   auto& S = h->s64;
   auto& F = h->s32;
   const int N = h->N;
@@ -1021,6 +1044,10 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
     }
   }
   CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
+  if (pend) {
+    *pend = PcgPending{&S, graph, false};
+    return;
+  }
   h->sync();
   if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
@@ -1092,15 +1119,16 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   int it = 0;
   double r2 = 0.0;
   double tol2_ref = 0.0;
+  // the PCG paths queue their scalars copy and are read after the one wait below (it carries r.r,
+  // the iteration count, tol2 and b.b)
+  PcgPending pend;
   if (h->mixed && h->s32.built) {
     run_mixed(h, tol, maxiter, &it, &r2);
     tol2_ref = tol * tol * h->red(R_BB);
   } else if (h->fp32_precond && h->s32.built && multilevel(h, h->s32)) {
-    run_pcg_mp(h, tol, maxiter, &it, &r2);
-    tol2_ref = h->h_sc->tol2;
+    run_pcg_mp(h, tol, maxiter, nullptr, nullptr, &pend);
   } else {
-    run_pcg<double>(h, h->s64, tol, maxiter, &it, &r2);
-    tol2_ref = h->h_sc->tol2;
+    run_pcg<double>(h, h->s64, tol, maxiter, nullptr, nullptr, &pend);
   }
   if (zero_mean) sub_mean(h, h->d_x);
   if (d_U != h->d_x) CK(cudaMemcpyAsync(d_U, h->d_x, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
@@ -1110,7 +1138,14 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_solve_ms = ms;
   if (h->prof) h->prof_fold();
-  const double bb0 = h->red(R_BB0);
+  double bb0;
+  if (pend.S) {
+    finish_pcg(h, pend, &it, &r2);
+    tol2_ref = h->h_sc->tol2;
+    bb0 = h->h_sc->red[R_BB0];
+  } else {
+    bb0 = h->red(R_BB0);
+  }
   if (iters) *iters = it;
   const double rr = std::sqrt(r2 / (bb0 + 1e-30));
   if (rel_res) *rel_res = rr;
