@@ -1058,133 +1058,12 @@ __device__ __forceinline__ void exch_aniso_row(const EnergyDev& op, int r, bool 
   az = group_sum<TPR>(az);
 }
 
-// g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E]
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_energy_grad(EnergyDev op, const double* __restrict__ m,
-                                                    const double* __restrict__ U, const double* __restrict__ Mn,
-                                                    double Bx, double By, double Bz, const double* __restrict__ Bbias,
-                                                    double inv_Vmag, double* __restrict__ g, Scalars* sc,
-                                                    double* part) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  double en = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
-    const int r = rb + threadIdx.x / TPR;
-    const bool valid = r < op.n_rows;
-    double ax, ay, az;
-    exch_aniso_row<TPR>(op, r, valid, lane, m, ax, ay, az);
-    double ux = 0, uy = 0, uz = 0;
-    if (valid) {
-      const int s = op.ptr[r], e = op.ptr[r + 1];
-      for (int k = s + lane; k < e; k += TPR) {
-        const double u = __ldg(U + op.col[k]);
-        ux += op.gx[k] * u;
-        uy += op.gy[k] * u;
-        uz += op.gz[k] * u;
-      }
-    }
-    ux = group_sum<TPR>(ux);
-    uy = group_sum<TPR>(uy);
-    uz = group_sum<TPR>(uz);
-    if (valid && lane == 0) {
-      const int a = op.rows[r];
-      double bx = Bx, by = By, bz = Bz;
-      if (Bbias) {
-        bx += Bbias[3 * a];
-        by += Bbias[3 * a + 1];
-        bz += Bbias[3 * a + 2];
-      }
-      const double mn = -2.0 * Mn[a];
-      const double zx = mn * bx, zy = mn * by, zz = mn * bz;
-      const double gx = (ax + ux) + zx, gy = (ay + uy) + zy, gz = (az + uz) + zz;
-      en += m[3 * a] * (gx + zx) + m[3 * a + 1] * (gy + zy) + m[3 * a + 2] * (gz + zz);
-      g[3 * a] = gx * inv_Vmag;
-      g[3 * a + 1] = gy * inv_Vmag;
-      g[3 * a + 2] = gz * inv_Vmag;
-    }
-  }
-  grid_reduce(en, 0.0, sc, part, R_E);
-}
-
-// out = C v / V_mag on the magnetic rows
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_local_grad(EnergyDev op, const double* __restrict__ v, double inv_Vmag,
-                                                   double* __restrict__ out) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
-    const int r = rb + threadIdx.x / TPR;
-    const bool valid = r < op.n_rows;
-    double ax, ay, az;
-    exch_aniso_row<TPR>(op, r, valid, lane, v, ax, ay, az);
-    if (valid && lane == 0) {
-      const int a = op.rows[r];
-      out[3 * a] = ax * inv_Vmag;
-      out[3 * a + 1] = ay * inv_Vmag;
-      out[3 * a + 2] = az * inv_Vmag;
-    }
-  }
-}
-
-// Inner-PCG operator P p = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows; p.Pp -> red[slot]
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_apply_P(EnergyDev op, const double* __restrict__ m,
-                                                const double* __restrict__ gext, const double* __restrict__ p,
-                                                double reg, double inv_Vmag, double* __restrict__ Ap, Scalars* sc,
-                                                double* part, int slot) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  double d = 0.0;
-  for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
-    const int r = rb + threadIdx.x / TPR;
-    const bool valid = r < op.n_rows;
-    double ax, ay, az;
-    exch_aniso_row<TPR>(op, r, valid, lane, p, ax, ay, az);
-    if (valid && lane == 0) {
-      const int a = op.rows[r];
-      const double cx = ax * inv_Vmag, cy = ay * inv_Vmag, cz = az * inv_Vmag;
-      const double mx = m[3 * a], my = m[3 * a + 1], mz = m[3 * a + 2];
-      const double mc = mx * cx + my * cy + mz * cz;
-      const double mg = mx * gext[3 * a] + my * gext[3 * a + 1] + mz * gext[3 * a + 2];
-      const double px = p[3 * a], py = p[3 * a + 1], pz = p[3 * a + 2];
-      const double ox = cx - mc * mx - mg * px + reg * px;
-      const double oy = cy - mc * my - mg * py + reg * py;
-      const double oz = cz - mc * mz - mg * pz + reg * pz;
-      Ap[3 * a] = ox;
-      Ap[3 * a + 1] = oy;
-      Ap[3 * a + 2] = oz;
-      d += px * ox + py * oy + pz * oz;
-    }
-  }
-  grid_reduce(d, 0.0, sc, part, slot);
-}
-
-// b = D m on the magnetic rows (other rows untouched)
-template <int TPR>
-__global__ void __launch_bounds__(BS) k_rhs(EnergyDev op, const double* __restrict__ m, double* __restrict__ b) {
-  constexpr int RPB = BS / TPR;
-  const int lane = threadIdx.x % TPR;
-  for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
-    const int r = rb + threadIdx.x / TPR;
-    const bool valid = r < op.n_rows;
-    double acc = 0.0;
-    if (valid) {
-      const int s = op.ptr[r], e = op.ptr[r + 1];
-      for (int k = s + lane; k < e; k += TPR) {
-        const int j = op.col[k];
-        acc += op.dx[k] * __ldg(m + 3 * j) + op.dy[k] * __ldg(m + 3 * j + 1) + op.dz[k] * __ldg(m + 3 * j + 2);
-      }
-    }
-    acc = group_sum<TPR>(acc);
-    if (valid && lane == 0) b[op.rows[r]] = acc;
-  }
-}
-
 // ------------------------------------------------------------------------------------------
 // The energy operator in sliced-ELL order, one thread per magnetic row.  On this part a warp-wide
-// FP64 instruction costs 16 SM cycles whatever its active lanes, so the lanes-per-row kernels above
-// spend most of their FP64 issue on idle lanes, shuffle reductions and a one-lane epilogue; here
-// every FP64 instruction does useful work for 32 rows and the loads are coalesced across the warp.
+// FP64 instruction costs 16 SM cycles whatever its active lanes, so lanes-per-row kernels over the
+// compressed rows (kept above only for the allocation-free entry point) spend most of their FP64
+// issue on idle lanes, shuffle reductions and a one-lane epilogue; here every FP64 instruction does
+// useful work for 32 rows and the loads are coalesced across the warp.
 // ------------------------------------------------------------------------------------------
 // Slices of 32 rows: entry k of lane l of slice s at sptr[s] + 32 k + l; padding entries carry zero
 // values and the row's own node as column (the per-node arrays are only read, never indexed out of
@@ -1259,7 +1138,7 @@ __device__ __forceinline__ void exch_aniso_sell(const EnergySell& op, int r, con
   }
 }
 
-// as k_energy_grad, sliced layout
+// g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E]
 __global__ void __launch_bounds__(BS) k_energy_grad_s(EnergySell op, const double* __restrict__ m,
                                                       const double* __restrict__ U, const double* __restrict__ Mn,
                                                       double Bx, double By, double Bz,
@@ -1298,7 +1177,7 @@ __global__ void __launch_bounds__(BS) k_energy_grad_s(EnergySell op, const doubl
   grid_reduce(en, 0.0, sc, part, R_E);
 }
 
-// as k_local_grad, sliced layout
+// out = C v / V_mag on the magnetic rows
 __global__ void __launch_bounds__(BS) k_local_grad_s(EnergySell op, const double* __restrict__ v, double inv_Vmag,
                                                      double* __restrict__ out) {
   for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
@@ -1311,7 +1190,7 @@ __global__ void __launch_bounds__(BS) k_local_grad_s(EnergySell op, const double
   }
 }
 
-// as k_apply_P, sliced layout
+// Pp = C p - (m.Cp) m - (m.g_ext) p + reg p on the magnetic rows; p.Pp -> red[slot]
 __global__ void __launch_bounds__(BS) k_apply_P_s(EnergySell op, const double* __restrict__ m,
                                                   const double* __restrict__ gext, const double* __restrict__ p,
                                                   double reg, double inv_Vmag, double* __restrict__ Ap, Scalars* sc,
@@ -1337,7 +1216,7 @@ __global__ void __launch_bounds__(BS) k_apply_P_s(EnergySell op, const double* _
   grid_reduce(d, 0.0, sc, part, slot);
 }
 
-// as k_rhs, sliced layout: b = D m on the magnetic rows
+// b = D m on the magnetic rows (other rows untouched)
 __global__ void __launch_bounds__(BS) k_rhs_s(EnergySell op, const double* __restrict__ m, double* __restrict__ b) {
   for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
     const int s = r >> 5, l = r & 31;
