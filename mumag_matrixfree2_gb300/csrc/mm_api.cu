@@ -1232,6 +1232,10 @@ double dev_dot(mm_problem* h, int n, const double* a, const double* b) {
   return h->red(R_A);
 }
 
+// reductions read together with one copy sit in consecutive slots
+static_assert(mmk::R_A == mmk::R_MAX + 1 && mmk::R_B == mmk::R_MAX + 2 && mmk::R_D == mmk::R_C + 1,
+              "consecutive reduction slots");
+
 double dev_absmax(mm_problem* h, int n, const double* a) {
   mmk::k_absmax<<<grid_vec(n), BS, 0, h->st>>>(n, a, h->d_sc, h->d_part);
   LAUNCH_CHECK();
@@ -1725,12 +1729,15 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     if (cg_family) {
       // preconditioned CG: HS beta (pcohen_hs, pcg) or PR beta (pcohen); pcg keeps d_prev unprojected
       c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm_inf), h->w_y, prm->pc_reg);
-      const double gsm = dev_absmax(h, n3, h->w_y);
+      // max|y| (R_MAX) and the two HS sums (R_A, R_B) read with one copy and one wait
+      mmk::k_absmax<<<grid_vec(n3), BS, 0, h->st>>>(n3, h->w_y, h->d_sc, h->d_part);
+      LAUNCH_CHECK();
       mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, h->d_sc, h->d_part);
       LAUNCH_CHECK();
-      const double* ab = h->red_n(R_A, 2);
-      const double num = ab[0];
-      const double den = (meth == MM_METHOD_PCOHEN ? dev_dot(h, n3, h->w_ys, h->w_gprev) : ab[1]) + 1e-30;
+      const double* mab = h->red_n(R_MAX, 3);
+      const double gsm = mab[0];
+      const double num = mab[1];
+      const double den = (meth == MM_METHOD_PCOHEN ? dev_dot(h, n3, h->w_ys, h->w_gprev) : mab[2]) + 1e-30;
       const double beta = (it % L == 0) ? 0.0 : std::max(0.0, num / den);
       pg = direction(h->w_y, h->w_dprev, beta, meth == MM_METHOD_PCG ? 0 : 1);
       conv_gnorm = gnorm = gsm;
