@@ -6,9 +6,10 @@ residual 1e-10 for the seeded initial magnetisation, on the 80 nm cube at 1.6 nm
 graded 200 nm air box (357,911 nodes, 2,058,000 tetrahedra).
 
   python bench.py [--gpus N --steps K --warmup W]          this project's CUDA path
-  python bench.py --impl reference [...]                   the reference algorithm on the host CPU
-                                                           (the numpy/scipy port: the reference's own
-                                                           code needs JAX/PyAMG or Intel MKL)
+  python bench.py --impl reference [...]                   the reference's C++ CPU path on all host
+                                                           cores (its source compiled against the
+                                                           MKL-API shim; the checked port of its entry
+                                                           points where the source is absent)
 
 The headline `value` is the plain FP64 method (device time of K solves, CUDA graph).  The same line
 carries the end-to-end rate through the host-pointer C-ABI call, the in-solve kernel profile (an
@@ -71,7 +72,6 @@ def parse():
                          "profiling their kernels)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
-    ap.add_argument("--ref-procs", type=int, default=0, help="reference arm worker processes (0: all cores)")
     ap.add_argument("--ref-budget-s", type=float, default=150.0, help="reference arm: cap on timed seconds")
     a = ap.parse_args()
     if a.steps is None:
@@ -201,81 +201,92 @@ class Clocks:
 
 
 # ------------------------------------------------------------------------------------------------
-# reference arm: the oracle port on the host cores
+# reference arm: the reference's C++ CPU path on the host cores
 # ------------------------------------------------------------------------------------------------
-_REF = {}
+def _omp_env():
+    """OpenMP on every host core, as the reference's README runs its C++ path (README.md:74-82); set
+    before the library (and its OpenMP runtime) is loaded."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.environ.setdefault("OMP_PROC_BIND", "true")
+    os.environ.setdefault("OMP_PLACES", "cores")
 
 
-def _ref_solve(_):
-    su, m0, N, tol = _REF["su"], _REF["m0"], _REF["N"], _REF["tol"]
-    _, it, _ = su(m0, np.zeros(N), tol, return_info=True)
-    return it
-
-
-def build_oracle_solver(knt, ijk, mats, tol):
+def cpu_problem(knt, ijk, mats, tol):
+    """The workload set up for the reference's C++ CPU path: oracle/_ref/libcpp_mkl_minimizer.so (the
+    reference's src/cpp/cpp_mkl_minimizer.cpp compiled unchanged against the MKL-API shim) where it
+    was built, else the port of its entry points (oracle/_build/libref_port.so, checked equal to it)."""
+    from oracle import build_ref, ref_cpp
     from oracle import fem as ofem
-    from oracle import poisson as opo
 
+    build_ref.build()
+    lib = ref_cpp.load("any")
+    if lib is None:
+        raise RuntimeError("the oracle's C++ libraries could not be built")
     A, K1, Js, k = mats
     p = ofem.make_problem(knt, ijk, A, K1, Js, k)
-    su = opo.SolveU(p, ofem.assembled_operators(p, parts=("A", "D")), cg_tol=tol)
-    return p, su
+    return lib, p, ref_cpp.CppProblem(lib, p, pardiso_tol=tol)
 
 
-def cpu_solves(knt, ijk, mats, m0, tol, n_solves):
-    """The oracle (numpy/scipy FP64 port of the reference's PCG + V-cycle), one thread, timed."""
-    p, su = build_oracle_solver(knt, ijk, mats, tol)
-    zero = np.zeros(p.N)
-    su(m0, zero, tol)  # warm the caches once
+def cpu_solve_rate(cp, m0, n):
+    """n demag solves (solve_poisson: D m, the shim's pardiso solve, masks), timed; (solves/s, iters)."""
     t0 = time.perf_counter()
-    its = []
-    for _ in range(n_solves):
-        _, it, _ = su(m0, zero, tol, return_info=True)
-        its.append(it)
+    for _ in range(n):
+        cp.solve_poisson(m0)
     dt = time.perf_counter() - t0
-    return n_solves / dt, its
+    return n / dt, cp.lib.last_solve()[0], dt
+
+
+def cpu_energy_rate(cp, m0, U, n):
+    """n calls of evaluate_energy_and_grad, timed: evaluations/s."""
+    B = np.array([0.0, 0.0, -0.3])
+    t0 = time.perf_counter()
+    for _ in range(n):
+        cp.energy_and_grad(m0, U, B)
+    return n / (time.perf_counter() - t0)
+
+
+def _lib_note(lib):
+    if lib.kind == "reference":
+        return ("the reference's src/cpp/cpp_mkl_minimizer.cpp compiled unchanged against the project's MKL-API "
+                "shim (PARDISO replaced by SA-AMG PCG to the same tolerance)")
+    return ("the port of the reference's C++ entry points over the MKL-API shim (the reference source is not "
+            "on this host; a CPU test checks the port equals the reference library)")
 
 
 def run_reference(a):
-    """Every step runs one cold-start solve in each of P forked worker processes (one thread each:
-    the scipy SpMV is single-threaded), so the rate uses all host cores."""
+    """Each step is one demag solve through the reference's C++ entry point solve_poisson
+    (src/cpp/cpp_mkl_minimizer.cpp:208-231): D m, the solve, the masks, with OpenMP on all host cores.
+    PARDISO's direct solve is replaced by the shim's SA-AMG PCG to the workload's tolerance."""
     rank, local, ws = dist()
     if rank != 0:
         return
-    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[v] = "1"
-    import multiprocessing as mp
-
+    _omp_env()
     knt, ijk, mats, m0 = workload_inputs(a.workload)
-    p, su = build_oracle_solver(knt, ijk, mats, a.tol)
-    P = a.ref_procs or os.cpu_count() or 1
-    _REF.update(su=su, m0=m0, N=p.N, tol=a.tol)
-    ctx = mp.get_context("fork")  # no CUDA context exists in this process
-    with ctx.Pool(P) as pool:
-        t_step = 0.0
-        for _ in range(max(1, a.warmup)):
-            t0 = time.perf_counter()
-            pool.map(_ref_solve, range(P))
-            t_step = time.perf_counter() - t0
-        steps = a.steps
-        if steps * t_step > a.ref_budget_s:
-            steps = max(1, int(a.ref_budget_s / t_step))
-        t0 = time.perf_counter()
-        its = []
-        for _ in range(steps):
-            its += pool.map(_ref_solve, range(P))
-        dt = time.perf_counter() - t0
-    v = P * steps / dt
+    t0 = time.perf_counter()
+    lib, p, cp = cpu_problem(knt, ijk, mats, a.tol)
+    setup_s = time.perf_counter() - t0
+    for _ in range(max(1, a.warmup)):
+        t1 = time.perf_counter()
+        U = cp.solve_poisson(m0)
+        t_step = time.perf_counter() - t1
+    steps = a.steps
+    if steps * t_step > a.ref_budget_s:
+        steps = max(1, int(a.ref_budget_s / t_step))
+    v, it, dt = cpu_solve_rate(cp, m0, steps)
+    rr = cp.lib.last_solve()[1]
+    evals = cpu_energy_rate(cp, m0, U, 10)
+    threads = lib.threads()
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": ws, "steps": steps,
         "steps_requested": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": a.workload, "nodes": int(p.N), "tets": int(len(ijk)), "tol": a.tol,
-                   "precond": "SA-AMG V(1,1) SPAI0", "pcg_iters_per_solve": its[0],
-                   "parallelism": f"{P} processes x 1 thread, one independent solve each per step"},
-        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": P, "kind": "port",
-                         "sample": f"{steps} steps x {P} concurrent cold-start solves of the full workload "
-                                   f"(numpy/scipy FP64 port of the reference PCG + SA-AMG V-cycle)"},
+                   "precond": "SA-AMG V(1,1) SPAI0 (shim)", "pcg_iters_per_solve": it, "rel_res": rr,
+                   "setup_s": setup_s, "parallelism": f"one process, {threads} OpenMP threads"},
+        "energy_grad_evals_per_s": evals,
+        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": lib.kind,
+                         "library": str(lib.path.relative_to(ROOT)),
+                         "sample": f"{steps} cold-start demag solves of the full workload, {_lib_note(lib)}"},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -470,6 +481,7 @@ def run_batch_leg(a):
 
 
 def run_ours(a):
+    _omp_env()  # the in-line CPU baseline's OpenMP runtime: every host core
     import torch
 
     rank, local, ws = dist()
@@ -618,10 +630,15 @@ def run_ours(a):
 
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
-        v_cpu, its_cpu = cpu_solves(knt, ijk, mats, m0, a.tol, 8)
-        cpu = {"value": v_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"8 cold-start solves of the same workload by the numpy/scipy FP64 oracle, one thread "
-                         f"({its_cpu[0]} PCG iterations each)"}
+        lib, _, cp = cpu_problem(knt, ijk, mats, a.tol)
+        U_cpu = cp.solve_poisson(m0)
+        v_cpu, it_cpu, _ = cpu_solve_rate(cp, m0, 10)
+        cpu = {"value": v_cpu, "unit": "solves/s", "cores": lib.threads(), "kind": lib.kind,
+               "library": str(lib.path.relative_to(ROOT)),
+               "energy_grad_evals_per_s": cpu_energy_rate(cp, m0, U_cpu, 10),
+               "sample": f"10 cold-start demag solves of the same workload ({it_cpu} PCG iterations each), "
+                         f"{_lib_note(lib)}"}
+        del cp
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": a.steps,

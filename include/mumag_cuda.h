@@ -76,6 +76,11 @@ typedef struct {
   double lr;            /* PNAG's initial line-search step; <= 0 means 0.1                           */
   double mu;            /* PNAG's momentum (0.9 in the reference)                                     */
   int phi_extrapolate;  /* PNAG: warm-start the look-ahead solve from 2 U - U_prev                    */
+  int cpp_semantics;    /* pcohen_hs / pcohen only: the conventions of the reference's C++ minimizer
+                           (--cpp-mkl, run_cpp_pcohen_hs_minimization, src/cpp/cpp_mkl_minimizer.cpp:
+                           542-763): an inner solve on the initial state counted in preco_iters, inner
+                           trips that stop on curvature or stagnation not counted, and the energy test
+                           of the convergence check against the energy two iterations back         */
 } mm_min_params;
 
 typedef struct {
@@ -176,6 +181,17 @@ int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const double* d_U, 
 /* Exchange + anisotropy Hessian action C v / V_mag.
  * Replaces local_grad_only (src/energy_kernels.py:190-195,272-338). */
 int mm_local_grad(mm_problem* h, const double* v, double* out);
+
+/* Inner preconditioned CG with the Steihaug exit on P y = g_tan_ext (N,3 host arrays; P the projected
+ * local Hessian of the state m for the full gradient g_ext, Jacobi preconditioner inv_M_prec of
+ * mm_set_node_weights), y = result.  Replaces solve_Py_g, src/cpp/cpp_mkl_minimizer.cpp:233-359
+ * (make_preconditioner_op.solve_Py_g, src/minimizers.py:413-490): at most max_iter iterations, stop
+ * at r.z <= tol^2 r0.z0, stagnation when 0.5 alpha rho <= stagnation_nu Q, y clipped to 10 |z_fb|,
+ * z_fb = g_tan_ext .* inv_M_prec when y is no descent direction.  *iters counts as the C++ function
+ * counts (a trip that stops on curvature or stagnation is not counted).  FP32 when the problem's
+ * inner precision is FP32. */
+int mm_solve_py_g(mm_problem* h, const double* m, const double* g_ext, const double* g_tan_ext, int max_iter,
+                  double tol, double reg, double stagnation_nu, double* y, int* iters);
 
 /* Diagonal of the exchange operator / V_mag (src/energy_kernels.py:492-566). */
 int mm_exchange_diagonal(mm_problem* h, double* d);

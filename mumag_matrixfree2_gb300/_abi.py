@@ -41,6 +41,7 @@ class MinParams(C.Structure):
         ("pc_force_eta", C.c_double), ("pc_force_alpha", C.c_double), ("pc_stagnation_nu", C.c_double),
         ("pc_reg", C.c_double), ("cg_tol", C.c_double), ("phi_tol", C.c_double), ("cg_maxiter", C.c_int),
         ("tn_iters", C.c_int), ("lr", C.c_double), ("mu", C.c_double), ("phi_extrapolate", C.c_int),
+        ("cpp_semantics", C.c_int),
     ]
 
 
@@ -78,6 +79,7 @@ SIGNATURES = {
     "mm_energy_grad_dev": (C.c_int, [_vp, _vp, _vp, _dp, _vp, _dp, _vp]),
     "mm_energy_grad_noalloc": (C.c_int, [_vp, _vp, _vp, _dp, _vp, _dp, _vp]),
     "mm_local_grad": (C.c_int, [_vp, _dp, _dp]),
+    "mm_solve_py_g": (C.c_int, [_vp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double, _dp, _ip]),
     "mm_exchange_diagonal": (C.c_int, [_vp, _dp]),
     "mm_rhs": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mm_apply_A": (C.c_int, [_vp, _dp, _dp]),

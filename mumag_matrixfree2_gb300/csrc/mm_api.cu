@@ -238,6 +238,7 @@ struct mm_problem {
   };
   std::vector<InnerGraph> inner_graphs;  // at most 8, oldest replaced first
   bool inner_graph_failed = false;
+  bool inner_cpp_count = false;  // solve_Py_g counts its trips as the reference's C++ minimizer does
   void drop_inner_graphs() {  // their launches hold the operator's arrays and the launch attributes
     if (inner_graphs.empty()) return;
     if (st) cudaStreamSynchronize(st);
@@ -1278,7 +1279,7 @@ template <class Op, class T>
 void run_inner(mm_problem* h, const Op& op, const double* m, const double* gext, const double* gte, double tol,
                double reg, T inv_Vmag, T* r, T* z, T* p, T* Ap, T* y, int max_iter, double nu) {
   const int N = h->N;
-  launch(h, mmk::k_in_setup, 1, 32, h->d_sc, max_iter, nu, tol * tol);
+  launch(h, mmk::k_in_setup, 1, 32, h->d_sc, max_iter, nu, tol * tol, h->inner_cpp_count ? 1 : 0);
   launch(h, mmk::k_in_init<T>, grid_vec(N), BS, N, gte, h->d_inv_M_prec, r, z, p, y, h->d_sc, h->d_part);
   h->n_launch += 2;
   const bool fp32 = std::is_same<T, float>::value;
@@ -1538,6 +1539,16 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
                      meth == MM_METHOD_PCOHEN_LBFGS;
   const bool exact = meth == MM_METHOD_PCOHEN_EXACT || meth == MM_METHOD_PCOHEN_HS_EXACT;
   const bool cg_family = meth == MM_METHOD_PCOHEN_HS || meth == MM_METHOD_PCOHEN || meth == MM_METHOD_PCG;
+  // the conventions of the reference's C++ minimizer (run_cpp_pcohen_hs_minimization,
+  // src/cpp/cpp_mkl_minimizer.cpp:542-763), which implements pcohen_hs and pcohen only
+  const bool cpp = prm->cpp_semantics != 0;
+  if (cpp && meth != MM_METHOD_PCOHEN_HS && meth != MM_METHOD_PCOHEN)
+    throw Fail{MM_ERR_ARG, "cpp_semantics applies to pcohen_hs and pcohen only"};
+  struct CountMode {  // restores the inner solve's counting on every exit
+    mm_problem* h;
+    ~CountMode() { h->inner_cpp_count = false; }
+  } count_mode{h};
+  h->inner_cpp_count = cpp;
   ensure_min_buffers(h, lbfgs ? std::max(1, prm->memory) : 0);
   MinCtx c{h, N, {B[0], B[1], B[2]}, prm->phi_tol > 0 ? prm->phi_tol : std::min(prm->cg_tol, 0.1 * prm->tau_f), prm};
   const int tn_iters = prm->tn_iters > 0 ? prm->tn_iters : 5;
@@ -1717,6 +1728,14 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     ++it;
   };
 
+  // C++ conventions: an inner solve on the initial state (its count goes into preco_iters; y_prev and
+  // d_prev = -y_prev are unused by the first step, cpp_mkl_minimizer.cpp:606-617), and the energy test
+  // of the convergence check against E_lag, the energy before the previous step (:620,723-726)
+  double E_lag = E;
+  if (cpp) {
+    c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm), h->w_ys, prm->pc_reg);
+    neg3(h->w_dprev, h->w_ys);
+  }
   while (!conv && it < prm->max_iter) {
     const double E_prev = E;
     mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->d_sc, h->d_part);
@@ -1981,7 +2000,8 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       dm = h->red(R_MAX);
     }
     const double E_new = ls.accepted ? ls.E : E_prev;
-    conv = check_conv(it, E_new, E_prev, dm, conv_gnorm, prm);
+    conv = check_conv(it, E_new, cpp ? E_lag : E_prev, dm, conv_gnorm, prm);
+    E_lag = E_prev;
     if (lbfgs) {
       const double* m_new = m_moves ? h->w_mt : m;
       const double* g_new = ls.accepted ? h->w_gt_trial : graw;
@@ -2664,6 +2684,32 @@ int mm_local_grad(mm_problem* h, const double* v, double* out) {
     local_grad_dev(h, h->d_v, h->d_out);
     CK(cudaMemcpyAsync(out, h->d_out, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     h->sync();
+    return MM_OK;
+  });
+}
+
+int mm_solve_py_g(mm_problem* h, const double* m, const double* g_ext, const double* g_tan_ext, int max_iter,
+                  double tol, double reg, double stagnation_nu, double* y, int* iters) {
+  if (!h || !m || !g_ext || !g_tan_ext || !y || !iters || max_iter < 0 || !(stagnation_nu >= 0.0)) return MM_ERR_ARG;
+  return guarded(h, [&] {
+    ensure_min_buffers(h, 0);
+    const size_t n3 = 3 * (size_t)h->N;
+    CK(cudaMemcpyAsync(h->w_mt, m, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->w_gt_trial, g_ext, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->w_gte, g_tan_ext, n3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    mm_min_params prm{};
+    prm.pc_iters = max_iter;
+    prm.pc_stagnation_nu = stagnation_nu;
+    MinCtx c{h, h->N, {0.0, 0.0, 0.0}, 0.0, &prm};
+    struct CountMode {
+      mm_problem* h;
+      ~CountMode() { h->inner_cpp_count = false; }
+    } count_mode{h};
+    h->inner_cpp_count = true;
+    const int it = solve_Py_g(c, h->w_mt, h->w_gt_trial, h->w_gte, tol, h->w_y, reg, max_iter, stagnation_nu);
+    CK(cudaMemcpyAsync(y, h->w_y, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    h->sync();
+    *iters = it;
     return MM_OK;
   });
 }

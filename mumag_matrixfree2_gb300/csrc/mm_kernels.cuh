@@ -55,7 +55,7 @@ struct Scalars {
   int in_stop;       // p.Pp <= 0 or stagnation: this iteration does not update y and r
   int in_done;       // the loop ends after this iteration
   int in_loops;      // graph-loop trips (hard stop for the conditional node)
-  int in_pad;
+  int in_cpp;        // 1: a trip that stops on curvature or stagnation is not counted (C++ minimizer)
 };
 
 // Scalar follow-ups computed once, by the block that finishes a reduction (so that no thread of
@@ -198,7 +198,7 @@ __device__ __forceinline__ void grid_finish(double v0, double v1, Scalars* sc, d
         sc->in_beta_f = (float)sc->in_beta;
         sc->in_rho = rho;
         sc->in_Q = sc->in_Q + sc->in_dq;
-        sc->in_it += 1;
+        sc->in_it += (sc->in_cpp && sc->in_stop) ? 0 : 1;
         sc->red[R_D] = (double)sc->in_it;  // read by the host with the fallback test's sums
         sc->in_done = sc->in_stop ||
                       !(sc->in_it < sc->in_max && rho > sc->in_target && rho > 1e-25 && rho < 1e20);
@@ -1337,9 +1337,10 @@ __device__ __forceinline__ void exch_rows(const EnergySell32& op, int r, const f
   exch_aniso_sell32(op, r, v, ax, ay, az);
 }
 
-__global__ void k_in_setup(Scalars* sc, int max_iter, double nu, double tol2) {
+__global__ void k_in_setup(Scalars* sc, int max_iter, double nu, double tol2, int cpp_count) {
   pdl_entry();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
+    sc->in_cpp = cpp_count;
     sc->in_max = max_iter;
     sc->in_nu = nu;
     sc->in_tol2 = tol2;

@@ -51,6 +51,7 @@ class MinimizerParams:
     lr: float = 0.1
     mu: float = 0.9
     phi_extrapolate: bool = True
+    cpp_semantics: bool = False  # the reference's C++ minimizer conventions (pcohen_hs / pcohen)
 
     def to_c(self) -> _abi.MinParams:
         if self.method not in _abi.METHODS:
@@ -65,7 +66,7 @@ class MinimizerParams:
             pc_stagnation_nu=self.pc_stagnation_nu, pc_reg=self.pc_reg, cg_tol=self.cg_tol,
             phi_tol=-1.0 if self.phi_tol is None else float(self.phi_tol), cg_maxiter=int(self.cg_maxiter),
             tn_iters=int(self.tn_iters), lr=float(self.lr), mu=float(self.mu),
-            phi_extrapolate=1 if self.phi_extrapolate else 0)
+            phi_extrapolate=1 if self.phi_extrapolate else 0, cpp_semantics=1 if self.cpp_semantics else 0)
 
 
 class Problem:
@@ -212,6 +213,17 @@ class Problem:
         out = np.empty((self.N, 3))
         self._check("mm_local_grad", lib().mm_local_grad(self.h, dptr(v), dptr(out)))
         return out
+
+    def solve_py_g(self, m, g_ext, g_tan_ext, max_iter, tol=0.0, reg=0.0, stagnation_nu=1e-3):
+        """Inner Steihaug PCG of the preconditioned minimizers (the reference's exported
+        ``solve_Py_g``, src/cpp/cpp_mkl_minimizer.cpp:233-359): (y (N,3), iterations)."""
+        m, ge, gt = f64(m, (self.N, 3)), f64(g_ext, (self.N, 3)), f64(g_tan_ext, (self.N, 3))
+        y = np.empty((self.N, 3))
+        it = C.c_int()
+        self._check("mm_solve_py_g", lib().mm_solve_py_g(self.h, dptr(m), dptr(ge), dptr(gt), int(max_iter),
+                                                         float(tol), float(reg), float(stagnation_nu), dptr(y),
+                                                         C.byref(it)))
+        return y, it.value
 
     def exchange_diagonal(self):
         d = np.empty(self.N)

@@ -153,6 +153,10 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--wg-gamma", type=int, default=5)
     ap.add_argument("--phi-extrapolate", action="store_true", default=True)
     ap.add_argument("--no-phi-extrapolate", action="store_false", dest="phi_extrapolate")
+    # src/loop.py:697,759-760,977: the reference selects its C++ minimizer with --cpp-mkl (default: on
+    # hosts without a GPU).  Here the GPU runs either way; the flag selects that minimizer's conventions
+    # for pcohen_hs / pcohen (counting and the lagged energy test of run_cpp_pcohen_hs_minimization).
+    ap.add_argument("--cpp-mkl", action=argparse.BooleanOptionalAction, default=None)
     ap.add_argument("--m0-dir", type=str, default="0,0,1")
     ap.add_argument("--out-dir", default="hyst_out")
     ap.add_argument("--snapshot-every", type=int, default=1, help="VTU snapshot every N steps (0: none)")
@@ -168,7 +172,6 @@ def parser() -> argparse.ArgumentParser:
     compat.add_argument("--tau-min", type=float, default=1e-6)
     compat.add_argument("--tau-max", type=float, default=1.0)
     compat.add_argument("--wg-threshold", type=float, default=1e-6)
-    compat.add_argument("--cpp-mkl", action=argparse.BooleanOptionalAction, default=None)
     compat.add_argument("--data-parallel", action="store_true")
     compat.add_argument("--benchmark", action="store_true")
     shell = ap.add_argument_group("shell generation (with --add-shell, which this backend refuses)")
@@ -248,7 +251,7 @@ def main(argv=None) -> dict:
                pc_auto=args.pc_auto, pc_force_eta=args.pc_force_eta, pc_force_alpha=args.pc_force_alpha,
                pc_stagnation_nu=args.pc_stagnation_nu, tn_iters=args.tn_iters, lr=args.lr, mu=args.mu,
                pc_reg=args.pc_reg, wg_gamma=args.wg_gamma, phi_extrapolate=args.phi_extrapolate,
-               bias_type=args.bias_type, bias_strength=args.bias_strength, L=args.L)
+               bias_type=args.bias_type, bias_strength=args.bias_strength, L=args.L, cpp_mkl=bool(args.cpp_mkl))
     m0_dir = np.array([float(x) for x in args.m0_dir.split(",")])
     for key, val in p2.items():
         if key == "m0_dir":

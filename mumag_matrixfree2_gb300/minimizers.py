@@ -75,7 +75,8 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
             phi_tol=float(params["phi_tol"]) if "phi_tol" in params else float(min(cg_tol, 0.1 * tau_f)),
             cg_maxiter=int(params.get("cg_maxiter", 2000)), tn_iters=int(params.get("tn_iters", 5)),
             lr=float(params.get("lr", 0.1)), mu=float(params.get("mu", 0.9)),
-            phi_extrapolate=bool(params.get("phi_extrapolate", False)))
+            phi_extrapolate=bool(params.get("phi_extrapolate", False)),
+            cpp_semantics=bool(params.get("cpp_mkl", False)))
         U0 = params.get("U0")
         if U0 is None:  # a device-resident m (torch CUDA tensor) gets a device U
             U0 = m0.new_zeros(prob.N) if hasattr(m0, "new_zeros") else np.zeros(prob.N)

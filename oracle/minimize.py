@@ -108,8 +108,13 @@ def apply_P(ops: Ops, m, g_ext, v, reg=0.0):
     return Cv - np.sum(m * Cv, axis=1, keepdims=True) * m - np.sum(m * g_ext, axis=1, keepdims=True) * v + reg * v
 
 
-def solve_Py_g(ops: Ops, m, g_ext, g_tan_ext, max_iter=20, tol=0.0, reg=0.0, stagnation_nu=1e-3):
-    """Inner PCG with Steihaug exit; returns (y, iterations), ``src/minimizers.py:413-490``."""
+def solve_Py_g(ops: Ops, m, g_ext, g_tan_ext, max_iter=20, tol=0.0, reg=0.0, stagnation_nu=1e-3, cpp_count=False):
+    """Inner PCG with Steihaug exit; returns (y, iterations), ``src/minimizers.py:413-490``.
+
+    The JAX path counts the trip that exits on negative curvature or stagnation; the C++ path
+    (``src/cpp/cpp_mkl_minimizer.cpp:277-309``) leaves the loop before counting it: ``cpp_count``
+    returns that count.
+    """
     y = np.zeros_like(g_tan_ext)
     r = g_tan_ext.copy()
     z = r * ops.inv_M_prec
@@ -135,6 +140,8 @@ def solve_Py_g(ops: Ops, m, g_ext, g_tan_ext, max_iter=20, tol=0.0, reg=0.0, sta
         rho = rho_next
         Q = Q + dq
         it += 1
+    if cpp_count and done:
+        it -= 1
     z_fb = g_tan_ext * ops.inv_M_prec
     yn, zn = float(np.linalg.norm(y)), float(np.linalg.norm(z_fb))
     if yn > 10.0 * zn:
@@ -181,14 +188,25 @@ METHODS = ("pcohen_hs", "lbfgs", "wg_np", "plbfgs", "cohen", "pcg", "pcohen", "p
            "dplbfgs", "tn_split", "tr", "ptr", "aapg", "aapg_exact", "pnag", "pcohen_lbfgs")
 
 
-def minimize(ops: Ops, m0, B, U0, prm: Params, method="pcohen_hs"):
+def minimize(ops: Ops, m0, B, U0, prm: Params, method="pcohen_hs", flavour="jax"):
     """``make_minimizer(...).minimize``: init (``src/minimizers.py:3408-3435``, with each method's
     ``init_state_fn``, ``:2993-3400``) then the step loop.
+
+    ``flavour="cpp"`` (methods "pcohen_hs" and "pcohen") follows the reference's C++ minimizer,
+    ``run_cpp_pcohen_hs_minimization`` (``src/cpp/cpp_mkl_minimizer.cpp:542-763``), where it differs
+    from the JAX path:
+
+    * an inner solve on the initial state is counted in ``preco_iters`` (``:606-611``);
+    * inner iterations are counted as the C++ loop counts them (see ``solve_Py_g``);
+    * the convergence test compares the new energy with the energy two iterations back: ``E_prev``
+      is assigned the current energy only after the test (``:620,723-726``).
 
     Returns (m, U, info) with info keys iters, E, gnorm, preco_iters, evals, demag_iters.
     """
     if method not in METHODS:
         raise NotImplementedError(method)
+    if flavour not in ("jax", "cpp") or (flavour == "cpp" and method not in ("pcohen_hs", "pcohen")):
+        raise NotImplementedError(f"{method} with flavour {flavour}")
     m = m0 / np.linalg.norm(m0, axis=1, keepdims=True)
     U, init_demag, _ = ops.solve_U(m, U0, prm.cg_tol)
     E, g_raw = ops.energy_and_grad(m, U, B)
@@ -198,7 +216,11 @@ def minimize(ops: Ops, m0, B, U0, prm: Params, method="pcohen_hs"):
     N = m.shape[0]
     L = prm.L or N
     st = dict(m=m, U=U, U_prev=U, g=g_tan_ext, g_raw=g_raw, y=g_tan_ext, d=-g_tan_ext, E=E, gnorm=gnorm, it=0,
-              conv=False, evals=1, preco=0, demag=int(init_demag))
+              conv=False, evals=1, preco=0, demag=int(init_demag), cpp=flavour == "cpp", E_lag=E)
+    if flavour == "cpp":
+        y0, pc0 = solve_Py_g(ops, m, g_raw, g_tan_ext, prm.pc_iters, _pc_tol(prm, gnorm), prm.pc_reg,
+                             prm.pc_stagnation_nu, cpp_count=True)
+        st.update(y=y0, d=-y0, preco=pc0)
     mem = prm.memory
     hist = dict(S=np.zeros((mem, N, 3)), Y=np.zeros((mem, N, 3)), rho=np.zeros(mem), hist_it=0)
     if method in ("lbfgs", "plbfgs", "dplbfgs"):
@@ -282,7 +304,9 @@ def _pcohen_hs_step(ops, st, B, prm, phi_tol, L, variant="pcohen_hs"):
     g_tan_ext = tangent_grad(m, g_raw)
     gnorm_inf = float(np.max(np.abs(g_tan)))
     pc_tol = _pc_tol(prm, gnorm_inf)
-    y, preco_it = solve_Py_g(ops, m, g_raw, g_tan_ext, prm.pc_iters, pc_tol, prm.pc_reg, prm.pc_stagnation_nu)
+    cpp = st.get("cpp", False)
+    y, preco_it = solve_Py_g(ops, m, g_raw, g_tan_ext, prm.pc_iters, pc_tol, prm.pc_reg, prm.pc_stagnation_nu,
+                             cpp_count=cpp)
     gnorm_smooth = float(np.max(np.abs(y)))
     diff_g = g_tan_ext - g_prev
     if variant == "pcohen":
@@ -299,10 +323,11 @@ def _pcohen_hs_step(ops, st, B, prm, phi_tol, L, variant="pcohen_hs"):
     pg = vdot(g_raw, d)
     tau, E_new, g_new, U_new, m_new, ev, dem = armijo_ls(
         ops, m, pg, H, E_prev, U, g_raw, B, phi_tol, prm.ls_eta1, prm.ls_eta2, prm.ls_C, prm.ls_c, 1.0, 15)
-    conv = check_convergence(st["it"], E_new, E_prev, m, m_new, gnorm_smooth, prm.tau_f, prm.eps_a)
+    conv = check_convergence(st["it"], E_new, st["E_lag"] if cpp else E_prev, m, m_new, gnorm_smooth, prm.tau_f,
+                             prm.eps_a)
     st.update(m=m_new, U=U_new, g=g_tan_ext, g_raw=g_new, y=y, d=d, E=E_new, gnorm=gnorm_smooth,
               it=st["it"] + 1, conv=conv, evals=st["evals"] + ev, preco=st["preco"] + preco_it,
-              demag=st["demag"] + dem, tau=tau)
+              demag=st["demag"] + dem, tau=tau, E_lag=E_prev)
 
 
 def _lbfgs_step(ops, st, B, prm, phi_tol):
