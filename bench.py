@@ -481,7 +481,8 @@ def run_batch_leg(a):
 
 
 def run_ours(a):
-    _omp_env()  # the in-line CPU baseline's OpenMP runtime: every host core
+    # no OpenMP binding here: the batched leg drives many problems from a pool of host threads, and
+    # the in-line CPU baseline takes the OpenMP default (one thread per host core)
     import torch
 
     rank, local, ws = dist()

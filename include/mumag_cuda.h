@@ -134,6 +134,8 @@ int mm_setup_level_export(mm_setup* s, int level, int* A_ptr, int* A_col, double
 /* Upload an oriented mesh with its materials (reduced units) and assemble the energy operator.
  * M_nodal: sum_e Js_e Ve / 4 per node; boundary_mask may be NULL (then the Poisson solve projects
  * out the mean, as make_solve_U does without a mask, src/poisson_solve.py:535-536).
+ * The problem lives on the CUDA device current at this call; every entry point taking the problem
+ * makes that device current for the call and restores the caller's device on return.
  * Replaces make_energy_kernels (src/energy_kernels.py:82-142) and the operator assembly of
  * src/amg_utils.py:741-789 / src/loop.py:1133-1166. */
 int mm_create(int n_nodes, int n_elems, const int* conn, const double* volume, const double* grad_phi,
@@ -160,15 +162,16 @@ int mm_energy_grad(mm_problem* h, const double* m, const double* U, const double
 int mm_energy_grad_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B_ext,
                        const double* d_B_bias, double* E, double* d_g);
 
-/* Energy and gradient for callers that cannot allocate device memory at call time — for example
- * code that records the call into its own CUDA graph (allocation is not capturable), or an
- * application that owns all device memory through a fixed pool and forbids allocations once it
- * runs.  No counterpart in the reference: it is mm_energy_grad_dev with the scratch of its energy
+/* Energy and gradient for callers that cannot allocate device memory at call time: an application
+ * that owns all device memory through a fixed pool reserved at start-up and forbids allocations
+ * while it runs (a cudaMalloc there could fail or stall the other work sharing the device).
+ * No counterpart in the reference: it is mm_energy_grad_dev with the scratch of its energy
  * reduction (one partial per block of 32 magnetic rows, a ticket counter and the total) held in a
  * file-scope static device array of MM_NOALLOC_SCRATCH_BYTES instead of the problem's workspace,
  * and it calls no allocating routine.  Inputs and outputs are caller-owned device pointers
  * (d_B_bias may be NULL); E is a host pointer, written after the problem's stream is synchronized.
  * Limit: at most MM_NOALLOC_MAX_ROWS magnetic rows (larger problems get MM_ERR_ARG).
+ * The work runs on the problem's device (the device current at mm_create, as for every entry point).
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress) for that
  * device; make that first call before any stream capture.  Every call shares the one array (its
  * ticket counter is cleared by each call), so calls that may overlap on the GPU — from different

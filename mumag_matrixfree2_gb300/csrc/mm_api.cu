@@ -144,6 +144,7 @@ thread_local std::string g_create_error;
 }  // namespace
 
 struct mm_problem {
+  int device = -1;  // the CUDA device current at mm_create; every entry point runs its work there
   int N = 0, E = 0, n_mat = 0;
   double V_mag = 1.0, inv_Vmag = 1.0;
   cudaStream_t st = nullptr;
@@ -1167,8 +1168,22 @@ void local_grad_dev(mm_problem* h, const double* d_v, double* d_out) {
   LAUNCH_CHECK();
 }
 
+// Makes a problem's device current for one entry-point call and restores the caller's device.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    int cur = -1;
+    if (dev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess)
+      prev = cur;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 template <class F>
 int guarded(mm_problem* h, F&& f) {
+  DeviceGuard device_guard(h ? h->device : -1);
   try {
     return f();
   } catch (const Fail& e) {
@@ -2153,7 +2168,8 @@ __global__ void __launch_bounds__(BS) k_energy_grad_noalloc(mmk::EnergyDev op, c
   }
 }
 
-// Device address of g_noalloc_scratch for the current device, looked up once per device.
+// Device address of g_noalloc_scratch for the current device, looked up once per device (the entry
+// point makes the problem's device current first, see guarded()).
 double* noalloc_scratch_for_current_device() {
   static std::mutex mu;
   static double* addr[256] = {};
@@ -2475,6 +2491,7 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
   *out = nullptr;
   mm_problem* h = new mm_problem();
   int rc = guarded(h, [&] {
+    CK(cudaGetDevice(&h->device));
     for (int e = 0; e < 4 * E; ++e)
       if (conn[e] < 0 || conn[e] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
     h->N = N;
@@ -2567,6 +2584,7 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
 
 int mm_destroy(mm_problem* h) {
   if (!h) return MM_ERR_ARG;
+  DeviceGuard device_guard(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->s64.exec) cudaGraphExecDestroy(h->s64.exec);
   if (h->s64.graph) cudaGraphDestroy(h->s64.graph);

@@ -156,7 +156,11 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
         }
       mtc::bulk_g2s(B, a.wk + ((size_t)cot * NCP + cp) * 54 * NT, (uint32_t)Bstage, &full[st]);
     };
-    for (int s = 0; s < NST && s < NCP; ++s) issue(s, s);
+    // bookkeeping for the failure path: chunks whose copies were issued / seen complete, the last
+    // chunk whose MMAs were committed and whether their completion was seen
+    int issued = 0, loaded = 0, committed = -1;
+    bool mma_seen = true;
+    for (int s = 0; s < NST && s < NCP; ++s, ++issued) issue(s, s);
     constexpr uint32_t IDESC = mtc::idesc_bf16(128, NT);
     bool ok = true;
     for (int cp = 0; cp < NCP && ok; ++cp) {
@@ -166,6 +170,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
         ok = false;
         break;
       }
+      loaded = cp + 1;
       mtc::tc_fence_after();
       const uint32_t As = mtc::smem_u32(Abuf + st * Astage);
       const uint32_t Bs = mtc::smem_u32(Bbuf + st * Bstage);
@@ -181,17 +186,28 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
         }
       }
       mtc::mma_commit(&done[st]);
+      committed = cp;
+      mma_seen = false;
       if (cp + NST < NCP) {
         if (!mtc::mbar_wait(&done[st], par)) {
           ok = false;
           break;
         }
+        mma_seen = true;  // a commit's arrival covers every earlier MMA of this thread
         issue(cp + NST, st);
+        ++issued;
       }
     }
     if (!ok) {
+      // A wait gave up: raise the (sticky) error flag, then drain before the tensor memory and the
+      // shared-memory stages are released: the MMAs committed last, then every copy still in flight,
+      // each wait bounded like the others.  If a drain wait gives up too, the memory is released
+      // with that work outstanding; the flag has already made every result of this launch, and
+      // every later call of the network, an error.
       *s_fail = 1;
       atomicExch(a.err, 1);
+      if (committed >= 0 && !mma_seen) mtc::mbar_wait(&done[committed % NST], (uint32_t)(committed / NST) & 1u);
+      for (int c = loaded; c < issued; ++c) mtc::mbar_wait(&full[c % NST], (uint32_t)(c / NST) & 1u);
     }
   }
   __syncthreads();

