@@ -108,6 +108,17 @@ int mm_boundary_mask(int n_nodes, int n_elems, const int* conn, double* mask);
 int mm_morton_order(int n_nodes, int n_elems, const double* knt, const int* conn, int* node_perm,
                     int* elem_perm);
 
+/* Degrees of the mesh's edge graph (nodes sharing an edge, the node itself excluded). */
+int mm_node_degrees(int n_nodes, int n_elems, const int* conn, int* degree);
+/* Reverse Cuthill-McKee node permutation of the mesh's edge graph: unvisited nodes start a
+ * breadth-first component in the order `seeds` (the nodes by increasing degree; NULL sorts them
+ * stably by degree), the newly reached neighbours of each node are ordered by increasing degree,
+ * equal degrees by node number, and the visit order reversed is node_perm.  Replaces the
+ * target="cpu" branch of reorder_mesh (src/reorder_mesh.py:53-83), whose call of scipy's
+ * reverse_cuthill_mckee passes a keyword scipy does not have; this orders the symmetric edge graph,
+ * as scipy.sparse.csgraph.reverse_cuthill_mckee does given the same seed order. */
+int mm_rcm_order(int n_nodes, int n_elems, const int* conn, const int* seeds, int* node_perm);
+
 /* ---- host-only setup (no GPU needed): the assembled operators and the SA hierarchy --------- */
 
 typedef struct mm_setup mm_setup;
@@ -295,17 +306,7 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * around every solver launch; each launch's device time is added to a slot named by its kind, AMG
  * level and precision.  For measurement only: the loop is slower than the graph. */
 #define MM_OPT_PROFILE 5
-/* MM_OPT_PERSISTENT (default 0): 1 runs the PCG iterations of a multilevel solve (direction, step
- * and the whole V-cycle, every level) in ONE cooperative launch whose blocks keep a fixed share of
- * the rows of every operator and meet at grid barriers between the phases, instead of the separate
- * kernels of the CUDA graph (MM_OPT_GRAPH).  Every barrier wait is bounded (1 s); a wait that runs
- * out ends the launch and the solve returns MM_ERR_CUDA.  Inner products are summed in a fixed order
- * (deterministic; they differ from the graph path at rounding level).  On the 80 nm cube (GB300) it
- * is slower than the graph (each of the ~15 grid barriers of an iteration costs ~3 us and the fixed
- * row shares leave fewer loads in flight), so it is off by default. */
-#define MM_OPT_PERSISTENT 6
-/* MM_OPT_PERSIST_BPSM: blocks per SM of that launch, 1..4 (0 = 4; capped by occupancy). */
-#define MM_OPT_PERSIST_BPSM 7
+/* Options 6 and 7 are unused (they selected a one-launch persistent PCG loop, since removed). */
 /* MM_OPT_PDL (default 1): launch the solver kernels with programmatic dependent launch, so each
  * kernel is scheduled while its predecessor drains (every solver kernel waits for its predecessor's
  * results at entry); 0 launches them normally.  Same results either way. */
@@ -330,6 +331,12 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * FP64 PCG (z the FP32 V-cycle's output, exact in FP32) runs on the operator split into FP32 pairs
  * a = hi + lo and sums in float-float (error ~2^-47 sum |a z|) on the FP32 pipes; 0 takes it in FP64. */
 #define MM_OPT_SPLIT_A0 11
+/* MM_OPT_FUSE_RESTRICT (bit mask, default 3): the V-cycle restricts with R_l (I - A_l S_l), formed
+ * once on the host, instead of a residual pass A_l followed by R_l: the pre-smoothing from zero
+ * makes x_l = S_l b_l, so b_{l+1} = R_l (b_l - A_l x_l) is one product with one operator (one kernel
+ * less per level, and fewer bytes than A_l and R_l together).  Bit 0 the FP64 solver, bit 1 the FP32
+ * one; mm_autotune keeps a bit only if the V-cycle is faster with it. */
+#define MM_OPT_FUSE_RESTRICT 12
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

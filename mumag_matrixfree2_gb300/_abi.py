@@ -61,6 +61,8 @@ SIGNATURES = {
     "mm_geom_compute": (C.c_int, [C.c_int, C.c_int, _dp, _ip, _ip, _dp, _dp, _dp]),
     "mm_boundary_mask": (C.c_int, [C.c_int, C.c_int, _ip, _dp]),
     "mm_morton_order": (C.c_int, [C.c_int, C.c_int, _dp, _ip, _ip, _ip]),
+    "mm_node_degrees": (C.c_int, [C.c_int, C.c_int, _ip, _ip]),
+    "mm_rcm_order": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _ip]),
     "mm_setup_create": (C.c_int, [C.c_int, C.c_int, _ip, _dp, _dp, _ip, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                   C.c_double, C.c_int, C.c_int, C.POINTER(_vp)]),
     "mm_setup_destroy": (C.c_int, [_vp]),
@@ -205,6 +207,23 @@ def morton_order(knt, conn):
     knt, conn = f64(knt), i32(np.asarray(conn)[:, :4])
     npm, epm = np.empty(knt.shape[0], np.int32), np.empty(conn.shape[0], np.int32)
     check("mm_morton_order", lib().mm_morton_order(knt.shape[0], conn.shape[0], dptr(knt), iptr(conn), iptr(npm), iptr(epm)))
+    return npm, epm
+
+
+def rcm_order(conn, n_nodes):
+    """Reverse Cuthill-McKee node and element permutations (the target="cpu" branch of reorder_mesh,
+    src/reorder_mesh.py:53-83).  Components start from the nodes in numpy's argsort order of their
+    degrees, the order scipy.sparse.csgraph.reverse_cuthill_mckee seeds from; elements are ordered by
+    the mean of their nodes' new numbers (numpy argsort, as the reference)."""
+    conn = i32(np.asarray(conn)[:, :4])
+    deg = np.empty(n_nodes, np.int32)
+    check("mm_node_degrees", lib().mm_node_degrees(n_nodes, conn.shape[0], iptr(conn), iptr(deg)))
+    seeds = np.ascontiguousarray(np.argsort(deg), dtype=np.int32)
+    npm = np.empty(n_nodes, np.int32)
+    check("mm_rcm_order", lib().mm_rcm_order(n_nodes, conn.shape[0], iptr(conn), iptr(seeds), iptr(npm)))
+    inv = np.empty(n_nodes, np.int32)
+    inv[npm] = np.arange(n_nodes, dtype=np.int32)
+    epm = np.argsort(np.mean(inv[conn], axis=1)).astype(np.int32)
     return npm, epm
 
 

@@ -9,13 +9,13 @@
 #include <functional>
 #include <stdexcept>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <type_traits>
 #include <vector>
 
 #include "../../include/mumag_cuda.h"
 #include "mm_kernels.cuh"
-#include "mm_persistent.cuh"
 #include "mm_setup.h"
 
 using mmk::BS;
@@ -89,6 +89,7 @@ struct DevMatT {
 template <class T>
 struct LevelT {
   DevMatT<T> A, P, R;
+  DevMatT<T> Rf;     // fused restriction R (I - A S) (levels below the coarsest), empty when not formed
   T* s = nullptr;    // smoother diagonal (SPAI0, or omega/(diag+eps) for Jacobi)
   T* b = nullptr;    // right-hand side (levels >= 1)
   T* x = nullptr;    // iterate (pre-smoothing, prolongation)
@@ -118,15 +119,6 @@ struct SolverT {
   T *W = nullptr, *Z = nullptr, *tvec = nullptr, *zvec = nullptr;
   int fn = 0, fc = 0;
   int64_t Tm_nnz = 0;
-  // persistent PCG loop (one cooperative launch per solve)
-  mmk::PLev<T>* d_plev = nullptr;     // level views on the device
-  mmk::GridBar* d_bar = nullptr;      // barrier state, cleared before each launch
-  mmk::GridBar* h_bar = nullptr;      // pinned copy read back after the launch
-  int pgrid = 0;                      // co-resident grid of the launch
-  const void* pkern = nullptr;        // the kernel variant it was sized for
-  int* d_bounds = nullptr;            // block bounds of every operator (3 per level, MAXG + 1 each)
-  int pgrid_bpsm = -1;                // blocks per SM it was sized for
-  bool persist_failed = false;
 };
 
 // Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
@@ -211,10 +203,11 @@ struct mm_problem {
   mmk::Scalars* d_sc32 = nullptr;
   mmk::Scalars* h_sc = nullptr;  // pinned
   bool use_graph = true;
-  bool persistent = false;       // MM_OPT_PERSISTENT
   bool pdl = true;               // MM_OPT_PDL
   int coarse_fuse = 1;           // MM_OPT_COARSE_FUSE: bit 0 the FP64 solver, bit 1 the FP32 solver
-  int persist_bpsm = 0;          // MM_OPT_PERSIST_BPSM (0 = default)
+  int fuse_restrict = 3;         // MM_OPT_FUSE_RESTRICT: bit 0 the FP64 solver, bit 1 the FP32 solver
+  std::vector<mm::HostCSR> rf_host;  // fused restrictions R_l (I - A_l S_l), formed for smoother rf_prec
+  int rf_prec = -1;
 
   // staging buffers for host-pointer calls
   double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
@@ -584,8 +577,32 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
   const double w = sizeof(T);
   const bool fuse = S.fused && ((h->coarse_fuse >> (sizeof(T) == 8 ? 0 : 1)) & 1);
   const int Ld = fuse ? L - 2 : L - 1;  // levels l < Ld compute a residual and restrict it
+  const bool fr_on = (h->fuse_restrict >> (sizeof(T) == 8 ? 0 : 1)) & 1;
+  // b_{l+1} = R_l res (res = b_l - A_l x_l), and the pre-smoothing x_{l+1} = s_{l+1} b_{l+1} unless
+  // level l+1 has none
+  auto restrict_into = [&](int l, const DevMatT<T>& M, const T* in, double mbytes) {
+    auto& c = lv[l];
+    auto& nx = lv[l + 1];
+    const bool no_pre = (l + 1 == L - 1) || (fuse && l + 1 == L - 2);
+    const double rbytes = mbytes + w * c.n + (no_pre ? 1.0 : 3.0) * w * nx.n;
+    tagged<T>(h, MM_PROF_RESTRICT, l, rbytes, [&] {
+      if (M.tpr == 1) {
+        launch(h, mmk::k_restrict<T>, grid_ilp(nx.n), BS, M.s, in, nx.b, no_pre ? nullptr : nx.s, nx.x, done);
+      } else {
+        const int g = grid_rows(nx.n, M.tpr);
+        TPR_SWITCH(M.tpr, (launch(h, mmk::k_restrict_csr<TP, T>, g, BS, M.c, in, nx.b, no_pre ? nullptr : nx.s,
+                                  nx.x, done)));
+      }
+      LAUNCH_CHECK();
+    });
+  };
   for (int l = 0; l < Ld; ++l) {
     auto& c = lv[l];
+    if (fr_on && c.Rf.nnz > 0) {
+      // x_l = s_l b_l (the pre-smoothing from zero, already written), so b_{l+1} = R_l (I - A_l S_l) b_l
+      restrict_into(l, c.Rf, l == 0 ? r : c.b, mat_bytes(c.Rf));
+      continue;
+    }
     if (l == 0 && in_loop) {
       tagged<T>(h, MM_PROF_VC_RESIDUAL0, 0, mat_bytes(c.A) + 3.0 * w * c.n, [&] {
         launch(h, mmk::k_vc_residual0<T>, grid_ilp(c.n), BS, c.A.s, c.x, r, c.res, sc);
@@ -595,21 +612,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
       tagged<T>(h, l == 0 ? MM_PROF_VC_RESIDUAL0 : MM_PROF_RESIDUAL, l, mat_bytes(c.A) + 3.0 * w * c.n,
                 [&] { spmv<1, T>(h, c.A, c.x, l == 0 ? r : c.b, nullptr, c.res, done); });
     }
-    auto& nx = lv[l + 1];
-    // no pre-smoothing on the coarsest level, nor on level L-2 when its correction is fused
-    const bool no_pre = (l + 1 == L - 1) || (fuse && l + 1 == L - 2);
-    const double rbytes = mat_bytes(c.R) + w * c.n + (no_pre ? 1.0 : 3.0) * w * nx.n;
-    tagged<T>(h, MM_PROF_RESTRICT, l, rbytes, [&] {
-      if (c.R.tpr == 1) {
-        launch(h, mmk::k_restrict<T>, grid_ilp(nx.n), BS, c.R.s, c.res, nx.b, no_pre ? nullptr : nx.s, nx.x,
-                                                                done);
-      } else {
-        const int g = grid_rows(nx.n, c.R.tpr);
-        TPR_SWITCH(c.R.tpr, (launch(h, mmk::k_restrict_csr<TP, T>, g, BS, c.R.c, c.res, nx.b,
-                                                                          no_pre ? nullptr : nx.s, nx.x, done)));
-      }
-      LAUNCH_CHECK();
-    });
+    restrict_into(l, c.R, c.res, mat_bytes(c.R));
   }
   if (fuse) {
     auto& c = lv[L - 2];
@@ -779,127 +782,6 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
 }
 
 template <class T>
-mmk::MatV<T> matv(const DevMatT<T>& M) {
-  mmk::MatV<T> v{};
-  v.tpr = M.tpr;
-  if (M.tpr == 1) {
-    v.n = M.s.n;
-    v.ptr = M.s.sptr;
-    v.col = M.s.col;
-    v.val = M.s.val;
-  } else {
-    v.n = M.c.n;
-    v.ptr = M.c.ptr;
-    v.col = M.c.col;
-    v.val = M.c.val;
-  }
-  return v;
-}
-
-// Block bounds of one operator for a G-block persistent launch: contiguous, equal ranges of slices
-// (sliced ELL) or rows (CSR).  G + 1 entries.  (Bounds balanced by stored entries were measured
-// slower on the 80 nm cube: the time of a phase follows the rows' load chains, not their entries.)
-std::vector<int> even_bounds(int n_rows, int tpr, int G) {
-  const int64_t units = tpr == 1 ? (n_rows + 31) / 32 : n_rows;
-  std::vector<int> b(G + 1);
-  for (int k = 0; k <= G; ++k) b[k] = (int)(units * k / G);
-  return b;
-}
-
-// Variant of the persistent kernel for `bpsm` blocks per SM: up to 2 blocks, 128 registers and two
-// rows in flight per thread; beyond, 64 registers (4 blocks per SM) and one row.
-template <class T>
-const void* persistent_variant(int bpsm) {
-  return bpsm <= 2 ? (const void*)mmk::k_pcg_persistent<T, 2, 2> : (const void*)mmk::k_pcg_persistent<T, 4, 1>;
-}
-
-// Level views (with the block bounds of every operator), barrier state and the co-resident grid of
-// the persistent loop: once per solver, and again when the blocks-per-SM option changes.  False when
-// the device cannot launch cooperatively.
-template <class T>
-bool setup_persistent(mm_problem* h, SolverT<T>& S) {
-  if (S.persist_failed) return false;
-  if (S.d_plev && S.pgrid_bpsm == h->persist_bpsm) return true;
-  int dev = 0, coop = 0, sms = 0, occ = 0;
-  const int want = h->persist_bpsm > 0 ? h->persist_bpsm : 4;
-  const void* kern = persistent_variant<T>(want);
-  CK(cudaGetDevice(&dev));
-  CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BS, 0));
-  if (!coop || occ < 1) {
-    S.persist_failed = true;
-    return false;
-  }
-  const int L = (int)S.lv.size();
-  const int G = std::min(sms * std::min(want, occ), MAXG);
-  S.pkern = kern;
-  S.pgrid = G;
-  S.pgrid_bpsm = h->persist_bpsm;
-  if (!S.d_plev) {
-    S.d_plev = h->alloc<mmk::PLev<T>>(L);
-    S.d_bar = h->alloc<mmk::GridBar>(1);
-    CK(cudaMallocHost(&S.h_bar, sizeof(mmk::GridBar)));
-    S.d_bounds = h->alloc<int>((size_t)3 * L * (MAXG + 1));
-  }
-  // bounds table: operator (l, j) (j = 0 A, 1 R, 2 P) at d_bounds + (3 l + j) (MAXG + 1)
-  std::vector<int> hb((size_t)3 * L * (MAXG + 1), 0);
-  std::vector<mmk::PLev<T>> hl(L);
-  auto put = [&](int l, int j, const mm::HostCSR& M, int tpr) {
-    const std::vector<int> b = even_bounds(M.n_rows, tpr, G);
-    std::copy(b.begin(), b.end(), hb.begin() + (size_t)(3 * l + j) * (MAXG + 1));
-    return S.d_bounds + (size_t)(3 * l + j) * (MAXG + 1);
-  };
-  for (int l = 0; l < L; ++l) {
-    const auto& d = S.lv[l];
-    const mm::AmgLevel& a = h->amg_h[l];
-    hl[l] = mmk::PLev<T>{};
-    hl[l].A = matv(d.A);
-    hl[l].A.bp = put(l, 0, a.A, d.A.tpr);
-    if (l < L - 1) {
-      hl[l].R = matv(d.R);
-      hl[l].R.bp = put(l, 1, a.R, d.R.tpr);
-      hl[l].P = matv(d.P);
-      hl[l].P.bp = put(l, 2, a.P, d.P.tpr);
-    }
-    hl[l].s = d.s;
-    hl[l].b = d.b;
-    hl[l].x = d.x;
-    hl[l].x2 = d.x2;
-    hl[l].res = d.res;
-    hl[l].n = d.n;
-  }
-  CK(cudaMemcpyAsync(S.d_plev, hl.data(), L * sizeof(mmk::PLev<T>), cudaMemcpyHostToDevice, h->st));
-  CK(cudaMemcpyAsync(S.d_bounds, hb.data(), hb.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));  // hl and hb are locals
-  return true;
-}
-
-// The PCG iterations as one cooperative launch (the state left by the initial residual and the
-// first preconditioner application is taken over from the scalars).
-template <class T>
-void launch_persistent(mm_problem* h, SolverT<T>& S) {
-  mmk::PcgArgs<T> a{};
-  a.lv = S.d_plev;
-  a.L = (int)S.lv.size();
-  a.Ainv = S.Ainv;
-  a.nc = S.n_coarse;
-  a.x = S.x;
-  a.r = S.r;
-  a.z = S.z;
-  a.p = S.p;
-  a.Ap = S.Ap;
-  a.sc = S.sc;
-  a.part = h->d_part;
-  a.bar = S.d_bar;
-  CK(cudaMemsetAsync(S.d_bar, 0, sizeof(mmk::GridBar), h->st));
-  void* args[] = {&a};
-  CK(cudaLaunchCooperativeKernel(S.pkern, dim3(S.pgrid), dim3(BS), args, 0, h->st));
-  ++h->n_launch;
-  CK(cudaMemcpyAsync(S.h_bar, S.d_bar, sizeof(mmk::GridBar), cudaMemcpyDeviceToHost, h->st));
-}
-
-template <class T>
 void drop_graph(SolverT<T>& S) {
   if (S.exec) cudaGraphExecDestroy(S.exec);
   if (S.graph) cudaGraphDestroy(S.graph);
@@ -913,12 +795,9 @@ void drop_graph(SolverT<T>& S) {
 struct PcgPending {
   SolverT<double>* S = nullptr;
   bool graph = false;
-  bool persist = false;
 };
 
 void finish_pcg(mm_problem* h, const PcgPending& pend, int* iters, double* r2_out) {
-  if (pend.persist && pend.S->h_bar->err != 0)
-    throw Fail{MM_ERR_CUDA, "persistent PCG: a grid-barrier wait ran out (blocks not co-resident?)"};
   if (pend.graph) h->n_launch += (int64_t)h->h_sc->loops * pend.S->iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -943,11 +822,8 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   });
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
   else apply_M_simple<T>(h, S, S.r, S.z, nullptr);
-  const bool persist = ml && h->persistent && !h->prof && setup_persistent<T>(h, S);
-  const bool graph = !persist && h->use_graph && !h->prof && build_loop_graph<T>(h, S);
-  if (persist) {
-    launch_persistent<T>(h, S);
-  } else if (graph) {
+  const bool graph = h->use_graph && !h->prof && build_loop_graph<T>(h, S);
+  if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
   } else if (h->prof) {
     // profiled: read `done` after every step so that no launch runs past convergence
@@ -971,13 +847,11 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   if constexpr (std::is_same<T, double>::value) {
     if (pend) {
-      *pend = PcgPending{&S, graph, persist};
+      *pend = PcgPending{&S, graph};
       return;
     }
   }
   h->sync();
-  if (persist && S.h_bar->err != 0)
-    throw Fail{MM_ERR_CUDA, "persistent PCG: a grid-barrier wait ran out (blocks not co-resident?)"};
   if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -1047,7 +921,7 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
   }
   CK(cudaMemcpyAsync(h->h_sc, S.sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   if (pend) {
-    *pend = PcgPending{&S, graph, false};
+    *pend = PcgPending{&S, graph};
     return;
   }
   h->sync();
@@ -2300,6 +2174,21 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
     dl.x2 = h->alloc<T>(dl.n);
     dl.res = h->alloc<T>(dl.n);
   }
+  if (amg && L >= 2) {
+    // fused restrictions R_l (I - A_l S_l) with the smoother of this hierarchy, formed once in FP64
+    if ((int)h->rf_host.size() != L - 1 || h->rf_prec != precond_type) {
+      h->rf_host.assign(L - 1, mm::HostCSR{});
+      for (int l = 0; l < L - 1; ++l) {
+        const mm::AmgLevel& hl = h->amg_h[l];
+        std::vector<double> sd(hl.A.n_rows);
+        for (int i = 0; i < hl.A.n_rows; ++i)
+          sd[i] = precond_type == MM_PRECOND_AMGCL ? hl.spai0[i] : 0.6667 / (hl.diag[i] + 1e-30);
+        h->rf_host[l] = mm::fused_restriction(hl.R, hl.A, sd);
+      }
+      h->rf_prec = precond_type;
+    }
+    for (int l = 0; l < L - 1; ++l) S.lv[l].Rf = h->upload_mat<T>(h->rf_host[l]);
+  }
   if (amg) {
     const mm::HostCSR& Ac = h->amg_h.back().A;
     S.n_coarse = Ac.n_rows;
@@ -2369,6 +2258,43 @@ int mm_morton_order(int N, int E, const double* knt, const int* conn, int* node_
   if (N <= 0 || E <= 0 || !knt || !conn || !node_perm || !elem_perm) return MM_ERR_ARG;
   return guarded(nullptr, [&] {
     mm::morton_order(N, E, knt, conn, node_perm, elem_perm);
+    return MM_OK;
+  });
+}
+
+int mm_node_degrees(int N, int E, const int* conn, int* degree) {
+  if (N <= 0 || E <= 0 || !conn || !degree) return MM_ERR_ARG;
+  return guarded(nullptr, [&] {
+    for (int64_t k = 0; k < 4 * (int64_t)E; ++k)
+      if (conn[k] < 0 || conn[k] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
+    std::vector<int> ptr, col;
+    mm::node_graph(N, E, conn, ptr, col);
+    for (int i = 0; i < N; ++i) degree[i] = ptr[i + 1] - ptr[i];
+    return MM_OK;
+  });
+}
+
+int mm_rcm_order(int N, int E, const int* conn, const int* seeds, int* node_perm) {
+  if (N <= 0 || E <= 0 || !conn || !node_perm) return MM_ERR_ARG;
+  return guarded(nullptr, [&] {
+    for (int64_t k = 0; k < 4 * (int64_t)E; ++k)
+      if (conn[k] < 0 || conn[k] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
+    std::vector<int> ptr, col;
+    mm::node_graph(N, E, conn, ptr, col);
+    std::vector<int> order(N);
+    if (seeds) {
+      std::vector<char> hit(N, 0);
+      for (int i = 0; i < N; ++i) {
+        if (seeds[i] < 0 || seeds[i] >= N || hit[seeds[i]]) throw Fail{MM_ERR_ARG, "seeds is not a permutation"};
+        hit[seeds[i]] = 1;
+        order[i] = seeds[i];
+      }
+    } else {
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int a, int b) { return ptr[a + 1] - ptr[a] < ptr[b + 1] - ptr[b]; });
+    }
+    mm::rcm_order(N, ptr, col, order.data(), node_perm);
     return MM_OK;
   });
 }
@@ -2593,8 +2519,6 @@ int mm_destroy(mm_problem* h) {
   h->drop_inner_graphs();
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
-  if (h->s64.h_bar) cudaFreeHost(h->s64.h_bar);
-  if (h->s32.h_bar) cudaFreeHost(h->s32.h_bar);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_after) cudaEventDestroy(h->ev_after);
@@ -3080,9 +3004,25 @@ void tune_solver(mm_problem* h, SolverT<T>& S, int reps, std::string& rep) {
     if (l < L - 1) {
       tune_csr<T>(h, S, c.R, h->amg_h[l].R, reps, "R", l, rep);
       tune_csr<T>(h, S, c.P, h->amg_h[l].P, reps, "P", l, rep);
+      if (c.Rf.nnz > 0 && (int)h->rf_host.size() > l) tune_csr<T>(h, S, c.Rf, h->rf_host[l], reps, "Rf", l, rep);
     }
   }
   drop_graph(S);
+}
+
+// V-cycle time with and without the fused restrictions in solver S; sets the bit if they win
+template <class T>
+std::string tune_fuse_restrict(mm_problem* h, SolverT<T>& S, int bit, int reps) {
+  if (!S.built || !multilevel(h, S) || S.lv.empty() || S.lv[0].Rf.nnz == 0) return "null";
+  const int saved = h->fuse_restrict;
+  float ms[2];
+  for (int on = 0; on < 2; ++on) {
+    h->fuse_restrict = on ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+    ms[on] = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+  }
+  h->fuse_restrict = ms[1] < ms[0] ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+  drop_graph(S);
+  return "{\"unfused_us\":" + std::to_string(1e3 * ms[0]) + ",\"fused_us\":" + std::to_string(1e3 * ms[1]) + "}";
 }
 
 // V-cycle time with and without the fused coarse correction in solver S; sets the bit if it wins
@@ -3116,8 +3056,11 @@ int mm_autotune(mm_problem* h, int reps, char* report, int report_len) {
     ops += "]";
     const std::string f64 = tune_fuse<double>(h, h->s64, 0, reps);
     const std::string f32 = tune_fuse<float>(h, h->s32, 1, reps);
+    const std::string r64 = tune_fuse_restrict<double>(h, h->s64, 0, reps);
+    const std::string r32 = tune_fuse_restrict<float>(h, h->s32, 1, reps);
     const std::string rep = "{\"operators\":" + ops + ",\"coarse_fuse\":{\"fp64\":" + f64 + ",\"fp32\":" + f32 +
-                            ",\"chosen\":" + std::to_string(h->coarse_fuse) + "}}";
+                            ",\"chosen\":" + std::to_string(h->coarse_fuse) + "},\"fuse_restrict\":{\"fp64\":" +
+                            r64 + ",\"fp32\":" + r32 + ",\"chosen\":" + std::to_string(h->fuse_restrict) + "}}";
     h->sync();
     if (report && report_len > 0) {
       const size_t n = std::min(rep.size(), (size_t)report_len - 1);
@@ -3182,14 +3125,13 @@ int mm_set_option(mm_problem* h, int option, int value) {
     h->coarse_fuse = value;
     return MM_OK;
   }
-  if (option == MM_OPT_PERSISTENT) {
-    if (value != 0 && value != 1) return MM_ERR_ARG;
-    h->persistent = value == 1;
-    return MM_OK;
-  }
-  if (option == MM_OPT_PERSIST_BPSM) {
-    if (value < 0 || value > 4) return MM_ERR_ARG;
-    h->persist_bpsm = value;
+  if (option == MM_OPT_FUSE_RESTRICT) {
+    if (value < 0 || value > 3) return MM_ERR_ARG;
+    if (h->fuse_restrict != value) {
+      drop_graph(h->s64);
+      drop_graph(h->s32);
+    }
+    h->fuse_restrict = value;
     return MM_OK;
   }
   if (option == MM_OPT_MIXED_ETA_E6) {

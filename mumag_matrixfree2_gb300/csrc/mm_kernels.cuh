@@ -345,6 +345,11 @@ constexpr int ILP = 2;
 // ~15 % slower than KU = 1 (more registers, fewer resident warps), so 1 is kept.
 constexpr int KU = 1;
 
+// Entry pairs of a sliced-ELL row whose column and value loads are issued before their gathers: a
+// row of 2 PF entries costs one chain (columns, then gathers) instead of PF chains.  The products
+// are summed in stored order whatever PF is.
+constexpr int PF = 1;
+
 // x loads: read-only path (the vector is not written during the kernel) or L2 (written by other
 // blocks of a persistent launch before the last grid barrier)
 template <bool CG, class T>
@@ -373,22 +378,26 @@ __device__ __forceinline__ void sell_rows_k(const int* __restrict__ sptr, const 
     }
     wmax = max(wmax, wp[q]);
   }
-  for (int j = 0; j < wmax; ++j) {
-    int2 c[R];
-    P2 v[R];
+  for (int j0 = 0; j0 < wmax; j0 += PF) {
+    int2 c[R][PF];
+    P2 v[R][PF];
 #pragma unroll
     for (int q = 0; q < R; ++q)
-      if (j < wp[q]) {
-        c[q] = __ldg(reinterpret_cast<const int2*>(col + base[q] + 64 * j));
-        v[q] = __ldg(reinterpret_cast<const P2*>(val + base[q] + 64 * j));
-      }
+#pragma unroll
+      for (int u = 0; u < PF; ++u)
+        if (j0 + u < wp[q]) {
+          c[q][u] = __ldg(reinterpret_cast<const int2*>(col + base[q] + 64 * (j0 + u)));
+          v[q][u] = __ldg(reinterpret_cast<const P2*>(val + base[q] + 64 * (j0 + u)));
+        }
 #pragma unroll
     for (int q = 0; q < R; ++q)
-      if (j < wp[q]) {
-        const T x0 = (T)ldx<CG>(x, c[q].x), x1 = (T)ldx<CG>(x, c[q].y);
-        acc[q] = fmaT<T>(v[q].x, x0, acc[q]);
-        acc[q] = fmaT<T>(v[q].y, x1, acc[q]);
-      }
+#pragma unroll
+      for (int u = 0; u < PF; ++u)
+        if (j0 + u < wp[q]) {
+          const T x0 = (T)ldx<CG>(x, c[q][u].x), x1 = (T)ldx<CG>(x, c[q][u].y);
+          acc[q] = fmaT<T>(v[q][u].x, x0, acc[q]);
+          acc[q] = fmaT<T>(v[q][u].y, x1, acc[q]);
+        }
   }
 }
 
@@ -612,22 +621,27 @@ __device__ __forceinline__ void sell_rows_df(const SellDF& A, const float* __res
     }
     wmax = max(wmax, wp[q]);
   }
-  for (int j = 0; j < wmax; ++j) {
-    int2 c[ILP];
-    float2 vh[ILP], vl[ILP];
+  for (int j0 = 0; j0 < wmax; j0 += PF) {
+    int2 c[ILP][PF];
+    float2 vh[ILP][PF], vl[ILP][PF];
 #pragma unroll
     for (int q = 0; q < ILP; ++q)
-      if (j < wp[q]) {
-        c[q] = __ldg(reinterpret_cast<const int2*>(A.col + base[q] + 64 * j));
-        vh[q] = __ldg(reinterpret_cast<const float2*>(A.hi + base[q] + 64 * j));
-        vl[q] = __ldg(reinterpret_cast<const float2*>(A.lo + base[q] + 64 * j));
-      }
+#pragma unroll
+      for (int u = 0; u < PF; ++u)
+        if (j0 + u < wp[q]) {
+          const int e = base[q] + 64 * (j0 + u);
+          c[q][u] = __ldg(reinterpret_cast<const int2*>(A.col + e));
+          vh[q][u] = __ldg(reinterpret_cast<const float2*>(A.hi + e));
+          vl[q][u] = __ldg(reinterpret_cast<const float2*>(A.lo + e));
+        }
 #pragma unroll
     for (int q = 0; q < ILP; ++q)
-      if (j < wp[q]) {
-        df_madd(vh[q].x, vl[q].x, __ldg(z + c[q].x), sh[q], sl[q]);
-        df_madd(vh[q].y, vl[q].y, __ldg(z + c[q].y), sh[q], sl[q]);
-      }
+#pragma unroll
+      for (int u = 0; u < PF; ++u)
+        if (j0 + u < wp[q]) {
+          df_madd(vh[q][u].x, vl[q][u].x, __ldg(z + c[q][u].x), sh[q], sl[q]);
+          df_madd(vh[q][u].y, vl[q][u].y, __ldg(z + c[q][u].y), sh[q], sl[q]);
+        }
   }
 }
 

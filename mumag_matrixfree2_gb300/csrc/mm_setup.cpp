@@ -203,6 +203,59 @@ void morton_order(int N, int E, const double* knt, const int* conn, int* node_pe
   std::stable_sort(elem_perm, elem_perm + E, [&](int a, int b) { return ekey[a] < ekey[b]; });
 }
 
+void node_graph(int N, int E, const int* conn, std::vector<int>& ptr, std::vector<int>& col) {
+  // every vertex of a tetrahedron has the element's three other vertices as neighbours
+  std::vector<int> cnt(N + 1, 0);
+  for (int64_t k = 0; k < 4 * (int64_t)E; ++k) cnt[conn[k] + 1] += 3;
+  for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> raw(cnt[N]);
+  std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+  for (int e = 0; e < E; ++e)
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        if (a != b) raw[fill[conn[4 * e + a]]++] = conn[4 * e + b];
+  ptr.assign(N + 1, 0);
+  parallel_chunks(N, setup_threads(N), [&](int, int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      std::sort(raw.begin() + cnt[i], raw.begin() + cnt[i + 1]);
+      const auto end = std::unique(raw.begin() + cnt[i], raw.begin() + cnt[i + 1]);
+      ptr[i + 1] = (int)(end - (raw.begin() + cnt[i]));
+    }
+  });
+  for (int i = 0; i < N; ++i) ptr[i + 1] += ptr[i];
+  col.resize(ptr[N]);
+  parallel_chunks(N, setup_threads(N), [&](int, int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i)
+      std::copy(raw.begin() + cnt[i], raw.begin() + cnt[i] + (ptr[i + 1] - ptr[i]), col.begin() + ptr[i]);
+  });
+}
+
+void rcm_order(int N, const std::vector<int>& ptr, const std::vector<int>& col, const int* seeds, int* perm) {
+  std::vector<int> order(N);
+  std::vector<char> seen(N, 0);
+  auto deg = [&](int v) { return ptr[v + 1] - ptr[v]; };
+  int n = 0;
+  for (int z = 0; z < N && n < N; ++z) {
+    const int seed = seeds[z];
+    if (seen[seed]) continue;
+    seen[seed] = 1;
+    order[n++] = seed;
+    for (int head = n - 1; head < n; ++head) {  // the queue is order[head .. n)
+      const int v = order[head];
+      const int first = n;
+      for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
+        const int u = col[k];
+        if (!seen[u]) {
+          seen[u] = 1;
+          order[n++] = u;
+        }
+      }
+      std::stable_sort(order.begin() + first, order.begin() + n, [&](int a, int b) { return deg(a) < deg(b); });
+    }
+  }
+  for (int i = 0; i < N; ++i) perm[i] = order[N - 1 - i];
+}
+
 // ---------------------------------------------------------------------------------------------
 // assembly helpers
 // ---------------------------------------------------------------------------------------------
@@ -514,6 +567,46 @@ static HostCSR spgemm(const HostCSR& A, const HostCSR& B) {
   concat_parallel(tcol, C.col);
   concat_parallel(tval, C.val);
   return C;
+}
+
+HostCSR fused_restriction(const HostCSR& R, const HostCSR& A, const std::vector<double>& s) {
+  HostCSR AS;
+  AS.n_rows = A.n_rows;
+  AS.n_cols = A.n_cols;
+  AS.ptr = A.ptr;
+  AS.col.resize(A.col.size());
+  AS.val.resize(A.val.size());
+  parallel_chunks((int64_t)A.col.size(), setup_threads(A.n_rows), [&](int, int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; ++k) {
+      AS.col[k] = A.col[k];
+      AS.val[k] = A.val[k] * s[A.col[k]];
+    }
+  });
+  const HostCSR C = spgemm(R, AS);
+  HostCSR F;
+  F.n_rows = R.n_rows;
+  F.n_cols = R.n_cols;
+  F.ptr.assign(F.n_rows + 1, 0);
+  F.col.reserve(C.col.size() + R.col.size());
+  F.val.reserve(C.col.size() + R.col.size());
+  for (int i = 0; i < R.n_rows; ++i) {  // F = R - C, merging two sorted rows
+    int a = R.ptr[i], b = C.ptr[i];
+    const int ae = R.ptr[i + 1], be = C.ptr[i + 1];
+    while (a < ae || b < be) {
+      const int ca = a < ae ? R.col[a] : R.n_cols;
+      const int cb = b < be ? C.col[b] : R.n_cols;
+      const int c = std::min(ca, cb);
+      double v = 0.0;
+      if (ca == c) v += R.val[a++];
+      if (cb == c) v -= C.val[b++];
+      if (v != 0.0) {
+        F.col.push_back(c);
+        F.val.push_back(v);
+      }
+    }
+    F.ptr[i + 1] = (int)F.col.size();
+  }
+  return F;
 }
 
 static std::vector<double> diag_of(const HostCSR& A) {

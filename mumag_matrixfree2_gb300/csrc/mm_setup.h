@@ -80,6 +80,14 @@ void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn
 void boundary_mask(int N, int E, const int* conn, double* mask);
 // Morton order (src/reorder_mesh.py:19-30,85-100); stable on ties
 void morton_order(int N, int E, const double* knt, const int* conn, int* node_perm, int* elem_perm);
+// Edge graph of a tetrahedral mesh: node i's neighbours (nodes sharing an edge with it), ascending,
+// without i itself
+void node_graph(int N, int E, const int* conn, std::vector<int>& ptr, std::vector<int>& col);
+// Reverse Cuthill-McKee order of a graph (src/reorder_mesh.py:53-83): unvisited nodes start a
+// component in the order `seeds` (nodes by increasing degree); each component is traversed
+// breadth-first, the newly reached neighbours of every node ordered by increasing degree (stable, so
+// equal degrees keep ascending node order); the visit order reversed is the permutation.
+void rcm_order(int N, const std::vector<int>& ptr, const std::vector<int>& col, const int* seeds, int* perm);
 
 // Poisson stiffness with Dirichlet identity rows/columns and regularisation (src/amg_utils.py:21-84)
 HostCSR assemble_poisson(int N, int E, const int* conn, const double* volume, const double* grad_phi,
@@ -95,6 +103,10 @@ void assemble_magnetoelastic(EnergyOp& op, int N, int E, const int* conn, const 
                              int n, const double* k1me, const double* k1me_p);
 
 std::vector<AmgLevel> build_amg(const HostCSR& A, const AmgParams& prm);
+
+// R (I - A S), S = diag(s): the restriction of the residual that a pre-smoothing from zero leaves,
+// x = S b, r = b - A x, b_c = R r = R (I - A S) b, as one operator (exact zeros dropped, columns sorted)
+HostCSR fused_restriction(const HostCSR& R, const HostCSR& A, const std::vector<double>& s);
 std::vector<double> dense_inverse(const HostCSR& A);  // row-major n x n; throws on singular
 
 }  // namespace mm

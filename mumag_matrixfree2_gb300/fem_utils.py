@@ -54,11 +54,11 @@ class MeshSetup:
 
 
 def prepare(knt, ijk, A_lookup, K1_lookup, Js_lookup, k_easy, with_boundary: bool = True,
-            reorder: bool = False) -> MeshSetup:
+            reorder: bool | str = False) -> MeshSetup:
     """Orient the mesh, compute volumes/gradients, V_mag, M_nodal and the Dirichlet mask.
 
-    With ``reorder`` the nodes and elements are first put in Morton order
-    (``src/reorder_mesh.py:85-117``).
+    With ``reorder`` ("gpu" or True: Morton order, ``src/reorder_mesh.py:85-117``; "cpu": reverse
+    Cuthill-McKee, ``:53-83``) the nodes and elements are first renumbered.
     """
     knt = np.ascontiguousarray(knt, dtype=np.float64)
     ijk = np.asarray(ijk)
@@ -67,7 +67,10 @@ def prepare(knt, ijk, A_lookup, K1_lookup, Js_lookup, k_easy, with_boundary: boo
         mat_id = mat_id + 1
     conn = ijk[:, :4].astype(np.int32)
     if reorder:
-        node_perm, elem_perm = _abi.morton_order(knt, conn)
+        if reorder == "cpu":
+            node_perm, elem_perm = _abi.rcm_order(conn, knt.shape[0])
+        else:
+            node_perm, elem_perm = _abi.morton_order(knt, conn)
         inv = np.empty_like(node_perm)
         inv[node_perm] = np.arange(len(node_perm), dtype=np.int32)
         knt = knt[node_perm]

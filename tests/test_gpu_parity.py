@@ -363,35 +363,6 @@ def test_fp32_preconditioner_keeps_the_fp64_pcg(cuda_ok, name):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_persistent_loop_matches_graph_loop(cuda_ok, precision):
-    """The one-launch PCG loop (grid barriers between the phases) against the graph of separate
-    kernels: same iterations (+-1), potentials equal to the PCG tolerance, and for every
-    blocks-per-SM choice a converged, bit-reproducible solve."""
-    s, p, _ = case("cube16_h2_air48")
-    probs = []
-    for persistent in (0, 1):
-        prob = fem_utils.make_problem(s)
-        prob.set_precision(precision)
-        prob.set_option("persistent", persistent)
-        prob.build_poisson(1e-12, "amgcl")
-        probs.append(prob)
-    m = random_state(p.N, seed=21, amplitude=0.2)
-    zero = np.zeros(p.N)
-    Ug, itg, rrg, rcg = probs[0].solve_u(m, zero, 1e-10)
-    Up, itp, rrp, rcp = probs[1].solve_u(m, zero, 1e-10)
-    assert rcg == 0 and rcp == 0 and rrp <= 1e-10
-    assert abs(itp - itg) <= 1, (itp, itg)
-    assert rel(Up, Ug) <= 1e-8
-    for bpsm in (1, 2, 4):
-        probs[1].set_option("persist_bpsm", bpsm)
-        U1, it1, rr1, rc1 = probs[1].solve_u(m, zero, 1e-10)
-        U2, it2, rr2, rc2 = probs[1].solve_u(m, zero, 1e-10)
-        assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - itg) <= 1
-        assert it1 == it2 and np.array_equal(U1, U2)
-        assert rel(U1, Ug) <= 1e-8
-
-
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, precision):
     """The two coarsest levels applied as x2 = T b + W (Z b) against the five level-by-level kernels:
     the same V-cycle (to rounding) and the same solve."""
@@ -417,6 +388,32 @@ def test_fused_coarse_correction_matches_the_level_by_level_vcycle(cuda_ok, prec
     U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
     assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1
     assert rel(U1, U0) <= 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32_precond"])
+def test_fused_restriction_matches_the_residual_pass(cuda_ok, precision):
+    """Restriction with R_l (I - A_l S_l) formed on the host against the residual kernel followed by
+    R_l: the same V-cycle (to rounding) and the same solve, with the oracle's iteration count."""
+    s, p, _ = case("cube40_h2_air200")
+    probs = []
+    for fr in (0, 3):
+        prob = fem_utils.make_problem(s)
+        prob.set_precision(precision)
+        prob.build_poisson(1e-12, "amgcl")
+        prob.set_option("fuse_restrict", fr)
+        probs.append(prob)
+    assert probs[0].n_levels >= 3
+    r = np.random.default_rng(43).standard_normal(s.N) * s.boundary_mask
+    z0, z1 = probs[0].precond(r), probs[1].precond(r)
+    assert rel(z1, z0) <= (1e-11 if precision == "fp64" else 1e-5)
+    m = random_state(s.N, seed=44, amplitude=0.05)
+    U0, it0, rr0, rc0 = probs[0].solve_u(m, np.zeros(s.N), 1e-10)
+    U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
+    assert rc1 == 0 and rr1 <= 1e-10 and abs(it1 - it0) <= 1
+    assert rel(U1, U0) <= 1e-8
+    if precision == "fp64":
+        _, it_o, _ = opo.SolveU(p, cg_tol=1e-10)(m, np.zeros(p.N), 1e-10, return_info=True)
+        assert abs(it1 - it_o) <= 1
 
 
 def test_autotuner_keeps_results_within_tolerance(cuda_ok):
