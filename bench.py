@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"],
                     help="solver of the main timed solves (fp64: the headline plain method; the others for "
                          "profiling their kernels)")
+    ap.add_argument("--fuse-restrict", choices=["auto", "off"], default="auto",
+                    help="fused restrictions R(I - A S) in the V-cycle: the autotuner's choice, or off (for A/B)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
     ap.add_argument("--ref-budget-s", type=float, default=150.0, help="reference arm: cap on timed seconds")
@@ -503,6 +505,8 @@ def run_ours(a):
     t0 = time.perf_counter()
     tune = prob.autotune(20)
     tune_s = time.perf_counter() - t0
+    if a.fuse_restrict == "off":
+        prob.set_option("fuse_restrict", 0)
     if a.no_graph:
         prob.set_option("graph", 0)
     N = s.N
@@ -561,6 +565,17 @@ def run_ours(a):
     achieved = top["bytes_per_launch"] / (top["ms_per_launch"] * 1e-3) / 1e9
     ms_cold, bytes_cold = prob.time_kernel("smooth", 20)
     lv = prob.amg_levels()
+    # energy + gradient evaluations: device time of the evaluation's kernels, L2 flushed before each
+    ms_e64, bytes_e64 = prob.time_kernel("energy", 20)
+    prob.set_option("energy_ff", 1)
+    ms_eff, bytes_eff = prob.time_kernel("energy", 20)
+    prob.set_option("energy_ff", -1)
+    energy = {"fp64": {"evals_per_s": 1e3 / ms_e64, "us_per_eval": 1e3 * ms_e64, "bytes_per_eval": bytes_e64,
+                       "frac_hbm": bytes_e64 / (ms_e64 * 1e-3) / 1e9 / peak},
+              "float_float": {"evals_per_s": 1e3 / ms_eff, "us_per_eval": 1e3 * ms_eff, "bytes_per_eval": bytes_eff,
+                              "frac_hbm": bytes_eff / (ms_eff * 1e-3) / 1e9 / peak},
+              "timing": "the kernels of one evaluation (float-float: the pair splits of m, k.m and U, then the "
+                        "operator), CUDA events, 256 MiB L2 flush before each of 20 repetitions"}
 
     mixed = None
     if not a.no_mixed:
@@ -620,6 +635,17 @@ def run_ours(a):
             loop["mixed_vs_fp64"] = {"Hc_rel_err": abs(lp["mixed"]["Hc_T"] - lp["fp64"]["Hc_T"]) / abs(lp["fp64"]["Hc_T"]),
                                      "same_switch_step": lp["mixed"]["switch_step"] == lp["fp64"]["switch_step"],
                                      "max_abs_dJ_T": float(np.max(np.abs(Jm - J64)))}
+        ref_loop = ROOT / "tests" / "golden" / f"ref_cpp_loop_{a.workload}.npz"
+        if ref_loop.exists() and abs(a.loop_dB - 0.1) < 1e-12:
+            # the reference's own C++ loop on this workload (--cpp-mkl path, fixture written from
+            # src/cpp/cpp_mkl_minimizer.cpp compiled against the MKL-API shim)
+            f = np.load(ref_loop)
+            Hc_r, sw_r = float(f["Hc_T"]), int(f["switch_index"])
+            loop["vs_reference_cpp_loop"] = {
+                "reference_Hc_T": Hc_r, "reference_switch_step": sw_r,
+                "reference_minimizer_iters": int(f["iters"].sum()),
+                **{p_: {"Hc_rel_err": abs(v["Hc_T"] - Hc_r) / Hc_r, "same_switch_step": v["switch_step"] == sw_r}
+                   for p_, v in lp.items()}}
         if "fp32_precond" in lp:
             Jq = lp["fp32_precond"].pop("_J")
             loop["fp32_precond"] = lp["fp32_precond"]
@@ -651,6 +677,8 @@ def run_ours(a):
                        "pcg_iters_per_solve": its[0], "rel_res": max(rrs), "setup_s": setup_s,
                        "autotune": {"seconds": tune_s, "operators_tuned": len(tune["operators"]),
                                     "coarse_fuse": tune["coarse_fuse"]["chosen"],
+                                    "fuse_restrict": tune.get("fuse_restrict"),
+                                    "fuse_restrict_used": a.fuse_restrict,
                                     "shapes": {f"{o['op']}{o['level']}_{o['precision']}":
                                                ("sell" if o["tpr"] == 1 else f"csr{o['tpr']}")
                                                for o in tune["operators"]}},
@@ -671,6 +699,7 @@ def run_ours(a):
                                           "frac": bytes_cold / (ms_cold * 1e-3) / 1e9 / peak,
                                           "timing": "alone, L2 flushed before each launch"}},
             "kernels": kernels,
+            "energy_grad": energy,
             "profiled_solve_ms": prof_ms / a.profile_steps,
             "mixed": mixed,
             "fp32_precond": fp32pc,

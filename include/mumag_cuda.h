@@ -337,6 +337,12 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * less per level, and fewer bytes than A_l and R_l together).  Bit 0 the FP64 solver, bit 1 the FP32
  * one; mm_autotune keeps a bit only if the V-cycle is faster with it. */
 #define MM_OPT_FUSE_RESTRICT 12
+/* MM_OPT_ENERGY_FF: energy and gradient evaluations in float-float (every stored value and the vectors
+ * m, U and k.m as FP32 pairs hi + lo, products and row sums on the FP32 pipes with about 2^-48
+ * relative error per term; the row totals, gradient and energy sum in FP64).  -1 (default) follows
+ * MM_OPT_PRECISION (on in MM_PRECISION_MIXED and MM_PRECISION_FP32_PRECOND), 0 FP64, 1 float-float.
+ * Problems with several easy axes or a magnetoelastic term always evaluate in FP64. */
+#define MM_OPT_ENERGY_FF 13
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

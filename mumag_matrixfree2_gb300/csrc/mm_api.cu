@@ -175,6 +175,11 @@ struct mm_problem {
   std::vector<double> kax_h;        // easy axes (n_mat, 3)
   mmk::EnergySell32 eops32{};      // FP32 exchange + anisotropy entries for the inner solve (lazy)
   bool eops32_ok = false;          // built and current (a new magnetoelastic term clears it)
+  mmk::EnergySellFF eopsff{};      // float-float energy operator (mixed-precision energy evaluations)
+  bool eopsff_ok = false;          // built and current (a new magnetoelastic term clears it)
+  bool eopsff_failed = false;      // an entry lies outside the range of the float-float pairs
+  int energy_ff = -1;              // MM_OPT_ENERGY_FF
+  float2 *w_mff = nullptr, *w_sff = nullptr, *w_uff = nullptr;
   int min_fp32 = -1;               // MM_OPT_MIN_FP32
   double* d_Mn = nullptr;
   double* d_inv_M_rel = nullptr;
@@ -322,6 +327,50 @@ struct mm_problem {
     d.mex = d.mey = nullptr;
     d.single_axis = eop.single_axis;
     d.axis0 = eop.axis0;
+  }
+  // whether energy evaluations run in float-float (one easy axis, no magnetoelastic term), building the
+  // pairs on first use
+  bool use_energy_ff() {
+    const bool want = energy_ff < 0 ? (mixed || fp32_precond) : energy_ff != 0;
+    if (!want || eop_h.n_rows == 0 || !eops.single_axis || eops.mex) return false;
+    if (eopsff_ok) return true;
+    if (eopsff_failed) return false;
+    double lo = 1e300, hi = 0.0;
+    for (const mm::dvec* v : {&eop_h.w, &eop_h.q, &eop_h.gx, &eop_h.gy, &eop_h.gz})
+      for (double x : *v)
+        if (x != 0.0) lo = std::min(lo, std::fabs(x)), hi = std::max(hi, std::fabs(x));
+    if (hi > 0.0 && (lo < 1e-30 || hi > 1e30)) {
+      eopsff_failed = true;
+      return false;
+    }
+    auto pairs = [&](const mm::dvec& a) {
+      std::vector<float2> out((size_t)eops_stored, make_float2(0.0f, 0.0f));
+      for (size_t k = 0; k < eops_pos.size(); ++k) {
+        const float hi32 = (float)a[k];
+        out[eops_pos[k]] = make_float2(hi32, (float)(a[k] - (double)hi32));
+      }
+      return upload(out);
+    };
+    mmk::EnergySellFF& d = eopsff;
+    d.n_rows = eops.n_rows;
+    d.rows = eops.rows;
+    d.sptr = eops.sptr;
+    d.col = eops.col;
+    d.w = pairs(eop_h.w);
+    d.q = pairs(eop_h.q);
+    d.gx = pairs(eop_h.gx);
+    d.gy = pairs(eop_h.gy);
+    d.gz = pairs(eop_h.gz);
+    d.kx = kax_h[3 * eops.axis0];
+    d.ky = kax_h[3 * eops.axis0 + 1];
+    d.kz = kax_h[3 * eops.axis0 + 2];
+    if (!w_mff) {
+      w_mff = alloc<float2>(3 * (size_t)N);
+      w_sff = alloc<float2>(N);
+      w_uff = alloc<float2>(N);
+    }
+    eopsff_ok = true;
+    return true;
   }
   // whether the inner solve runs in FP32, building its entries on first use; false also when an entry
   // of the operator lies outside the range FP32 represents with full precision
@@ -1029,11 +1078,28 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   return (it >= maxiter && r2 > tol2_ref) ? MM_MAXITER : MM_OK;
 }
 
-double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
-                  double* d_g) {
+// the launches of one energy and gradient evaluation (m.(g + g_z) into red[R_E]): float-float in the
+// mixed-precision problems (MM_OPT_ENERGY_FF), else FP64
+void enqueue_energy(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
+                    double* d_g) {
+  if (h->use_energy_ff()) {
+    const mmk::EnergySellFF& o = h->eopsff;
+    mmk::k_split_m_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_m, o.kx, o.ky, o.kz, h->w_mff, h->w_sff);
+    mmk::k_split_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_U, h->w_uff);
+    mmk::k_energy_grad_ff<<<grid_elem(o.n_rows), BS, 0, h->st>>>(o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0],
+                                                                  B[1], B[2], d_bias, h->inv_Vmag, d_g, h->d_sc,
+                                                                  h->d_part);
+    LAUNCH_CHECK();
+    return;
+  }
   mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
                                                                      d_bias, h->inv_Vmag, d_g, h->d_sc, h->d_part);
   LAUNCH_CHECK();
+}
+
+double energy_dev(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
+                  double* d_g) {
+  enqueue_energy(h, d_m, d_U, B, d_bias, d_g);
   return 0.5 * h->red(R_E) * h->inv_Vmag;
 }
 
@@ -2741,6 +2807,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
       h->eop.mex = h->eop.mey = nullptr;
       h->eops.mex = h->eops.mey = nullptr;
       h->eops32_ok = false;
+      h->eopsff_ok = false;
       h->drop_inner_graphs();
       return MM_OK;
     }
@@ -2751,6 +2818,7 @@ int mm_set_magnetoelastic(mm_problem* h, int n, const double* k1me, const double
     h->eops.mex = h->upload_eop_sell<double>(h->eop_h.mx, 0.0);
     h->eops.mey = h->upload_eop_sell<double>(h->eop_h.my, 0.0);
     h->eops32_ok = false;
+      h->eopsff_ok = false;
     h->drop_inner_graphs();
     h->sync();
     return MM_OK;
@@ -2895,10 +2963,8 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
                                                                 nullptr, (double*)nullptr);
         LAUNCH_CHECK();
       } else if (kernel == MM_KERNEL_ENERGY) {
-        mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, h->d_m, h->d_U, h->d_Mn, 0.0, 0.0,
-                                                                           1.0, nullptr, h->inv_Vmag, h->d_g, h->d_sc,
-                                                                           h->d_part);
-        LAUNCH_CHECK();
+        const double B[3] = {0.0, 0.0, 1.0};
+        enqueue_energy(h, h->d_m, h->d_U, B, nullptr, h->d_g);
       } else {
         local_grad_dev(h, h->d_m, h->d_out);
       }
@@ -2912,6 +2978,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
     } else if (kernel == MM_KERNEL_SMOOTH) {
       const double nnz = (double)l0->A.nnz;
       nbytes = nnz * 12.0 + ((N + 31) / 32 + 1.0) * 4.0 + N * 8.0 * 4.0;
+    } else if (kernel == MM_KERNEL_ENERGY && h->use_energy_ff()) {
+      // entries: col, (hi, lo) of w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3);
+      // the pair splits: m (3) and U read, their pairs and those of k.m written
+      nbytes = nnzE * (4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0 + N * (8.0 * 4.0 + 8.0 * 5.0);
     } else if (kernel == MM_KERNEL_ENERGY) {
       // entries: col, mat, w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3)
       nbytes = nnzE * (4.0 + 4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0;
@@ -3123,6 +3193,11 @@ int mm_set_option(mm_problem* h, int option, int value) {
       drop_graph(h->s32);
     }
     h->coarse_fuse = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_ENERGY_FF) {
+    if (value < -1 || value > 1) return MM_ERR_ARG;
+    h->energy_ff = value;
     return MM_OK;
   }
   if (option == MM_OPT_FUSE_RESTRICT) {

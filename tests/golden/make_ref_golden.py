@@ -9,10 +9,12 @@ what the GPU tests compare with, since the library cannot run on the GPU host:
   ``solve_poisson`` (U), ``solve_Py_g`` after 1 and after 10 inner iterations, and three field steps
   of ``run_cpp_pcohen_hs_minimization`` from the seeded initial state (iterations, evaluations, inner
   iterations, energy and m); vectors at every ``stride``-th node plus whole-vector sums;
-* ``ref_cpp_loop_cube40_h2_air200.npz``: the field sweep +8 -> -8 T in 0.1 T steps (161 fields) of
-  the reference's ``--cpp-mkl`` loop on the 40 nm cube: J(B), energies, iteration counts.
+* ``ref_cpp_loop_<workload>.npz``: the field sweep +8 -> -8 T in 0.1 T steps (161 fields) of the
+  reference's ``--cpp-mkl`` loop on the 40 nm cube and (with ``--cube80``) the 80 nm cube: J(B),
+  energies, iteration counts, the coercive field and the switching step.
 
-Usage: ``python tests/golden/make_ref_golden.py [--no-loop]`` (a few minutes on 8 cores).
+Usage: ``python tests/golden/make_ref_golden.py [--no-loop] [--cube80]`` (a few minutes on 8 cores;
+the 80 nm loop takes about half an hour).
 """
 
 import sys
@@ -65,8 +67,7 @@ def case_fixture(lib, name: str, stride: int) -> None:
     print("wrote", out.name, "E", E, "steps", [st[:4] for st in steps])
 
 
-def loop_fixture(lib) -> None:
-    name = "cube40_h2_air200"
+def loop_fixture(lib, name: str = "cube40_h2_air200") -> None:
     s, p, Js_ref = H.case(name)
     cp = ref_cpp.CppProblem(lib, p)
     prm = H.ref_min_params()
@@ -95,6 +96,8 @@ def main(argv) -> None:
         case_fixture(lib, name, stride)
     if "--no-loop" not in argv:
         loop_fixture(lib)
+    if "--cube80" in argv:
+        loop_fixture(lib, "cube80_h1.6_air200")
 
 
 if __name__ == "__main__":

@@ -57,6 +57,45 @@ def test_energy_multi_axis(cuda_ok):
     assert abs(E - E0) <= RTOL * abs(E0) and rel(g, g0) <= RTOL
 
 
+def test_float_float_energy_matches_fp64(cuda_ok):
+    """The float-float energy operator of the mixed-precision problems (MM_OPT_ENERGY_FF) against the
+    FP64 one and the oracle: energy to 1e-12 relative, gradient to 1e-11 of its largest entry; a
+    problem with several easy axes keeps the FP64 evaluation (bit-identical)."""
+    s, p, _ = case("cube16_h2_air48")
+    m = random_state(p.N, seed=31)
+    U = np.random.default_rng(32).standard_normal(p.N)
+    B = np.array([0.1, -0.05, -0.3])
+    probs = {}
+    for ff in (0, 1):
+        prob = fem_utils.make_problem(s)
+        prob.set_option("energy_ff", ff)
+        probs[ff] = prob
+    E64, g64 = probs[0].energy_and_grad(m, U, B)
+    Eff, gff = probs[1].energy_and_grad(m, U, B)
+    assert abs(Eff - E64) <= 1e-12 * abs(E64)
+    assert rel(gff, g64) <= 1e-11
+    E0, g0 = ofem.energy_and_grad_mf(p, m, U, B)
+    assert abs(Eff - E0) <= RTOL * abs(E0) and rel(gff, g0) <= RTOL
+    ms, nbytes = probs[1].time_kernel("energy", 5)
+    assert ms > 0 and nbytes > 0
+    from mumag_matrixfree2_gb300 import synthetic as syn
+
+    knt, ijk = syn.box_mesh(syn.WORKLOADS["cube8_h2_air24"])
+    ijk = ijk.copy()
+    right = knt[ijk[:, :4]].mean(axis=1)[:, 0] > 0
+    ijk[(ijk[:, 4] == 1) & right, 4] = 3  # half of the magnet gets a tilted easy axis
+    A, K1, Js, k, _ = syn.reduced_materials([syn.Material(), syn.AIR,
+                                             syn.Material(axis=(np.sin(0.3), 0.0, np.cos(0.3)))])
+    s2 = fem_utils.prepare(knt, ijk, A, K1, Js, k)
+    a, b = fem_utils.make_problem(s2), fem_utils.make_problem(s2)
+    b.set_option("energy_ff", 1)
+    m2 = random_state(s2.N, seed=33)
+    U2 = np.random.default_rng(34).standard_normal(s2.N)
+    Ea, ga = a.energy_and_grad(m2, U2, B)
+    Eb, gb = b.energy_and_grad(m2, U2, B)
+    assert Ea == Eb and np.array_equal(ga, gb)
+
+
 def test_local_hessian_rhs_and_diagonal(small):
     s, p, ops, prob = small
     v = np.random.default_rng(6).standard_normal((p.N, 3))
