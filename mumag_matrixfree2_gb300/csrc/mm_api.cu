@@ -1078,17 +1078,19 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   return (it >= maxiter && r2 > tol2_ref) ? MM_MAXITER : MM_OK;
 }
 
+// lanes per magnetic row of the float-float energy kernel
+constexpr int EFF_TPR = 4;
+
 // the launches of one energy and gradient evaluation (m.(g + g_z) into red[R_E]): float-float in the
 // mixed-precision problems (MM_OPT_ENERGY_FF), else FP64
 void enqueue_energy(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
                     double* d_g) {
   if (h->use_energy_ff()) {
     const mmk::EnergySellFF& o = h->eopsff;
-    mmk::k_split_m_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_m, o.kx, o.ky, o.kz, h->w_mff, h->w_sff);
-    mmk::k_split_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_U, h->w_uff);
-    mmk::k_energy_grad_ff<<<grid_elem(o.n_rows), BS, 0, h->st>>>(o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0],
-                                                                  B[1], B[2], d_bias, h->inv_Vmag, d_g, h->d_sc,
-                                                                  h->d_part);
+    mmk::k_split_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_m, d_U, o.kx, o.ky, o.kz, h->w_mff, h->w_sff,
+                                                       h->w_uff);
+    mmk::k_energy_grad_ff<EFF_TPR><<<grid_rows(o.n_rows, EFF_TPR), BS, 0, h->st>>>(
+        o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0], B[1], B[2], d_bias, h->inv_Vmag, d_g, h->d_sc, h->d_part);
     LAUNCH_CHECK();
     return;
   }

@@ -1285,70 +1285,100 @@ __device__ __forceinline__ float2 ff_split(double v) {
   return make_float2(h, (float)(v - (double)h));
 }
 
-// the float-float pairs of m (3N) and of s = k.m (N, formed in FP64 as the FP64 kernel forms k.v)
-__global__ void __launch_bounds__(BS) k_split_m_ff(int N, const double* __restrict__ m, double kx, double ky,
-                                                   double kz, float2* __restrict__ mff, float2* __restrict__ sff) {
+// the float-float pairs of m (3N), of s = k.m (N, formed in FP64 as the FP64 kernel forms k.v) and of U
+__global__ void __launch_bounds__(BS) k_split_ff(int N, const double* __restrict__ m, const double* __restrict__ U,
+                                                 double kx, double ky, double kz, float2* __restrict__ mff,
+                                                 float2* __restrict__ sff, float2* __restrict__ uff) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double x = m[3 * i], y = m[3 * i + 1], z = m[3 * i + 2];
     mff[3 * i] = ff_split(x);
     mff[3 * i + 1] = ff_split(y);
     mff[3 * i + 2] = ff_split(z);
     sff[i] = ff_split(fma(kz, z, fma(ky, y, kx * x)));
+    uff[i] = ff_split(U[i]);
   }
 }
 
-__global__ void __launch_bounds__(BS) k_split_ff(int n, const double* __restrict__ x, float2* __restrict__ out) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = ff_split(x[i]);
+// (sh, sl) += (h2, l2) from the lane `o` places down
+__device__ __forceinline__ void ff_shfl_add(float& sh, float& sl, int o) {
+  const float h2 = __shfl_down_sync(0xffffffffu, sh, o);
+  const float l2 = __shfl_down_sync(0xffffffffu, sl, o);
+  float t, err;
+  Acc<float>::two_sum(sh, h2, t, err);
+  sh = t;
+  sl += err + l2;
 }
 
-// g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E] (FP64)
+// g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E] (FP64).
+// TPR lanes per row (133k magnetic rows would give one thread per row too few warps to hide the
+// gather latency): lane q takes entries q, q + TPR, ..., and the row's float-float sums are merged
+// over its lanes by a fixed shuffle tree (FP32 shuffles and adds), so the result is deterministic.
+template <int TPR>
 __global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const float2* __restrict__ mff,
                                                        const float2* __restrict__ sff, const float2* __restrict__ uff,
                                                        const double* __restrict__ m, const double* __restrict__ Mn,
                                                        double Bx, double By, double Bz,
                                                        const double* __restrict__ Bbias, double inv_Vmag,
                                                        double* __restrict__ g, Scalars* sc, double* part) {
+  static_assert(TPR >= 1 && TPR <= 32 && (TPR & (TPR - 1)) == 0, "TPR: a power of two up to 32");
+  constexpr int RPB = BS / TPR;
+  const int q = threadIdx.x % TPR;
   double en = 0.0;
-  for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
-    const int s = r >> 5, l = r & 31;
-    const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+  for (int rb = blockIdx.x * RPB; rb < op.n_rows; rb += gridDim.x * RPB) {
+    const int r = rb + threadIdx.x / TPR;
+    const bool valid = r < op.n_rows;
     float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f, azh = 0.f, azl = 0.f, th = 0.f, tl = 0.f;
     float uxh = 0.f, uxl = 0.f, uyh = 0.f, uyl = 0.f, uzh = 0.f, uzl = 0.f;
-#pragma unroll 2
-    for (int k = 0; k < wd; ++k) {
-      const int at = base + (k << 5) + l;
-      const int j = __ldg(op.col + at);
-      const float2 w = __ldg(op.w + at), q = __ldg(op.q + at);
-      const float2 gx = __ldg(op.gx + at), gy = __ldg(op.gy + at), gz = __ldg(op.gz + at);
-      const float2 mx = __ldg(mff + 3 * j), my = __ldg(mff + 3 * j + 1), mz = __ldg(mff + 3 * j + 2);
-      const float2 sj = __ldg(sff + j), u = __ldg(uff + j);
-      ff_madd(w.x, w.y, mx.x, mx.y, axh, axl);
-      ff_madd(w.x, w.y, my.x, my.y, ayh, ayl);
-      ff_madd(w.x, w.y, mz.x, mz.y, azh, azl);
-      ff_madd(q.x, q.y, sj.x, sj.y, th, tl);
-      ff_madd(gx.x, gx.y, u.x, u.y, uxh, uxl);
-      ff_madd(gy.x, gy.y, u.x, u.y, uyh, uyl);
-      ff_madd(gz.x, gz.y, u.x, u.y, uzh, uzl);
+    if (valid) {
+      const int s = r >> 5, l = r & 31;
+      const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+      for (int k = q; k < wd; k += TPR) {
+        const int at = base + (k << 5) + l;
+        const int j = __ldg(op.col + at);
+        const float2 w = __ldg(op.w + at), qq = __ldg(op.q + at);
+        const float2 gx = __ldg(op.gx + at), gy = __ldg(op.gy + at), gz = __ldg(op.gz + at);
+        const float2 mx = __ldg(mff + 3 * j), my = __ldg(mff + 3 * j + 1), mz = __ldg(mff + 3 * j + 2);
+        const float2 sj = __ldg(sff + j), u = __ldg(uff + j);
+        ff_madd(w.x, w.y, mx.x, mx.y, axh, axl);
+        ff_madd(w.x, w.y, my.x, my.y, ayh, ayl);
+        ff_madd(w.x, w.y, mz.x, mz.y, azh, azl);
+        ff_madd(qq.x, qq.y, sj.x, sj.y, th, tl);
+        ff_madd(gx.x, gx.y, u.x, u.y, uxh, uxl);
+        ff_madd(gy.x, gy.y, u.x, u.y, uyh, uyl);
+        ff_madd(gz.x, gz.y, u.x, u.y, uzh, uzl);
+      }
     }
-    const double t = (double)th + (double)tl;
-    const double ax = fma(-t, op.kx, (double)axh + (double)axl);
-    const double ay = fma(-t, op.ky, (double)ayh + (double)ayl);
-    const double az = fma(-t, op.kz, (double)azh + (double)azl);
-    const double ux = (double)uxh + (double)uxl, uy = (double)uyh + (double)uyl, uz = (double)uzh + (double)uzl;
-    const int a = __ldg(op.rows + r);
-    double bx = Bx, by = By, bz = Bz;
-    if (Bbias) {
-      bx += Bbias[3 * a];
-      by += Bbias[3 * a + 1];
-      bz += Bbias[3 * a + 2];
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) {
+      ff_shfl_add(axh, axl, o);
+      ff_shfl_add(ayh, ayl, o);
+      ff_shfl_add(azh, azl, o);
+      ff_shfl_add(th, tl, o);
+      ff_shfl_add(uxh, uxl, o);
+      ff_shfl_add(uyh, uyl, o);
+      ff_shfl_add(uzh, uzl, o);
     }
-    const double mn = -2.0 * Mn[a];
-    const double zx = mn * bx, zy = mn * by, zz = mn * bz;
-    const double gxr = (ax + ux) + zx, gyr = (ay + uy) + zy, gzr = (az + uz) + zz;
-    en += m[3 * a] * (gxr + zx) + m[3 * a + 1] * (gyr + zy) + m[3 * a + 2] * (gzr + zz);
-    g[3 * a] = gxr * inv_Vmag;
-    g[3 * a + 1] = gyr * inv_Vmag;
-    g[3 * a + 2] = gzr * inv_Vmag;
+    if (valid && q == 0) {
+      const double t = (double)th + (double)tl;
+      const double ax = fma(-t, op.kx, (double)axh + (double)axl);
+      const double ay = fma(-t, op.ky, (double)ayh + (double)ayl);
+      const double az = fma(-t, op.kz, (double)azh + (double)azl);
+      const double ux = (double)uxh + (double)uxl, uy = (double)uyh + (double)uyl, uz = (double)uzh + (double)uzl;
+      const int a = __ldg(op.rows + r);
+      double bx = Bx, by = By, bz = Bz;
+      if (Bbias) {
+        bx += Bbias[3 * a];
+        by += Bbias[3 * a + 1];
+        bz += Bbias[3 * a + 2];
+      }
+      const double mn = -2.0 * Mn[a];
+      const double zx = mn * bx, zy = mn * by, zz = mn * bz;
+      const double gxr = (ax + ux) + zx, gyr = (ay + uy) + zy, gzr = (az + uz) + zz;
+      en += m[3 * a] * (gxr + zx) + m[3 * a + 1] * (gyr + zy) + m[3 * a + 2] * (gzr + zz);
+      g[3 * a] = gxr * inv_Vmag;
+      g[3 * a + 1] = gyr * inv_Vmag;
+      g[3 * a + 2] = gzr * inv_Vmag;
+    }
   }
   grid_reduce(en, 0.0, sc, part, R_E);
 }
