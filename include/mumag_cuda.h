@@ -89,6 +89,8 @@ typedef struct {
   int status;
   double demag_seconds;       /* device time of the demag solves (CUDA events around each)            */
   double demag_wall_seconds;  /* host time spent in the demag solve calls (the rest is the minimizer's) */
+  int device_loop;            /* 1: the iterations ran as one device graph (MM_OPT_MIN_GRAPH); the two
+                                 demag times then cover the solve of the initial state only           */
 } mm_min_info;
 
 /* ---- setup helpers ------------------------------------------------------------------------ */
@@ -343,6 +345,15 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * MM_OPT_PRECISION (on in MM_PRECISION_MIXED and MM_PRECISION_FP32_PRECOND), 0 FP64, 1 float-float.
  * Problems with several easy axes or a magnetoelastic term always evaluate in FP64. */
 #define MM_OPT_ENERGY_FF 13
+/* MM_OPT_MIN_GRAPH (default 1): mm_minimize runs the iterations of pcohen_hs, pcohen and pcg as one
+ * CUDA graph: the minimizer loop is a conditional WHILE node, the inner preconditioner solve, the
+ * Armijo trials and each trial's demag PCG are WHILE nodes nested in it, and the decisions between
+ * kernels (forcing tolerance, clipping and fallback, beta, descent test, step expansion and
+ * contraction, the U1-U4 test) are single-thread kernels, so a call waits on the host once.  Same
+ * kernels, grids and reductions as the host-driven loop (0), hence the same results; the host loop
+ * runs for the other methods, with MM_OPT_PROFILE, without MM_OPT_GRAPH and in MM_PRECISION_MIXED
+ * (whose refinement steps are decided on the host). */
+#define MM_OPT_MIN_GRAPH 14
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

@@ -49,7 +49,7 @@ class MinInfo(C.Structure):
     _fields_ = [
         ("iters", C.c_int), ("evals", C.c_int), ("preco_iters", C.c_int), ("demag_iters", C.c_int),
         ("E", C.c_double), ("gnorm", C.c_double), ("seconds", C.c_double), ("status", C.c_int),
-        ("demag_seconds", C.c_double), ("demag_wall_seconds", C.c_double),
+        ("demag_seconds", C.c_double), ("demag_wall_seconds", C.c_double), ("device_loop", C.c_int),
     ]
 
 

@@ -113,6 +113,7 @@ struct SolverT {
   cudaGraphExec_t exec = nullptr;
   bool graph_failed = false;
   int64_t iter_launches = 0;          // kernels in one loop trip
+  int epoch = 0;                      // advanced whenever the loop's launches change (graph dropped)
   // fused coarse correction of levels L-2 .. L-1 (x2 = T b + W (Z b)), when eligible
   bool fused = false;
   mmk::CsrT<T> Tm{};
@@ -239,6 +240,7 @@ struct mm_problem {
   bool inner_graph_failed = false;
   bool inner_cpp_count = false;  // solve_Py_g counts its trips as the reference's C++ minimizer does
   void drop_inner_graphs() {  // their launches hold the operator's arrays and the launch attributes
+    drop_min_graphs();
     if (inner_graphs.empty()) return;
     if (st) cudaStreamSynchronize(st);
     for (auto& ig : inner_graphs) {
@@ -246,6 +248,29 @@ struct mm_problem {
       cudaGraphDestroy(ig.g);
     }
     inner_graphs.clear();
+  }
+  // device-driven minimizer iterations (MM_OPT_MIN_GRAPH): one graph per set of buffers and settings
+  int min_graph = 1;
+  bool min_graph_failed = false;
+  cudaStream_t aux_st[3] = {nullptr, nullptr, nullptr};  // capture streams of the nested loop bodies
+  int cap_depth = 0;
+  mmk::MinScal* d_ms = nullptr;
+  mmk::MinScal* h_ms = nullptr;  // pinned
+  struct MinGraph {
+    std::vector<uintptr_t> key;
+    cudaGraph_t g;
+    cudaGraphExec_t ex;
+    int64_t per_outer, per_ls, per_pcg, per_in;  // kernels of one trip of each loop (launch count)
+  };
+  std::vector<MinGraph> min_graphs;  // at most 4, oldest replaced first
+  void drop_min_graphs() {
+    if (min_graphs.empty()) return;
+    if (st) cudaStreamSynchronize(st);
+    for (auto& mg : min_graphs) {
+      cudaGraphExecDestroy(mg.ex);
+      cudaGraphDestroy(mg.g);
+    }
+    min_graphs.clear();
   }
   double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
   double* min_bias_buf = nullptr;  // its storage
@@ -837,6 +862,7 @@ void drop_graph(SolverT<T>& S) {
   S.exec = nullptr;
   S.graph = nullptr;
   S.graph_failed = false;
+  ++S.epoch;
 }
 
 // A PCG solve whose final scalars copy is queued but not yet waited for (solve_dev waits once, after
@@ -854,9 +880,9 @@ void finish_pcg(mm_problem* h, const PcgPending& pend, int* iters, double* r2_ou
 
 // PCG on S.x (initial guess in, solution out) for the right-hand side S.b; stops on the recursive
 // residual r.r <= tol^2 b.b or maxiter (src/poisson_solve.py:422-478).  Returns iterations and r.r.
+// the work of a PCG solve before its loop: b.b, the scalars, r0 = b - A x0 and z0 = M^-1 r0
 template <class T>
-void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out,
-             PcgPending* pend = nullptr) {
+void enqueue_pcg_start(mm_problem* h, SolverT<T>& S, double tol, int maxiter) {
   const int N = h->N;
   dotT<T>(h, N, S.b, (const T*)nullptr, S.sc, R_BB);
   launch(h, mmk::k_pcg_init_scalars, 1, 32, S.sc, tol, maxiter);
@@ -871,6 +897,12 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
   });
   if (ml) enqueue_vcycle<T>(h, S, S.r, S.z, false, nullptr);
   else apply_M_simple<T>(h, S, S.r, S.z, nullptr);
+}
+
+template <class T>
+void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out,
+             PcgPending* pend = nullptr) {
+  enqueue_pcg_start<T>(h, S, tol, maxiter);
   const bool graph = h->use_graph && !h->prof && build_loop_graph<T>(h, S);
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
@@ -936,7 +968,7 @@ void enqueue_iteration_mp(mm_problem* h) {
   enqueue_vcycle<float>(h, F, F.r, F.z, true, &S.sc->done, S.sc, df ? nullptr : S.z);
 }
 
-void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out, PcgPending* pend = nullptr) {
+void enqueue_pcg_mp_start(mm_problem* h, double tol, int maxiter) {
   auto& S = h->s64;
   auto& F = h->s32;
   const int N = h->N;
@@ -953,6 +985,11 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
   launch(h, mmk::k_split_mp, grid_elem(N), BS, N, S.r, F.lv[0].s, F.r, F.lv[0].x);
   LAUNCH_CHECK();
   enqueue_vcycle<float>(h, F, F.r, F.z, false, nullptr, S.sc, df ? nullptr : S.z);
+}
+
+void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out, PcgPending* pend = nullptr) {
+  auto& S = h->s64;
+  enqueue_pcg_mp_start(h, tol, maxiter);
   const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
@@ -1084,18 +1121,20 @@ constexpr int EFF_TPR = 4;
 // the launches of one energy and gradient evaluation (m.(g + g_z) into red[R_E]): float-float in the
 // mixed-precision problems (MM_OPT_ENERGY_FF), else FP64
 void enqueue_energy(mm_problem* h, const double* d_m, const double* d_U, const double* B, const double* d_bias,
-                    double* d_g) {
+                    double* d_g, const double* d_B = nullptr) {
   if (h->use_energy_ff()) {
     const mmk::EnergySellFF& o = h->eopsff;
     mmk::k_split_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_m, d_U, o.kx, o.ky, o.kz, h->w_mff, h->w_sff,
                                                        h->w_uff);
     mmk::k_energy_grad_ff<EFF_TPR><<<grid_rows(o.n_rows, EFF_TPR), BS, 0, h->st>>>(
-        o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0], B[1], B[2], d_bias, h->inv_Vmag, d_g, h->d_sc, h->d_part);
+        o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0], B[1], B[2], d_B, d_bias, h->inv_Vmag, d_g, h->d_sc,
+        h->d_part);
     LAUNCH_CHECK();
     return;
   }
   mmk::k_energy_grad_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, d_m, d_U, h->d_Mn, B[0], B[1], B[2],
-                                                                     d_bias, h->inv_Vmag, d_g, h->d_sc, h->d_part);
+                                                                     d_B, d_bias, h->inv_Vmag, d_g, h->d_sc,
+                                                                     h->d_part);
   LAUNCH_CHECK();
 }
 
@@ -1487,6 +1526,323 @@ void accept_trial(mm_problem* h, double*& m, double*& U, double*& graw) {
   std::swap(graw, h->w_gt_trial);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Device-driven iterations of pcohen_hs, pcohen and pcg (MM_OPT_MIN_GRAPH).  One graph holds the
+// minimizer loop as a WHILE node; the inner preconditioner solve, the Armijo trials and each trial's
+// demag PCG are WHILE nodes nested in it, and every decision the host loop takes between kernels is
+// a k_min_* / k_ls_* kernel over MinScal.  A field step then waits on the host once.  The launches
+// and reductions are the host loop's (same grids), so the results are the same to the last bit.
+// ---------------------------------------------------------------------------------------------
+
+// WHILE (hnd) { body } appended to the graph that h->st is capturing.  The conditional node takes the
+// stream's current dependencies; its body is captured on the auxiliary stream of this nesting depth
+// (h->st is swapped for it meanwhile); the node then becomes the stream's only dependency.  The
+// first launch after the node is a plain one (a programmatic edge leaves only a kernel node).
+template <class Body>
+void capture_nested_while(mm_problem* h, cudaGraphConditionalHandle hnd, Body&& body) {
+  if (h->cap_depth >= 3) throw Fail{MM_ERR_STATE, "minimizer graph: loops nested too deeply"};
+  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t ndeps = 0;
+  CK(cudaStreamGetCaptureInfo(h->st, &status, nullptr, &g, &deps, &edges, &ndeps));
+  if (status != cudaStreamCaptureStatusActive) throw Fail{MM_ERR_STATE, "minimizer graph: no capture"};
+  std::vector<cudaGraphNode_t> dv(deps, deps + ndeps);
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hnd;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  CK(cudaGraphAddNode(&node, g, dv.empty() ? nullptr : dv.data(), nullptr, dv.size(), &cp));
+  cudaStream_t& aux = h->aux_st[h->cap_depth];
+  if (!aux) CK(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+  CK(cudaStreamBeginCaptureToGraph(aux, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  cudaStream_t saved = h->st;
+  h->st = aux;
+  ++h->cap_depth;
+  bool ok = true;
+  Fail err{MM_OK, ""};
+  try {
+    body();
+  } catch (const Fail& f) {
+    ok = false;
+    err = f;
+  }
+  h->st = saved;
+  --h->cap_depth;
+  cudaGraph_t out = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(aux, &out);
+  if (!ok) throw err;
+  CK(e);
+  CK(cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+}
+
+// The demag solve of a line-search trial: solve_dev's work, kernels only, with the PCG loop (FP64 or
+// FP32-preconditioned) as a nested WHILE node; its iterations go to MinScal.
+void enqueue_demag_nested(mm_problem* h, const double* m, double* U, double tol, int maxiter,
+                          cudaGraphConditionalHandle hnd, mmk::MinScal* ms, int64_t* per_trip) {
+  const int N = h->N;
+  mmk::k_copy_vec<<<grid_vec(N), BS, 0, h->st>>>(N, U, h->d_x);
+  LAUNCH_CHECK();
+  if (!h->has_mask) {
+    mmk::k_zero_vec<<<grid_vec(N), BS, 0, h->st>>>(N, h->d_b);
+    LAUNCH_CHECK();
+  }
+  mmk::k_rhs_s<<<grid_elem(h->eops.n_rows), BS, 0, h->st>>>(h->eops, m, h->d_b);
+  LAUNCH_CHECK();
+  dot(h, N, h->d_b, nullptr, R_BB0);
+  if (!h->has_mask) {
+    sub_mean(h, h->d_b);
+    sub_mean(h, h->d_x);
+  }
+  auto& S = h->s64;
+  const bool mp = h->fp32_precond && h->s32.built && multilevel(h, h->s32);
+  if (mp) enqueue_pcg_mp_start(h, tol, maxiter);
+  else enqueue_pcg_start<double>(h, S, tol, maxiter);
+  mmk::k_cond_set<<<1, 32, 0, h->st>>>(hnd, 1u);  // the loop graph's default: one trip at least
+  LAUNCH_CHECK();
+  capture_nested_while(h, hnd, [&] {
+    const int64_t b0 = h->n_launch;
+    if (mp) enqueue_iteration_mp(h);
+    else enqueue_iteration<double>(h, S);
+    launch(h, mmk::k_set_cond, 1, 32, hnd, S.sc);
+    *per_trip = h->n_launch - b0 + 1;
+  });
+  if (!h->has_mask) sub_mean(h, h->d_x);
+  mmk::k_copy_vec<<<grid_vec(N), BS, 0, h->st>>>(N, h->d_x, U);
+  LAUNCH_CHECK();
+  mmk::k_min_demag<<<1, 32, 0, h->st>>>(S.sc, ms);
+  LAUNCH_CHECK();
+}
+
+// The inner preconditioner solve P y = g_tan_ext (solve_Py_g) with its forcing tolerance, clipping
+// and fallback formed on the device.
+template <class Op, class T>
+void enqueue_inner_nested(mm_problem* h, const Op& op, const double* m, const double* gext, const double* gte,
+                          double reg, T inv_Vmag, T* r, T* z, T* p, T* Ap, T* y, cudaGraphConditionalHandle hnd,
+                          mmk::MinScal* ms, int64_t* per_trip) {
+  const int N = h->N;
+  mmk::k_min_in_setup<<<1, 32, 0, h->st>>>(h->d_sc, ms);
+  LAUNCH_CHECK();
+  launch(h, mmk::k_in_init<T>, grid_vec(N), BS, N, gte, h->d_inv_M_prec, r, z, p, y, h->d_sc, h->d_part);
+  LAUNCH_CHECK();
+  mmk::k_cond_set<<<1, 32, 0, h->st>>>(hnd, 1u);
+  LAUNCH_CHECK();
+  const T reg_t = (T)reg;
+  capture_nested_while(h, hnd, [&] {
+    enqueue_inner_trip<Op, T>(h, op, m, gext, reg_t, inv_Vmag, r, z, p, Ap, y);
+    launch(h, mmk::k_in_cond, 1, 32, hnd, h->d_sc);
+  });
+  *per_trip = 4;
+}
+
+// Runs the iterations of pcohen_hs / pcohen / pcg from the state minimize_dev has set up (it = 0)
+// through the cached graph of these buffers and settings.  Returns false, with nothing queued, when
+// no graph can be built (the caller then runs its host loop).
+uint64_t bits_of(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, sizeof(b));
+  return b;
+}
+
+bool minimize_graph(mm_problem* h, MinCtx& c, double* m, double* U, double E0, bool cpp, int* it_out,
+                    double* E_out, double* gnorm_out, bool* conv_out) {
+  const mm_min_params* prm = c.prm;
+  const int N = h->N, n3 = 3 * N;
+  const int meth = prm->method;
+  const bool pr = meth == MM_METHOD_PCOHEN;
+  const int proj = meth == MM_METHOD_PCG ? 0 : 1;
+  const int cg_maxiter = prm->cg_maxiter > 0 ? prm->cg_maxiter : 2000;
+  const bool mixed_solve = h->mixed && h->s32.built;  // FP64 refinement steps decided on the host
+  if (!h->min_graph || h->min_graph_failed || !h->use_graph || h->prof || mixed_solve || prm->max_iter <= 0)
+    return false;
+  // lazily built operators first: nothing may allocate while the stream captures
+  const bool fp32 = h->inner_fp32();
+  const bool ff = h->use_energy_ff();
+  const bool mp = h->fp32_precond && h->s32.built && multilevel(h, h->s32);
+  if (mp) h->use_a0df();
+  if (!h->d_ms) {
+    h->d_ms = h->alloc<mmk::MinScal>(1);
+    CK(cudaMallocHost(&h->h_ms, sizeof(mmk::MinScal)));
+  }
+  double* graw = h->w_graw;
+  const std::vector<uintptr_t> key = {
+      (uintptr_t)m, (uintptr_t)U, (uintptr_t)graw, (uintptr_t)h->w_gte, (uintptr_t)h->w_gprev,
+      (uintptr_t)h->w_y, (uintptr_t)h->w_ys, (uintptr_t)h->w_d, (uintptr_t)h->w_dprev, (uintptr_t)h->w_mt,
+      (uintptr_t)h->w_Ut, (uintptr_t)h->w_gt_trial, (uintptr_t)h->d_min_bias, (uintptr_t)pr, (uintptr_t)proj,
+      (uintptr_t)fp32, (uintptr_t)ff, (uintptr_t)mp, (uintptr_t)h->pdl, (uintptr_t)h->s64.epoch,
+      (uintptr_t)h->s32.epoch, (uintptr_t)cg_maxiter, (uintptr_t)bits_of(c.phi_tol), (uintptr_t)bits_of(prm->pc_reg)};
+  mm_problem::MinGraph* mg = nullptr;
+  for (auto& x : h->min_graphs)
+    if (x.key == key) mg = &x;
+  if (!mg) {
+    mm_problem::MinGraph ng{key, nullptr, nullptr, 0, 0, 0, 0};
+    bool ok = cudaGraphCreate(&ng.g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle hnd[4];  // outer loop, inner solve, line search, demag PCG
+    for (int i = 0; i < 4 && ok; ++i) ok = cudaGraphConditionalHandleCreate(&hnd[i], ng.g, 0, 0) == cudaSuccess;
+    const int64_t saved = h->n_launch;
+    if (ok) ok = cudaStreamBeginCaptureToGraph(h->st, ng.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess;
+    if (ok) {
+      mmk::MinScal* ms = h->d_ms;
+      mmk::Scalars* sc = h->d_sc;
+      double* part = h->d_part;
+      const int ge = grid_vec(N), g3 = grid_vec(n3);
+      const int gdot = std::min(grid_ilp(n3), g_vec_cap);
+      try {
+        mmk::k_min_start<<<1, 32, 0, h->st>>>(hnd[0], ms);
+        LAUNCH_CHECK();
+        capture_nested_while(h, hnd[0], [&] {
+          const int64_t o0 = h->n_launch;
+          int64_t ls_body = 0;
+          mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, sc, part);
+          LAUNCH_CHECK();
+          // y = P^-1 g_tan_ext with clipping and the z_fb fallback (solve_Py_g)
+          if (fp32) {
+            enqueue_inner_nested<mmk::EnergySell32, float>(h, h->eops32, m, graw, h->w_gte, prm->pc_reg, 1.0f,
+                                                           h->w_r3f, h->w_z3f, h->w_p3f, h->w_Ap3f, h->w_yf, hnd[1],
+                                                           ms, &ng.per_in);
+            mmk::k_fallback_dots32<<<ge, BS, 0, h->st>>>(N, h->w_yf, h->w_gte, h->d_inv_M_prec, h->w_z3, sc, part);
+          } else {
+            enqueue_inner_nested<mmk::EnergySell, double>(h, h->eops, m, graw, h->w_gte, prm->pc_reg, h->inv_Vmag,
+                                                          h->w_r3, h->w_z3, h->w_p3, h->w_Ap3, h->w_y, hnd[1], ms,
+                                                          &ng.per_in);
+            mmk::k_fallback_dots<<<ge, BS, 0, h->st>>>(N, h->w_y, h->w_gte, h->d_inv_M_prec, h->w_z3, sc, part);
+          }
+          LAUNCH_CHECK();
+          mmk::k_min_clip<<<1, 32, 0, h->st>>>(sc, ms);
+          LAUNCH_CHECK();
+          if (fp32) mmk::k_widen_clip<<<g3, BS, 0, h->st>>>(n3, h->w_yf, ms, h->w_y);
+          else mmk::k_scale_clip<<<g3, BS, 0, h->st>>>(n3, h->w_y, ms);
+          LAUNCH_CHECK();
+          mmk::k_dot_flag<<<gdot, BS, 0, h->st>>>(&ms->flag, n3, h->w_y, h->w_gte, sc, part, R_A);
+          LAUNCH_CHECK();
+          mmk::k_min_fallback<<<1, 32, 0, h->st>>>(sc, ms);
+          LAUNCH_CHECK();
+          mmk::k_copy_flag<<<g3, BS, 0, h->st>>>(&ms->flag2, n3, h->w_z3, h->w_y);
+          LAUNCH_CHECK();
+          // beta (HS, or PR over y_prev.g_prev), direction with the descent safeguard, g_raw.d
+          mmk::k_absmax<<<grid_vec(n3), BS, 0, h->st>>>(n3, h->w_y, sc, part);
+          LAUNCH_CHECK();
+          mmk::k_dot2diff<<<g3, BS, 0, h->st>>>(n3, h->w_y, h->w_dprev, h->w_gte, h->w_gprev, sc, part);
+          LAUNCH_CHECK();
+          if (pr) dot(h, n3, h->w_ys, h->w_gprev, R_C);
+          mmk::k_min_beta<<<1, 32, 0, h->st>>>(sc, ms);
+          LAUNCH_CHECK();
+          mmk::k_direction_ms<<<ge, BS, 0, h->st>>>(N, m, h->w_y, h->w_dprev, ms, h->w_gte, graw, h->w_d, sc, part,
+                                                   proj);
+          LAUNCH_CHECK();
+          mmk::k_min_descent<<<1, 32, 0, h->st>>>(sc, ms);
+          LAUNCH_CHECK();
+          mmk::k_neg_flag<<<g3, BS, 0, h->st>>>(&ms->flag, n3, h->w_y, h->w_d);
+          LAUNCH_CHECK();
+          mmk::k_dot_flag<<<gdot, BS, 0, h->st>>>(&ms->flag, n3, graw, h->w_d, sc, part, R_A);
+          LAUNCH_CHECK();
+          mmk::k_min_pg<<<1, 32, 0, h->st>>>(sc, ms);
+          LAUNCH_CHECK();
+          mmk::k_cross<<<ge, BS, 0, h->st>>>(N, m, h->w_d, h->w_H);
+          LAUNCH_CHECK();
+          // curvilinear Armijo search: each trial R(m, H, s), its demag solve (warm-started from the
+          // previous trial's potential) and its energy
+          mmk::k_copy_vec<<<grid_vec(N), BS, 0, h->st>>>(N, U, h->w_Ut);
+          LAUNCH_CHECK();
+          mmk::k_ls_init<<<1, 32, 0, h->st>>>(hnd[2], ms);
+          LAUNCH_CHECK();
+          capture_nested_while(h, hnd[2], [&] {
+            const int64_t l0 = h->n_launch;
+            int64_t pcg_trip = 0;
+            mmk::k_cayley_ms<<<grid_vec(N), BS, 0, h->st>>>(N, m, h->w_H, ms, h->w_mt);
+            LAUNCH_CHECK();
+            enqueue_demag_nested(h, h->w_mt, h->w_Ut, c.phi_tol, cg_maxiter, hnd[3], ms, &pcg_trip);
+            enqueue_energy(h, h->w_mt, h->w_Ut, c.B, h->d_min_bias, h->w_gt_trial, &ms->B[0]);
+            mmk::k_ls_decide<<<1, 32, 0, h->st>>>(hnd[2], sc, ms, h->inv_Vmag);
+            LAUNCH_CHECK();
+            // the kernels of the PCG loop body are counted from the loop's trips, not per trial
+            ls_body = h->n_launch - l0;
+            ng.per_pcg = pcg_trip;
+            ng.per_ls = ls_body - (pcg_trip - 1);
+          });
+          mmk::k_ls_finish<<<1, 32, 0, h->st>>>(ms);
+          LAUNCH_CHECK();
+          mmk::k_absmaxdiff<<<g3, BS, 0, h->st>>>(n3, h->w_mt, m, sc, part);
+          LAUNCH_CHECK();
+          mmk::k_min_advance<<<g3, BS, 0, h->st>>>(n3, N, ms, m, h->w_mt, U, h->w_Ut, graw,
+                                                  h->w_gt_trial, h->w_gprev, h->w_gte, h->w_dprev, h->w_d,
+                                                  pr ? h->w_ys : nullptr, h->w_y);
+          LAUNCH_CHECK();
+          mmk::k_min_conv<<<1, 32, 0, h->st>>>(hnd[0], sc, ms);
+          LAUNCH_CHECK();
+          ng.per_outer = (h->n_launch - o0) - ls_body;
+        });
+      } catch (const Fail&) {
+        ok = false;
+      }
+      cudaGraph_t out = nullptr;
+      const bool end_ok = cudaStreamEndCapture(h->st, &out) == cudaSuccess;
+      ok = ok && end_ok;
+    }
+    h->n_launch = saved;
+    if (ok) ok = cudaGraphInstantiate(&ng.ex, ng.g, 0) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();  // clear the failed attempt's error; the host loop runs instead
+      if (ng.ex) cudaGraphExecDestroy(ng.ex);
+      if (ng.g) cudaGraphDestroy(ng.g);
+      h->min_graph_failed = true;
+      return false;
+    }
+    if (h->min_graphs.size() >= 4) {
+      CK(cudaStreamSynchronize(h->st));
+      cudaGraphExecDestroy(h->min_graphs.front().ex);
+      cudaGraphDestroy(h->min_graphs.front().g);
+      h->min_graphs.erase(h->min_graphs.begin());
+    }
+    h->min_graphs.push_back(ng);
+    mg = &h->min_graphs.back();
+  }
+  // this call's parameters and starting scalars
+  mmk::MinScal& s = *h->h_ms;
+  s = mmk::MinScal{};
+  s.max_iter = prm->max_iter;
+  s.L = prm->L > 0 ? prm->L : N;
+  s.pr = pr ? 1 : 0;
+  s.pc_auto = prm->pc_auto;
+  s.pc_iters = prm->pc_iters;
+  s.max_evals = prm->ls_max_evals > 0 ? prm->ls_max_evals : 15;
+  s.cpp = cpp ? 1 : 0;
+  s.pc_force_eta = prm->pc_force_eta;
+  s.pc_force_alpha = prm->pc_force_alpha;
+  s.pc_nu = prm->pc_stagnation_nu;
+  s.eta1 = prm->ls_eta1;
+  s.eta2 = prm->ls_eta2;
+  s.C = prm->ls_C;
+  s.c = prm->ls_c;
+  s.s0 = 1.0;
+  s.tau_f = prm->tau_f;
+  s.eps_a = prm->eps_a;
+  s.u2_bound = std::sqrt(prm->tau_f) * 2.0;
+  s.u3_root = std::pow(prm->tau_f, 1.0 / 3.0);
+  for (int k = 0; k < 3; ++k) s.B[k] = c.B[k];
+  s.E = E0;
+  s.E_lag = E0;
+  CK(cudaMemcpyAsync(h->d_ms, h->h_ms, sizeof(mmk::MinScal), cudaMemcpyHostToDevice, h->st));
+  CK(cudaGraphLaunch(mg->ex, h->st));
+  CK(cudaMemcpyAsync(h->h_ms, h->d_ms, sizeof(mmk::MinScal), cudaMemcpyDeviceToHost, h->st));
+  h->sync();
+  c.evals += (int)s.evals;
+  c.preco += (int)s.preco;
+  c.demag += (int)s.demag;
+  h->n_launch += 1 + (int64_t)s.outer_loops * mg->per_outer + s.evals * mg->per_ls + s.pcg_trips * mg->per_pcg +
+                 s.in_trips * mg->per_in;
+  *it_out = s.it;
+  *E_out = s.E;
+  *gnorm_out = s.gsm;
+  *conv_out = s.conv != 0;
+  return true;
+}
+
 int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const mm_min_params* prm,
                  mm_min_info* info) {
   const int N = h->N, n3 = 3 * N;
@@ -1693,7 +2049,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     c.preco += solve_Py_g(c, m, graw, h->w_gte, pc_tol_of(gnorm), h->w_ys, prm->pc_reg);
     neg3(h->w_dprev, h->w_ys);
   }
-  while (!conv && it < prm->max_iter) {
+  // pcohen_hs / pcohen / pcg: the iterations as one device graph where it can be built
+  const bool on_device = cg_family && minimize_graph(h, c, m, U, E, cpp, &it, &E, &gnorm, &conv);
+  while (!on_device && !conv && it < prm->max_iter) {
     const double E_prev = E;
     mmk::k_tangent2<<<ge, BS, 0, h->st>>>(N, m, graw, h->d_inv_M_rel, h->w_gt, h->w_gte, h->d_sc, h->d_part);
     LAUNCH_CHECK();
@@ -2025,6 +2383,7 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
     info->status = (it >= prm->max_iter && !conv) ? MM_MAXITER : MM_OK;
     info->demag_seconds = 1e-3 * c.demag_ms;
     info->demag_wall_seconds = c.demag_wall;
+    info->device_loop = on_device ? 1 : 0;
   }
   return std::isfinite(E) ? MM_OK : MM_NONFINITE;
 }
@@ -2585,8 +2944,11 @@ int mm_destroy(mm_problem* h) {
   if (h->s32.exec) cudaGraphExecDestroy(h->s32.exec);
   if (h->s32.graph) cudaGraphDestroy(h->s32.graph);
   h->drop_inner_graphs();
+  for (cudaStream_t a : h->aux_st)
+    if (a) cudaStreamDestroy(a);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_sc) cudaFreeHost(h->h_sc);
+  if (h->h_ms) cudaFreeHost(h->h_ms);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_after) cudaEventDestroy(h->ev_after);
@@ -3209,6 +3571,12 @@ int mm_set_option(mm_problem* h, int option, int value) {
       drop_graph(h->s32);
     }
     h->fuse_restrict = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_MIN_GRAPH) {
+    if (value != 0 && value != 1) return MM_ERR_ARG;
+    h->min_graph = value;
+    h->min_graph_failed = false;
     return MM_OK;
   }
   if (option == MM_OPT_MIXED_ETA_E6) {

@@ -1155,9 +1155,14 @@ __device__ __forceinline__ void exch_aniso_sell(const EnergySell& op, int r, con
 // g = (K m + G U + g_z) / V_mag on the magnetic rows; m.(g_quad + 2 g_z) -> red[R_E]
 __global__ void __launch_bounds__(BS) k_energy_grad_s(EnergySell op, const double* __restrict__ m,
                                                       const double* __restrict__ U, const double* __restrict__ Mn,
-                                                      double Bx, double By, double Bz,
+                                                      double Bx, double By, double Bz, const double* __restrict__ Bd,
                                                       const double* __restrict__ Bbias, double inv_Vmag,
                                                       double* __restrict__ g, Scalars* sc, double* part) {
+  if (Bd) {  // the applied field from device memory (a graph replayed for several fields)
+    Bx = Bd[0];
+    By = Bd[1];
+    Bz = Bd[2];
+  }
   double en = 0.0;
   for (int r = blockIdx.x * BS + threadIdx.x; r < op.n_rows; r += gridDim.x * BS) {
     double ax, ay, az;
@@ -1317,10 +1322,15 @@ template <int TPR>
 __global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const float2* __restrict__ mff,
                                                        const float2* __restrict__ sff, const float2* __restrict__ uff,
                                                        const double* __restrict__ m, const double* __restrict__ Mn,
-                                                       double Bx, double By, double Bz,
+                                                       double Bx, double By, double Bz, const double* __restrict__ Bd,
                                                        const double* __restrict__ Bbias, double inv_Vmag,
                                                        double* __restrict__ g, Scalars* sc, double* part) {
   static_assert(TPR >= 1 && TPR <= 32 && (TPR & (TPR - 1)) == 0, "TPR: a power of two up to 32");
+  if (Bd) {
+    Bx = Bd[0];
+    By = Bd[1];
+    Bz = Bd[2];
+  }
   constexpr int RPB = BS / TPR;
   const int q = threadIdx.x % TPR;
   double en = 0.0;
@@ -1649,8 +1659,8 @@ __global__ void __launch_bounds__(BS) k_tangent(int N, const double* __restrict_
 }
 
 // Cayley update with renormalisation: out = cayley(m, H, tau)
-__global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__ m, const double* __restrict__ H,
-                                               double tau, double* __restrict__ out) {
+__device__ __forceinline__ void cayley_rows(int N, const double* __restrict__ m, const double* __restrict__ H,
+                                            double tau, double* __restrict__ out) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double k0 = 0.5 * tau * H[3 * i], k1 = 0.5 * tau * H[3 * i + 1], k2 = 0.5 * tau * H[3 * i + 2];
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
@@ -1668,6 +1678,11 @@ __global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__
     out[3 * i + 1] = n1 * inr;
     out[3 * i + 2] = n2 * inr;
   }
+}
+
+__global__ void __launch_bounds__(BS) k_cayley(int N, const double* __restrict__ m, const double* __restrict__ H,
+                                               double tau, double* __restrict__ out) {
+  cayley_rows(N, m, H, tau, out);
 }
 
 // m <- m / |m|
@@ -1778,10 +1793,10 @@ __global__ void __launch_bounds__(BS) k_dot2diff(int n, const double* __restrict
 }
 
 // d = -y + beta * P_m(d_prev) (d_prev itself when proj == 0); d.gte -> red[R_A]; g_raw.d -> red[R_B]
-__global__ void __launch_bounds__(BS) k_direction(int N, const double* __restrict__ m, const double* __restrict__ y,
-                                                  const double* __restrict__ dprev, double beta,
-                                                  const double* __restrict__ gte, const double* __restrict__ graw,
-                                                  double* __restrict__ d, Scalars* sc, double* part, int proj) {
+__device__ __forceinline__ void direction_rows(int N, const double* __restrict__ m, const double* __restrict__ y,
+                                               const double* __restrict__ dprev, double beta,
+                                               const double* __restrict__ gte, const double* __restrict__ graw,
+                                               double* __restrict__ d, Scalars* sc, double* part, int proj) {
   double s1 = 0.0, s2 = 0.0;
   for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
     const double m0 = m[3 * i], m1 = m[3 * i + 1], m2 = m[3 * i + 2];
@@ -1795,6 +1810,13 @@ __global__ void __launch_bounds__(BS) k_direction(int N, const double* __restric
     s2 += graw[3 * i] * d0 + graw[3 * i + 1] * d1 + graw[3 * i + 2] * d2;
   }
   grid_reduce(s1, s2, sc, part, R_A, R_B);
+}
+
+__global__ void __launch_bounds__(BS) k_direction(int N, const double* __restrict__ m, const double* __restrict__ y,
+                                                  const double* __restrict__ dprev, double beta,
+                                                  const double* __restrict__ gte, const double* __restrict__ graw,
+                                                  double* __restrict__ d, Scalars* sc, double* part, int proj) {
+  direction_rows(N, m, y, dprev, beta, gte, graw, d, sc, part, proj);
 }
 
 // H = m x d
@@ -1907,6 +1929,290 @@ __global__ void __launch_bounds__(BS) k_fallback_dots(int N, const double* __res
   }
   grid_reduce(yy, zz, sc, part, R_A, R_B);
   grid_reduce(yg, 0.0, sc, part, R_C);
+}
+
+// ------------------------------------------------------------------------------------------
+// The preconditioned CG minimizers (pcohen_hs, pcohen, pcg) iterated on the device: every decision
+// the host loop takes between kernels (the inner solve's forcing tolerance, clipping and fallback,
+// beta, the descent test, the Armijo search's expansion and contraction, the U1-U4 test) restated as
+// single-thread kernels over MinScal, so that one CUDA graph with WHILE nodes runs whole iterations:
+// the inner preconditioner solve and the line-search trials (each with its demag PCG) are nested
+// loops.  Same formulas and the same reduction kernels as the host loop.
+// ------------------------------------------------------------------------------------------
+struct MinScal {
+  // parameters of the call
+  int max_iter, L, pr, pc_auto, pc_iters, max_evals, cpp;
+  double pc_force_eta, pc_force_alpha, pc_nu, eta1, eta2, C, c, s0;
+  double tau_f, eps_a, u2_bound, u3_root;  // sqrt(tau_f) 2 and tau_f^(1/3), formed on the host
+  double B[3];
+  // outer state
+  int it, conv, outer_loops, flag, flag2, accepted, phase, it_exp, it_con, ls_loops;
+  double E, E_new, E_lag, gsm, beta, pg, cf;
+  // line search
+  double s, s_min, d_v, E_v, E0;
+  // counters
+  long long evals, preco, demag;
+  long long in_trips, pcg_trips;  // WHILE trips of the inner solves and of the demag PCG loops
+};
+
+__device__ __forceinline__ bool lead_thread() { return threadIdx.x == 0 && blockIdx.x == 0; }
+
+// condition of a WHILE node entered next (a nested node takes no default value per entry)
+__global__ void k_cond_set(cudaGraphConditionalHandle hnd, unsigned value) {
+  if (lead_thread()) cudaGraphSetConditional(hnd, value);
+}
+
+__global__ void __launch_bounds__(BS) k_copy_vec(int n, const double* __restrict__ src, double* __restrict__ dst) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(BS) k_zero_vec(int n, double* __restrict__ dst) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) dst[i] = 0.0;
+}
+
+// the outer loop's first trip
+__global__ void k_min_start(cudaGraphConditionalHandle hnd, MinScal* ms) {
+  if (lead_thread()) {
+    ms->outer_loops = 0;
+    ms->conv = 0;
+    cudaGraphSetConditional(hnd, (ms->it < ms->max_iter) ? 1u : 0u);
+  }
+}
+
+// the inner solve's start (k_in_setup) with the forcing tolerance min(eta, max|g_tan|^alpha) formed
+// here from red[R_MAX] of k_tangent2
+__global__ void k_min_in_setup(Scalars* sc, MinScal* ms) {
+  if (lead_thread()) {
+    const double gn = sc->red[R_MAX];
+    const double tol = ms->pc_auto ? fmin(ms->pc_force_eta, pow(gn, ms->pc_force_alpha)) : 0.0;
+    sc->in_cpp = ms->cpp;
+    sc->in_max = ms->pc_iters;
+    sc->in_nu = ms->pc_nu;
+    sc->in_tol2 = tol * tol;
+    sc->in_it = 0;
+    sc->in_Q = 0.0;
+    sc->in_stop = 0;
+    sc->in_done = 0;
+    sc->in_loops = 0;
+    sc->red[R_D] = 0.0;
+  }
+}
+
+// the inner solve's end: clipping factor from |y|^2 and |z_fb|^2 (red[R_A], red[R_B]); its
+// iteration count (red[R_D]) into preco
+__global__ void k_min_clip(Scalars* sc, MinScal* ms) {
+  if (lead_thread()) {
+    const double yn = sqrt(sc->red[R_A]), zn = sqrt(sc->red[R_B]);
+    const int clip = yn > 10.0 * zn;
+    ms->flag = clip;
+    ms->cf = clip ? 10.0 * zn / (yn + 1e-30) : 1.0;
+    ms->preco += (long long)sc->red[R_D];
+    ms->in_trips += sc->in_loops;
+  }
+}
+
+// y *= cf when clipping (FP64 inner solve)
+__global__ void __launch_bounds__(BS) k_scale_clip(int n, double* __restrict__ y, const MinScal* ms) {
+  if (!ms->flag) return;
+  const double a = ms->cf;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * y[i];
+}
+
+// y = cf * fl64(yf) (FP32 inner solve; cf = 1 without clipping)
+__global__ void __launch_bounds__(BS) k_widen_clip(int n, const float* __restrict__ yf, const MinScal* ms,
+                                                   double* __restrict__ y) {
+  const double a = ms->cf;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * (double)yf[i];
+}
+
+// k_dot when *flag (the same reduction; nothing, not even the slot, is touched otherwise)
+__global__ void __launch_bounds__(BS) k_dot_flag(const int* flag, int n, const double* __restrict__ x,
+                                                 const double* __restrict__ y, Scalars* sc, double* part, int slot) {
+  if (!*flag) return;
+  Acc<double> acc;
+  ROW_LOOP(n) {
+    int row[ILP];
+    rows_of(rb, row);
+#pragma unroll
+    for (int q = 0; q < ILP; ++q)
+      if (row[q] < n) acc.add(x[row[q]], y[row[q]]);
+  }
+  grid_finish(block_total(acc), 0.0, sc, part, slot, -1, POST_NONE);
+}
+
+// not a descent direction (y.g_tan_ext at most 1e-12: red[R_C] of the inner solve's end, or red[R_A]
+// recomputed after clipping): fall back to z_fb
+__global__ void k_min_fallback(Scalars* sc, MinScal* ms) {
+  if (lead_thread()) ms->flag2 = !((ms->flag ? sc->red[R_A] : sc->red[R_C]) > 1e-12);
+}
+
+// dst = src when *flag
+__global__ void __launch_bounds__(BS) k_copy_flag(const int* flag, int n, const double* __restrict__ src,
+                                                  double* __restrict__ dst) {
+  if (!*flag) return;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) dst[i] = src[i];
+}
+
+// beta: Hestenes-Stiefel y.(g - g_prev) / (d_prev.(g - g_prev) + 1e-30) (red[R_A], red[R_B]) or
+// Polak-Ribiere over y_prev.g_prev (red[R_C]); 0 on restarts; max|y| (red[R_MAX]) kept for the test
+__global__ void k_min_beta(Scalars* sc, MinScal* ms) {
+  if (lead_thread()) {
+    ms->gsm = sc->red[R_MAX];
+    const double num = sc->red[R_A];
+    const double den = (ms->pr ? sc->red[R_C] : sc->red[R_B]) + 1e-30;
+    ms->beta = (ms->it % ms->L == 0) ? 0.0 : fmax(0.0, num / den);
+  }
+}
+
+// k_direction with beta from MinScal
+__global__ void __launch_bounds__(BS) k_direction_ms(int N, const double* __restrict__ m, const double* __restrict__ y,
+                                                     const double* __restrict__ dprev, const MinScal* ms,
+                                                     const double* __restrict__ gte, const double* __restrict__ graw,
+                                                     double* __restrict__ d, Scalars* sc, double* part, int proj) {
+  direction_rows(N, m, y, dprev, ms->beta, gte, graw, d, sc, part, proj);
+}
+
+// d.g_tan_ext > 0 (red[R_A]): d must become -y; g_raw.d from red[R_B]
+__global__ void k_min_descent(Scalars* sc, MinScal* ms) {
+  if (lead_thread()) {
+    ms->flag = sc->red[R_A] > 0.0;
+    ms->pg = sc->red[R_B];
+  }
+}
+
+// d = -1 y + 0 d when *flag (the host loop's k_axpby form)
+__global__ void __launch_bounds__(BS) k_neg_flag(const int* flag, int n, const double* __restrict__ y,
+                                                 double* __restrict__ d) {
+  if (!*flag) return;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) d[i] = -1.0 * y[i] + 0.0 * d[i];
+}
+
+// g_raw.d recomputed after the descent fix (red[R_A] of k_dot_flag)
+__global__ void k_min_pg(Scalars* sc, MinScal* ms) {
+  if (lead_thread() && ms->flag) ms->pg = sc->red[R_A];
+}
+
+// Armijo search start (src/minimizers.py:265-385): no search when g_raw.d >= 0
+__global__ void k_ls_init(cudaGraphConditionalHandle hnd, MinScal* ms) {
+  if (lead_thread()) {
+    ms->E0 = ms->E;
+    ms->s = ms->s0;
+    ms->s_min = 0.0;
+    ms->it_exp = ms->it_con = 0;
+    ms->d_v = 0.0;
+    ms->E_v = ms->E;
+    ms->ls_loops = 0;
+    ms->accepted = 0;
+    ms->phase = (ms->pg >= 0.0) ? 2 : 0;  // 0 expansion, 1 contraction, 2 done
+    cudaGraphSetConditional(hnd, ms->phase != 2 ? 1u : 0u);
+  }
+}
+
+// Cayley update with the trial step from MinScal
+__global__ void __launch_bounds__(BS) k_cayley_ms(int N, const double* __restrict__ m, const double* __restrict__ H,
+                                                  const MinScal* ms, double* __restrict__ out) {
+  cayley_rows(N, m, H, ms->s, out);
+}
+
+// the demag PCG iterations of a trial (sc->it) into the counter
+__global__ void k_min_demag(const Scalars* sc, MinScal* ms) {
+  if (lead_thread()) {
+    ms->demag += sc->it;
+    ms->pcg_trips += sc->loops;
+  }
+}
+
+// one trial's test d = (E_t - E0) / (s pg + 1e-30) and the next step: expansion while
+// |1 - d| < eta2 and d >= 0 (s_min = s, s *= C), then contraction s = s_min + c (s - s_min) until
+// d >= eta1 and d < 1e10; at most max_evals trials each; the loop is bounded besides by its trips
+__global__ void k_ls_decide(cudaGraphConditionalHandle hnd, const Scalars* sc, MinScal* ms, double inv_Vmag) {
+  if (!lead_thread()) return;
+  double E_t = 0.5 * sc->red[R_E] * inv_Vmag;
+  if (!isfinite(E_t)) E_t = 1e20;
+  const double d = (E_t - ms->E0) / (ms->s * ms->pg + 1e-30);
+  ms->d_v = d;
+  ms->E_v = E_t;
+  ms->ls_loops += 1;
+  if (ms->phase == 0) {
+    const bool stop = (fabs(1.0 - d) >= ms->eta2) || (d < 0.0);
+    if (!stop) {
+      ms->s_min = ms->s;
+      ms->s = ms->C * ms->s;
+    }
+    ms->it_exp += 1;
+    if (stop || ms->it_exp >= ms->max_evals) {
+      const bool ok = (d >= ms->eta1) && (d < 1e10);
+      if (ok) {
+        ms->phase = 2;
+      } else {
+        ms->phase = 1;
+        ms->s = ms->s_min + ms->c * (ms->s - ms->s_min);
+      }
+    }
+  } else if (ms->phase == 1) {
+    ms->it_con += 1;
+    const bool ok = (d >= ms->eta1) && (d < 1e10);
+    if (ok || ms->it_con >= ms->max_evals) ms->phase = 2;
+    else ms->s = ms->s_min + ms->c * (ms->s - ms->s_min);
+  }
+  const bool more = ms->phase != 2 && ms->ls_loops <= 2 * ms->max_evals + 2;
+  cudaGraphSetConditional(hnd, more ? 1u : 0u);
+}
+
+// the search's result: the last trial is kept when its d >= 0
+__global__ void k_ls_finish(MinScal* ms) {
+  if (lead_thread()) {
+    const int trials = ms->it_exp + ms->it_con;
+    ms->evals += trials;
+    ms->accepted = (ms->pg < 0.0 && trials > 0 && ms->d_v >= 0.0) ? 1 : 0;
+    ms->E_new = ms->accepted ? ms->E_v : ms->E;
+  }
+}
+
+// Gill-Murray-Wright U1-U4 on the accepted step (max|m_new - m| in red[R_MAX]) and the next trip's
+// condition (src/minimizers.py:160-172)
+__global__ void k_min_conv(cudaGraphConditionalHandle hnd, const Scalars* sc, MinScal* ms) {
+  if (!lead_thread()) return;
+  const double dm = ms->accepted ? sc->red[R_MAX] : 0.0;
+  const double E_new = ms->E_new, E_prev = ms->E;
+  const double E_ref = ms->cpp ? ms->E_lag : E_prev;  // the C++ minimizer tests against the lagged energy
+  bool conv = false;
+  if (ms->it > 0) {
+    const bool u1 = (E_ref - E_new) < ms->tau_f * (1.0 + fabs(E_new));
+    const bool u2 = dm < ms->u2_bound;
+    const bool u3 = ms->gsm <= ms->u3_root * (1.0 + fabs(E_new));
+    const bool u4 = ms->gsm < ms->eps_a;
+    conv = (u1 && u2 && u3) || u4;
+  }
+  ms->conv = conv ? 1 : 0;
+  ms->E_lag = E_prev;
+  ms->E = E_new;
+  ms->it += 1;
+  ms->outer_loops += 1;
+  const bool more = !conv && ms->it < ms->max_iter && ms->outer_loops <= ms->max_iter + 2;
+  cudaGraphSetConditional(hnd, more ? 1u : 0u);
+}
+
+// accepted step: m, U, g_raw <- the trial's; then g_prev <- g_tan_ext, d_prev <- d (y_prev <- y
+// when ys != nullptr), the copies that stand for the host loop's buffer swaps
+__global__ void __launch_bounds__(BS) k_min_advance(int n3, int N, const MinScal* ms, double* __restrict__ m,
+                                                    const double* __restrict__ mt, double* __restrict__ U,
+                                                    const double* __restrict__ Ut, double* __restrict__ graw,
+                                                    const double* __restrict__ gt, double* __restrict__ gprev,
+                                                    const double* __restrict__ gte, double* __restrict__ dprev,
+                                                    const double* __restrict__ d, double* __restrict__ ys,
+                                                    const double* __restrict__ y) {
+  const bool acc = ms->accepted != 0;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n3; i += gridDim.x * BS) {
+    if (acc) {
+      m[i] = mt[i];
+      graw[i] = gt[i];
+      if (i < N) U[i] = Ut[i];
+    }
+    gprev[i] = gte[i];
+    dprev[i] = d[i];
+    if (ys) ys[i] = y[i];
+  }
 }
 
 }  // namespace mmk

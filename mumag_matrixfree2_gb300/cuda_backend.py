@@ -290,7 +290,7 @@ class Problem:
         return m, U, dict(iters=info.iters, evals=info.evals, preco_iters=info.preco_iters,
                           demag_iters=info.demag_iters, E=info.E, gnorm=info.gnorm, time=info.seconds,
                           status=info.status, demag_time=info.demag_seconds,
-                          demag_wall_time=info.demag_wall_seconds)
+                          demag_wall_time=info.demag_wall_seconds, device_loop=bool(info.device_loop))
 
     def time_kernel(self, kernel: str, reps: int = 20):
         """(mean ms per launch with L2 flushed before each, algorithmic bytes per launch)."""
@@ -302,7 +302,8 @@ class Problem:
     def set_option(self, name: str, value: int):
         opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5, "pdl": 8,
                 "coarse_fuse": 9, "min_fp32": 10,
-                "split_a0": 11, "fuse_restrict": 12, "energy_ff": 13}
+                "split_a0": 11, "fuse_restrict": 12, "energy_ff": 13,
+                "min_graph": 14}
         self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
 
     def autotune(self, reps: int = 20) -> dict:

@@ -148,12 +148,15 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
                         node_volumes, M_nodal, B_bias=None, precond_type: str = "amgcl", order: int = 3,
                         energy_assembly: str = "segment_sum", grad_backend: str = "stored_grad_phi",
                         chunk_elems: int = 200_000, boundary_mask=None, *, mode: str = "assembled",
-                        precision: str = "fp64", write_files: bool = True, **_unused) -> dict[str, Any]:
+                        precision: str = "fp64", write_files: bool = True, device_loop: bool = True,
+                        **_unused) -> dict[str, Any]:
     """Sweep the applied field and minimise at every value (``src/hysteresis_loop.py:226-657``).
 
     Returns {"out_dir", "csv_path", "last_m", "last_U", "history", "steps"} where history rows are
     (B_ext [T], J_par [T], mx, my, mz, E [J/m^3]) as in the reference and steps holds per-step
-    (iters, evals, preco_iters, demag_iters, seconds).
+    (iters, evals, preco_iters, demag_iters, seconds).  ``device_loop`` (an addition) runs the CG
+    minimizers' iterations as one device graph per field step (MM_OPT_MIN_GRAPH); False keeps the
+    host-driven loop.
     """
     out_dir = Path(params.out_dir)
     csv_path = out_dir / params.csv_name
@@ -166,6 +169,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     # one device problem for the solver and the minimizer: the energy operator and the hierarchy are
     # built once (make_minimizer finds this problem in the geometry's cache)
     prob = problem_for_geom(geom, A_lookup, K1_lookup, Js_lookup, k_easy_lookup, V_mag, M_nodal, boundary_mask)
+    prob.set_option("min_graph", int(bool(device_loop)))
     solve_U = make_solve_U(geom, Js_lookup, precond_type=precond_type, cg_maxiter=params.cg_maxiter,
                            cg_tol=params.cg_tol, poisson_reg=params.poisson_reg, boundary_mask=boundary_mask,
                            mode=mode, precision=precision, problem=prob)
@@ -188,7 +192,8 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
     B_vals = field_values(params.B_start, params.B_end, params.dB, params.loop)
     history, steps = [], []
     config_idx, J_last = 0, None
-    total = dict(time=0.0, iters=0, preco=0, evals=0, demag=0, demag_time=0.0, demag_wall_time=0.0)
+    total = dict(time=0.0, iters=0, preco=0, evals=0, demag=0, demag_time=0.0, demag_wall_time=0.0,
+                 device_loop_steps=0)
     for step_idx, Bmag in enumerate(B_vals):
         t0 = time.perf_counter()
         m, U, info = minimize(m, Bmag * h, U0=U, max_iter=params.max_iter, tau_f=params.tau_f, eps_a=params.eps_a,
@@ -217,6 +222,7 @@ def run_hysteresis_loop(points, geom, A_lookup, K1_lookup, Js_lookup, k_easy_loo
         total["demag"] += info["demag_iters"]
         total["demag_time"] += info.get("demag_time", 0.0)
         total["demag_wall_time"] += info.get("demag_wall_time", 0.0)
+        total["device_loop_steps"] += int(bool(info.get("device_loop", False)))
         # a state is saved on the first step, then when J moved by mstep or, without mstep, every
         # snapshot_every steps; each save after the first starts a new configuration index
         if J_last is None:

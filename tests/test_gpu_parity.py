@@ -341,6 +341,36 @@ def test_inner_solve_graph_equals_host_polled_loop(cuda_ok, inner):
     assert np.array_equal(m1, m0_) and np.array_equal(U1, U0)
 
 
+@pytest.mark.parametrize("method,precision,cpp", [("pcohen_hs", "fp64", False), ("pcohen", "fp64", False),
+                                                  ("pcg", "fp64", False), ("pcohen_hs", "fp32_precond", False),
+                                                  ("pcohen_hs", "fp64", True), ("pcohen", "fp32_precond", True)])
+def test_device_minimizer_graph_equals_host_loop(cuda_ok, method, precision, cpp):
+    """MM_OPT_MIN_GRAPH: the CG minimizers' iterations as one graph (the minimizer loop with the inner
+    solve, the Armijo trials and their demag PCG as nested WHILE nodes) take the host-driven loop's
+    iterations, evaluations, inner and demag iterations and reach its state bit for bit, on a first
+    call and on a second field that replays the cached graph; the info says which loop ran."""
+    s, p, _ = case("cube16_h2_air48")
+    m0 = random_state(p.N, seed=19, amplitude=0.2)
+    runs = {}
+    for g in (1, 0):
+        prob = fem_utils.make_problem(s)
+        if precision != "fp64":
+            prob.set_precision(precision)
+        prob.build_poisson(1e-12, "amgcl")
+        prob.set_option("min_graph", g)
+        mp = MinimizerParams(method=method, max_iter=40, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, cpp_semantics=cpp)
+        m1, U1, i1 = prob.minimize(np.array([0.0, 0.0, -0.3]), m0, np.zeros(p.N), mp)
+        m2, U2, i2 = prob.minimize(np.array([0.02, 0.0, -0.6]), m1, U1, mp)
+        runs[g] = ((m1, U1, i1), (m2, U2, i2))
+    for (mg, Ug, ig), (mh, Uh, ih) in zip(runs[1], runs[0]):
+        assert ig["device_loop"] and not ih["device_loop"]
+        for k in ("iters", "evals", "preco_iters", "demag_iters", "status"):
+            assert ig[k] == ih[k], (k, ig[k], ih[k])
+        assert ig["evals"] > ig["iters"] > 2
+        assert ig["E"] == ih["E"] and ig["gnorm"] == ih["gnorm"]
+        assert np.array_equal(mg, mh) and np.array_equal(Ug, Uh)
+
+
 @pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
 def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     """FP32 correction solves inside FP64 iterative refinement: the true FP64 residual meets the
