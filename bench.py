@@ -572,22 +572,26 @@ def run_ours(a):
     lv = prob.amg_levels()
     # energy + gradient evaluations: device time of the evaluation's kernels, L2 flushed before each
     ms_e64, bytes_e64 = prob.time_kernel("energy", 20)
-    prob.set_option("energy_ff", 1)
-    ms_eff, bytes_eff = prob.time_kernel("energy", 20)
-    prob.set_option("energy_ff", -1)
     energy = {"fp64": {"evals_per_s": 1e3 / ms_e64, "us_per_eval": 1e3 * ms_e64, "bytes_per_eval": bytes_e64,
                        "frac_hbm": bytes_e64 / (ms_e64 * 1e-3) / 1e9 / peak},
-              "float_float": {"evals_per_s": 1e3 / ms_eff, "us_per_eval": 1e3 * ms_eff, "bytes_per_eval": bytes_eff,
-                              "frac_hbm": bytes_eff / (ms_eff * 1e-3) / 1e9 / peak},
               "timing": "the kernels of one evaluation (float-float: the pair splits of m, k.m and U, then the "
                         "operator), CUDA events, 256 MiB L2 flush before each of 20 repetitions"}
+
+    def energy_ff(pr, tune):
+        """the float-float evaluation of a mixed-precision problem, with its autotuned lanes per row"""
+        ms, nb = pr.time_kernel("energy", 20)
+        ff = tune.get("energy_ff") or {}
+        return {"evals_per_s": 1e3 / ms, "us_per_eval": 1e3 * ms, "bytes_per_eval": nb,
+                "frac_hbm": nb / (ms * 1e-3) / 1e9 / peak, "speedup_vs_fp64": ms_e64 / ms,
+                "lanes_per_row": ff.get("chosen"), "autotune_us": ff.get("us")}
 
     mixed = None
     if not a.no_mixed:
         pm = fem_utils.make_problem(s)
         pm.set_precision("mixed")
         pm.build_poisson(1e-12, "amgcl")
-        pm.autotune(20)
+        tune_mx = pm.autotune(20)
+        energy["float_float"] = energy_ff(pm, tune_mx)
         timed_solves(pm, m_dev, U_dev, flush, a.tol, a.warmup)
         barrier(ws)
         mx_ms, mx_its, mx_rr, mx_outer = timed_solves(pm, m_dev, U_dev, flush, a.tol, a.steps)

@@ -354,6 +354,9 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * runs for the other methods, with MM_OPT_PROFILE, without MM_OPT_GRAPH and in MM_PRECISION_MIXED
  * (whose refinement steps are decided on the host). */
 #define MM_OPT_MIN_GRAPH 14
+/* MM_OPT_ENERGY_FF_LANES: lanes per magnetic row of the float-float energy kernel (1, 2, 4 or 8;
+ * default 4; mm_autotune times each with L2 flushed and keeps the fastest). */
+#define MM_OPT_ENERGY_FF_LANES 15
 int mm_set_option(mm_problem* h, int option, int value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,

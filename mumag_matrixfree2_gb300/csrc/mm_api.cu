@@ -180,7 +180,8 @@ struct mm_problem {
   bool eopsff_ok = false;          // built and current (a new magnetoelastic term clears it)
   bool eopsff_failed = false;      // an entry lies outside the range of the float-float pairs
   int energy_ff = -1;              // MM_OPT_ENERGY_FF
-  float2 *w_mff = nullptr, *w_sff = nullptr, *w_uff = nullptr;
+  mmk::NodesFF w_ff{};             // the node records it gathers
+  int eff_tpr = 4;                 // its lanes per magnetic row (mm_autotune)
   int min_fp32 = -1;               // MM_OPT_MIN_FP32
   double* d_Mn = nullptr;
   double* d_inv_M_rel = nullptr;
@@ -368,31 +369,45 @@ struct mm_problem {
       eopsff_failed = true;
       return false;
     }
-    auto pairs = [&](const mm::dvec& a) {
-      std::vector<float2> out((size_t)eops_stored, make_float2(0.0f, 0.0f));
+    auto split = [](double v) {
+      const float hi32 = (float)v;
+      return make_float2(hi32, (float)(v - (double)hi32));
+    };
+    auto quads = [&](const mm::dvec& a, const mm::dvec& b) {  // (a_hi, a_lo, b_hi, b_lo) per entry
+      std::vector<float4> out((size_t)eops_stored, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
       for (size_t k = 0; k < eops_pos.size(); ++k) {
-        const float hi32 = (float)a[k];
-        out[eops_pos[k]] = make_float2(hi32, (float)(a[k] - (double)hi32));
+        const float2 x = split(a[k]), y = split(b[k]);
+        out[eops_pos[k]] = make_float4(x.x, x.y, y.x, y.y);
       }
       return upload(out);
     };
+    std::vector<float2> gz2((size_t)eops_stored, make_float2(0.0f, 0.0f));
+    for (size_t k = 0; k < eops_pos.size(); ++k) gz2[eops_pos[k]] = split(eop_h.gz[k]);
     mmk::EnergySellFF& d = eopsff;
     d.n_rows = eops.n_rows;
     d.rows = eops.rows;
     d.sptr = eops.sptr;
     d.col = eops.col;
-    d.w = pairs(eop_h.w);
-    d.q = pairs(eop_h.q);
-    d.gx = pairs(eop_h.gx);
-    d.gy = pairs(eop_h.gy);
-    d.gz = pairs(eop_h.gz);
+    d.wq = quads(eop_h.w, eop_h.q);
+    d.gxy = quads(eop_h.gx, eop_h.gy);
+    d.gz = upload(gz2);
     d.kx = kax_h[3 * eops.axis0];
     d.ky = kax_h[3 * eops.axis0 + 1];
     d.kz = kax_h[3 * eops.axis0 + 2];
-    if (!w_mff) {
-      w_mff = alloc<float2>(3 * (size_t)N);
-      w_sff = alloc<float2>(N);
-      w_uff = alloc<float2>(N);
+    d.kfx = split(d.kx);
+    d.kfy = split(d.ky);
+    d.kfz = split(d.kz);
+    std::vector<char> seen(N, 0);
+    for (int j : eop_h.col) seen[j] = 1;
+    std::vector<int> touched;
+    for (int i = 0; i < N; ++i)
+      if (seen[i]) touched.push_back(i);
+    d.n_touched = (int)touched.size();
+    d.touched = upload(touched);
+    if (!w_ff.hi) {
+      w_ff.hi = alloc<float4>(N);
+      w_ff.lo = alloc<float4>(N);
+      w_ff.u = alloc<float2>(N);
     }
     eopsff_ok = true;
     return true;
@@ -1115,8 +1130,16 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   return (it >= maxiter && r2 > tol2_ref) ? MM_MAXITER : MM_OK;
 }
 
-// lanes per magnetic row of the float-float energy kernel
-constexpr int EFF_TPR = 4;
+// the float-float operator pass with TP lanes per magnetic row
+template <int TP>
+void energy_ff_rows(mm_problem* h, const double* d_m, const double* B, const double* d_B, const double* d_bias,
+                    double* d_g) {
+  const mmk::EnergySellFF& o = h->eopsff;
+  const mmk::NodesFF& nf = h->w_ff;
+  mmk::k_energy_grad_ff<TP><<<grid_rows(o.n_rows, TP), BS, 0, h->st>>>(o, nf.hi, nf.lo, nf.u, d_m, h->d_Mn, B[0], B[1],
+                                                                      B[2], d_B, d_bias, h->inv_Vmag, d_g, h->d_sc,
+                                                                      h->d_part);
+}
 
 // the launches of one energy and gradient evaluation (m.(g + g_z) into red[R_E]): float-float in the
 // mixed-precision problems (MM_OPT_ENERGY_FF), else FP64
@@ -1124,11 +1147,16 @@ void enqueue_energy(mm_problem* h, const double* d_m, const double* d_U, const d
                     double* d_g, const double* d_B = nullptr) {
   if (h->use_energy_ff()) {
     const mmk::EnergySellFF& o = h->eopsff;
-    mmk::k_split_ff<<<grid_elem(h->N), BS, 0, h->st>>>(h->N, d_m, d_U, o.kx, o.ky, o.kz, h->w_mff, h->w_sff,
-                                                       h->w_uff);
-    mmk::k_energy_grad_ff<EFF_TPR><<<grid_rows(o.n_rows, EFF_TPR), BS, 0, h->st>>>(
-        o, h->w_mff, h->w_sff, h->w_uff, d_m, h->d_Mn, B[0], B[1], B[2], d_B, d_bias, h->inv_Vmag, d_g, h->d_sc,
-        h->d_part);
+    const mmk::NodesFF& nf = h->w_ff;
+    mmk::k_split_ff<<<grid_elem(o.n_touched), BS, 0, h->st>>>(o.n_touched, o.touched, d_m, d_U, o.kx, o.ky, o.kz,
+                                                               nf);
+    LAUNCH_CHECK();
+    switch (h->eff_tpr) {
+      case 1: energy_ff_rows<1>(h, d_m, B, d_B, d_bias, d_g); break;
+      case 2: energy_ff_rows<2>(h, d_m, B, d_B, d_bias, d_g); break;
+      case 8: energy_ff_rows<8>(h, d_m, B, d_B, d_bias, d_g); break;
+      default: energy_ff_rows<4>(h, d_m, B, d_B, d_bias, d_g); break;
+    }
     LAUNCH_CHECK();
     return;
   }
@@ -3344,8 +3372,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms, double* byte
       nbytes = nnz * 12.0 + ((N + 31) / 32 + 1.0) * 4.0 + N * 8.0 * 4.0;
     } else if (kernel == MM_KERNEL_ENERGY && h->use_energy_ff()) {
       // entries: col, (hi, lo) of w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3);
-      // the pair splits: m (3) and U read, their pairs and those of k.m written
-      nbytes = nnzE * (4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0 + N * (8.0 * 4.0 + 8.0 * 5.0);
+      // the pair splits of the nodes the rows read: the node list, m (3) and U read, the pairs of m, k.m
+      // and U written
+      nbytes = nnzE * (4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0 +
+               (double)h->eopsff.n_touched * (4.0 + 8.0 * 4.0 + 8.0 * 5.0);
     } else if (kernel == MM_KERNEL_ENERGY) {
       // entries: col, mat, w, q, G(3); rows: row id, ptr; nodes: m (3), U, M_nodal, g (3)
       nbytes = nnzE * (4.0 + 4.0 + 8.0 * 5.0) + nrE * 8.0 + nrE * 8.0 * 8.0;
@@ -3476,6 +3506,49 @@ std::string tune_fuse(mm_problem* h, SolverT<T>& S, int bit, int reps) {
   return "{\"unfused_us\":" + std::to_string(1e3 * ms[0]) + ",\"fused_us\":" + std::to_string(1e3 * ms[1]) + "}";
 }
 
+// lanes per magnetic row of the float-float energy kernel: each of 1, 2, 4, 8 timed over reps
+// evaluations of the current state with L2 flushed before each (in a loop the demag solve between
+// two evaluations evicts the operator), the fastest kept
+std::string tune_energy_ff(mm_problem* h, int reps) {
+  if (!h->use_energy_ff()) return "null";
+  const double B[3] = {0.0, 0.0, 1.0};
+  const size_t flush_n = (size_t)256 << 20;  // 256 MiB > L2
+  char* flush = nullptr;
+  CK(cudaMalloc(&flush, flush_n));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::string rep = "{\"us\":{";
+  float best = 1e30f;
+  int best_tpr = h->eff_tpr;
+  for (int tpr : {1, 2, 4, 8}) {
+    h->eff_tpr = tpr;
+    enqueue_energy(h, h->d_m, h->d_U, B, nullptr, h->d_g);  // warm-up
+    float ms = 0.f;
+    for (int r = 0; r < reps; ++r) {
+      CK(cudaMemsetAsync(flush, r & 0xff, flush_n, h->st));
+      CK(cudaEventRecord(e0, h->st));
+      enqueue_energy(h, h->d_m, h->d_U, B, nullptr, h->d_g);
+      CK(cudaEventRecord(e1, h->st));
+      CK(cudaEventSynchronize(e1));
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, e0, e1));
+      ms += t / reps;
+    }
+    rep += (tpr > 1 ? ",\"" : "\"") + std::to_string(tpr) + "\":" + std::to_string(1e3 * ms);
+    if (ms < best) {
+      best = ms;
+      best_tpr = tpr;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(flush);
+  h->eff_tpr = best_tpr;
+  h->drop_min_graphs();  // captured evaluations hold the old launch shape
+  return rep + "},\"chosen\":" + std::to_string(best_tpr) + "}";
+}
+
 }  // namespace
 
 extern "C" {
@@ -3492,9 +3565,10 @@ int mm_autotune(mm_problem* h, int reps, char* report, int report_len) {
     const std::string f32 = tune_fuse<float>(h, h->s32, 1, reps);
     const std::string r64 = tune_fuse_restrict<double>(h, h->s64, 0, reps);
     const std::string r32 = tune_fuse_restrict<float>(h, h->s32, 1, reps);
+    const std::string eff = tune_energy_ff(h, reps);
     const std::string rep = "{\"operators\":" + ops + ",\"coarse_fuse\":{\"fp64\":" + f64 + ",\"fp32\":" + f32 +
                             ",\"chosen\":" + std::to_string(h->coarse_fuse) + "},\"fuse_restrict\":{\"fp64\":" +
-                            r64 + ",\"fp32\":" + r32 + ",\"chosen\":" + std::to_string(h->fuse_restrict) + "}}";
+                            r64 + ",\"fp32\":" + r32 + ",\"chosen\":" + std::to_string(h->fuse_restrict) + "},\"energy_ff\":" + eff + "}";
     h->sync();
     if (report && report_len > 0) {
       const size_t n = std::min(rep.size(), (size_t)report_len - 1);
@@ -3571,6 +3645,12 @@ int mm_set_option(mm_problem* h, int option, int value) {
       drop_graph(h->s32);
     }
     h->fuse_restrict = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_ENERGY_FF_LANES) {
+    if (value != 1 && value != 2 && value != 4 && value != 8) return MM_ERR_ARG;
+    if (h->eff_tpr != value) h->drop_min_graphs();
+    h->eff_tpr = value;
     return MM_OK;
   }
   if (option == MM_OPT_MIN_GRAPH) {

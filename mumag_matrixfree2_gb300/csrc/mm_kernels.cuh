@@ -1265,12 +1265,20 @@ struct EnergySellFF {
   const int* rows;
   const int* sptr;
   const int* col;
-  const float2* w;  // (hi, lo) pairs in the sliced order of EnergySell
-  const float2* q;
-  const float2* gx;
-  const float2* gy;
-  const float2* gz;
+  const float4* wq;   // (w_hi, w_lo, q_hi, q_lo) in the sliced order of EnergySell
+  const float4* gxy;  // (gx_hi, gx_lo, gy_hi, gy_lo)
+  const float2* gz;   // (gz_hi, gz_lo)
   double kx, ky, kz;  // the easy axis
+  float2 kfx, kfy, kfz;  // and its float-float pairs
+  int n_touched;         // nodes that magnetic rows read (their columns), the only ones split
+  const int* touched;
+};
+
+// the float-float node values an entry gathers, in three records (three gathers per entry)
+struct NodesFF {
+  float4* hi;  // (mx, my, mz, k.m) high parts
+  float4* lo;  // their low parts
+  float2* u;   // (U_hi, U_lo)
 };
 
 // (sh, sl) += (ah + al) (bh + bl), the al bl term dropped
@@ -1290,17 +1298,26 @@ __device__ __forceinline__ float2 ff_split(double v) {
   return make_float2(h, (float)(v - (double)h));
 }
 
-// the float-float pairs of m (3N), of s = k.m (N, formed in FP64 as the FP64 kernel forms k.v) and of U
-__global__ void __launch_bounds__(BS) k_split_ff(int N, const double* __restrict__ m, const double* __restrict__ U,
-                                                 double kx, double ky, double kz, float2* __restrict__ mff,
-                                                 float2* __restrict__ sff, float2* __restrict__ uff) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < N; i += gridDim.x * BS) {
+// (sh, sl) = (ah + al) + (bh + bl)
+__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float& sh, float& sl) {
+  float t, err;
+  Acc<float>::two_sum(ah, bh, t, err);
+  sh = t;
+  sl = (al + bl) + err;
+}
+
+// the float-float pairs of m, of s = k.m (formed in FP64 as the FP64 kernel forms k.v) and of U, for
+// the nodes the magnetic rows read
+__global__ void __launch_bounds__(BS) k_split_ff(int n, const int* __restrict__ nodes, const double* __restrict__ m,
+                                                 const double* __restrict__ U, double kx, double ky, double kz,
+                                                 NodesFF nf) {
+  for (int t = blockIdx.x * BS + threadIdx.x; t < n; t += gridDim.x * BS) {
+    const int i = __ldg(nodes + t);
     const double x = m[3 * i], y = m[3 * i + 1], z = m[3 * i + 2];
-    mff[3 * i] = ff_split(x);
-    mff[3 * i + 1] = ff_split(y);
-    mff[3 * i + 2] = ff_split(z);
-    sff[i] = ff_split(fma(kz, z, fma(ky, y, kx * x)));
-    uff[i] = ff_split(U[i]);
+    const float2 a = ff_split(x), b = ff_split(y), c = ff_split(z), s = ff_split(fma(kz, z, fma(ky, y, kx * x)));
+    nf.hi[i] = make_float4(a.x, b.x, c.x, s.x);
+    nf.lo[i] = make_float4(a.y, b.y, c.y, s.y);
+    nf.u[i] = ff_split(U[i]);
   }
 }
 
@@ -1319,8 +1336,8 @@ __device__ __forceinline__ void ff_shfl_add(float& sh, float& sl, int o) {
 // gather latency): lane q takes entries q, q + TPR, ..., and the row's float-float sums are merged
 // over its lanes by a fixed shuffle tree (FP32 shuffles and adds), so the result is deterministic.
 template <int TPR>
-__global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const float2* __restrict__ mff,
-                                                       const float2* __restrict__ sff, const float2* __restrict__ uff,
+__global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const float4* __restrict__ nh,
+                                                       const float4* __restrict__ nl, const float2* __restrict__ nu,
                                                        const double* __restrict__ m, const double* __restrict__ Mn,
                                                        double Bx, double By, double Bz, const double* __restrict__ Bd,
                                                        const double* __restrict__ Bbias, double inv_Vmag,
@@ -1342,19 +1359,20 @@ __global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const fl
     if (valid) {
       const int s = r >> 5, l = r & 31;
       const int base = __ldg(op.sptr + s), wd = (__ldg(op.sptr + s + 1) - base) >> 5;
+#pragma unroll 2
       for (int k = q; k < wd; k += TPR) {
         const int at = base + (k << 5) + l;
         const int j = __ldg(op.col + at);
-        const float2 w = __ldg(op.w + at), qq = __ldg(op.q + at);
-        const float2 gx = __ldg(op.gx + at), gy = __ldg(op.gy + at), gz = __ldg(op.gz + at);
-        const float2 mx = __ldg(mff + 3 * j), my = __ldg(mff + 3 * j + 1), mz = __ldg(mff + 3 * j + 2);
-        const float2 sj = __ldg(sff + j), u = __ldg(uff + j);
-        ff_madd(w.x, w.y, mx.x, mx.y, axh, axl);
-        ff_madd(w.x, w.y, my.x, my.y, ayh, ayl);
-        ff_madd(w.x, w.y, mz.x, mz.y, azh, azl);
-        ff_madd(qq.x, qq.y, sj.x, sj.y, th, tl);
-        ff_madd(gx.x, gx.y, u.x, u.y, uxh, uxl);
-        ff_madd(gy.x, gy.y, u.x, u.y, uyh, uyl);
+        const float4 wq = __ldg(op.wq + at), gxy = __ldg(op.gxy + at);
+        const float2 gz = __ldg(op.gz + at);
+        const float4 h = __ldg(nh + j), o = __ldg(nl + j);
+        const float2 u = __ldg(nu + j);
+        ff_madd(wq.x, wq.y, h.x, o.x, axh, axl);
+        ff_madd(wq.x, wq.y, h.y, o.y, ayh, ayl);
+        ff_madd(wq.x, wq.y, h.z, o.z, azh, azl);
+        ff_madd(wq.z, wq.w, h.w, o.w, th, tl);
+        ff_madd(gxy.x, gxy.y, u.x, u.y, uxh, uxl);
+        ff_madd(gxy.z, gxy.w, u.x, u.y, uyh, uyl);
         ff_madd(gz.x, gz.y, u.x, u.y, uzh, uzl);
       }
     }
@@ -1369,11 +1387,15 @@ __global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const fl
       ff_shfl_add(uzh, uzl, o);
     }
     if (valid && q == 0) {
-      const double t = (double)th + (double)tl;
-      const double ax = fma(-t, op.kx, (double)axh + (double)axl);
-      const double ay = fma(-t, op.ky, (double)ayh + (double)ayl);
-      const double az = fma(-t, op.kz, (double)azh + (double)azl);
-      const double ux = (double)uxh + (double)uxl, uy = (double)uyh + (double)uyl, uz = (double)uzh + (double)uzl;
+      // a - t k and then + u in float-float; one widening per component (the FP64 pipe issues a
+      // warp-wide instruction in 16 cycles whatever its active lanes)
+      ff_madd(-th, -tl, op.kfx.x, op.kfx.y, axh, axl);
+      ff_madd(-th, -tl, op.kfy.x, op.kfy.y, ayh, ayl);
+      ff_madd(-th, -tl, op.kfz.x, op.kfz.y, azh, azl);
+      ff_add(axh, axl, uxh, uxl, axh, axl);
+      ff_add(ayh, ayl, uyh, uyl, ayh, ayl);
+      ff_add(azh, azl, uzh, uzl, azh, azl);
+      const double ax = (double)axh + (double)axl, ay = (double)ayh + (double)ayl, az = (double)azh + (double)azl;
       const int a = __ldg(op.rows + r);
       double bx = Bx, by = By, bz = Bz;
       if (Bbias) {
@@ -1383,7 +1405,7 @@ __global__ void __launch_bounds__(BS) k_energy_grad_ff(EnergySellFF op, const fl
       }
       const double mn = -2.0 * Mn[a];
       const double zx = mn * bx, zy = mn * by, zz = mn * bz;
-      const double gxr = (ax + ux) + zx, gyr = (ay + uy) + zy, gzr = (az + uz) + zz;
+      const double gxr = ax + zx, gyr = ay + zy, gzr = az + zz;
       en += m[3 * a] * (gxr + zx) + m[3 * a + 1] * (gyr + zy) + m[3 * a + 2] * (gzr + zz);
       g[3 * a] = gxr * inv_Vmag;
       g[3 * a + 1] = gyr * inv_Vmag;

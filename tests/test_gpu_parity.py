@@ -71,11 +71,13 @@ def test_float_float_energy_matches_fp64(cuda_ok):
         prob.set_option("energy_ff", ff)
         probs[ff] = prob
     E64, g64 = probs[0].energy_and_grad(m, U, B)
-    Eff, gff = probs[1].energy_and_grad(m, U, B)
-    assert abs(Eff - E64) <= 1e-12 * abs(E64)
-    assert rel(gff, g64) <= 1e-11
     E0, g0 = ofem.energy_and_grad_mf(p, m, U, B)
-    assert abs(Eff - E0) <= RTOL * abs(E0) and rel(gff, g0) <= RTOL
+    for lanes in (1, 2, 8, 4):  # every lane count of the kernel (the shuffle merge of the row sums)
+        probs[1].set_option("energy_ff_lanes", lanes)
+        Eff, gff = probs[1].energy_and_grad(m, U, B)
+        assert abs(Eff - E64) <= 1e-12 * abs(E64), lanes
+        assert rel(gff, g64) <= 1e-11, lanes
+        assert abs(Eff - E0) <= RTOL * abs(E0) and rel(gff, g0) <= RTOL
     ms, nbytes = probs[1].time_kernel("energy", 5)
     assert ms > 0 and nbytes > 0
     from mumag_matrixfree2_gb300 import synthetic as syn
