@@ -64,9 +64,11 @@ def parse():
     ap.add_argument("--loop-dB", type=float, default=0.1, help="field step of the loop leg [T]")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start leg")
     ap.add_argument("--learned-steps", type=int, default=2000, help="training steps of the learned leg")
-    ap.add_argument("--batch-particles", type=int, default=64,
-                    help="particles of the batched leg (256 in the full workload; 0 skips the leg)")
+    ap.add_argument("--batch-particles", type=int, default=256,
+                    help="particles of the batched leg (256: the full workload; 0 skips the leg)")
     ap.add_argument("--batch-workers", type=int, default=16, help="host threads of the batched leg")
+    ap.add_argument("--batch-precision", default="fp32_precond", choices=["fp64", "mixed", "fp32_precond"],
+                    help="solver precision of the batched leg")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp32_precond"],
                     help="solver of the main timed solves (fp64: the headline plain method; the others for "
                          "profiling their kernels)")
@@ -472,18 +474,19 @@ def run_batch_leg(a):
     """Batched uneven particles: tri-axial ellipsoids (semi-axes U(5, 25) nm, 1.5 nm voxels, own graded
     air box of edge 5x the largest semi-axis, per-particle easy axis, K1, Js and A; seed 0), each swept
     +6 T -> -6 T along z in 0.1 T steps; all particles concurrently (one problem and CUDA stream per
-    particle, a pool of host threads), mixed precision."""
+    particle, a pool of host threads), in --batch-precision (default the FP64 PCG with the FP32 V-cycle,
+    float-float energy and FP32 inner solve, whose field steps run as one device graph each)."""
     from mumag_matrixfree2_gb300 import batch
     from mumag_matrixfree2_gb300 import synthetic as syn
 
     ps = syn.random_particles(256, seed=0)[:a.batch_particles]
     B = syn.field_values(6.0, -6.0, 0.1)
-    r = batch.run_batch(ps, B, workers=a.batch_workers, precision="mixed")
+    r = batch.run_batch(ps, B, workers=a.batch_workers, precision=a.batch_precision)
     res = r.pop("results")
     r["Hc_T"] = {"p50": float(np.percentile([x.Hc_T for x in res], 50)),
                  "min": float(min(x.Hc_T for x in res)), "max": float(max(x.Hc_T for x in res))}
     r["workload"] = (f"{len(ps)} of 256 ellipsoids (seed 0), +6 T -> -6 T in 0.1 T steps along z, pcohen_hs, "
-                     "eps_a 1e-6, PCG tol 1e-10, mixed precision")
+                     f"eps_a 1e-6, PCG tol 1e-10, {a.batch_precision} solver")
     return r
 
 

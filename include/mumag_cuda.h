@@ -419,7 +419,10 @@ int mm_unet_get_params(mm_unet* u, float* params);
 int mm_unet_get_grads(mm_unet* u, float* grads);           /* of the last mm_unet_backward */
 /* x: [nb][G^3][4] FP32 host array; y (may be NULL): [nb][G^3] output channel 0. */
 int mm_unet_forward(mm_unet* u, const float* x, int nb, float* y);
-/* Device-pointer variant; d_x NULL runs on the input already voxelised by mm_unet_voxelise_dev.  With
+/* The _dev entry points below read and write the caller's device arrays on the network's own stream
+ * after the work queued so far on the legacy default stream (a caller that writes them on another
+ * stream synchronises that stream first); every call but the graph forward waits for its results.
+ * Device-pointer variant; d_x NULL runs on the input already voxelised by mm_unet_voxelise_dev.  With
  * d_x and d_y both NULL (the in-solve path) the forward runs as a CUDA graph (captured at the second
  * such call for each batch size <= 8) and the call does not wait: a convolution's error is reported
  * by the next waiting call (mm_unet_interp_add_dev, mm_unet_sync). */

@@ -779,6 +779,15 @@ struct mm_unet {
     UCK(cudaMemsetAsync(q, 0, n * sizeof(uint4), st));
     return q;
   }
+  // The network runs on its own non-blocking stream: an entry point that reads or writes a caller's
+  // device arrays first orders that stream after the work queued so far on the legacy default stream
+  // (where a caller such as torch queues the writes of those arrays).
+  void after_caller() {
+    if (!ev_after) UCK(cudaEventCreateWithFlags(&ev_after, cudaEventDisableTiming));
+    UCK(cudaEventRecord(ev_after, cudaStreamLegacy));
+    UCK(cudaStreamWaitEvent(st, ev_after, 0));
+  }
+
   void check_err() {
     int e = 0;
     UCK(cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1183,6 +1192,7 @@ int mm_unet_forward_dev(mm_unet* u, const float* d_x, int nb, float* d_y) {
       forward_graph(u, nb);
       return MM_OK;
     }
+    u->after_caller();
     if (d_x) {
       mmn::k_pack_input<<<grid1d((long long)nv), 256, 0, u->st>>>(d_x, u->vol[0], u->T[T_X], nb);
       UCK(cudaGetLastError());
@@ -1211,6 +1221,7 @@ int mm_unet_backward(mm_unet* u, const float* target, int nb, double* loss) {
 int mm_unet_backward_dev(mm_unet* u, const float* d_target, int nb, double* loss) {
   if (!u || !d_target || nb < 1 || nb != u->nb_fwd) return MM_ERR_ARG;
   return uguard(u, [&] {
+    u->after_caller();
     const double L = u->backward(d_target, nb);
     if (loss) *loss = L;
     return MM_OK;
@@ -1236,6 +1247,7 @@ int mm_unet_voxelise_dev(mm_unet* u, int sample, int n_vox, const int* d_idx4, c
   if (!u || sample < 0 || sample >= u->B || n_vox != u->G * u->G * u->G || !d_idx4 || !d_w4 || !d_f3 || !d_f1)
     return MM_ERR_ARG;
   return uguard(u, [&] {
+    u->after_caller();
     mmn::k_voxelise<<<grid1d(n_vox), 256, 0, u->st>>>(d_idx4, d_w4, n_vox, d_f3, nullptr, d_f1, scale3, scale1,
                                                        u->vol[0], u->T[T_X], sample);
     UCK(cudaGetLastError());
@@ -1249,6 +1261,7 @@ int mm_unet_interp_add_dev(mm_unet* u, int sample, int n, const int* d_node, con
     return MM_ERR_ARG;
   return uguard(u, [&] {
     if (n > 0) {
+      u->after_caller();
       mmn::k_interp_add<<<grid1d(n), 256, 0, u->st>>>(d_node, d_idx8, d_w8, n, u->T[T_OUT], u->vol[0], 2, sample,
                                                         scale, d_U);
       UCK(cudaGetLastError());
