@@ -46,7 +46,7 @@ L2_FLUSH_BYTES = 256 << 20
 KERNEL_FN = {"pcg_dir": "k_pcg_dir", "pcg_step": "k_pcg_step", "vc_residual0": "k_vc_residual0",
              "smooth0": "k_smooth_dot", "init_residual": "k_init_residual", "coarse": "k_dense_mv",
              "residual": "k_sell", "smooth": "k_sell", "prolong": "k_sell", "restrict": "k_restrict",
-             "coarse_a": "k_coarse_a", "coarse_b": "k_coarse_b"}
+             "coarse_a": "k_coarse_a", "coarse_b": "k_coarse_b", "coarse_cycle": "k_coarse_cycle"}
 
 
 def parse():

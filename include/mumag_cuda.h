@@ -357,7 +357,17 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 /* MM_OPT_ENERGY_FF_LANES: lanes per magnetic row of the float-float energy kernel (1, 2, 4 or 8;
  * default 4; mm_autotune times each with L2 flushed and keeps the fastest). */
 #define MM_OPT_ENERGY_FF_LANES 15
+/* MM_OPT_COARSE_CYCLE (bit mask, default 0; mm_autotune keeps what is faster): with four levels, the
+ * fused restriction at level 1 and the fused coarse correction, the V-cycle runs levels 1 .. 3 (the
+ * level-1 restriction, both coarse-correction phases, the level-1 prolongation and post-smoothing)
+ * in one cooperative launch with grid barriers instead of five launches; bit-identical results.
+ * Bit 0 the FP64 solver, bit 1 the FP32 solver. */
+#define MM_OPT_COARSE_CYCLE 16
 int mm_set_option(mm_problem* h, int option, int value);
+/* The current value of MM_OPT_COARSE_CYCLE, MM_OPT_FUSE_RESTRICT, MM_OPT_COARSE_FUSE,
+ * MM_OPT_ENERGY_FF_LANES or MM_OPT_MIN_GRAPH (after mm_autotune, or after a loop graph that could not
+ * hold the cooperative launch turned MM_OPT_COARSE_CYCLE off). */
+int mm_get_option(mm_problem* h, int option, int* value);
 
 /* Autotuner (after mm_build_poisson): for every compressed-row operator of the hierarchy (coarse levels,
  * restrictions, prolongations; both precisions) tries 2, 4, 8, 16 and 32 lanes per row, each timed as
@@ -382,7 +392,8 @@ int mm_autotune(mm_problem* h, int reps, char* report, int report_len);
 #define MM_PROF_INIT_RESIDUAL 9 /* r = b - A x at the start of a PCG solve                        */
 #define MM_PROF_COARSE_A 10     /* fused coarse correction: t = T b and z = Z b (level L-2)        */
 #define MM_PROF_COARSE_B 11     /* fused coarse correction: x2 = t + W z (level L-2)               */
-#define MM_PROF_KINDS 12
+#define MM_PROF_COARSE_CYCLE 12 /* levels 1 .. 3 in one cooperative launch (MM_OPT_COARSE_CYCLE)   */
+#define MM_PROF_KINDS 13
 #define MM_PROF_LEVELS 16
 #define MM_PROF_SLOTS (2 * MM_PROF_LEVELS * MM_PROF_KINDS)
 /* Copy the per-slot totals since the last reset: launches, summed device time [ms] and the

@@ -21,7 +21,7 @@ METHODS = {"pcohen_hs": 0, "lbfgs": 1, "wg_np": 2, "plbfgs": 3, "cohen": 4, "pcg
 KERNELS = {"spmv_A": 0, "smooth": 1, "energy": 2, "hessian": 3}
 # in-solve profile slots: slot = (fp32 * PROF_LEVELS + level) * len(PROF_KINDS) + kind
 PROF_KINDS = ("pcg_dir", "pcg_step", "vc_residual0", "residual", "restrict", "coarse", "prolong", "smooth0",
-              "smooth", "init_residual", "coarse_a", "coarse_b")
+              "smooth", "init_residual", "coarse_a", "coarse_b", "coarse_cycle")
 PROF_LEVELS = 16
 PROF_SLOTS = 2 * PROF_LEVELS * len(PROF_KINDS)
 
@@ -98,6 +98,7 @@ SIGNATURES = {
     "mm_minimize_dev": (C.c_int, [_vp, _dp, _vp, _vp, C.POINTER(MinParams), C.POINTER(MinInfo)]),
     "mm_time_kernel": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "mm_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "mm_get_option": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mm_autotune": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
     "mm_profile_read": (C.c_int, [_vp, _lp, _dp, _dp]),
     "mm_profile_reset": (C.c_int, [_vp]),

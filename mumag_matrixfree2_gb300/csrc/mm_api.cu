@@ -120,6 +120,9 @@ struct SolverT {
   T *W = nullptr, *Z = nullptr, *tvec = nullptr, *zvec = nullptr;
   int fn = 0, fc = 0;
   int64_t Tm_nnz = 0;
+  // one-launch coarse cycle (levels 1 .. 3): its grid barrier and its co-resident grid
+  mmk::GridBar* bar = nullptr;
+  int coop_grid = 0;
 };
 
 // Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
@@ -213,6 +216,7 @@ struct mm_problem {
   bool pdl = true;               // MM_OPT_PDL
   int coarse_fuse = 1;           // MM_OPT_COARSE_FUSE: bit 0 the FP64 solver, bit 1 the FP32 solver
   int fuse_restrict = 3;         // MM_OPT_FUSE_RESTRICT: bit 0 the FP64 solver, bit 1 the FP32 solver
+  int coarse_cycle = 0;          // MM_OPT_COARSE_CYCLE: bit 0 the FP64 solver, bit 1 the FP32 solver
   std::vector<mm::HostCSR> rf_host;  // fused restrictions R_l (I - A_l S_l), formed for smoother rf_prec
   int rf_prec = -1;
 
@@ -685,7 +689,12 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
       LAUNCH_CHECK();
     });
   };
-  for (int l = 0; l < Ld; ++l) {
+  // levels 1 .. 3 in one cooperative launch when the hierarchy has that shape (four levels, fused
+  // restriction at level 1, fused coarse correction, compressed rows on level 1)
+  const bool cc_on = ((h->coarse_cycle >> (sizeof(T) == 8 ? 0 : 1)) & 1) && fuse && fr_on && L == 4 &&
+                     lv[0].Rf.nnz > 0 && lv[1].Rf.nnz > 0 && lv[1].Rf.tpr > 1 && lv[1].P.tpr > 1 &&
+                     lv[1].A.tpr > 1 && S.bar && S.coop_grid > 0;
+  for (int l = 0; l < (cc_on ? 1 : Ld); ++l) {
     auto& c = lv[l];
     if (fr_on && c.Rf.nnz > 0) {
       // x_l = s_l b_l (the pre-smoothing from zero, already written), so b_{l+1} = R_l (I - A_l S_l) b_l
@@ -703,7 +712,46 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     }
     restrict_into(l, c.R, c.res, mat_bytes(c.R));
   }
-  if (fuse) {
+  if (cc_on) {
+    auto& l1 = lv[1];
+    auto& l2 = lv[2];
+    mmk::CoarseCycle<T> cc{};
+    cc.Rf1 = l1.Rf.c;
+    cc.P1 = l1.P.c;
+    cc.A1 = l1.A.c;
+    cc.Tm = S.Tm;
+    cc.tpr_rf1 = l1.Rf.tpr;
+    cc.tpr_p1 = l1.P.tpr;
+    cc.tpr_a1 = l1.A.tpr;
+    cc.b1 = l1.b;
+    cc.x1 = l1.x;
+    cc.s1 = l1.s;
+    cc.x2_1 = l1.x2;
+    cc.b2 = l2.b;
+    cc.Z = S.Z;
+    cc.W = S.W;
+    cc.nc = S.fc;
+    cc.gT = grid_rows(S.fn, 32);
+    cc.tvec = S.tvec;
+    cc.zvec = S.zvec;
+    cc.x2_2 = l2.x2;
+    const double bytes = mat_bytes(l1.Rf) + mat_bytes(l1.P) + mat_bytes(l1.A) + 4.0 * ((double)S.Tm.n + 1.0) +
+                         (4.0 + w) * (double)S.Tm_nnz + 2.0 * w * (double)S.fc * S.fn + w * 7.0 * l1.n +
+                         w * 6.0 * l2.n;
+    tagged<T>(h, MM_PROF_COARSE_CYCLE, 1, bytes, [&] {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(S.coop_grid);
+      cfg.blockDim = dim3(BS);
+      cfg.stream = h->st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      CK(cudaLaunchKernelEx(&cfg, mmk::k_coarse_cycle<T>, cc, S.bar, sc, done));
+      LAUNCH_CHECK();
+    });
+  } else if (fuse) {
     auto& c = lv[L - 2];
     const int n = S.fn, nc = S.fc;
     const double tbytes = (double)S.Tm.n + 1.0;
@@ -725,7 +773,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
       LAUNCH_CHECK();
     });
   }
-  for (int l = (fuse ? L - 3 : L - 2); l >= 0; --l) {
+  for (int l = (cc_on ? 0 : fuse ? L - 3 : L - 2); l >= 0; --l) {
     auto& c = lv[l];
     tagged<T>(h, MM_PROF_PROLONG, l, mat_bytes(c.P) + w * lv[l + 1].n + 2.0 * w * c.n,
               [&] { spmv<3, T>(h, c.P, lv[l + 1].x2, c.x, nullptr, c.x, done); });  // x += P e
@@ -870,6 +918,16 @@ bool build_loop_graph(mm_problem* h, SolverT<T>& S) {
   return build_loop_graph(h, S, [&] { enqueue_iteration<T>(h, S); });
 }
 
+// the loop graph, or, when it cannot be built with the one-launch coarse cycle in it, without that
+template <class T, class Iter>
+bool loop_graph_or_retry(mm_problem* h, SolverT<T>& S, Iter&& iteration) {
+  if (build_loop_graph(h, S, iteration)) return true;
+  if (h->coarse_cycle == 0) return false;
+  h->coarse_cycle = 0;
+  S.graph_failed = false;
+  return build_loop_graph(h, S, iteration);
+}
+
 template <class T>
 void drop_graph(SolverT<T>& S) {
   if (S.exec) cudaGraphExecDestroy(S.exec);
@@ -887,7 +945,13 @@ struct PcgPending {
   bool graph = false;
 };
 
+// the one-launch coarse cycle records a grid barrier that gave up waiting in the PCG's scalars
+void check_barrier(const mmk::Scalars* sc) {
+  if (sc->bar_err) throw Fail{MM_ERR_CUDA, "a grid barrier of the one-launch coarse cycle gave up waiting"};
+}
+
 void finish_pcg(mm_problem* h, const PcgPending& pend, int* iters, double* r2_out) {
+  check_barrier(h->h_sc);
   if (pend.graph) h->n_launch += (int64_t)h->h_sc->loops * pend.S->iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -918,7 +982,7 @@ template <class T>
 void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, double* r2_out,
              PcgPending* pend = nullptr) {
   enqueue_pcg_start<T>(h, S, tol, maxiter);
-  const bool graph = h->use_graph && !h->prof && build_loop_graph<T>(h, S);
+  const bool graph = h->use_graph && !h->prof && loop_graph_or_retry(h, S, [&] { enqueue_iteration<T>(h, S); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
   } else if (h->prof) {
@@ -948,6 +1012,7 @@ void run_pcg(mm_problem* h, SolverT<T>& S, double tol, int maxiter, int* iters, 
     }
   }
   h->sync();
+  check_barrier(h->h_sc);
   if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -1005,7 +1070,7 @@ void enqueue_pcg_mp_start(mm_problem* h, double tol, int maxiter) {
 void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out, PcgPending* pend = nullptr) {
   auto& S = h->s64;
   enqueue_pcg_mp_start(h, tol, maxiter);
-  const bool graph = h->use_graph && !h->prof && build_loop_graph(h, S, [&] { enqueue_iteration_mp(h); });
+  const bool graph = h->use_graph && !h->prof && loop_graph_or_retry(h, S, [&] { enqueue_iteration_mp(h); });
   if (graph) {
     CK(cudaGraphLaunch(S.exec, h->st));
   } else {
@@ -1026,6 +1091,7 @@ void run_pcg_mp(mm_problem* h, double tol, int maxiter, int* iters, double* r2_o
     return;
   }
   h->sync();
+  check_barrier(h->h_sc);
   if (graph) h->n_launch += (int64_t)h->h_sc->loops * S.iter_launches;
   if (iters) *iters = h->h_sc->it;
   if (r2_out) *r2_out = h->h_sc->red[R_R2];
@@ -1858,7 +1924,9 @@ bool minimize_graph(mm_problem* h, MinCtx& c, double* m, double* U, double E0, b
   CK(cudaMemcpyAsync(h->d_ms, h->h_ms, sizeof(mmk::MinScal), cudaMemcpyHostToDevice, h->st));
   CK(cudaGraphLaunch(mg->ex, h->st));
   CK(cudaMemcpyAsync(h->h_ms, h->d_ms, sizeof(mmk::MinScal), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(mmk::Scalars), cudaMemcpyDeviceToHost, h->st));
   h->sync();
+  check_barrier(h->h_sc);
   c.evals += (int)s.evals;
   c.preco += (int)s.preco;
   c.demag += (int)s.demag;
@@ -2664,6 +2732,18 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
     // only where the dense factors stay small: Z = Ainv M costs nc^2 n host FLOPs, W and Z hold n nc each
     const double n = h->amg_h[L - 2].A.n_rows, nc = h->amg_h[L - 1].A.n_rows;
     if (nc <= 256 && n * nc <= 4194304.0) build_fused_coarse<T>(h, S, precond_type);
+  }
+  if (amg && L == 4 && S.fused) {
+    // the one-launch coarse cycle: a grid that is co-resident (the cooperative launch checks it) and
+    // the barrier it synchronises on
+    int coop = 0, per_sm = 0, sms = 0;
+    CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mmk::k_coarse_cycle<T>, BS, 0));
+    if (coop && per_sm > 0) {
+      S.bar = h->alloc<mmk::GridBar>(1);
+      S.coop_grid = per_sm * sms;
+    }
   }
   S.built = true;
 }
@@ -3506,6 +3586,23 @@ std::string tune_fuse(mm_problem* h, SolverT<T>& S, int bit, int reps) {
   return "{\"unfused_us\":" + std::to_string(1e3 * ms[0]) + ",\"fused_us\":" + std::to_string(1e3 * ms[1]) + "}";
 }
 
+// V-cycle time with levels 1 .. 3 in one cooperative launch and with five; sets the bit if the one
+// launch wins (a loop graph that cannot hold the cooperative launch turns it off again)
+template <class T>
+std::string tune_coarse_cycle(mm_problem* h, SolverT<T>& S, int bit, int reps) {
+  if (!S.built || !multilevel(h, S) || !S.bar || S.coop_grid <= 0) return "null";
+  const int saved = h->coarse_cycle;
+  float ms[2];
+  for (int on = 0; on < 2; ++on) {
+    h->coarse_cycle = on ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+    ms[on] = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+  }
+  h->coarse_cycle = ms[1] < ms[0] ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+  drop_graph(S);
+  return "{\"five_launches_us\":" + std::to_string(1e3 * ms[0]) + ",\"one_launch_us\":" +
+         std::to_string(1e3 * ms[1]) + "}";
+}
+
 // lanes per magnetic row of the float-float energy kernel: each of 1, 2, 4, 8 timed over reps
 // evaluations of the current state with L2 flushed before each (in a loop the demag solve between
 // two evaluations evicts the operator), the fastest kept
@@ -3566,9 +3663,13 @@ int mm_autotune(mm_problem* h, int reps, char* report, int report_len) {
     const std::string r64 = tune_fuse_restrict<double>(h, h->s64, 0, reps);
     const std::string r32 = tune_fuse_restrict<float>(h, h->s32, 1, reps);
     const std::string eff = tune_energy_ff(h, reps);
+    const std::string c64 = tune_coarse_cycle<double>(h, h->s64, 0, reps);
+    const std::string c32 = tune_coarse_cycle<float>(h, h->s32, 1, reps);
     const std::string rep = "{\"operators\":" + ops + ",\"coarse_fuse\":{\"fp64\":" + f64 + ",\"fp32\":" + f32 +
                             ",\"chosen\":" + std::to_string(h->coarse_fuse) + "},\"fuse_restrict\":{\"fp64\":" +
-                            r64 + ",\"fp32\":" + r32 + ",\"chosen\":" + std::to_string(h->fuse_restrict) + "},\"energy_ff\":" + eff + "}";
+                            r64 + ",\"fp32\":" + r32 + ",\"chosen\":" + std::to_string(h->fuse_restrict) + "},\"energy_ff\":" + eff +
+                            ",\"coarse_cycle\":{\"fp64\":" + c64 + ",\"fp32\":" + c32 +
+                            ",\"chosen\":" + std::to_string(h->coarse_cycle) + "}}";
     h->sync();
     if (report && report_len > 0) {
       const size_t n = std::min(rep.size(), (size_t)report_len - 1);
@@ -3577,6 +3678,18 @@ int mm_autotune(mm_problem* h, int reps, char* report, int report_len) {
     }
     return MM_OK;
   });
+}
+
+int mm_get_option(mm_problem* h, int option, int* value) {
+  if (!h || !value) return MM_ERR_ARG;
+  switch (option) {
+    case MM_OPT_COARSE_CYCLE: *value = h->coarse_cycle; return MM_OK;
+    case MM_OPT_FUSE_RESTRICT: *value = h->fuse_restrict; return MM_OK;
+    case MM_OPT_COARSE_FUSE: *value = h->coarse_fuse; return MM_OK;
+    case MM_OPT_ENERGY_FF_LANES: *value = h->eff_tpr; return MM_OK;
+    case MM_OPT_MIN_GRAPH: *value = h->min_graph; return MM_OK;
+    default: return MM_ERR_ARG;
+  }
 }
 
 int mm_set_option(mm_problem* h, int option, int value) {
@@ -3645,6 +3758,15 @@ int mm_set_option(mm_problem* h, int option, int value) {
       drop_graph(h->s32);
     }
     h->fuse_restrict = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_COARSE_CYCLE) {
+    if (value < 0 || value > 3) return MM_ERR_ARG;
+    if (h->coarse_cycle != value) {
+      drop_graph(h->s64);
+      drop_graph(h->s32);
+    }
+    h->coarse_cycle = value;
     return MM_OK;
   }
   if (option == MM_OPT_ENERGY_FF_LANES) {

@@ -36,7 +36,7 @@ struct Scalars {
   int maxiter;
   int loops;        // graph-loop trips (hard stop for the conditional node)
   int rz_valid;     // 0 until the first r.z of a solve is reduced
-  int pad;
+  int bar_err;      // a grid barrier of the one-launch coarse cycle gave up waiting (sticky)
   double red[NRED];
   unsigned cnt[NRED];
   // the minimizer's inner (preconditioner) solve, driven on the device
@@ -801,16 +801,14 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ai
 // (compressed rows of T = 2S - S A S on level L-2); each block gT + r computes z_r = (Z b)_r for one
 // row of the dense nc x n matrix Z = Ainv R (I - A S) with all its threads (fixed-order block sum).
 // Both read only b, the restricted residual of level L-2.
+// virtual block vb of gT + nc (the kernel's own block, or one of the one-launch coarse cycle's)
 template <class T>
-__global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict__ Z, int nc, const T* __restrict__ b,
-                                                 T* __restrict__ t, T* __restrict__ z, int gT,
-                                                 const int* __restrict__ done) {
-  pdl_entry();
-  if (done && *done) return;
+__device__ __forceinline__ void coarse_a_block(const CsrT<T>& Tm, const T* __restrict__ Z, const T* __restrict__ b,
+                                               T* __restrict__ t, T* __restrict__ z, int gT, int vb) {
   const int n = Tm.n;
-  if ((int)blockIdx.x < gT) {
+  if (vb < gT) {
     const int lane = threadIdx.x & 31;
-    for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
+    for (int row = vb * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
       T acc = T(0);
       const int e = __ldg(Tm.ptr + row + 1);
       for (int k = __ldg(Tm.ptr + row) + lane; k < e; k += 32) acc = fmaT<T>(__ldg(Tm.val + k), __ldg(b + __ldg(Tm.col + k)), acc);
@@ -819,7 +817,7 @@ __global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict
       if (lane == 0) t[row] = acc;
     }
   } else {
-    const int r = (int)blockIdx.x - gT;
+    const int r = vb - gT;
     const T* zr = Z + (size_t)r * n;
     double acc = 0.0;
     for (int k = threadIdx.x; k < n; k += BS) acc = fma((double)__ldg(zr + k), (double)__ldg(b + k), acc);
@@ -828,17 +826,23 @@ __global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict__ Z, int nc, const T* __restrict__ b,
+                                                 T* __restrict__ t, T* __restrict__ z, int gT,
+                                                 const int* __restrict__ done) {
+  pdl_entry();
+  if (done && *done) return;
+  coarse_a_block<T>(Tm, Z, b, t, z, gT, (int)blockIdx.x);
+}
+
 // Fused coarse correction, second phase: x2 = t + W z (W dense n x nc, row-major, W = (I - S A) P),
 // one warp per row.  x2 is level L-2's post-smoothed iterate, exactly as the V-cycle's levels
 // L-2 .. L-1 would leave it (same linear map, summed in a different order).
 template <class T>
-__global__ void __launch_bounds__(BS) k_coarse_b(int n, int nc, const T* __restrict__ W, const T* __restrict__ t,
-                                                 const T* __restrict__ z, T* __restrict__ x2,
-                                                 const int* __restrict__ done) {
-  pdl_entry();
-  if (done && *done) return;
+__device__ __forceinline__ void coarse_b_rows(int n, int nc, const T* __restrict__ W, const T* __restrict__ t,
+                                              const T* __restrict__ z, T* __restrict__ x2, int vb, int nvb) {
   const int lane = threadIdx.x & 31;
-  for (int row = blockIdx.x * (BS / 32) + threadIdx.x / 32; row < n; row += gridDim.x * (BS / 32)) {
+  for (int row = vb * (BS / 32) + threadIdx.x / 32; row < n; row += nvb * (BS / 32)) {
     const T* wr = W + (size_t)row * nc;
     T acc = T(0);
     for (int k = lane; k < nc; k += 32) acc = fmaT<T>(__ldg(wr + k), __ldg(z + k), acc);
@@ -846,6 +850,114 @@ __global__ void __launch_bounds__(BS) k_coarse_b(int n, int nc, const T* __restr
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) x2[row] = __ldg(t + row) + acc;
   }
+}
+
+template <class T>
+__global__ void __launch_bounds__(BS) k_coarse_b(int n, int nc, const T* __restrict__ W, const T* __restrict__ t,
+                                                 const T* __restrict__ z, T* __restrict__ x2,
+                                                 const int* __restrict__ done) {
+  pdl_entry();
+  if (done && *done) return;
+  coarse_b_rows<T>(n, nc, W, t, z, x2, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// ------------------------------------------------------------------------------------------
+// The V-cycle's levels 1 .. 3 of a four-level hierarchy in one cooperative launch (fused restriction
+// at level 1, fused coarse correction on levels 2 .. 3): b2 = Rf1 b1 | t = T b2, z = Z b2 |
+// x2_2 = t + W z | x1 += P1 x2_2 | x2_1 = x1 + s1 (b1 - A1 x1), five stages separated by grid
+// barriers instead of five launches.  Every row is computed exactly as by the separate kernels (same
+// lanes per row, same order), so the V-cycle's result is bit-identical.
+// ------------------------------------------------------------------------------------------
+struct GridBar {
+  unsigned arrive;  // blocks arrived at the current barrier
+  unsigned gen;     // barrier generation
+};
+
+// all blocks of the (co-resident, cooperative) grid meet; a wait is bounded: after ~2^22 polls the
+// block records the failure in sc->bar_err and goes on (later barriers then do not wait at all), so
+// a lost block cannot hang the GPU; the host turns the flag into an error
+__device__ __forceinline__ void grid_sync(GridBar* bar, Scalars* sc) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(bar->gen), arrive(bar->arrive);
+    cuda::atomic_ref<int, cuda::thread_scope_device> err(sc->bar_err);
+    const unsigned g = gen.load(cuda::memory_order_relaxed);
+    __threadfence();
+    if (arrive.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x - 1) {
+      arrive.store(0u, cuda::memory_order_relaxed);
+      gen.store(g + 1u, cuda::memory_order_release);
+    } else if (err.load(cuda::memory_order_relaxed) == 0) {
+      unsigned polls = 0;
+      while (gen.load(cuda::memory_order_acquire) == g) {
+        if (++polls > (1u << 22)) {
+          err.store(1, cuda::memory_order_relaxed);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <int TPR, int MODE, class T>
+__device__ __forceinline__ void csr_rows(const CsrT<T>& A, const T* __restrict__ x, const T* b,
+                                         const T* __restrict__ s, T* y, int vb, int nvb) {
+  constexpr int RPB = BS / TPR;
+  const int lane = threadIdx.x % TPR;
+  for (int rb = vb * RPB; rb < A.n; rb += nvb * RPB) {
+    const int row = rb + threadIdx.x / TPR;
+    const bool valid = row < A.n;
+    const T ax = csr_row<TPR, T>(A, x, row, valid, lane);
+    if (valid && lane == 0) {
+      if (MODE == 0) y[row] = ax;                                    // restriction into b
+      else if (MODE == 2) y[row] = x[row] + s[row] * (b[row] - ax);  // post-smoothing
+      else y[row] = b[row] + ax;                                     // prolongation
+    }
+  }
+}
+
+template <int MODE, class T>
+__device__ __forceinline__ void csr_rows_tpr(int tpr, const CsrT<T>& A, const T* __restrict__ x, const T* b,
+                                             const T* __restrict__ s, T* y) {
+  const int vb = blockIdx.x, nvb = gridDim.x;
+  switch (tpr) {
+    case 2: csr_rows<2, MODE, T>(A, x, b, s, y, vb, nvb); break;
+    case 4: csr_rows<4, MODE, T>(A, x, b, s, y, vb, nvb); break;
+    case 8: csr_rows<8, MODE, T>(A, x, b, s, y, vb, nvb); break;
+    case 16: csr_rows<16, MODE, T>(A, x, b, s, y, vb, nvb); break;
+    default: csr_rows<32, MODE, T>(A, x, b, s, y, vb, nvb); break;
+  }
+}
+
+template <class T>
+struct CoarseCycle {
+  CsrT<T> Rf1, P1, A1, Tm;
+  int tpr_rf1, tpr_p1, tpr_a1;
+  const T* b1;  // level-1 right-hand side (the restricted level-0 residual)
+  T* x1;        // level-1 iterate (pre-smoothed s1 b1 on entry)
+  const T* s1;
+  T* x2_1;      // level-1 post-smoothed iterate (the prolongation's input on level 0)
+  T* b2;
+  const T *Z, *W;
+  int nc, gT;
+  T *tvec, *zvec, *x2_2;
+};
+
+template <class T>
+__global__ void __launch_bounds__(BS) k_coarse_cycle(CoarseCycle<T> c, GridBar* bar, Scalars* sc,
+                                                     const int* __restrict__ done) {
+  if (done && *done) return;  // uniform: every block reads the same flag, set before this launch
+  csr_rows_tpr<0, T>(c.tpr_rf1, c.Rf1, c.b1, nullptr, nullptr, c.b2);
+  grid_sync(bar, sc);
+  for (int vb = blockIdx.x; vb < c.gT + c.nc; vb += gridDim.x) coarse_a_block<T>(c.Tm, c.Z, c.b2, c.tvec, c.zvec, c.gT, vb);
+  grid_sync(bar, sc);
+  coarse_b_rows<T>(c.Tm.n, c.nc, c.W, c.tvec, c.zvec, c.x2_2, (int)blockIdx.x, (int)gridDim.x);
+  grid_sync(bar, sc);
+  csr_rows_tpr<3, T>(c.tpr_p1, c.P1, c.x2_2, c.x1, nullptr, c.x1);
+  grid_sync(bar, sc);
+  csr_rows_tpr<2, T>(c.tpr_a1, c.A1, c.x1, c.b1, c.s1, c.x2_1);
 }
 
 // post-smoothing y = x + s .* (b - A x); with `part` it also reduces b.y into red[R_RZ]

@@ -299,12 +299,18 @@ class Problem:
                                                            C.byref(nb)))
         return ms.value, nb.value
 
+    OPTIONS = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5, "pdl": 8,
+               "coarse_fuse": 9, "min_fp32": 10, "split_a0": 11, "fuse_restrict": 12, "energy_ff": 13,
+               "min_graph": 14, "energy_ff_lanes": 15, "coarse_cycle": 16}
+
     def set_option(self, name: str, value: int):
-        opts = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5, "pdl": 8,
-                "coarse_fuse": 9, "min_fp32": 10,
-                "split_a0": 11, "fuse_restrict": 12, "energy_ff": 13,
-                "min_graph": 14, "energy_ff_lanes": 15}
-        self._check("mm_set_option", lib().mm_set_option(self.h, opts[name], int(value)))
+        self._check("mm_set_option", lib().mm_set_option(self.h, self.OPTIONS[name], int(value)))
+
+    def get_option(self, name: str) -> int:
+        """coarse_cycle, fuse_restrict, coarse_fuse, energy_ff_lanes or min_graph as now in effect."""
+        v = C.c_int()
+        self._check("mm_get_option", lib().mm_get_option(self.h, self.OPTIONS[name], C.byref(v)))
+        return v.value
 
     def autotune(self, reps: int = 20) -> dict:
         """Time the launch shapes of the hierarchy's operators and the fused coarse correction on this

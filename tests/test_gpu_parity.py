@@ -487,6 +487,38 @@ def test_fused_restriction_matches_the_residual_pass(cuda_ok, precision):
         assert abs(it1 - it_o) <= 1
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_precond", "mixed"])
+def test_coarse_cycle_in_one_launch_equals_five_launches(cuda_ok, precision):
+    """MM_OPT_COARSE_CYCLE: the V-cycle's levels 1 .. 3 of the 80 nm cube's four-level hierarchy in one
+    cooperative launch with grid barriers give the five-launch V-cycle's results bit for bit (same
+    rows, same lanes per row, same order): the same preconditioned vector, the same solve inside the
+    PCG loop graph, and the profiled (host-polled) solve runs the one-launch kernel once per V-cycle."""
+    s, p, _ = case("cube80_h1.6_air200")
+    probs = []
+    for cc in (0, 3):
+        prob = fem_utils.make_problem(s)
+        if precision != "fp64":
+            prob.set_precision(precision)
+        assert prob.build_poisson(1e-12, "amgcl") == 4
+        prob.set_option("coarse_cycle", cc)
+        probs.append(prob)
+    if precision == "fp64":
+        r = np.random.default_rng(45).standard_normal(s.N) * s.boundary_mask
+        assert np.array_equal(probs[0].precond(r), probs[1].precond(r))
+    m = random_state(s.N, seed=46, amplitude=0.05)
+    U0, it0, rr0, rc0 = probs[0].solve_u(m, np.zeros(s.N), 1e-10)
+    U1, it1, rr1, rc1 = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
+    assert probs[1].get_option("coarse_cycle") == 3  # the loop graph held the cooperative launch
+    assert rc0 == rc1 == 0 and it0 == it1 and rr0 == rr1 and np.array_equal(U0, U1)
+    probs[1].set_option("profile", 1)
+    probs[1].profile(reset=True)
+    U2, it2, _, _ = probs[1].solve_u(m, np.zeros(s.N), 1e-10)
+    rows = {(r["kernel"], r["precision"]): r["launches"] for r in probs[1].profile(reset=True)}
+    cycles = [n for (k, _), n in rows.items() if k == "coarse_cycle"]
+    assert cycles and min(cycles) > 0 and not any(k == "coarse_a" for k, _ in rows)
+    assert np.array_equal(U2, U1)
+
+
 def test_autotuner_keeps_results_within_tolerance(cuda_ok):
     """The autotuner changes launch shapes and the coarse path only: the solve converges to the same
     potential with the same iterations (+-1), and the report covers every compressed-row operator."""
