@@ -122,7 +122,9 @@ struct SolverT {
   int64_t Tm_nnz = 0;
   // one-launch coarse cycle (levels 1 .. 3): its grid barrier and its co-resident grid
   mmk::GridBar* bar = nullptr;
-  int coop_grid = 0;
+  int coop_grid = 0;     // blocks of the launch (the autotuner picks 1, 2, 4 or all co-resident per SM)
+  int coop_max = 0;      // co-resident blocks of the whole GPU
+  int sms = 0;
 };
 
 // Layout choice: one thread per row when the rows alone fill the GPU (>= 64Ki rows), else enough
@@ -2742,7 +2744,8 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mmk::k_coarse_cycle<T>, BS, 0));
     if (coop && per_sm > 0) {
       S.bar = h->alloc<mmk::GridBar>(1);
-      S.coop_grid = per_sm * sms;
+      S.coop_max = S.coop_grid = per_sm * sms;
+      S.sms = sms;
     }
   }
   S.built = true;
@@ -3592,15 +3595,27 @@ template <class T>
 std::string tune_coarse_cycle(mm_problem* h, SolverT<T>& S, int bit, int reps) {
   if (!S.built || !multilevel(h, S) || !S.bar || S.coop_grid <= 0) return "null";
   const int saved = h->coarse_cycle;
-  float ms[2];
-  for (int on = 0; on < 2; ++on) {
-    h->coarse_cycle = on ? (saved | (1 << bit)) : (saved & ~(1 << bit));
-    ms[on] = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+  h->coarse_cycle = saved & ~(1 << bit);
+  const float ms_off = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+  // fewer blocks make each grid barrier cheaper and each stage less parallel: 1, 2, 4 per SM or all
+  h->coarse_cycle = saved | (1 << bit);
+  std::string rep = "{\"five_launches_us\":" + std::to_string(1e3 * ms_off) + ",\"one_launch_us\":{";
+  float best = 1e30f;
+  int best_grid = S.coop_max;
+  for (int per : {1, 2, 4, 0}) {
+    const int grid = per ? std::min(per * S.sms, S.coop_max) : S.coop_max;
+    S.coop_grid = grid;
+    const float ms = time_ms<T>(h, reps, [&] { enqueue_precond<T>(h, S, S.r, S.z); });
+    rep += (per != 1 ? ",\"" : "\"") + std::to_string(grid) + "\":" + std::to_string(1e3 * ms);
+    if (ms < best) {
+      best = ms;
+      best_grid = grid;
+    }
   }
-  h->coarse_cycle = ms[1] < ms[0] ? (saved | (1 << bit)) : (saved & ~(1 << bit));
+  S.coop_grid = best_grid;
+  h->coarse_cycle = best < ms_off ? (saved | (1 << bit)) : (saved & ~(1 << bit));
   drop_graph(S);
-  return "{\"five_launches_us\":" + std::to_string(1e3 * ms[0]) + ",\"one_launch_us\":" +
-         std::to_string(1e3 * ms[1]) + "}";
+  return rep + "}}";
 }
 
 // lanes per magnetic row of the float-float energy kernel: each of 1, 2, 4, 8 timed over reps

@@ -500,6 +500,7 @@ def test_coarse_cycle_in_one_launch_equals_five_launches(cuda_ok, precision):
         if precision != "fp64":
             prob.set_precision(precision)
         assert prob.build_poisson(1e-12, "amgcl") == 4
+        prob.set_option("coarse_fuse", 3)  # the one-launch cycle covers the fused coarse correction
         prob.set_option("coarse_cycle", cc)
         probs.append(prob)
     if precision == "fp64":
