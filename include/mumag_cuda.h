@@ -363,6 +363,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * in one cooperative launch with grid barriers instead of five launches; bit-identical results.
  * Bit 0 the FP64 solver, bit 1 the FP32 solver. */
 #define MM_OPT_COARSE_CYCLE 16
+/* MM_OPT_CSR_LANES (after mm_build_poisson): every compressed-row operator of the hierarchy (coarse
+ * levels, R, P and the fused restrictions) read with this many lanes per row (2, 4, 8, 16 or 32);
+ * mm_autotune chooses per operator among these and one thread per row. */
+#define MM_OPT_CSR_LANES 17
 int mm_set_option(mm_problem* h, int option, int value);
 /* The current value of MM_OPT_COARSE_CYCLE, MM_OPT_FUSE_RESTRICT, MM_OPT_COARSE_FUSE,
  * MM_OPT_ENERGY_FF_LANES or MM_OPT_MIN_GRAPH (after mm_autotune, or after a loop graph that could not

@@ -3775,6 +3775,20 @@ int mm_set_option(mm_problem* h, int option, int value) {
     h->fuse_restrict = value;
     return MM_OK;
   }
+  if (option == MM_OPT_CSR_LANES) {
+    if (value != 2 && value != 4 && value != 8 && value != 16 && value != 32) return MM_ERR_ARG;
+    if (!h->poisson_built) return MM_ERR_STATE;
+    auto set_all = [&](auto& S) {
+      for (auto& c : S.lv)
+        for (auto* M : {&c.A, &c.R, &c.P, &c.Rf})
+          if (M->c.n > 0 && M->tpr != 1) M->tpr = value;
+      drop_graph(S);
+    };
+    set_all(h->s64);
+    set_all(h->s32);
+    h->drop_inner_graphs();
+    return MM_OK;
+  }
   if (option == MM_OPT_COARSE_CYCLE) {
     if (value < 0 || value > 3) return MM_ERR_ARG;
     if (h->coarse_cycle != value) {

@@ -520,6 +520,31 @@ def test_coarse_cycle_in_one_launch_equals_five_launches(cuda_ok, precision):
     assert np.array_equal(U2, U1)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_precond"])
+def test_every_compressed_row_shape_gives_the_same_solve(cuda_ok, precision):
+    """MM_OPT_CSR_LANES: every compressed-row operator read with 2 .. 32 lanes per row (the shapes the
+    autotuner chooses among): the same preconditioned vector to rounding and the same solve
+    (iterations +-1, potential to 1e-10 of its scale) on the 80 nm cube's four levels."""
+    s, p, _ = case("cube80_h1.6_air200")
+    m = random_state(s.N, seed=47, amplitude=0.05)
+    r = np.random.default_rng(48).standard_normal(s.N) * s.boundary_mask
+    ref = None
+    for lanes in (8, 2, 4, 16, 32):
+        prob = fem_utils.make_problem(s)
+        if precision != "fp64":
+            prob.set_precision(precision)
+        prob.build_poisson(1e-12, "amgcl")
+        prob.set_option("csr_lanes", lanes)
+        z = prob.precond(r)
+        U, it, rr, rc = prob.solve_u(m, np.zeros(s.N), 1e-10)
+        assert rc == 0 and rr <= 1e-10
+        if ref is None:
+            ref = (z, U, it)
+            continue
+        assert rel(z, ref[0]) <= 1e-12, lanes
+        assert abs(it - ref[2]) <= 1 and rel(U, ref[1]) <= 1e-10, lanes
+
+
 def test_autotuner_keeps_results_within_tolerance(cuda_ok):
     """The autotuner changes launch shapes and the coarse path only: the solve converges to the same
     potential with the same iterations (+-1), and the report covers every compressed-row operator."""
