@@ -711,6 +711,42 @@ void assemble_magnetoelastic(EnergyOp& op, int N, int E, const int* conn, const 
   }
 }
 
+// rho(D^-1 A) by the power method from a fixed pseudo-random start (Knuth's multiplicative hash of the
+// row index), `steps` products, times `safety` (the method approaches rho from below).  Row sums in
+// column order (threaded by rows) and norms as left-to-right serial sums, so that a numpy
+// restatement with cumulative sums reproduces the estimate.
+static double power_rho(const HostCSR& A, const std::vector<double>& d, int steps, double safety) {
+  const int n = A.n_rows;
+  if (n == 0) return 1.0;
+  std::vector<double> dinv(n), x(n), y(n);
+  for (int i = 0; i < n; ++i) {
+    dinv[i] = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
+    x[i] = (double)(((uint64_t)i * 2654435761ull) % 4294967296ull) / 4294967296.0 - 0.5;
+  }
+  auto norm = [](const std::vector<double>& v) {
+    double s = 0.0;
+    for (double e : v) s += e * e;
+    return std::sqrt(s);
+  };
+  double nx = norm(x), lam = 1.0;
+  const int nt = setup_threads(A.ptr[n]);
+  for (int s = 0; s < steps; ++s) {
+    parallel_chunks(n, nt, [&](int, int64_t r0, int64_t r1) {
+      for (int64_t i = r0; i < r1; ++i) {
+        double acc = 0.0;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) acc += A.val[k] * x[A.col[k]];
+        y[i] = dinv[i] * acc;
+      }
+    });
+    const double ny = norm(y);
+    if (!(ny > 0.0 && nx > 0.0)) break;
+    lam = ny / nx;
+    for (int i = 0; i < n; ++i) x[i] = y[i] / ny;
+    nx = 1.0;
+  }
+  return safety * lam;
+}
+
 std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
   std::vector<AmgLevel> levels;
   levels.reserve(prm.max_levels);
@@ -743,18 +779,9 @@ std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
       }
       T.ptr[i + 1] = (int)T.col.size();
     }
-    // Gershgorin bound of rho(D^-1 A) and damped-Jacobi smoothing
+    // damped-Jacobi smoothing with omega = (4/3) / rho(D^-1 A)
     const std::vector<double>& d = levels.back().diag;
-    double rho = 0.0;
-    bool any = false;
-    for (int i = 0; i < n; ++i) {
-      if (std::fabs(d[i]) <= 0.0) continue;
-      double rs = 0.0;
-      for (int k = Acur.ptr[i]; k < Acur.ptr[i + 1]; ++k) rs += std::fabs(Acur.val[k]);
-      rho = any ? std::max(rho, rs / std::fabs(d[i])) : rs / std::fabs(d[i]);
-      any = true;
-    }
-    if (!any) rho = 1.0;
+    const double rho = power_rho(Acur, d, prm.rho_steps, prm.rho_safety);
     double omega = (4.0 / 3.0) / rho;
     HostCSR AT = spgemm(Acur, T);
     HostCSR P;

@@ -70,7 +70,9 @@ struct AmgLevel {
 struct AmgParams {
   int max_levels = 10;
   int max_coarse = 1000;
-  double theta0 = 0.08;
+  double theta0 = 0.12;    // strength threshold on the finest level, halved per level
+  int rho_steps = 20;      // power-method steps of the smoothing's spectral-radius estimate
+  double rho_safety = 1.05;
 };
 
 // geometry (src/loop.py:56-102)

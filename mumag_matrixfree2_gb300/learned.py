@@ -282,14 +282,18 @@ class WarmStart:
 
     The network has no biases (they are held at zero), so it is positively homogeneous,
     f(a x) = a f(x): one trained network serves every step size, and a prediction needs no
-    per-sample normalisation on the device.  Input channels: dm * jsf (3) and c_U * U_a * jsf (1),
-    with c_U fixed when training starts so that both kinds of channel have comparable magnitudes;
+    per-sample normalisation on the device.  Input channels: dm * jsf (3) and c_U * U_a * jsf (1).
+    The exact change U_b - U_a = A^-1 D (m_b - m_a) depends on dm alone, so c_U is 0 by default (the
+    U channel holds zeros); with u_channel=True it is fixed when training starts so that both kinds of
+    channel have comparable magnitudes (the ratio then varies by orders of magnitude between pairs
+    with large and with tiny dm, which made training much worse on the 80 nm cube);
     output: U_b - U_a.  Training pairs are normalised by 1 / max|dm| (conditioning only).
 
     State fields on the grid (float32, [G^3, 5]): m * jsf (3), U * jsf (1), U (1).
     """
 
-    def __init__(self, setup, grid: int = 64, margin: float = 20.0, batch: int = 8, params=None, seed: int = 0):
+    def __init__(self, setup, grid: int = 64, margin: float = 20.0, batch: int = 8, params=None, seed: int = 0,
+                 u_channel: bool = False):
         import torch
 
         self.torch = torch
@@ -315,6 +319,7 @@ class WarmStart:
         self.net = UNet(grid, batch, params, seed)
         self.net._check("mm_unet_set_bias_training", _abi.lib().mm_unet_set_bias_training(self.net.h, 0))
         self.batch = batch
+        self.u_channel = u_channel
         self.c_U = None
         self._x = torch.zeros((batch, self.V, 4), dtype=torch.float32, device=dev)
         self._t = torch.zeros((batch, self.V), dtype=torch.float32, device=dev)
@@ -343,7 +348,10 @@ class WarmStart:
         return s
 
     def calibrate(self, states, pairs):
-        """c_U = median max|dm| / median max|U jsf| over the pairs."""
+        """c_U = median max|dm| / median max|U jsf| over the pairs (0 without the U channel)."""
+        if not self.u_channel:
+            self.c_U = 0.0
+            return self.c_U
         dm = [float((states[b][:, :3] - states[a][:, :3]).abs().max()) for a, b in pairs[:: max(1, len(pairs) // 64)]]
         um = [float(states[a][:, 3].abs().max()) for a, b in pairs[:: max(1, len(pairs) // 64)]]
         self.c_U = float(np.median(dm) / max(np.median(um), 1e-30))

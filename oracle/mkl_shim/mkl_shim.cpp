@@ -134,7 +134,7 @@ Csr multiply(const Csr& A, const Csr& B) {
 // ----------------------------------------------------------------------------------------------
 // smoothed-aggregation hierarchy and the PCG that stands in for PARDISO's direct solve
 // ----------------------------------------------------------------------------------------------
-constexpr double kTheta = 0.08;    // strength threshold on the finest level, halved per coarser level
+constexpr double kTheta = 0.12;    // strength threshold on the finest level, halved per coarser level
 constexpr int kMaxCoarse = 1000;   // the coarsest level is factorised densely
 constexpr int kMaxLevels = 10;
 constexpr int kMaxIter = 2000;
@@ -218,8 +218,8 @@ int aggregate(const Csr& A, double theta, std::vector<int>& agg) {
     return na;
 }
 
-// P = (I - omega D^-1 A) T with T the normalised aggregate indicator and omega = 4 / (3 rho),
-// rho the Gershgorin bound of D^-1 A.
+// P = (I - omega D^-1 A) T with T the normalised aggregate indicator and omega = 4 / (3 rho), rho
+// 1.05 x the power-method estimate of rho(D^-1 A) after 20 products from a fixed pseudo-random start.
 Csr prolongator(const Csr& A, const std::vector<int>& agg, int na) {
     const int n = A.n;
     std::vector<int> size(na, 0);
@@ -236,17 +236,35 @@ Csr prolongator(const Csr& A, const std::vector<int>& agg, int na) {
         }
         T.p[i + 1] = static_cast<int>(T.c.size());
     }
-    std::vector<double> dinv(n, 0.0);
-    double rho = 0.0;
+    std::vector<double> dinv(n, 0.0), x(n), y(n);
     for (int i = 0; i < n; ++i) {
-        double d = 0.0, s = 0.0;
-        for (int k = A.p[i]; k < A.p[i + 1]; ++k) {
-            s += std::fabs(A.v[k]);
+        double d = 0.0;
+        for (int k = A.p[i]; k < A.p[i + 1]; ++k)
             if (A.c[k] == i) d = A.v[k];
-        }
         dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
-        if (d != 0.0) rho = std::max(rho, s / std::fabs(d));
+        x[i] = static_cast<double>((static_cast<unsigned long long>(i) * 2654435761ull) % 4294967296ull) /
+                   4294967296.0 - 0.5;
     }
+    auto norm = [](const std::vector<double>& v) {
+        double s = 0.0;
+        for (double e : v) s += e * e;
+        return std::sqrt(s);
+    };
+    double nx = norm(x), rho = 0.0;
+    for (int it = 0; it < 20 && n > 0; ++it) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int k = A.p[i]; k < A.p[i + 1]; ++k) acc += A.v[k] * x[A.c[k]];
+            y[i] = dinv[i] * acc;
+        }
+        const double ny = norm(y);
+        if (!(ny > 0.0 && nx > 0.0)) break;
+        rho = ny / nx;
+        for (int i = 0; i < n; ++i) x[i] = y[i] / ny;
+        nx = 1.0;
+    }
+    rho *= 1.05;
     const double omega = rho > 0.0 ? 4.0 / (3.0 * rho) : 0.0;
     Csr AT = multiply(A, T);
     Csr P;

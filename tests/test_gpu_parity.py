@@ -142,7 +142,7 @@ def test_solve_cfg_mesh_and_determinism(cuda_ok):
     s, p, _ = case("cube40_h2_air200")
     prob = fem_utils.make_problem(s)
     nl = prob.build_poisson(1e-12, "amgcl")
-    assert nl == 3
+    assert nl == 4
     su = opo.SolveU(p, ofem.assembled_operators(p, parts=("A", "D")), cg_tol=1e-10)
     m = random_state(p.N, seed=12, amplitude=0.05)
     U0, it0, rr0 = su(m, np.zeros(p.N), 1e-10, return_info=True)

@@ -174,13 +174,14 @@ def test_device_transfer_matches_host_transfer(sweeps):
 
 def test_trained_warm_start_saves_pcg_iterations(sweeps):
     """Trained on the plain solver's own sweeps, the network's prediction of U_b - U_a on a held-out
-    sweep beats U_a alone, and PCG to the same tolerance needs fewer iterations from it."""
+    sweep beats U_a alone (median grid error at least 30 % below the untrained network's), and PCG to
+    the same tolerance needs fewer iterations from it."""
     prob, ws, train, pairs, ev, nodal = sweeps
     ev_pairs = [(i, i + 1) for i in range(len(ev) - 1)]
     err0 = np.median([ws.predict_grid(ev[a], ev[b])[1] for a, b in ev_pairs])
     ws.train(train, pairs, steps=1500, lr=1e-3)
     err1 = np.median([ws.predict_grid(ev[a], ev[b])[1] for a, b in ev_pairs])
-    assert err1 < 0.6 * err0, (err0, err1)
+    assert err1 < 0.7 * err0 and err1 < 1.0, (err0, err1)
     base = learn = 0
     for k in range(len(nodal) - 1):
         (ma, Ua), (mb, Ub) = nodal[k], nodal[k + 1]
