@@ -797,18 +797,20 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ai
   }
 }
 
-// Fused coarse correction, first phase.  Blocks [0, gT) compute t = T b, one warp per row of T
-// (compressed rows of T = 2S - S A S on level L-2); each block gT + r computes z_r = (Z b)_r for one
-// row of the dense nc x n matrix Z = Ainv R (I - A S) with all its threads (fixed-order block sum).
-// Both read only b, the restricted residual of level L-2.
-// virtual block vb of gT + nc (the kernel's own block, or one of the one-launch coarse cycle's)
+// Fused coarse correction, first phase.  Block r < nc computes z_r = (Z b)_r for one row of the dense
+// nc x n matrix Z = Ainv R (I - A S) with all its threads (fixed-order block sum) - these long dot
+// products go first, so that they overlap the rest instead of forming the kernel's tail; blocks
+// nc .. nc + gT compute t = T b, one warp per row of T (compressed rows of T = 2S - S A S on level
+// L-2).  Both read only b, the restricted residual of level L-2.
+// virtual block vb of nc + gT (the kernel's own block, or one of the one-launch coarse cycle's)
 template <class T>
 __device__ __forceinline__ void coarse_a_block(const CsrT<T>& Tm, const T* __restrict__ Z, const T* __restrict__ b,
-                                               T* __restrict__ t, T* __restrict__ z, int gT, int vb) {
+                                               T* __restrict__ t, T* __restrict__ z, int gT, int nc, int vb) {
   const int n = Tm.n;
-  if (vb < gT) {
+  if (vb >= nc) {
+    const int tb = vb - nc;
     const int lane = threadIdx.x & 31;
-    for (int row = vb * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
+    for (int row = tb * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
       T acc = T(0);
       const int e = __ldg(Tm.ptr + row + 1);
       for (int k = __ldg(Tm.ptr + row) + lane; k < e; k += 32) acc = fmaT<T>(__ldg(Tm.val + k), __ldg(b + __ldg(Tm.col + k)), acc);
@@ -817,9 +819,10 @@ __device__ __forceinline__ void coarse_a_block(const CsrT<T>& Tm, const T* __res
       if (lane == 0) t[row] = acc;
     }
   } else {
-    const int r = vb - gT;
+    const int r = vb;
     const T* zr = Z + (size_t)r * n;
     double acc = 0.0;
+#pragma unroll 4
     for (int k = threadIdx.x; k < n; k += BS) acc = fma((double)__ldg(zr + k), (double)__ldg(b + k), acc);
     acc = block_sum(acc);
     if (threadIdx.x == 0) z[r] = (T)acc;
@@ -832,23 +835,32 @@ __global__ void __launch_bounds__(BS) k_coarse_a(CsrT<T> Tm, const T* __restrict
                                                  const int* __restrict__ done) {
   pdl_entry();
   if (done && *done) return;
-  coarse_a_block<T>(Tm, Z, b, t, z, gT, (int)blockIdx.x);
+  coarse_a_block<T>(Tm, Z, b, t, z, gT, nc, (int)blockIdx.x);
 }
 
 // Fused coarse correction, second phase: x2 = t + W z (W dense n x nc, row-major, W = (I - S A) P),
-// one warp per row.  x2 is level L-2's post-smoothed iterate, exactly as the V-cycle's levels
-// L-2 .. L-1 would leave it (same linear map, summed in a different order).
+// CB_LANES lanes per row (a row of ~250 entries: 31 multiply-adds per lane and three shuffle levels,
+// where a warp per row spent as many FP64 issue slots on its five-level reduction as on the row).
+// x2 is level L-2's post-smoothed iterate, exactly as the V-cycle's levels L-2 .. L-1 would leave it
+// (same linear map, summed in a different order).
+constexpr int CB_LANES = 8;
+
 template <class T>
 __device__ __forceinline__ void coarse_b_rows(int n, int nc, const T* __restrict__ W, const T* __restrict__ t,
                                               const T* __restrict__ z, T* __restrict__ x2, int vb, int nvb) {
-  const int lane = threadIdx.x & 31;
-  for (int row = vb * (BS / 32) + threadIdx.x / 32; row < n; row += nvb * (BS / 32)) {
-    const T* wr = W + (size_t)row * nc;
+  constexpr int RPB = BS / CB_LANES;
+  const int q = threadIdx.x % CB_LANES;
+  for (int rb = vb * RPB; rb < n; rb += nvb * RPB) {
+    const int row = rb + threadIdx.x / CB_LANES;
     T acc = T(0);
-    for (int k = lane; k < nc; k += 32) acc = fmaT<T>(__ldg(wr + k), __ldg(z + k), acc);
+    if (row < n) {
+      const T* wr = W + (size_t)row * nc;
+#pragma unroll 4
+      for (int k = q; k < nc; k += CB_LANES) acc = fmaT<T>(__ldg(wr + k), __ldg(z + k), acc);
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) x2[row] = __ldg(t + row) + acc;
+    for (int o = CB_LANES / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (row < n && q == 0) x2[row] = __ldg(t + row) + acc;
   }
 }
 
@@ -951,7 +963,8 @@ __global__ void __launch_bounds__(BS) k_coarse_cycle(CoarseCycle<T> c, GridBar* 
   if (done && *done) return;  // uniform: every block reads the same flag, set before this launch
   csr_rows_tpr<0, T>(c.tpr_rf1, c.Rf1, c.b1, nullptr, nullptr, c.b2);
   grid_sync(bar, sc);
-  for (int vb = blockIdx.x; vb < c.gT + c.nc; vb += gridDim.x) coarse_a_block<T>(c.Tm, c.Z, c.b2, c.tvec, c.zvec, c.gT, vb);
+  for (int vb = blockIdx.x; vb < c.gT + c.nc; vb += gridDim.x)
+    coarse_a_block<T>(c.Tm, c.Z, c.b2, c.tvec, c.zvec, c.gT, c.nc, vb);
   grid_sync(bar, sc);
   coarse_b_rows<T>(c.Tm.n, c.nc, c.W, c.tvec, c.zvec, c.x2_2, (int)blockIdx.x, (int)gridDim.x);
   grid_sync(bar, sc);
