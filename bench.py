@@ -74,6 +74,9 @@ def parse():
                          "profiling their kernels)")
     ap.add_argument("--fuse-restrict", choices=["auto", "off"], default="auto",
                     help="fused restrictions R(I - A S) in the V-cycle: the autotuner's choice, or off (for A/B)")
+    ap.add_argument("--coarse-cycle", choices=["auto", "off"], default="auto",
+                    help="V-cycle levels 1-3 in one cooperative launch: the autotuner's choice, or off (under a "
+                         "profiler that serialises launches the tuner favours the one launch)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled PCG loop instead of the CUDA graph (for per-kernel launch lists)")
     ap.add_argument("--ref-budget-s", type=float, default=150.0, help="reference arm: cap on timed seconds")
@@ -515,6 +518,8 @@ def run_ours(a):
     tune_s = time.perf_counter() - t0
     if a.fuse_restrict == "off":
         prob.set_option("fuse_restrict", 0)
+    if a.coarse_cycle == "off":
+        prob.set_option("coarse_cycle", 0)
     if a.no_graph:
         prob.set_option("graph", 0)
     N = s.N
@@ -695,6 +700,7 @@ def run_ours(a):
                        "autotune": {"seconds": tune_s, "operators_tuned": len(tune["operators"]),
                                     "coarse_fuse": tune["coarse_fuse"]["chosen"],
                                     "fuse_restrict": tune.get("fuse_restrict"),
+                                    "coarse_cycle": tune.get("coarse_cycle"),
                                     "fuse_restrict_used": a.fuse_restrict,
                                     "shapes": {f"{o['op']}{o['level']}_{o['precision']}":
                                                ("sell" if o["tpr"] == 1 else f"csr{o['tpr']}")

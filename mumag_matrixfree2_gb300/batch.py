@@ -36,8 +36,9 @@ class ParticleResult:
 
 
 def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64", params: MinimizerParams | None = None,
-                 seed: int = 0) -> ParticleResult:
-    """Mesh, set up and sweep one particle (called from a worker thread)."""
+                 seed: int = 0, theta_e3: int = 0) -> ParticleResult:
+    """Mesh, set up and sweep one particle (called from a worker thread); theta_e3 > 0 sets the
+    hierarchy's strength threshold (MM_OPT_SA_THETA_E3)."""
     t0 = time.perf_counter()
     knt, ijk = syn.ellipsoid_mesh(p)
     A, K1, Js, k, Js_ref = syn.reduced_materials([p.material, syn.AIR])
@@ -45,6 +46,8 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
     prob = fem_utils.make_problem(s)
     if precision != "fp64":
         prob.set_precision(precision)
+    if theta_e3 > 0:
+        prob.set_option("sa_theta_e3", theta_e3)
     prob.build_poisson(1e-12, "amgcl")
     avg = NodalAverages(s.geom.conn, s.geom.volume, s.geom.mat_id, s.Js_lookup, s.N)
     prm = params or MinimizerParams(method="pcohen_hs", tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10)
@@ -65,7 +68,7 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
 
 
 def run_batch(particles, B_T, h_dir=(0.0, 0.0, 1.0), workers: int = 16, precision: str = "fp64",
-              params: MinimizerParams | None = None) -> dict:
+              params: MinimizerParams | None = None, theta_e3: int = 0) -> dict:
     """Sweep every particle through B_T [T] with `workers` concurrent host threads (one problem and
     CUDA stream each).  Returns per-particle results and the aggregate throughput."""
     import torch
@@ -76,7 +79,7 @@ def run_batch(particles, B_T, h_dir=(0.0, 0.0, 1.0), workers: int = 16, precisio
 
     def job(i):
         torch.cuda.set_device(dev)
-        r = run_particle(i, particles[i], B_T, h_dir, precision, params)
+        r = run_particle(i, particles[i], B_T, h_dir, precision, params, theta_e3=theta_e3)
         with lock:
             done.append(r)
         return r
