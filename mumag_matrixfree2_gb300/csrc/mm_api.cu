@@ -1667,6 +1667,9 @@ void capture_nested_while(mm_problem* h, cudaGraphConditionalHandle hnd, Body&& 
   } catch (const Fail& f) {
     ok = false;
     err = f;
+  } catch (...) {  // the capture is ended and the stream restored whatever the body threw
+    ok = false;
+    err = Fail{MM_ERR_STATE, "minimizer graph: capture of a loop body failed"};
   }
   h->st = saved;
   --h->cap_depth;
@@ -1874,7 +1877,7 @@ bool minimize_graph(mm_problem* h, MinCtx& c, double* m, double* U, double E0, b
           LAUNCH_CHECK();
           ng.per_outer = (h->n_launch - o0) - ls_body;
         });
-      } catch (const Fail&) {
+      } catch (...) {
         ok = false;
       }
       cudaGraph_t out = nullptr;
