@@ -734,7 +734,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     cc.Z = S.Z;
     cc.W = S.W;
     cc.nc = S.fc;
-    cc.gT = grid_rows(S.fn, 32);
+    cc.gT = grid_rows(S.fn, mmk::CA_LANES);
     cc.tvec = S.tvec;
     cc.zvec = S.zvec;
     cc.x2_2 = l2.x2;
@@ -761,7 +761,7 @@ void enqueue_vcycle(mm_problem* h, SolverT<T>& S, const T* r, T* z, bool in_loop
     tagged<T>(h, MM_PROF_COARSE_A, L - 2,
               4.0 * tbytes + (4.0 + w) * (double)S.Tm_nnz + w * ((double)nc * n + 2.0 * n + nc),
               [&] {
-                const int gT = grid_rows(n, 32);
+                const int gT = grid_rows(n, mmk::CA_LANES);
                 launch(h, mmk::k_coarse_a<T>, gT + nc, BS, S.Tm, S.Z, nc, c.b, S.tvec, S.zvec, gT, done);
                 LAUNCH_CHECK();
               });

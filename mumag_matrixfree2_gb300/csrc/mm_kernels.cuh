@@ -800,23 +800,26 @@ __global__ void __launch_bounds__(BS) k_dense_mv(int n, const T* __restrict__ Ai
 // Fused coarse correction, first phase.  Block r < nc computes z_r = (Z b)_r for one row of the dense
 // nc x n matrix Z = Ainv R (I - A S) with all its threads (fixed-order block sum) - these long dot
 // products go first, so that they overlap the rest instead of forming the kernel's tail; blocks
-// nc .. nc + gT compute t = T b, one warp per row of T (compressed rows of T = 2S - S A S on level
-// L-2).  Both read only b, the restricted residual of level L-2.
+// nc .. nc + gT compute t = T b with CA_LANES lanes per row of T (compressed rows of T = 2S - S A S on
+// level L-2, several hundred entries each; a warp per row: eight lanes per row, with fewer FP64
+// reduction steps but a quarter of the warps, made the 80 nm cube's kernel 20 -> 24 us slower).
+// Both read only b, the restricted residual of level L-2.
 // virtual block vb of nc + gT (the kernel's own block, or one of the one-launch coarse cycle's)
+constexpr int CA_LANES = 32;
+
 template <class T>
 __device__ __forceinline__ void coarse_a_block(const CsrT<T>& Tm, const T* __restrict__ Z, const T* __restrict__ b,
                                                T* __restrict__ t, T* __restrict__ z, int gT, int nc, int vb) {
   const int n = Tm.n;
   if (vb >= nc) {
+    constexpr int RPB = BS / CA_LANES;
     const int tb = vb - nc;
-    const int lane = threadIdx.x & 31;
-    for (int row = tb * (BS / 32) + threadIdx.x / 32; row < n; row += gT * (BS / 32)) {
-      T acc = T(0);
-      const int e = __ldg(Tm.ptr + row + 1);
-      for (int k = __ldg(Tm.ptr + row) + lane; k < e; k += 32) acc = fmaT<T>(__ldg(Tm.val + k), __ldg(b + __ldg(Tm.col + k)), acc);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) t[row] = acc;
+    const int lane = threadIdx.x % CA_LANES;
+    for (int rb = tb * RPB; rb < n; rb += gT * RPB) {
+      const int row = rb + threadIdx.x / CA_LANES;
+      const bool valid = row < n;
+      const T acc = csr_row<CA_LANES, T>(Tm, b, row, valid, lane);
+      if (valid && lane == 0) t[row] = acc;
     }
   } else {
     const int r = vb;
