@@ -747,11 +747,11 @@ static double power_rho(const HostCSR& A, const std::vector<double>& d, int step
   return safety * lam;
 }
 
-std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
+static std::vector<AmgLevel> build_amg_theta(const HostCSR& A0, const AmgParams& prm, double theta0) {
   std::vector<AmgLevel> levels;
   levels.reserve(prm.max_levels);
   HostCSR next = A0;
-  double theta = prm.theta0;
+  double theta = theta0;
   while (true) {
     levels.emplace_back();
     AmgLevel& L = levels.back();
@@ -813,6 +813,13 @@ std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
     L.agg = std::move(agg);
     theta *= 0.5;
   }
+  return levels;
+}
+
+std::vector<AmgLevel> build_amg(const HostCSR& A0, const AmgParams& prm) {
+  if (prm.theta0 > 0.0) return build_amg_theta(A0, prm, prm.theta0);
+  std::vector<AmgLevel> levels = build_amg_theta(A0, prm, 0.115);
+  if (levels.size() > 4) levels = build_amg_theta(A0, prm, 0.1);
   return levels;
 }
 

@@ -134,7 +134,8 @@ Csr multiply(const Csr& A, const Csr& B) {
 // ----------------------------------------------------------------------------------------------
 // smoothed-aggregation hierarchy and the PCG that stands in for PARDISO's direct solve
 // ----------------------------------------------------------------------------------------------
-constexpr double kTheta = 0.12;    // strength threshold on the finest level, halved per coarser level
+constexpr double kTheta = 0.115;   // strength threshold on the finest level, halved per coarser level
+constexpr double kThetaFallback = 0.1;  // when kTheta gives more than four levels
 constexpr int kMaxCoarse = 1000;   // the coarsest level is factorised densely
 constexpr int kMaxLevels = 10;
 constexpr int kMaxIter = 2000;
@@ -382,12 +383,11 @@ bool read_matrix(int n, const double* a, const int* ia, const int* ja, int base,
     return true;
 }
 
-Solver* build_solver(Csr&& A0) {
+Solver* build_solver_theta(const Csr& A0, double theta) {
     auto* s = new Solver();
     s->n = A0.n;
     s->lv.emplace_back();
-    s->lv.back().A = std::move(A0);
-    double theta = kTheta;
+    s->lv.back().A = A0;
     while (static_cast<int>(s->lv.size()) < kMaxLevels && s->lv.back().A.n > kMaxCoarse) {
         Level& f = s->lv.back();
         std::vector<int> agg;
@@ -407,6 +407,15 @@ Solver* build_solver(Csr&& A0) {
     if (!dense_cholesky(c.A, s->chol)) {
         delete s;
         return nullptr;
+    }
+    return s;
+}
+
+Solver* build_solver(Csr&& A0) {
+    Solver* s = build_solver_theta(A0, kTheta);
+    if (s && s->lv.size() > 4) {
+        delete s;
+        s = build_solver_theta(A0, kThetaFallback);
     }
     return s;
 }

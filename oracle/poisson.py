@@ -6,8 +6,8 @@ The reference builds its hierarchy with PyAMG (``src/poisson_solve.py:596-598``)
 The hierarchy here is the project's own smoothed aggregation, the same algorithm the product's C++
 setup implements; integer aggregation must match it bit for bit:
 
-* symmetric strength: off-diagonal a_ij is strong when a_ij^2 > theta^2 |a_ii a_jj|, theta = 0.12 on
-  the finest level, halved on every coarser level;
+* symmetric strength: off-diagonal a_ij is strong when a_ij^2 > theta^2 |a_ii a_jj|, theta = 0.115
+  on the finest level (0.1 when 0.115 gives more than four levels), halved on every coarser level;
 * standard three-pass greedy aggregation in node order (Vanek, Mandel and Brezina 1996): (1) a node
   whose strong neighbours are all free seeds an aggregate with them; (2) a free node joins the
   aggregate of its first aggregated strong neighbour (aggregates as they stood after pass 1);
@@ -30,7 +30,8 @@ import scipy.sparse as sp
 
 from .fem import spai0_diagonal
 
-THETA0 = 0.12
+THETA0 = 0.115
+THETA0_FALLBACK = 0.1  # when THETA0 gives more than four levels
 RHO_STEPS = 20
 RHO_SAFETY = 1.05
 
@@ -155,8 +156,13 @@ class Hierarchy:
     levels: list[Level] = field(default_factory=list)
 
 
-def build_hierarchy(A: sp.csr_matrix, max_levels: int = 10, max_coarse: int = 1000, theta0: float = THETA0) -> Hierarchy:
-    """SA-AMG setup (the project's own restatement; the reference calls PyAMG here)."""
+def build_hierarchy(A: sp.csr_matrix, max_levels: int = 10, max_coarse: int = 1000,
+                    theta0: float | None = None) -> Hierarchy:
+    """SA-AMG setup (the project's own restatement; the reference calls PyAMG here).  Without theta0:
+    THETA0, or THETA0_FALLBACK when THETA0 gives more than four levels."""
+    if theta0 is None:
+        H = build_hierarchy(A, max_levels, max_coarse, THETA0)
+        return H if len(H.levels) <= 4 else build_hierarchy(A, max_levels, max_coarse, THETA0_FALLBACK)
     H = Hierarchy()
     Acur = A.tocsr()
     Acur.sort_indices()
