@@ -1,9 +1,9 @@
 """Learned demag warm start on the GPU (no counterpart in the reference).
 
 A 3D U-Net (``mm_unet_*`` in libmumag_cuda) predicts the change of the demag potential caused by a
-change of magnetisation, from the voxelised change of m and the voxelised previous potential.  The
-demag solve then starts from ``U_last + interp(prediction)`` instead of ``U_last`` and runs PCG to the
-same tolerance, so the plain solver stays the judge of the prediction.
+change of magnetisation, from the voxelised change of m (and, optionally, the voxelised previous
+potential).  The demag solve then starts from ``U_last + interp(prediction)`` instead of ``U_last``
+and runs PCG to the same tolerance, so the result does not depend on the prediction's quality.
 
 Because the potential is linear in m (A U = D m), the map the network learns is the linear demag
 operator applied to dm; inputs and targets are normalised by the largest |dm| so that one network
