@@ -373,6 +373,27 @@ def test_device_minimizer_graph_equals_host_loop(cuda_ok, method, precision, cpp
         assert np.array_equal(mg, mh) and np.array_equal(Ug, Uh)
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "none"])
+def test_device_minimizer_graph_with_single_level_preconditioners(cuda_ok, precond):
+    """The minimizer graph with the Jacobi or no preconditioner in its demag solves (one-level
+    preconditioners; a copy node that a conditional body cannot hold makes the capture fall back to
+    the host loop): the same counts and state as the host-driven loop either way."""
+    s, p, _ = case("cube8_h2_air24")
+    m0 = random_state(p.N, seed=21, amplitude=0.2)
+    out = {}
+    for g in (1, 0):
+        prob = fem_utils.make_problem(s)
+        prob.build_poisson(1e-12, precond)
+        prob.set_option("min_graph", g)
+        mp = MinimizerParams(method="pcohen_hs", max_iter=25, tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10)
+        out[g] = prob.minimize(np.array([0.0, 0.0, -0.3]), m0, np.zeros(p.N), mp)
+    (mg, Ug, ig), (mh, Uh, ih) = out[1], out[0]
+    assert not ih["device_loop"]
+    for k in ("iters", "evals", "preco_iters", "demag_iters"):
+        assert ig[k] == ih[k], (k, ig[k], ih[k])
+    assert np.array_equal(mg, mh) and np.array_equal(Ug, Uh)
+
+
 @pytest.mark.parametrize("name", ["cube8_h2_air24", "cube40_h2_air200"])
 def test_mixed_precision_meets_the_fp64_tolerance(cuda_ok, name):
     """FP32 correction solves inside FP64 iterative refinement: the true FP64 residual meets the
