@@ -368,9 +368,11 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
  * mm_autotune chooses per operator among these and one thread per row. */
 #define MM_OPT_CSR_LANES 17
 /* MM_OPT_SA_THETA_E3 (before mm_build_poisson): the smoothed-aggregation strength threshold on the
- * finest level in thousandths (halved per coarser level); 0 (default): 0.115, or 0.1 when 0.115
- * gives more than four levels. */
+ * finest level in thousandths; 0 (default): 0.115, or 0.1 when 0.115 gives more than four levels. */
 #define MM_OPT_SA_THETA_E3 18
+/* MM_OPT_SA_FACTOR_E3 (before mm_build_poisson): each coarser level's strength threshold as a
+ * multiple of the finer level's, in thousandths; 0 (default): 0.35. */
+#define MM_OPT_SA_FACTOR_E3 19
 int mm_set_option(mm_problem* h, int option, int value);
 /* The current value of MM_OPT_COARSE_CYCLE, MM_OPT_FUSE_RESTRICT, MM_OPT_COARSE_FUSE,
  * MM_OPT_ENERGY_FF_LANES or MM_OPT_MIN_GRAPH (after mm_autotune, or after a loop graph that could not

@@ -220,6 +220,7 @@ struct mm_problem {
   int fuse_restrict = 3;         // MM_OPT_FUSE_RESTRICT: bit 0 the FP64 solver, bit 1 the FP32 solver
   int coarse_cycle = 0;          // MM_OPT_COARSE_CYCLE: bit 0 the FP64 solver, bit 1 the FP32 solver
   int sa_theta_e3 = 0;           // MM_OPT_SA_THETA_E3 (0: the setup's default)
+  int sa_factor_e3 = 0;          // MM_OPT_SA_FACTOR_E3 (0: the setup's default)
   std::vector<mm::HostCSR> rf_host;  // fused restrictions R_l (I - A_l S_l), formed for smoother rf_prec
   int rf_prec = -1;
 
@@ -3087,6 +3088,7 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
       prm.max_levels = max_levels > 0 ? max_levels : 10;
       prm.max_coarse = max_coarse > 0 ? max_coarse : 1000;
       if (h->sa_theta_e3 > 0) prm.theta0 = 1e-3 * h->sa_theta_e3;
+      if (h->sa_factor_e3 > 0) prm.theta_factor = 1e-3 * h->sa_factor_e3;
       h->amg_h = mm::build_amg(A, prm);
     } else {
       h->amg_h.clear();
@@ -3779,6 +3781,12 @@ int mm_set_option(mm_problem* h, int option, int value) {
       drop_graph(h->s32);
     }
     h->fuse_restrict = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_SA_FACTOR_E3) {
+    if (value < 0 || value > 1000) return MM_ERR_ARG;
+    if (h->poisson_built) return MM_ERR_STATE;
+    h->sa_factor_e3 = value;
     return MM_OK;
   }
   if (option == MM_OPT_SA_THETA_E3) {

@@ -811,7 +811,7 @@ static std::vector<AmgLevel> build_amg_theta(const HostCSR& A0, const AmgParams&
     L.P = std::move(P);
     L.R = std::move(R);
     L.agg = std::move(agg);
-    theta *= 0.5;
+    theta *= prm.theta_factor;
   }
   return levels;
 }

@@ -134,7 +134,8 @@ Csr multiply(const Csr& A, const Csr& B) {
 // ----------------------------------------------------------------------------------------------
 // smoothed-aggregation hierarchy and the PCG that stands in for PARDISO's direct solve
 // ----------------------------------------------------------------------------------------------
-constexpr double kTheta = 0.115;   // strength threshold on the finest level, halved per coarser level
+constexpr double kTheta = 0.115;   // strength threshold on the finest level
+constexpr double kThetaFactor = 0.35;  // each coarser level's threshold relative to the finer one
 constexpr double kThetaFallback = 0.1;  // when kTheta gives more than four levels
 constexpr int kMaxCoarse = 1000;   // the coarsest level is factorised densely
 constexpr int kMaxLevels = 10;
@@ -392,7 +393,7 @@ Solver* build_solver_theta(const Csr& A0, double theta) {
         Level& f = s->lv.back();
         std::vector<int> agg;
         const int na = aggregate(f.A, theta, agg);
-        theta *= 0.5;
+        theta *= kThetaFactor;
         if (na == 0 || na >= f.A.n) break;
         f.P = prolongator(f.A, agg, na);
         f.R = transpose(f.P);

@@ -7,7 +7,7 @@ The hierarchy here is the project's own smoothed aggregation, the same algorithm
 setup implements; integer aggregation must match it bit for bit:
 
 * symmetric strength: off-diagonal a_ij is strong when a_ij^2 > theta^2 |a_ii a_jj|, theta = 0.115
-  on the finest level (0.1 when 0.115 gives more than four levels), halved on every coarser level;
+  on the finest level (0.1 when 0.115 gives more than four levels), times 0.35 on every coarser level;
 * standard three-pass greedy aggregation in node order (Vanek, Mandel and Brezina 1996): (1) a node
   whose strong neighbours are all free seeds an aggregate with them; (2) a free node joins the
   aggregate of its first aggregated strong neighbour (aggregates as they stood after pass 1);
@@ -32,6 +32,7 @@ from .fem import spai0_diagonal
 
 THETA0 = 0.115
 THETA0_FALLBACK = 0.1  # when THETA0 gives more than four levels
+THETA_FACTOR = 0.35    # each coarser level's threshold relative to the finer one
 RHO_STEPS = 20
 RHO_SAFETY = 1.05
 
@@ -185,7 +186,7 @@ def build_hierarchy(A: sp.csr_matrix, max_levels: int = 10, max_coarse: int = 10
         Ac.sort_indices()
         lvl.P, lvl.R, lvl.agg = P, R, agg
         Acur = Ac
-        theta *= 0.5
+        theta *= THETA_FACTOR
     last = H.levels[-1]
     last.A_inv = np.linalg.inv(last.A.toarray())
     return H
