@@ -486,6 +486,8 @@ def run_batch_leg(a):
     B = syn.field_values(6.0, -6.0, 0.1)
     r = batch.run_batch(ps, B, workers=a.batch_workers, precision=a.batch_precision)
     res = r.pop("results")
+    # the device's kernel rate while the sweeps run (launches of all particles over the sweeps' mean wall time)
+    r["gpu_launches_per_s_in_sweeps"] = r["gpu_launches_total"] / max(1e-9, r["sweep_s_total"] / r["workers"])
     r["Hc_T"] = {"p50": float(np.percentile([x.Hc_T for x in res], 50)),
                  "min": float(min(x.Hc_T for x in res)), "max": float(max(x.Hc_T for x in res))}
     r["workload"] = (f"{len(ps)} of 256 ellipsoids (seed 0), +6 T -> -6 T in 0.1 T steps along z, pcohen_hs, "

@@ -32,6 +32,7 @@ class ParticleResult:
     J: list = field(default_factory=list)
     pcg_iters: int = 0
     min_iters: int = 0
+    launches: int = 0  # kernels the sweep launched (graph nodes included)
     Hc_T: float = 0.0
 
 
@@ -55,6 +56,7 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
     h = np.asarray(h_dir, np.float64)
     m = syn.initial_state(s.N, seed=seed, direction=tuple(h))
     U = np.zeros(s.N)
+    launches0 = prob.launch_count()
     for B in B_T:
         t1 = time.perf_counter()
         m, U, info = prob.minimize((float(B) / Js_ref) * h, m, U, prm)
@@ -62,6 +64,7 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
         res.J.append(avg.J_parallel(m, h) * Js_ref)
         res.pcg_iters += info["demag_iters"]
         res.min_iters += info["iters"]
+    res.launches = prob.launch_count() - launches0
     res.Hc_T = coercive_field(np.asarray(B_T), np.asarray(res.J))
     prob.close()
     return res
@@ -99,4 +102,5 @@ def run_batch(particles, B_T, h_dir=(0.0, 0.0, 1.0), workers: int = 16, precisio
             "nodes": {"min": int(min(r.nodes for r in done)), "median": int(np.median([r.nodes for r in done])),
                       "max": int(max(r.nodes for r in done)), "total": int(sum(r.nodes for r in done))},
             "pcg_iters_total": int(sum(r.pcg_iters for r in done)),
+            "gpu_launches_total": int(sum(r.launches for r in done)),
             "results": done}

@@ -139,6 +139,33 @@ int choose_tpr(int64_t rows, int64_t nnz) {
 
 thread_local std::string g_create_error;
 
+// Pinned host blocks for the problems' scalar read-backs (Scalars, MinScal), kept in a process-wide
+// free list and never returned: cudaFreeHost waits for the work of every stream on the device, so
+// freeing them with each problem would stall all other problems whenever one is destroyed.
+constexpr size_t PINNED_BLOCK = (std::max(sizeof(mmk::Scalars), sizeof(mmk::MinScal)) + 255) / 256 * 256;
+std::mutex g_pinned_mu;
+std::vector<void*> g_pinned_free;
+
+void* pinned_get() {
+  void* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    if (!g_pinned_free.empty()) {
+      p = g_pinned_free.back();
+      g_pinned_free.pop_back();
+    }
+  }
+  if (!p) CK(cudaHostAlloc(&p, PINNED_BLOCK, cudaHostAllocPortable));
+  std::memset(p, 0, PINNED_BLOCK);
+  return p;
+}
+
+void pinned_put(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned_free.push_back(p);
+}
+
 }  // namespace
 
 struct mm_problem {
@@ -285,17 +312,20 @@ struct mm_problem {
   double* min_bias_buf = nullptr;  // its storage
   cudaEvent_t ev_after = nullptr;  // ordering point taken on another stream (mm_scale_correction_async)
 
+  // Device buffers come from the device's stream-ordered pool on the problem's stream and go back to
+  // it with cudaFreeAsync (mm_destroy): unlike cudaMalloc / cudaFree, neither waits for the work other
+  // problems have queued on the device, so problems can be created and destroyed while others run.
   template <class T>
   T* alloc(size_t n) {
     void* p = nullptr;
     if (n == 0) n = 1;
-    CK(cudaMalloc(&p, n * sizeof(T)));
+    if (!st) throw Fail{MM_ERR_CUDA, "device allocation before the problem's stream exists"};
+    CK(cudaMallocAsync(&p, n * sizeof(T), st));
     allocs.push_back(p);
     // zeroed: reused device memory can hold any bit pattern (a NaN in an FP32 view of old FP64 data),
     // and a vector read once with a zero factor (the first direction's beta p) must not carry it in.
     // On the problem's own stream, ahead of any copy into the buffer (that stream does not order with
     // the legacy default stream).
-    if (!st) throw Fail{MM_ERR_CUDA, "device allocation before the problem's stream exists"};
     CK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
     return (T*)p;
   }
@@ -1767,7 +1797,7 @@ bool minimize_graph(mm_problem* h, MinCtx& c, double* m, double* U, double E0, b
   if (mp) h->use_a0df();
   if (!h->d_ms) {
     h->d_ms = h->alloc<mmk::MinScal>(1);
-    CK(cudaMallocHost(&h->h_ms, sizeof(mmk::MinScal)));
+    h->h_ms = (mmk::MinScal*)pinned_get();
   }
   double* graw = h->w_graw;
   const std::vector<uintptr_t> key = {
@@ -2857,6 +2887,7 @@ int mm_setup_create(int N, int E, const int* conn, const double* volume, const d
   *out = nullptr;
   mm_setup* s = new mm_setup();
   const int rc = guarded(nullptr, [&] {
+    mm::SetupScope scope;
     for (int e = 0; e < 4 * E; ++e)
       if (conn[e] < 0 || conn[e] >= N) throw Fail{MM_ERR_ARG, "connectivity index out of range"};
     s->eop = mm::assemble_energy(N, E, conn, volume, grad_phi, mat_id, n_mat, A_lookup, K1_lookup, Js_lookup, k_easy);
@@ -2983,6 +3014,7 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     h->grad_phi.assign(grad_phi, grad_phi + 12 * (size_t)E);
     h->has_mask = boundary_mask != nullptr;
     if (h->has_mask) h->mask_h.assign(boundary_mask, boundary_mask + N);
+    mm::SetupScope scope;
     h->eop_h = mm::assemble_energy(N, E, conn, volume, grad_phi, mat_id, n_mat, A_lookup, K1_lookup, Js_lookup,
                                    k_easy);
     const mm::EnergyOp& o = h->eop_h;
@@ -3038,7 +3070,7 @@ int mm_create(int N, int E, const int* conn, const double* volume, const double*
     CK(cudaMemsetAsync(h->d_sc, 0, sizeof(mmk::Scalars), h->st));  // ticket counters start at zero
     h->d_sc32 = h->alloc<mmk::Scalars>(1);
     CK(cudaMemsetAsync(h->d_sc32, 0, sizeof(mmk::Scalars), h->st));
-    CK(cudaMallocHost(&h->h_sc, sizeof(mmk::Scalars)));
+    h->h_sc = (mmk::Scalars*)pinned_get();
     h->sync();
     return MM_OK;
   });
@@ -3062,9 +3094,14 @@ int mm_destroy(mm_problem* h) {
   h->drop_inner_graphs();
   for (cudaStream_t a : h->aux_st)
     if (a) cudaStreamDestroy(a);
-  for (void* p : h->allocs) cudaFree(p);
-  if (h->h_sc) cudaFreeHost(h->h_sc);
-  if (h->h_ms) cudaFreeHost(h->h_ms);
+  // stream-ordered frees behind everything the stream holds (it was synchronized above); the stream
+  // is destroyed below without a wait, and the pool takes the memory back when the stream reaches them
+  for (void* p : h->allocs) {
+    if (h->st) cudaFreeAsync(p, h->st);
+    else cudaFree(p);
+  }
+  pinned_put(h->h_sc);
+  pinned_put(h->h_ms);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_after) cudaEventDestroy(h->ev_after);
@@ -3078,6 +3115,7 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
   if (!h || precond_type < MM_PRECOND_NONE || precond_type > MM_PRECOND_AMGCL) return MM_ERR_ARG;
   return guarded(h, [&] {
     if (h->poisson_built) throw Fail{MM_ERR_STATE, "Poisson operator already built"};
+    mm::SetupScope scope;
     h->reg = reg;
     h->precond = precond_type;
     mm::HostCSR A = mm::assemble_poisson(h->N, h->E, h->conn.data(), h->volume.data(), h->grad_phi.data(),

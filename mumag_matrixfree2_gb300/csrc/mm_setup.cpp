@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <numeric>
 #include <stdexcept>
@@ -12,11 +13,20 @@
 
 namespace mm {
 
-// Host threads of the setup: the machine's hardware threads, at most 16.
+static std::atomic<int> g_active_setups{0};
+
+SetupScope::SetupScope() { g_active_setups.fetch_add(1, std::memory_order_relaxed); }
+SetupScope::~SetupScope() { g_active_setups.fetch_sub(1, std::memory_order_relaxed); }
+
+// Host threads of one parallel pass: the machine's hardware threads (at most 16) shared among the
+// setups running at once, and no more than one per 4,096 items.  The thread count changes only the
+// speed: every pass gives the same result for any count.
 static int setup_threads(int64_t n) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int active = std::max(1, g_active_setups.load(std::memory_order_relaxed));
+  const int64_t budget = std::max<int64_t>(1, (int64_t)hw / active);
   const int64_t by_work = std::max<int64_t>(1, n / 4096);
-  return (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), by_work);
+  return (int)std::min<int64_t>(budget, by_work);
 }
 
 // f(t, begin, end) on contiguous chunks of [0, n), one chunk per thread (chunk t of nt in order), so

@@ -80,6 +80,16 @@ struct AmgParams {
   double rho_safety = 1.05;
 };
 
+// Counts the setups running at once in this process while it lives: each parallel pass of a setup
+// takes the host's threads (at most 16) divided by that count, so that many problems set up
+// concurrently (one per host thread) share the cores instead of each spawning 16 threads.
+struct SetupScope {
+  SetupScope();
+  ~SetupScope();
+  SetupScope(const SetupScope&) = delete;
+  SetupScope& operator=(const SetupScope&) = delete;
+};
+
 // geometry (src/loop.py:56-102)
 void geom_compute(int N, int E, const double* knt, const int* conn_in, int* conn_out, double* volume,
                   double* JinvT, double* grad_phi);

@@ -103,3 +103,30 @@ def test_rcm_order_equals_scipy(name):
     # the renumbered mesh has a smaller bandwidth than the grid order
     bw = lambda c: int(np.max(np.ptp(c, axis=1)))  # noqa: E731
     assert bw(inv[conn]) < bw(conn)
+
+
+def test_concurrent_setups_equal_a_lone_setup():
+    """Setups running at once share the host's threads (fewer threads per parallel pass); every pass
+    gives the same result for any thread count, so each concurrent hierarchy equals a lone one bit for
+    bit.  The C-ABI calls release the GIL, so the four setups overlap."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    s, _, _ = case("cube40_h2_air200")
+
+    def build(_=None):
+        hs = _abi.HostSetup(s.geom.conn, s.geom.volume, s.geom.grad_phi, s.geom.mat_id, s.A_lookup, s.K1_lookup,
+                            s.Js_lookup, s.k_easy, mask=s.boundary_mask, n_nodes=s.N)
+        return hs.energy_op(), hs.levels()
+
+    e0, lv0 = build()
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        runs = list(ex.map(build, range(4)))
+    for e, lv in runs:
+        for k in ("rows", "ptr", "col", "mat", "w", "q", "G", "D", "diag_exchange"):
+            assert np.array_equal(e[k], e0[k]), k
+        assert len(lv) == len(lv0)
+        for a, b in zip(lv, lv0):
+            assert np.array_equal(a["agg"], b["agg"])
+            for k in ("A", "P"):
+                if k in b:
+                    assert (a[k] != b[k]).nnz == 0 and np.array_equal(a[k].indices, b[k].indices), k
