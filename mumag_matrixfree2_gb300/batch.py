@@ -37,7 +37,7 @@ class ParticleResult:
 
 
 def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64", params: MinimizerParams | None = None,
-                 seed: int = 0, theta_e3: int = 0) -> ParticleResult:
+                 seed: int = 0, theta_e3: int = 0, max_coarse: int = 1000) -> ParticleResult:
     """Mesh, set up and sweep one particle (called from a worker thread); theta_e3 > 0 sets the
     hierarchy's strength threshold (MM_OPT_SA_THETA_E3)."""
     t0 = time.perf_counter()
@@ -49,7 +49,7 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
         prob.set_precision(precision)
     if theta_e3 > 0:
         prob.set_option("sa_theta_e3", theta_e3)
-    prob.build_poisson(1e-12, "amgcl")
+    prob.build_poisson(1e-12, "amgcl", max_coarse=max_coarse)
     avg = NodalAverages(s.geom.conn, s.geom.volume, s.geom.mat_id, s.Js_lookup, s.N)
     prm = params or MinimizerParams(method="pcohen_hs", tau_f=1e-8, eps_a=1e-6, cg_tol=1e-10, pc_iters=10)
     res = ParticleResult(index, s.N, int(ijk.shape[0]), time.perf_counter() - t0)
@@ -71,7 +71,7 @@ def run_particle(index: int, p: syn.Particle, B_T, h_dir, precision: str = "fp64
 
 
 def run_batch(particles, B_T, h_dir=(0.0, 0.0, 1.0), workers: int = 16, precision: str = "fp64",
-              params: MinimizerParams | None = None, theta_e3: int = 0) -> dict:
+              params: MinimizerParams | None = None, theta_e3: int = 0, max_coarse: int = 1000) -> dict:
     """Sweep every particle through B_T [T] with `workers` concurrent host threads (one problem and
     CUDA stream each).  Returns per-particle results and the aggregate throughput."""
     import torch
@@ -82,7 +82,7 @@ def run_batch(particles, B_T, h_dir=(0.0, 0.0, 1.0), workers: int = 16, precisio
 
     def job(i):
         torch.cuda.set_device(dev)
-        r = run_particle(i, particles[i], B_T, h_dir, precision, params, theta_e3=theta_e3)
+        r = run_particle(i, particles[i], B_T, h_dir, precision, params, theta_e3=theta_e3, max_coarse=max_coarse)
         with lock:
             done.append(r)
         return r

@@ -250,6 +250,19 @@ struct mm_problem {
   int sa_factor_e3 = 0;          // MM_OPT_SA_FACTOR_E3 (0: the setup's default)
   std::vector<mm::HostCSR> rf_host;  // fused restrictions R_l (I - A_l S_l), formed for smoother rf_prec
   int rf_prec = -1;
+  // host factors shared by the FP64 and FP32 copies of the hierarchy (formed once, O(nc^3) and
+  // O(nc^2 n)): the coarsest level's dense inverse and the fused coarse correction for smoother fc_prec
+  std::vector<double> ainv_host;
+  struct FusedCoarseHost {
+    bool ok = false;
+    std::vector<double> tv, W, Z;
+  };
+  FusedCoarseHost fc_host;
+  int fc_prec = -1;
+  const std::vector<double>& coarse_inverse() {
+    if (ainv_host.empty()) ainv_host = mm::dense_inverse(amg_h.back().A);
+    return ainv_host;
+  }
 
   // staging buffers for host-pointer calls
   double *d_m = nullptr, *d_U = nullptr, *d_g = nullptr, *d_v = nullptr, *d_out = nullptr, *d_bias = nullptr;
@@ -2653,12 +2666,13 @@ extern "C" int mm_energy_grad_noalloc(mm_problem* h, const double* d_m, const do
 // L-2 .. L-1 map the restricted residual b to the post-smoothed iterate
 //   x2 = (I - S A) (S + P Ainv R (I - A S)) b + S b = T b + W (Z b),
 //   T = 2S - S A S (A's pattern), W = (I - S A) P (n x nc), Z = Ainv R (I - A S) (nc x n).
-template <class T>
-void build_fused_coarse(mm_problem* h, SolverT<T>& S, int precond_type) {
+// The host factors T, W, Z in FP64 (fc.ok false when a row of A has no stored diagonal).
+void form_fused_coarse(mm_problem* h, int precond_type, mm_problem::FusedCoarseHost& fc) {
   const int L = (int)h->amg_h.size();
   const mm::AmgLevel& a = h->amg_h[L - 2];
   const mm::HostCSR &A = a.A, &P = a.P, &R = a.R;
   const int n = A.n_rows, nc = h->amg_h[L - 1].A.n_rows;
+  fc = mm_problem::FusedCoarseHost{};
   std::vector<double> sd(n);
   for (int i = 0; i < n; ++i) sd[i] = precond_type == MM_PRECOND_AMGCL ? a.spai0[i] : 0.6667 / (a.diag[i] + 1e-30);
   std::vector<double> tv(A.nnz());
@@ -2686,7 +2700,7 @@ void build_fused_coarse(mm_problem* h, SolverT<T>& S, int precond_type) {
       const int row = R.col[k];
       for (int q = A.ptr[row]; q < A.ptr[row + 1]; ++q) M[(size_t)r * n + A.col[q]] -= R.val[k] * A.val[q] * sd[A.col[q]];
     }
-  const std::vector<double> Ainv = mm::dense_inverse(h->amg_h[L - 1].A);
+  const std::vector<double>& Ainv = h->coarse_inverse();
   std::vector<double> Zd((size_t)nc * n, 0.0);
   for (int r = 0; r < nc; ++r)
     for (int q = 0; q < nc; ++q) {
@@ -2695,13 +2709,30 @@ void build_fused_coarse(mm_problem* h, SolverT<T>& S, int precond_type) {
       double* zr = &Zd[(size_t)r * n];
       for (int j = 0; j < n; ++j) zr[j] += c * mq[j];
     }
+  fc.tv = std::move(tv);
+  fc.W = std::move(Wd);
+  fc.Z = std::move(Zd);
+  fc.ok = true;
+}
+
+template <class T>
+void build_fused_coarse(mm_problem* h, SolverT<T>& S, int precond_type) {
+  if (h->fc_prec != precond_type) {
+    form_fused_coarse(h, precond_type, h->fc_host);
+    h->fc_prec = precond_type;
+  }
+  const mm_problem::FusedCoarseHost& fc = h->fc_host;
+  if (!fc.ok) return;
+  const int L = (int)h->amg_h.size();
+  const mm::HostCSR& A = h->amg_h[L - 2].A;
+  const int n = A.n_rows, nc = h->amg_h[L - 1].A.n_rows;
   S.Tm.n = n;
   S.Tm.ptr = h->upload(A.ptr);
   S.Tm.col = h->upload(A.col);
-  S.Tm.val = h->upload_as<T>(tv);
+  S.Tm.val = h->upload_as<T>(fc.tv);
   S.Tm_nnz = A.nnz();
-  S.W = h->upload_as<T>(Wd);
-  S.Z = h->upload_as<T>(Zd);
+  S.W = h->upload_as<T>(fc.W);
+  S.Z = h->upload_as<T>(fc.Z);
   S.tvec = h->alloc<T>(n);
   S.zvec = h->alloc<T>(nc);
   S.fn = n;
@@ -2752,7 +2783,7 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
   if (amg) {
     const mm::HostCSR& Ac = h->amg_h.back().A;
     S.n_coarse = Ac.n_rows;
-    S.Ainv = h->upload_as<T>(mm::dense_inverse(Ac));
+    S.Ainv = h->upload_as<T>(h->coarse_inverse());
   } else {
     std::vector<double> jac(h->N, 1.0), dg(h->N, 0.0);
     for (int r = 0; r < A.n_rows; ++r)
