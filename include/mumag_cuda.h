@@ -373,6 +373,10 @@ int mm_time_kernel(mm_problem* h, int kernel, int reps, double* ms_per_launch, d
 /* MM_OPT_SA_FACTOR_E3 (before mm_build_poisson): each coarser level's strength threshold as a
  * multiple of the finer level's, in thousandths; 0 (default): 0.35. */
 #define MM_OPT_SA_FACTOR_E3 19
+/* MM_OPT_SA_FILTER_E6 (before mm_build_poisson): the level-1 operator's weak couplings
+ * (|a_ij| + |a_ji| < 2 eps sqrt(|a_ii a_jj|)) moved into its diagonal, eps in millionths; 0 (default):
+ * 0.002; negative: the plain Galerkin operator. */
+#define MM_OPT_SA_FILTER_E6 20
 int mm_set_option(mm_problem* h, int option, int value);
 /* The current value of MM_OPT_COARSE_CYCLE, MM_OPT_FUSE_RESTRICT, MM_OPT_COARSE_FUSE,
  * MM_OPT_ENERGY_FF_LANES or MM_OPT_MIN_GRAPH (after mm_autotune, or after a loop graph that could not

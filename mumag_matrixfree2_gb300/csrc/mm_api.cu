@@ -248,6 +248,7 @@ struct mm_problem {
   int coarse_cycle = 0;          // MM_OPT_COARSE_CYCLE: bit 0 the FP64 solver, bit 1 the FP32 solver
   int sa_theta_e3 = 0;           // MM_OPT_SA_THETA_E3 (0: the setup's default)
   int sa_factor_e3 = 0;          // MM_OPT_SA_FACTOR_E3 (0: the setup's default)
+  int sa_filter_e6 = 0;          // MM_OPT_SA_FILTER_E6 (0: the setup's default, < 0: no filtering)
   std::vector<mm::HostCSR> rf_host;  // fused restrictions R_l (I - A_l S_l), formed for smoother rf_prec
   int rf_prec = -1;
   // host factors shared by the FP64 and FP32 copies of the hierarchy (formed once, O(nc^3) and
@@ -3158,6 +3159,8 @@ int mm_build_poisson(mm_problem* h, double reg, int precond_type, int max_levels
       prm.max_coarse = max_coarse > 0 ? max_coarse : 1000;
       if (h->sa_theta_e3 > 0) prm.theta0 = 1e-3 * h->sa_theta_e3;
       if (h->sa_factor_e3 > 0) prm.theta_factor = 1e-3 * h->sa_factor_e3;
+      if (h->sa_filter_e6 > 0) prm.filter_eps = 1e-6 * h->sa_filter_e6;
+      if (h->sa_filter_e6 < 0) prm.filter_eps = 0.0;
       h->amg_h = mm::build_amg(A, prm);
     } else {
       h->amg_h.clear();
@@ -3856,6 +3859,12 @@ int mm_set_option(mm_problem* h, int option, int value) {
     if (value < 0 || value > 1000) return MM_ERR_ARG;
     if (h->poisson_built) return MM_ERR_STATE;
     h->sa_factor_e3 = value;
+    return MM_OK;
+  }
+  if (option == MM_OPT_SA_FILTER_E6) {
+    if (value > 100000) return MM_ERR_ARG;
+    if (h->poisson_built) return MM_ERR_STATE;
+    h->sa_filter_e6 = value;
     return MM_OK;
   }
   if (option == MM_OPT_SA_THETA_E3) {

@@ -302,7 +302,7 @@ class Problem:
     OPTIONS = {"graph": 1, "precision": 2, "mixed_eta_e6": 3, "grid_cap": 4, "profile": 5, "pdl": 8,
                "coarse_fuse": 9, "min_fp32": 10, "split_a0": 11, "fuse_restrict": 12, "energy_ff": 13,
                "min_graph": 14, "energy_ff_lanes": 15, "coarse_cycle": 16, "csr_lanes": 17, "sa_theta_e3": 18,
-               "sa_factor_e3": 19}
+               "sa_factor_e3": 19, "sa_filter_e6": 20}
 
     def set_option(self, name: str, value: int):
         self._check("mm_set_option", lib().mm_set_option(self.h, self.OPTIONS[name], int(value)))

@@ -137,6 +137,7 @@ Csr multiply(const Csr& A, const Csr& B) {
 constexpr double kTheta = 0.115;   // strength threshold on the finest level
 constexpr double kThetaFactor = 0.35;  // each coarser level's threshold relative to the finer one
 constexpr double kThetaFallback = 0.1;  // when kTheta gives more than four levels
+constexpr double kFilterEps = 0.002;    // weak couplings of the level-1 operator moved into its diagonal
 constexpr int kMaxCoarse = 1000;   // the coarsest level is factorised densely
 constexpr int kMaxLevels = 10;
 constexpr int kMaxIter = 2000;
@@ -291,6 +292,43 @@ Csr prolongator(const Csr& A, const std::vector<int>& agg, int na) {
     return P;
 }
 
+// A without its weak off-diagonal couplings, |a_ij| + |a_ji| < 2 eps sqrt(|a_ii a_jj|) (a_ji = 0 when
+// not stored), each row's weak values summed from zero in column order and added to its diagonal.
+Csr filter_weak(const Csr& A, double eps) {
+    const int n = A.n;
+    std::vector<double> d(n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int k = A.p[i]; k < A.p[i + 1]; ++k)
+            if (A.c[k] == i) d[i] = A.v[k];
+    auto value_at = [&](int r, int c) {
+        for (int k = A.p[r]; k < A.p[r + 1]; ++k)
+            if (A.c[k] == c) return A.v[k];
+        return 0.0;
+    };
+    Csr B;
+    B.n = n;
+    B.m = A.m;
+    B.p.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        double lump = 0.0;
+        const int first = static_cast<int>(B.c.size());
+        int diag = -1;
+        for (int k = A.p[i]; k < A.p[i + 1]; ++k) {
+            const int j = A.c[k];
+            if (j != i && std::fabs(A.v[k]) + std::fabs(value_at(j, i)) < 2.0 * eps * std::sqrt(std::fabs(d[i] * d[j]))) {
+                lump += A.v[k];
+                continue;
+            }
+            if (j == i) diag = static_cast<int>(B.c.size());
+            B.c.push_back(j);
+            B.v.push_back(A.v[k]);
+        }
+        if (diag >= first && diag >= 0) B.v[diag] = B.v[diag] + lump;
+        B.p[i + 1] = static_cast<int>(B.c.size());
+    }
+    return B;
+}
+
 bool dense_cholesky(const Csr& A, std::vector<double>& L) {
     const int n = A.n;
     L.assign(static_cast<size_t>(n) * n, 0.0);
@@ -399,6 +437,7 @@ Solver* build_solver_theta(const Csr& A0, double theta) {
         f.R = transpose(f.P);
         Csr AP = multiply(f.A, f.P);
         Csr Ac = multiply(f.R, AP);
+        if (s->lv.size() == 1) Ac = filter_weak(Ac, kFilterEps);
         f.sm = spai0(f.A);
         s->lv.emplace_back();
         s->lv.back().A = std::move(Ac);

@@ -18,7 +18,9 @@ setup implements; integer aggregation must match it bit for bit:
   rho(D^-1 A) after 20 steps from a fixed pseudo-random start (Knuth's multiplicative hash of the row
   index), every norm a left-to-right sum so that the C++ setup reproduces it;
 * Galerkin A_c = P^T A P, R = P^T; stop at ``max_coarse`` unknowns or ``max_levels`` levels; dense
-  inverse on the coarsest level.
+  inverse on the coarsest level;
+* the level-1 Galerkin operator without its weak couplings (|a_ij| + |a_ji| < 2 * 0.002 *
+  sqrt(|a_ii a_jj|)), which are added to the diagonal of their row before level 2 is built from it.
 """
 
 from __future__ import annotations
@@ -33,6 +35,7 @@ from .fem import spai0_diagonal
 THETA0 = 0.115
 THETA0_FALLBACK = 0.1  # when THETA0 gives more than four levels
 THETA_FACTOR = 0.35    # each coarser level's threshold relative to the finer one
+FILTER_EPS = 0.002     # weak couplings of the level-1 operator moved into its diagonal
 RHO_STEPS = 20
 RHO_SAFETY = 1.05
 
@@ -141,6 +144,32 @@ def smooth_prolongator(A: sp.csr_matrix, T: sp.csr_matrix) -> sp.csr_matrix:
     return P
 
 
+def filter_weak(A: sp.csr_matrix, eps: float) -> sp.csr_matrix:
+    """A without its weak off-diagonal couplings, |a_ij| + |a_ji| < 2 eps sqrt(|a_ii a_jj|) (a_ji = 0
+    when not stored), each row's weak values summed from zero in column order and added to its
+    diagonal (row sums kept)."""
+    A = A.tocsr()
+    A.sort_indices()
+    n = A.shape[0]
+    rows = np.repeat(np.arange(n), np.diff(A.indptr))
+    cols = A.indices
+    d = A.diagonal()
+    At = A.T.tocsr()
+    At.sort_indices()
+    if np.array_equal(At.indptr, A.indptr) and np.array_equal(At.indices, A.indices):
+        aji = At.data
+    else:
+        aji = np.asarray(A[cols, rows]).ravel()
+    weak = (rows != cols) & (np.abs(A.data) + np.abs(aji) < 2.0 * eps * np.sqrt(np.abs(d[rows] * d[cols])))
+    lump = np.bincount(rows[weak], weights=A.data[weak], minlength=n)
+    keep = ~weak
+    data, r, c = A.data[keep].copy(), rows[keep], cols[keep]
+    on_diag = r == c
+    data[on_diag] = data[on_diag] + lump[r[on_diag]]
+    indptr = np.concatenate([[0], np.cumsum(np.bincount(r, minlength=n))]).astype(A.indptr.dtype)
+    return sp.csr_matrix((data, c.copy(), indptr), shape=A.shape)
+
+
 @dataclass
 class Level:
     A: sp.csr_matrix
@@ -184,6 +213,8 @@ def build_hierarchy(A: sp.csr_matrix, max_levels: int = 10, max_coarse: int = 10
         R.sort_indices()
         Ac = (R @ Acur @ P).tocsr()
         Ac.sort_indices()
+        if len(H.levels) == 1 and FILTER_EPS > 0:
+            Ac = filter_weak(Ac, FILTER_EPS)
         lvl.P, lvl.R, lvl.agg = P, R, agg
         Acur = Ac
         theta *= THETA_FACTOR
