@@ -334,6 +334,11 @@ struct mm_problem {
     void* p = nullptr;
     if (n == 0) n = 1;
     if (!st) throw Fail{MM_ERR_CUDA, "device allocation before the problem's stream exists"};
+    // an allocation on a capturing stream would become a graph node whose memory lives only while
+    // the graph runs: every buffer is made before a capture begins
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) throw Fail{MM_ERR_STATE, "device allocation while the stream captures"};
     CK(cudaMallocAsync(&p, n * sizeof(T), st));
     allocs.push_back(p);
     // zeroed: reused device memory can hold any bit pattern (a NaN in an FP32 view of old FP64 data),
