@@ -630,3 +630,38 @@ def test_solves_on_reused_device_memory(cuda_ok):
                 ref = U
             assert rel(U, ref) <= 1e-8
             del pr
+
+
+def test_level1_filter_keeps_the_solve(cuda_ok):
+    """The level-1 operator without its weak couplings (the default) against the plain Galerkin one
+    (MM_OPT_SA_FILTER_E6 < 0): fewer entries with the row sums kept, each hierarchy equal to the
+    oracle's built the same way, and both solves at the tolerance with the oracle's iterations."""
+    s, p, _ = case("cube40_h2_air200")
+    ops = ofem.assembled_operators(p, parts=("A", "D"))
+    m = random_state(s.N, seed=44, amplitude=0.05)
+    res = {}
+    for opt in (0, -1):
+        prob = fem_utils.make_problem(s)
+        prob.set_option("sa_filter_e6", opt)
+        prob.build_poisson(1e-12, "amgcl")
+        res[opt] = (prob, prob.amg_levels())
+    A1f, A1 = res[0][1][1]["A"], res[-1][1][1]["A"]
+    assert A1f.nnz < 0.7 * A1.nnz  # 40 nm cube: 305,284 of 476,414 entries
+    scale = abs(A1).max()
+    assert np.abs(np.asarray(A1f.sum(axis=1)) - np.asarray(A1.sum(axis=1))).max() <= 1e-12 * scale
+    saved = opo.FILTER_EPS
+    try:
+        for opt, eps in ((0, 0.002), (-1, 0.0)):
+            opo.FILTER_EPS = eps
+            H = opo.build_hierarchy(ops["A"])
+            prob, lv = res[opt]
+            assert [x["A"].shape[0] for x in lv] == [lvl.A.shape[0] for lvl in H.levels]
+            for a, b in zip(lv, H.levels):
+                assert abs(a["A"] - b.A).max() <= 1e-13 * abs(b.A).max()
+            su = opo.SolveU(p, ops, cg_tol=1e-10, hierarchy=H)
+            U_o, it_o, _ = su(m, np.zeros(p.N), 1e-10, return_info=True)
+            U, it, rr, rc = prob.solve_u(m, np.zeros(s.N), 1e-10)
+            assert rc == 0 and rr <= 1e-10 and abs(it - it_o) <= 1
+            assert rel(U, U_o) <= 1e-8
+    finally:
+        opo.FILTER_EPS = saved

@@ -181,3 +181,29 @@ def test_oracle_minimizer_decreases_energy():
         m, U, info = omin.minimize(O, m0, B, np.zeros(p.N), prm, method)
         assert info["E"] < E0
         assert np.allclose(np.linalg.norm(m, axis=1), 1.0)
+
+
+def test_filter_weak_keeps_row_sums_and_symmetry():
+    """The level-1 filter of the oracle's hierarchy: a symmetric decision (|a_ij| + |a_ji| against
+    2 eps sqrt(|a_ii a_jj|)), the dropped values added to their row's diagonal (row sums kept), the
+    kept off-diagonal entries untouched."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(5)
+    n = 80
+    M = sp.random(n, n, density=0.15, random_state=rng, format="csr")
+    M.data = M.data * rng.choice([-1.0, 1.0], size=M.nnz) * np.exp(-6.0 * rng.random(M.nnz))
+    A = (M + M.T).tocsr()
+    A = (A + sp.diags(np.asarray(abs(A).sum(axis=1)).ravel() + 1.0)).tocsr()
+    A.sort_indices()
+    eps = 0.01
+    F = opo.filter_weak(A, eps)
+    assert F.nnz < A.nnz
+    assert abs(F - F.T).max() == 0.0
+    assert np.allclose(np.asarray(F.sum(axis=1)).ravel(), np.asarray(A.sum(axis=1)).ravel(), rtol=1e-14, atol=1e-14)
+    d = A.diagonal()
+    C = F.tocoo()
+    off = C.row != C.col
+    kept = np.asarray(abs(A)[C.row[off], C.col[off]]).ravel() * 2.0
+    assert np.all(kept >= 2.0 * eps * np.sqrt(np.abs(d[C.row[off]] * d[C.col[off]])))
+    assert np.array_equal(np.asarray(A[C.row[off], C.col[off]]).ravel(), C.data[off])
