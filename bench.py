@@ -627,6 +627,20 @@ def run_ours(a):
                   "rel_res_fp64_max": max(q_rr),
                   "method": "the FP64 PCG (FP64 iterate, residual, directions, finest-level products and inner "
                             "products; the plain method's stopping test) with the V-cycle applied in FP32"}
+        # the same in-solve kernel profile for this solver (FP32 V-cycle kernels: 4-byte values)
+        pq.set_option("profile", 1)
+        pq.profile(reset=True)
+        timed_solves(pq, m_dev, U_dev, flush, a.tol, a.profile_steps)
+        qrows = pq.profile(reset=True)
+        pq.set_option("profile", 0)
+        qtot = sum(r["total_ms"] for r in qrows)
+        fp32pc["kernels"] = []
+        for r in qrows[:10]:
+            gbs = r["bytes_per_launch"] / (r["ms_per_launch"] * 1e-3) / 1e9
+            fp32pc["kernels"].append({"kernel": r["kernel"], "level": r["level"],
+                                      "launches_per_solve": r["launches"] / a.profile_steps,
+                                      "us_per_launch": 1e3 * r["ms_per_launch"], "share": r["total_ms"] / qtot,
+                                      "bytes_per_launch": r["bytes_per_launch"], "GBps": gbs, "frac_hbm": gbs / peak})
 
     learned_leg = None
     if not a.no_learned:
