@@ -276,6 +276,8 @@ struct mm_problem {
          *w_tmp = nullptr, *w_mprev = nullptr, *w_gtprev = nullptr, *w_ys = nullptr, *w_x1 = nullptr,
          *w_x2 = nullptr, *w_x3 = nullptr, *w_x4 = nullptr, *w_U2 = nullptr, *w_U3 = nullptr;
   std::vector<double*> w_S, w_Y;
+  double* d_lb = nullptr;  // L-BFGS scalars on the device: rho[lb_mem], alpha[lb_mem], gamma
+  int lb_mem = 0;
   float *w_r3f = nullptr, *w_z3f = nullptr, *w_p3f = nullptr, *w_Ap3f = nullptr, *w_yf = nullptr;
   struct InnerGraph {              // the inner solve's WHILE graph for one (m, g_ext, y, reg, precision)
     const double* m;
@@ -1361,6 +1363,10 @@ void ensure_min_buffers(mm_problem* h, int memory) {
     }
     h->min_ready = true;
   }
+  if (memory > h->lb_mem) {
+    h->d_lb = h->alloc<double>(2 * (size_t)memory + 1);
+    h->lb_mem = memory;
+  }
   while ((int)h->w_S.size() < memory) {
     double* s = h->alloc<double>(n3);
     double* y = h->alloc<double>(n3);
@@ -2068,41 +2074,43 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
   int it = 0;
   bool conv = false;
 
-  // L-BFGS two-loop recursion on g_tan_ext; `initial(q, out)` applies the initial inverse Hessian
+  // L-BFGS two-loop recursion on g_tan_ext; `initial(q, out)` applies the initial inverse Hessian.
+  // The recursion's scalars (rho, alpha, the dots) stay on the device: the history's length and slots
+  // are known on the host, so no step waits for a host read.
+  double* d_rho = h->d_lb;
+  double* d_alpha = h->d_lb ? h->d_lb + h->lb_mem : nullptr;
+  double* d_gamma = h->d_lb ? h->d_lb + 2 * h->lb_mem : nullptr;
   auto two_loop = [&](double* out, auto&& initial) {
     const int n_hist = std::min(hist_it, mem);
-    std::vector<double> alphas(mem, 0.0);
     double* q = h->w_y;
     copy3(q, h->w_gte);
     for (int i = 0; i < n_hist; ++i) {
       const int idx = ((hist_it - 1 - i) % mem + mem) % mem;
-      const double a = rho_h[idx] * dev_dot(h, n3, h->w_S[idx], q);
-      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, -a, h->w_Y[idx], 1.0, q);
+      dot(h, n3, h->w_S[idx], q, R_A);
+      mmk::k_lb_first<<<g3, BS, 0, h->st>>>(n3, d_rho + idx, h->d_sc, R_A, d_alpha + idx, h->w_Y[idx], q);
       LAUNCH_CHECK();
-      alphas[idx] = a;
     }
     initial(q, out);
     for (int i = 0; i < n_hist; ++i) {
       const int idx = ((hist_it - n_hist + i) % mem + mem) % mem;
-      const double bta = rho_h[idx] * dev_dot(h, n3, h->w_Y[idx], out);
-      mmk::k_axpby<<<g3, BS, 0, h->st>>>(n3, alphas[idx] - bta, h->w_S[idx], 1.0, out);
+      dot(h, n3, h->w_Y[idx], out, R_A);
+      mmk::k_lb_second<<<g3, BS, 0, h->st>>>(n3, d_rho + idx, d_alpha + idx, h->d_sc, R_A, h->w_S[idx], out);
       LAUNCH_CHECK();
     }
   };
   // initial Hessian of the plain L-BFGS: gamma q .* inv_M_rel, gamma = s.y / y.(y .* inv_M_rel) clipped
   auto lbfgs_initial = [&](const double* q, double* out, bool clip) {
     const int last = ((hist_it - 1) % mem + mem) % mem;
-    double gamma = 1.0;
     if (hist_it > 0) {
       mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, h->w_Y[last], h->d_inv_M_rel, h->w_tmp, h->d_sc, h->d_part, R_B);
       LAUNCH_CHECK();
-      const double yMy = h->red(R_B);
-      gamma = dev_dot(h, n3, h->w_S[last], h->w_Y[last]) / (yMy + 1e-30);
+      dot(h, n3, h->w_S[last], h->w_Y[last], R_A);
     }
-    if (clip) gamma = std::min(std::max(gamma, 1e-3), 1e3);
+    mmk::k_lb_gamma<<<1, 32, 0, h->st>>>(h->d_sc, R_A, R_B, hist_it > 0 ? 1 : 0, clip ? 1 : 0, d_gamma);
+    LAUNCH_CHECK();
     mmk::k_scale3_dot<<<ge, BS, 0, h->st>>>(N, q, h->d_inv_M_rel, out, h->d_sc, h->d_part, R_B);
     LAUNCH_CHECK();
-    mmk::k_scale<<<g3, BS, 0, h->st>>>(n3, gamma, out);
+    mmk::k_scale_dev<<<g3, BS, 0, h->st>>>(n3, d_gamma, out);
     LAUNCH_CHECK();
   };
   // history update at m_new: s = P(d tau), y = P(g_new) - P(g_tan_ext) (optionally replaced by `y_fix`),
@@ -2133,6 +2141,9 @@ int minimize_dev(mm_problem* h, const double* B, double*& m, double*& U, const m
       copy3(h->w_S[idx], s_new);
       copy3(h->w_Y[idx], h->w_r3);
       rho_h[idx] = 1.0 / (curv + 1e-30);
+      if (!d_rho) throw Fail{MM_ERR_STATE, "L-BFGS history without its device scalars"};
+      mmk::k_set_value<<<1, 32, 0, h->st>>>(d_rho + idx, rho_h[idx]);
+      LAUNCH_CHECK();
       ++hist_it;
     }
   };

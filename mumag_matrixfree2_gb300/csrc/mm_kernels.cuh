@@ -1891,10 +1891,55 @@ __global__ void __launch_bounds__(BS) k_xpay(int n, const double* __restrict__ x
   for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = x[i] + a * y[i];
 }
 
+__device__ __forceinline__ double axpby_elem(double a, double x, double b, double y) { return a * x + b * y; }
+
 // y = a * x + b * y
 __global__ void __launch_bounds__(BS) k_axpby(int n, double a, const double* __restrict__ x, double b,
                                               double* __restrict__ y) {
-  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = a * x[i] + b * y[i];
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = axpby_elem(a, x[i], b, y[i]);
+}
+
+// L-BFGS two-loop recursion with its scalars on the device (no host read between the steps):
+// first loop, a = rho * (s.q) from red[slot], stored in *alpha, then q = -a y + q
+__global__ void __launch_bounds__(BS) k_lb_first(int n, const double* __restrict__ rho, const Scalars* sc, int slot,
+                                                 double* __restrict__ alpha, const double* __restrict__ y,
+                                                 double* __restrict__ q) {
+  const double a = __dmul_rn(*rho, sc->red[slot]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *alpha = a;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) q[i] = axpby_elem(-a, y[i], 1.0, q[i]);
+}
+
+// second loop: c = alpha - rho * (y.out) from red[slot], then out = c s + out
+__global__ void __launch_bounds__(BS) k_lb_second(int n, const double* __restrict__ rho,
+                                                  const double* __restrict__ alpha, const Scalars* sc, int slot,
+                                                  const double* __restrict__ s, double* __restrict__ out) {
+  const double c = __dsub_rn(*alpha, __dmul_rn(*rho, sc->red[slot]));
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) out[i] = axpby_elem(c, s[i], 1.0, out[i]);
+}
+
+// initial inverse-Hessian scale of the plain L-BFGS: gamma = (s.y) / (y.(M y) + 1e-30) from red[slot_sy]
+// and red[slot_ymy] (1 without history), clipped to [1e-3, 1e3] when clip
+__global__ void k_lb_gamma(const Scalars* sc, int slot_sy, int slot_ymy, int has_hist, int clip,
+                           double* __restrict__ gamma) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double g = 1.0;
+  if (has_hist) g = __ddiv_rn(sc->red[slot_sy], __dadd_rn(sc->red[slot_ymy], 1e-30));
+  if (clip) {
+    g = (g < 1e-3) ? 1e-3 : g;
+    g = (1e3 < g) ? 1e3 : g;
+  }
+  *gamma = g;
+}
+
+// y *= *a (a scalar on the device)
+__global__ void __launch_bounds__(BS) k_scale_dev(int n, const double* __restrict__ a, double* __restrict__ y) {
+  const double s = *a;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) y[i] = s * y[i];
+}
+
+// *dst = v
+__global__ void k_set_value(double* __restrict__ dst, double v) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *dst = v;
 }
 
 // y *= a
