@@ -1204,7 +1204,9 @@ int run_mixed(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out
 }
 
 // demag solve with the potential in d_U (in/out)
-int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters, double* rel_res) {
+// h_out (host, or null): the potential is also copied there, behind the solve and inside its one wait
+int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters, double* rel_res,
+              double* h_out = nullptr) {
   if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called before a solve"};
   CK(cudaEventRecord(h->ev0, h->st));
   if (d_U != h->d_x) CK(cudaMemcpyAsync(h->d_x, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
@@ -1231,7 +1233,12 @@ int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int max
   if (zero_mean) sub_mean(h, h->d_x);
   if (d_U != h->d_x) CK(cudaMemcpyAsync(d_U, h->d_x, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   CK(cudaEventRecord(h->ev1, h->st));
-  CK(cudaEventSynchronize(h->ev1));
+  if (h_out) {
+    CK(cudaMemcpyAsync(h_out, h->d_x, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  } else {
+    CK(cudaEventSynchronize(h->ev1));
+  }
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_solve_ms = ms;
@@ -3344,10 +3351,7 @@ int mm_solve_u(mm_problem* h, const double* m, double* U, double tol, int maxite
   return guarded(h, [&] {
     CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    const int rc = solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res);
-    CK(cudaMemcpyAsync(U, h->d_U, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    h->sync();
-    return rc;
+    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U);
   });
 }
 
@@ -3357,10 +3361,7 @@ int mm_solve_u_x0(mm_problem* h, const double* m, const double* x0, double* U_ou
   return guarded(h, [&] {
     CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(h->d_U, x0, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    const int rc = solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res);
-    CK(cudaMemcpyAsync(U_out, h->d_U, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    h->sync();
-    return rc;
+    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U_out);
   });
 }
 
