@@ -327,6 +327,8 @@ struct mm_problem {
   double* d_min_bias = nullptr;    // per-node bias field of the minimizer's energy evaluations (or null)
   double* min_bias_buf = nullptr;  // its storage
   cudaEvent_t ev_after = nullptr;  // ordering point taken on another stream (mm_scale_correction_async)
+  cudaStream_t st_copy = nullptr;  // a second copy engine's stream for the host-array solves' initial guess
+  cudaEvent_t ev_copy = nullptr;
 
   // Device buffers come from the device's stream-ordered pool on the problem's stream and go back to
   // it with cudaFreeAsync (mm_destroy): unlike cudaMalloc / cudaFree, neither waits for the work other
@@ -1204,13 +1206,16 @@ int run_mixed(mm_problem* h, double tol, int maxiter, int* iters, double* r2_out
 }
 
 // demag solve with the potential in d_U (in/out)
-// h_out (host, or null): the potential is also copied there, behind the solve and inside its one wait
+// h_out (host, or null): the potential is also copied there, behind the solve and inside its one wait.
+// x0_ready (or null): an event the initial guess d_U waits for (its copy from the host on another
+// stream, which then overlaps the right-hand side)
 int solve_dev(mm_problem* h, const double* d_m, double* d_U, double tol, int maxiter, int* iters, double* rel_res,
-              double* h_out = nullptr) {
+              double* h_out = nullptr, cudaEvent_t x0_ready = nullptr) {
   if (!h->poisson_built) throw Fail{MM_ERR_STATE, "mm_build_poisson must be called before a solve"};
   CK(cudaEventRecord(h->ev0, h->st));
-  if (d_U != h->d_x) CK(cudaMemcpyAsync(h->d_x, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   enqueue_rhs(h, d_m);
+  if (x0_ready) CK(cudaStreamWaitEvent(h->st, x0_ready, 0));
+  if (d_U != h->d_x) CK(cudaMemcpyAsync(h->d_x, d_U, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   const bool zero_mean = !h->has_mask;
   if (zero_mean) {
     sub_mean(h, h->d_b);
@@ -3160,6 +3165,8 @@ int mm_destroy(mm_problem* h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_after) cudaEventDestroy(h->ev_after);
+  if (h->ev_copy) cudaEventDestroy(h->ev_copy);
+  if (h->st_copy) cudaStreamDestroy(h->st_copy);
   for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -3346,12 +3353,24 @@ int mm_precond(mm_problem* h, const double* r, double* z) {
   });
 }
 
+// The initial guess's upload on the problem's second copy stream, behind the work already queued on
+// its stream (which may still read d_U); returns the event the solve waits on before using it.
+static cudaEvent_t upload_x0(mm_problem* h, const double* x0) {
+  if (!h->st_copy) CK(cudaStreamCreateWithFlags(&h->st_copy, cudaStreamNonBlocking));
+  if (!h->ev_copy) CK(cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  CK(cudaStreamWaitEvent(h->st_copy, h->ev_copy, 0));
+  CK(cudaMemcpyAsync(h->d_U, x0, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st_copy));
+  CK(cudaEventRecord(h->ev_copy, h->st_copy));
+  return h->ev_copy;
+}
+
 int mm_solve_u(mm_problem* h, const double* m, double* U, double tol, int maxiter, int* iters, double* rel_res) {
   if (!h || !m || !U || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;
   return guarded(h, [&] {
     CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_U, U, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U);
+    const cudaEvent_t ready = upload_x0(h, U);
+    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U, ready);
   });
 }
 
@@ -3360,8 +3379,8 @@ int mm_solve_u_x0(mm_problem* h, const double* m, const double* x0, double* U_ou
   if (!h || !m || !x0 || !U_out || !(tol >= 0) || maxiter < 0) return MM_ERR_ARG;
   return guarded(h, [&] {
     CK(cudaMemcpyAsync(h->d_m, m, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_U, x0, h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U_out);
+    const cudaEvent_t ready = upload_x0(h, x0);
+    return solve_dev(h, h->d_m, h->d_U, tol, maxiter, iters, rel_res, U_out, ready);
   });
 }
 
