@@ -2803,9 +2803,12 @@ void build_solver(mm_problem* h, SolverT<T>& S, const mm::HostCSR& A, bool amg, 
         std::vector<double> sd(hl.A.n_rows);
         for (int i = 0; i < hl.A.n_rows; ++i)
           sd[i] = precond_type == MM_PRECOND_AMGCL ? hl.spai0[i] : 0.6667 / (hl.diag[i] + 1e-30);
-        h->rf_host[l] = mm::fused_restriction(hl.R, hl.A, sd);
+        // from R A when the setup kept it (no second sparse product), else from R and A
+        h->rf_host[l] = hl.RA.ptr.empty() ? mm::fused_restriction(hl.R, hl.A, sd)
+                                          : mm::fused_restriction_ra(hl.R, hl.RA, sd);
       }
       h->rf_prec = precond_type;
+      for (mm::AmgLevel& hl : h->amg_h) hl.RA = mm::HostCSR{};  // its one use is above
     }
     for (int l = 0; l < L - 1; ++l) S.lv[l].Rf = h->upload_mat<T>(h->rf_host[l]);
   }
@@ -2957,6 +2960,7 @@ int mm_setup_create(int N, int E, const int* conn, const double* volume, const d
       prm.max_levels = max_levels > 0 ? max_levels : 10;
       prm.max_coarse = max_coarse > 0 ? max_coarse : 1000;
       s->amg = mm::build_amg(A, prm);
+      for (mm::AmgLevel& l : s->amg) l.RA = mm::HostCSR{};
     }
     return MM_OK;
   });

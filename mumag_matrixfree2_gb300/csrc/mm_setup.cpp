@@ -619,6 +619,45 @@ HostCSR fused_restriction(const HostCSR& R, const HostCSR& A, const std::vector<
   return F;
 }
 
+HostCSR fused_restriction_ra(const HostCSR& R, const HostCSR& RA, const std::vector<double>& s) {
+  const int n = R.n_rows;
+  std::vector<int> cnt(n + 1, 0);
+  std::vector<std::vector<int>> tcol;
+  std::vector<std::vector<double>> tval;
+  const int nt = setup_threads(RA.ptr[n]);
+  tcol.resize(nt);
+  tval.resize(nt);
+  // F = R - RA diag(s), merging two sorted rows, exact zeros dropped; rows in chunks, concatenated in order
+  parallel_chunks(n, nt, [&](int t, int64_t r0, int64_t r1) {
+    for (int64_t i = r0; i < r1; ++i) {
+      int a = R.ptr[i], b = RA.ptr[i], len = 0;
+      const int ae = R.ptr[i + 1], be = RA.ptr[i + 1];
+      while (a < ae || b < be) {
+        const int ca = a < ae ? R.col[a] : R.n_cols;
+        const int cb = b < be ? RA.col[b] : R.n_cols;
+        const int c = std::min(ca, cb);
+        double v = 0.0;
+        if (ca == c) v += R.val[a++];
+        if (cb == c) v -= RA.val[b++] * s[c];
+        if (v != 0.0) {
+          tcol[t].push_back(c);
+          tval[t].push_back(v);
+          ++len;
+        }
+      }
+      cnt[i + 1] = len;
+    }
+  });
+  HostCSR F;
+  F.n_rows = n;
+  F.n_cols = R.n_cols;
+  F.ptr.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) F.ptr[i + 1] = F.ptr[i] + cnt[i + 1];
+  concat_parallel(tcol, F.col);
+  concat_parallel(tval, F.val);
+  return F;
+}
+
 static std::vector<double> diag_of(const HostCSR& A) {
   std::vector<double> d(A.n_rows, 0.0);
   parallel_chunks(A.n_rows, setup_threads(A.n_rows), [&](int, int64_t r0, int64_t r1) {
@@ -873,6 +912,7 @@ static std::vector<AmgLevel> build_amg_theta(const HostCSR& A0, const AmgParams&
     HostCSR R = transpose(P);
     HostCSR RA = spgemm(R, Acur);
     next = spgemm(RA, P);
+    L.RA = std::move(RA);
     if (levels.size() == 1 && prm.filter_eps > 0.0) next = filter_weak(next, prm.filter_eps);
     L.P = std::move(P);
     L.R = std::move(R);

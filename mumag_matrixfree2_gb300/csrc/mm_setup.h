@@ -63,6 +63,7 @@ struct EnergyOp {
 
 struct AmgLevel {
   HostCSR A, P, R;
+  HostCSR RA;  // R A, the Galerkin product's first factor, kept for the fused restriction (may be freed)
   std::vector<double> spai0, diag;
   std::vector<int> agg;  // aggregate of each row (-1 = none), empty on the coarsest level
 };
@@ -127,6 +128,8 @@ std::vector<AmgLevel> build_amg(const HostCSR& A, const AmgParams& prm);
 // R (I - A S), S = diag(s): the restriction of the residual that a pre-smoothing from zero leaves,
 // x = S b, r = b - A x, b_c = R r = R (I - A S) b, as one operator (exact zeros dropped, columns sorted)
 HostCSR fused_restriction(const HostCSR& R, const HostCSR& A, const std::vector<double>& s);
+// the same from the product RA = R A: R - (R A) S, with no second sparse product
+HostCSR fused_restriction_ra(const HostCSR& R, const HostCSR& RA, const std::vector<double>& s);
 std::vector<double> dense_inverse(const HostCSR& A);  // row-major n x n; throws on singular
 
 }  // namespace mm
